@@ -1,0 +1,167 @@
+/*
+ * gbfem.h -- C ABI of the GB300 (sm_103a) corotational-tetrahedron FEM implicit-Euler step.
+ *
+ * One handle is one deformable body: OpenSurgSim's Fem3DRepresentation with
+ * Fem3DElementCorotationalTetrahedron elements, IntegrationScheme EULER_IMPLICIT and
+ * LinearSolver CONJUGATEGRADIENT. All device memory belongs to the handle; every array passed in
+ * is copied during the call. No function throws; every function returns a gbfem_status and the
+ * message of the last failure is available from gbfem_last_error.
+ *
+ * Threading matches the reference's FreeMotion: one handle is used by one thread at a time;
+ * different handles may be used concurrently (each has its own CUDA stream).
+ *
+ * Reference interfaces replaced (paths inside the OpenSurgSim tree):
+ *   SurgSim/Physics/Fem3DRepresentation.h        setFem/loadFem, setInitialState, initialize
+ *   SurgSim/Physics/FemRepresentation.cpp:232-294 update(dt)
+ *   SurgSim/Math/OdeSolverEulerImplicit.h:33-76    solve, setNewtonRaphson*
+ *   SurgSim/Math/LinearSparseSolveAndInverse.h:98-123  LinearSparseSolveAndInverseCG
+ *   SurgSim/Math/OdeState.h:38-207                 positions, velocities, boundary conditions
+ */
+#ifndef GBFEM_H
+#define GBFEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBFEM_API __attribute__((visibility("default")))
+#else
+#define GBFEM_API
+#endif
+
+/* Status codes. The reference throws SurgSim::Framework::AssertionFailure for invalid input
+ * (Framework/Assert.h:77-95) and deactivates a representation whose state is not finite
+ * (FemRepresentation.cpp:285-293); these codes carry the same outcomes across the ABI. */
+typedef enum gbfem_status
+{
+	GBFEM_OK = 0,
+	GBFEM_INVALID_ARG = 1,          /* bad sizes, indices, materials or parameters */
+	GBFEM_DEGENERATE_ELEMENT = 2,   /* rest tetrahedron not invertible (|det V| <= 1e-12) */
+	GBFEM_CG_MAXITER = 3,           /* CG stopped at maxIterations; the step was still applied */
+	GBFEM_NONFINITE = 4,            /* state became NaN/Inf; the handle is deactivated */
+	GBFEM_CUDA_ERROR = 5,
+	GBFEM_INACTIVE = 6,             /* step called on a deactivated handle: no-op */
+	GBFEM_OUT_OF_MEMORY = 7
+} gbfem_status;
+
+/* Arithmetic of the step. */
+typedef enum gbfem_precision
+{
+	GBFEM_PRECISION_FP64 = 0,   /* plain form: FP64 throughout */
+	GBFEM_PRECISION_MIXED = 1   /* FP32 element kernels and CG, FP64 iterative refinement */
+} gbfem_precision;
+
+typedef struct gbfem_handle_s* gbfem_handle;
+
+/* Mesh: Fem3DRepresentation::setFem (Fem3DRepresentation.cpp:70-126) + per-element material
+ * (FemElement3DParameter) + OdeState boundary conditions (OdeState.cpp:115-142). */
+typedef struct gbfem_mesh_desc
+{
+	int32_t num_nodes;
+	const double* rest_positions;   /* [3 * num_nodes], node-major x,y,z */
+	int32_t num_tets;
+	const int32_t* tets;            /* [4 * num_tets] node ids */
+	const double* young_modulus;    /* [num_tets] */
+	const double* poisson_ratio;    /* [num_tets] */
+	const double* mass_density;     /* [num_tets] */
+	int32_t num_bc_dofs;
+	const int32_t* bc_dofs;         /* dof ids 3*node+axis; duplicates are ignored */
+} gbfem_mesh_desc;
+
+typedef struct gbfem_params
+{
+	double rayleigh_mass;           /* FemRepresentation RayleighDampingMass (alpha) */
+	double rayleigh_stiffness;      /* FemRepresentation RayleighDampingStiffness (beta) */
+	double gravity[3];              /* Representation.cpp:36 default (0, -9.81, 0) */
+	int32_t gravity_enabled;
+	int32_t newton_max_iterations;  /* OdeSolverEulerImplicit default 1 */
+	double newton_epsilon;          /* default 1e-5 (infinity norm of the solution variation) */
+	double cg_tolerance;            /* LinearSparseSolveAndInverseCG::setTolerance */
+	int32_t cg_max_iterations;      /* setMaxIterations; <= 0 selects Eigen's default 2n */
+	int32_t precision;              /* gbfem_precision */
+	int32_t device;                 /* CUDA device ordinal */
+	int32_t reserved[7];
+} gbfem_params;
+
+/* Per-call statistics of the last gbfem_step. */
+typedef struct gbfem_stats
+{
+	int32_t steps;                  /* steps applied */
+	int32_t cg_iterations;          /* summed over steps and Newton iterations (Eigen's count) */
+	int32_t cg_max_iterations_hit;  /* number of solves that stopped at maxIterations */
+	int32_t refinement_sweeps;      /* mixed precision: FP64 residual evaluations */
+	double cg_relative_residual;    /* of the last solve: sqrt(|r|^2/|b|^2) */
+	double ms_element, ms_assemble, ms_solve, ms_update;  /* device time per phase (if timed) */
+	int32_t singular_g;             /* element updates that hit the singular-G early return */
+	int32_t polar_fallbacks;        /* element updates that took the SVD polar path */
+	int32_t active;
+	int32_t reserved[5];
+} gbfem_stats;
+
+/* Flags for gbfem_step. */
+#define GBFEM_STEP_TIME_PHASES 1u   /* record per-phase device times (adds events) */
+#define GBFEM_STEP_KEEP_SYSTEM 2u   /* keep the full S / rhs / f of the last solve for export */
+
+GBFEM_API gbfem_status gbfem_params_default(gbfem_params* out);
+
+/* Build a body: copies the mesh, precomputes rest quantities (Fem3DElementTetrahedron.cpp:92-216,
+ * Fem3DElementCorotationalTetrahedron.cpp:48-75), the sparsity pattern and the element-to-nonzero
+ * maps (FemRepresentation.cpp:85-132). The state starts at rest with zero velocity. */
+GBFEM_API gbfem_status gbfem_create(const gbfem_mesh_desc* mesh, const gbfem_params* params, gbfem_handle* out);
+GBFEM_API gbfem_status gbfem_destroy(gbfem_handle h);
+
+/* FemRepresentation::update(dt) repeated nsteps times (OdeSolverEulerImplicit::solve with
+ * computeCompliance = false). Returns GBFEM_NONFINITE (and deactivates) when the state stops being
+ * finite, GBFEM_CG_MAXITER when a solve hit maxIterations, GBFEM_INACTIVE when deactivated. */
+GBFEM_API gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flags);
+GBFEM_API gbfem_status gbfem_get_stats(gbfem_handle h, gbfem_stats* out);
+
+/* OdeState positions / velocities, host arrays of 3*num_nodes doubles (either may be NULL). */
+GBFEM_API gbfem_status gbfem_get_state(gbfem_handle h, double* x, double* v);
+GBFEM_API gbfem_status gbfem_set_state(gbfem_handle h, const double* x, const double* v);
+/* v[dofs[i]] = values[i]: prescribe the velocity of (boundary-condition) dofs before a step. */
+GBFEM_API gbfem_status gbfem_set_velocities(gbfem_handle h, int32_t count, const int32_t* dofs,
+											const double* values);
+/* Device pointers of the state (FP64, 3*num_nodes each), valid until gbfem_destroy. */
+GBFEM_API gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v);
+/* The CUDA stream the handle launches on (a cudaStream_t). */
+GBFEM_API gbfem_status gbfem_stream(gbfem_handle h, void** stream);
+GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
+
+/* Sizes: dofs n = 3*num_nodes, scalar nonzeros of the pattern. */
+GBFEM_API gbfem_status gbfem_get_sizes(gbfem_handle h, int64_t* num_dofs, int64_t* nnz);
+/* Global pattern in CSC (Eigen ColMajor, int StorageIndex): colptr[n+1], rowidx[nnz], rows sorted.
+ * The pattern is structurally symmetric, so these are also the CSR arrays. */
+GBFEM_API gbfem_status gbfem_get_pattern(gbfem_handle h, int32_t* colptr, int32_t* rowidx);
+/* Element-to-nonzero map: map[e*144 + (3a+i)*12 + 3b+j] = CSC slot of global entry
+ * (3*tet[e][a]+i, 3*tet[e][b]+j) -- the slots FemElement::assembleMatrixBlocksNoInitialize writes. */
+GBFEM_API gbfem_status gbfem_get_scatter(gbfem_handle h, int32_t* map);
+/* System of the last solve (requires GBFEM_STEP_KEEP_SYSTEM on that step): S values in CSC order
+ * with boundary conditions applied (full, not mirrored), rhs[n], and the force vector f[n]. */
+GBFEM_API gbfem_status gbfem_get_system(gbfem_handle h, double* S_csc, double* rhs, double* f);
+
+/* Human-readable message of the last failure on h (or of the last failed create when h is NULL). */
+GBFEM_API gbfem_status gbfem_last_error(gbfem_handle h, char* buf, size_t len);
+
+/* ---- LinearSparseSolveAndInverseCG on a caller matrix (LinearSparseSolveAndInverse.cpp:99-129).
+ * Jacobi-preconditioned CG reading only the lower triangle (row >= col) of the CSC matrix, zero
+ * initial guess, stop when |r|^2 < max(tol^2 |b|^2, DBL_MIN) or after max_iterations
+ * (<= 0: 2n). Host arrays in, host solution out. */
+typedef struct gbfem_cg_s* gbfem_cg;
+GBFEM_API gbfem_status gbfem_cg_create(int32_t n, const int32_t* colptr, const int32_t* rowidx,
+									   const double* values, int32_t device, gbfem_cg* out);
+GBFEM_API gbfem_status gbfem_cg_set_tolerance(gbfem_cg cg, double tolerance);
+GBFEM_API gbfem_status gbfem_cg_set_max_iterations(gbfem_cg cg, int32_t max_iterations);
+GBFEM_API gbfem_status gbfem_cg_solve(gbfem_cg cg, const double* b, double* x, int32_t* iterations,
+									  double* relative_residual);
+GBFEM_API gbfem_status gbfem_cg_destroy(gbfem_cg cg);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFEM_H */

@@ -1,0 +1,196 @@
+"""One deformable body on the GPU: a thin Python handle over the gbfem C ABI."""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GbfemError, dptr, iptr
+
+
+class Body:
+    """A corotational-tetrahedron body stepped by backward Euler + Jacobi-PCG on one GPU.
+
+    Mirrors ``FemRepresentation::update`` semantics (``FemRepresentation.cpp:232-294``): one
+    Newton iteration by default, CG reading the lower triangle, boundary-condition dofs fixed, the
+    body deactivated when its state stops being finite.
+    """
+
+    def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
+                 gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5,
+                 cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0):
+        L = _lib.load()
+        self._nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64).ravel()
+        self._tets = np.ascontiguousarray(mesh.tets, dtype=np.int32).ravel()
+        self._E = np.ascontiguousarray(mesh.young, dtype=np.float64)
+        self._nu = np.ascontiguousarray(mesh.poisson, dtype=np.float64)
+        self._rho = np.ascontiguousarray(mesh.density, dtype=np.float64)
+        self._bc = np.ascontiguousarray(mesh.bc_dofs, dtype=np.int32)
+        d = _lib.MeshDesc()
+        d.num_nodes = self._nodes.size // 3
+        d.rest_positions = dptr(self._nodes)
+        d.num_tets = self._tets.size // 4
+        d.tets = iptr(self._tets)
+        d.young_modulus = dptr(self._E)
+        d.poisson_ratio = dptr(self._nu)
+        d.mass_density = dptr(self._rho)
+        d.num_bc_dofs = self._bc.size
+        d.bc_dofs = iptr(self._bc) if self._bc.size else None
+        p = _lib.Params()
+        L.gbfem_params_default(ctypes.byref(p))
+        p.rayleigh_mass = rayleigh_mass
+        p.rayleigh_stiffness = rayleigh_stiffness
+        p.gravity[0], p.gravity[1], p.gravity[2] = gravity
+        p.gravity_enabled = 1 if gravity_enabled else 0
+        p.newton_max_iterations = newton_max_iterations
+        p.newton_epsilon = newton_epsilon
+        p.cg_tolerance = cg_tolerance
+        p.cg_max_iterations = cg_max_iterations
+        p.precision = precision
+        p.device = device
+        self.params = p
+        h = ctypes.c_void_p()
+        st = L.gbfem_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
+        if st != _lib.GBFEM_OK:
+            raise GbfemError(st, _lib.last_error(None))
+        self._h = h
+        self.num_nodes = d.num_nodes
+        self.num_tets = d.num_tets
+        n, nnz = ctypes.c_int64(), ctypes.c_int64()
+        L.gbfem_get_sizes(h, ctypes.byref(n), ctypes.byref(nnz))
+        self.n = n.value
+        self.nnz = nnz.value
+        self.last_status = _lib.GBFEM_OK
+
+    @classmethod
+    def from_scene(cls, scene, **over):
+        kw = dict(rayleigh_mass=scene.rayleigh_mass, rayleigh_stiffness=scene.rayleigh_stiffness,
+                  gravity=scene.gravity, cg_tolerance=scene.cg_tolerance, cg_max_iterations=scene.cg_max_iterations)
+        kw.update(over)
+        return cls(scene.mesh, **kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().gbfem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st, allow=()):
+        if st != _lib.GBFEM_OK and st not in allow:
+            raise GbfemError(st, _lib.last_error(self._h))
+        return st
+
+    def step(self, dt, nsteps=1, flags=0, raise_on=(_lib.GBFEM_CUDA_ERROR, _lib.GBFEM_OUT_OF_MEMORY,
+                                                   _lib.GBFEM_INVALID_ARG)):
+        """Advance nsteps; returns the status (NONFINITE/CG_MAXITER/INACTIVE are returned, not raised)."""
+        st = _lib.load().gbfem_step(self._h, float(dt), int(nsteps), int(flags))
+        self.last_status = st
+        if st in raise_on:
+            raise GbfemError(st, _lib.last_error(self._h))
+        return st
+
+    def stats(self) -> dict:
+        s = _lib.Stats()
+        _lib.load().gbfem_get_stats(self._h, ctypes.byref(s))
+        return s.as_dict()
+
+    def state(self):
+        x = np.empty(self.n)
+        v = np.empty(self.n)
+        self._check(_lib.load().gbfem_get_state(self._h, dptr(x), dptr(v)))
+        return x, v
+
+    def set_state(self, x=None, v=None):
+        xa = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        va = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        self._check(_lib.load().gbfem_set_state(self._h, dptr(xa) if xa is not None else None,
+                                                dptr(va) if va is not None else None))
+
+    def set_velocities(self, dofs, values):
+        dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(_lib.load().gbfem_set_velocities(self._h, dofs.size, iptr(dofs), dptr(values)))
+
+    def device_state(self):
+        x, v = ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.load().gbfem_device_state(self._h, ctypes.byref(x), ctypes.byref(v))
+        return x.value, v.value
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _lib.load().gbfem_stream(self._h, ctypes.byref(s))
+        return s.value
+
+    def reactivate(self):
+        _lib.load().gbfem_reactivate(self._h)
+
+    def pattern(self):
+        colptr = np.empty(self.n + 1, dtype=np.int32)
+        rowidx = np.empty(self.nnz, dtype=np.int32)
+        self._check(_lib.load().gbfem_get_pattern(self._h, iptr(colptr), iptr(rowidx)))
+        return colptr, rowidx
+
+    def scatter(self):
+        m = np.empty(self.num_tets * 144, dtype=np.int32)
+        self._check(_lib.load().gbfem_get_scatter(self._h, iptr(m)))
+        return m
+
+    def system(self):
+        S, rhs, f = np.empty(self.nnz), np.empty(self.n), np.empty(self.n)
+        self._check(_lib.load().gbfem_get_system(self._h, dptr(S), dptr(rhs), dptr(f)))
+        return dict(S=S, rhs=rhs, f=f)
+
+
+class CgSolver:
+    """``LinearSparseSolveAndInverseCG`` on the GPU for a caller CSC matrix."""
+
+    def __init__(self, colptr, rowidx, values, device=0):
+        self._colptr = np.ascontiguousarray(colptr, dtype=np.int32)
+        self._rowidx = np.ascontiguousarray(rowidx, dtype=np.int32)
+        self._vals = np.ascontiguousarray(values, dtype=np.float64)
+        self.n = self._colptr.size - 1
+        h = ctypes.c_void_p()
+        L = _lib.load()
+        st = L.gbfem_cg_create(self.n, iptr(self._colptr), iptr(self._rowidx), dptr(self._vals), device,
+                               ctypes.byref(h))
+        if st != _lib.GBFEM_OK:
+            raise GbfemError(st, _lib.last_error(None))
+        self._h = h
+
+    def set_tolerance(self, tol):
+        _lib.load().gbfem_cg_set_tolerance(self._h, float(tol))
+
+    def set_max_iterations(self, it):
+        _lib.load().gbfem_cg_set_max_iterations(self._h, int(it))
+
+    def solve(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty_like(b)
+        it = ctypes.c_int32()
+        res = ctypes.c_double()
+        st = _lib.load().gbfem_cg_solve(self._h, dptr(b), dptr(x), ctypes.byref(it), ctypes.byref(res))
+        if st not in (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER):
+            raise GbfemError(st, "cg solve failed")
+        return x, it.value, res.value, st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().gbfem_cg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

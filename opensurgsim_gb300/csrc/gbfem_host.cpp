@@ -1,0 +1,1012 @@
+// gbfem_host.cpp -- host side of the gbfem C ABI: validation, rest precompute, sparsity pattern
+// and element-to-nonzero maps, step orchestration on the handle's CUDA stream.
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfem.h"
+#include "gbfem_internal.h"
+
+using namespace gbfem;
+
+namespace {
+
+thread_local std::string g_lastCreateError;
+
+template <typename T>
+struct DevBuf
+{
+	T* p = nullptr;
+	size_t n = 0;
+	cudaError_t alloc(size_t count)
+	{
+		free();
+		n = count;
+		if (count == 0) return cudaSuccess;
+		return cudaMalloc(&p, count * sizeof(T));
+	}
+	cudaError_t upload(const T* src, size_t count, cudaStream_t s)
+	{
+		cudaError_t e = alloc(count);
+		if (e != cudaSuccess || count == 0) return e;
+		return cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
+	}
+	void free()
+	{
+		if (p) cudaFree(p);
+		p = nullptr;
+		n = 0;
+	}
+};
+
+double det3v(const double* a, const double* b, const double* c)
+{
+	return a[0] * b[1] * c[2] + a[2] * b[0] * c[1] + a[1] * b[2] * c[0] - a[2] * b[1] * c[0] - a[1] * b[0] * c[2] -
+		   a[0] * b[2] * c[1];
+}
+
+double det33(const double m[3][3])
+{
+	return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+		   m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+}
+
+// Inverse of the 4x4 homogeneous rest matrix with the |det| > 1e-12 check of
+// Fem3DElementCorotationalTetrahedron.cpp:57-72.
+bool inverse44(const double a[4][4], double inv[4][4])
+{
+	double cof[4][4];
+	for (int i = 0; i < 4; ++i)
+		for (int j = 0; j < 4; ++j)
+		{
+			double m[3][3];
+			int r = 0;
+			for (int ii = 0; ii < 4; ++ii)
+			{
+				if (ii == i) continue;
+				int c = 0;
+				for (int jj = 0; jj < 4; ++jj)
+					if (jj != j) m[r][c++] = a[ii][jj];
+				++r;
+			}
+			cof[i][j] = (((i + j) & 1) ? -1.0 : 1.0) * det33(m);
+		}
+	double d = 0;
+	for (int j = 0; j < 4; ++j) d += a[0][j] * cof[0][j];
+	if (!(std::fabs(d) > 1e-12)) return false;
+	for (int i = 0; i < 4; ++i)
+		for (int j = 0; j < 4; ++j) inv[i][j] = cof[j][i] / d;
+	return true;
+}
+
+}  // namespace
+
+struct gbfem_handle_s
+{
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	gbfem_params prm{};
+	int N = 0, E = 0, n = 0;
+	int nb = 0, nl = 0;
+	int64_t nnz = 0;
+	bool active = true;
+	std::string err;
+	gbfem_stats stats{};
+
+	// host structure
+	std::vector<int32_t> tets;
+	std::vector<int> adjPtr, adj;  // node adjacency incl. self (sorted) = BSR structure
+	std::vector<double> cmass;     // per element rho V / 20 (consistent mass coefficient)
+	std::vector<uint8_t> bcMask;
+
+	// device
+	DevBuf<int4> d_tets;
+	DevBuf<double> d_rest, d_xrest, d_lmass, d_nmass;
+	DevBuf<int> d_brow, d_bcol, d_cptr, d_cidx, d_iptr, d_iidx;
+	DevBuf<int4> d_lblk;
+	DevBuf<uint8_t> d_bc;
+	DevBuf<double> d_x, d_v, d_xt, d_vt;
+	DevBuf<double> d_kslots, d_rhsE, d_A, d_invdiag, d_rhs, d_dv, d_dvPrev, d_r, d_p, d_q, d_part;
+	DevBuf<int> d_counters;
+	DevBuf<CgCtl> d_ctl;
+	CgCtl* h_ctl = nullptr;
+	DevBuf<int> d_idx;      // scratch for gbfem_set_velocities
+	DevBuf<double> d_vals;
+
+	// export of the full system (allocated on first use)
+	bool haveSystem = false;
+	DevBuf<double> d_kfull, d_fE, d_S, d_smass, d_f;
+	DevBuf<int> d_sptr, d_sidx, d_srow, d_scol;
+
+	DevBody body() const
+	{
+		DevBody b;
+		b.N = N;
+		b.E = E;
+		b.n = n;
+		b.nb = nb;
+		b.nl = nl;
+		b.tets = d_tets.p;
+		b.rest = d_rest.p;
+		b.xrest = d_xrest.p;
+		b.brow = d_brow.p;
+		b.bcol = d_bcol.p;
+		b.lblk = d_lblk.p;
+		b.cptr = d_cptr.p;
+		b.cidx = d_cidx.p;
+		b.lmass = d_lmass.p;
+		b.iptr = d_iptr.p;
+		b.iidx = d_iidx.p;
+		b.nmass = d_nmass.p;
+		b.bc = d_bc.p;
+		return b;
+	}
+
+	Launch launch() const
+	{
+		Launch L;
+		L.stream = stream;
+		int g = (n + 255) / 256;
+		L.vecGrid = std::max(1, std::min(g, 152 * 8));
+		return L;
+	}
+
+	int blockPos(int I, int J) const
+	{
+		auto b = adj.begin() + adjPtr[I], e = adj.begin() + adjPtr[I + 1];
+		auto it = std::lower_bound(b, e, J);
+		return (it != e && *it == J) ? (int)(it - adj.begin()) : -1;
+	}
+	int64_t cscSlot(int r, int c) const
+	{
+		int I = r / 3, i = r % 3, J = c / 3, j = c % 3;
+		int pos = blockPos(J, I);  // position of I in adj(J)
+		if (pos < 0) return -1;
+		int deg = adjPtr[J + 1] - adjPtr[J];
+		return 9LL * adjPtr[J] + 3LL * j * deg + 3LL * (pos - adjPtr[J]) + i;
+	}
+
+	void release()
+	{
+		if (h_ctl) cudaFreeHost(h_ctl);
+		h_ctl = nullptr;
+		DevBuf<int4>* b4[] = {&d_tets, &d_lblk};
+		for (auto* b : b4) b->free();
+		DevBuf<double>* bd[] = {&d_rest, &d_xrest, &d_lmass, &d_nmass, &d_x, &d_v, &d_xt, &d_vt, &d_kslots,
+								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
+								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f};
+		for (auto* b : bd) b->free();
+		DevBuf<int>* bi[] = {&d_brow, &d_bcol, &d_cptr, &d_cidx, &d_iptr, &d_iidx, &d_counters, &d_idx,
+							 &d_sptr, &d_sidx, &d_srow, &d_scol};
+		for (auto* b : bi) b->free();
+		d_bc.free();
+		d_ctl.free();
+		if (stream) cudaStreamDestroy(stream);
+		stream = nullptr;
+	}
+};
+
+namespace {
+
+gbfem_status fail(gbfem_handle h, gbfem_status st, const std::string& msg)
+{
+	if (h)
+		h->err = msg;
+	else
+		g_lastCreateError = msg;
+	return st;
+}
+
+#define GB_CUDA(h, call)                                                                                 \
+	do                                                                                                   \
+	{                                                                                                    \
+		cudaError_t e_ = (call);                                                                         \
+		if (e_ != cudaSuccess)                                                                           \
+			return fail(h, e_ == cudaErrorMemoryAllocation ? GBFEM_OUT_OF_MEMORY : GBFEM_CUDA_ERROR,     \
+						std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+	} while (0)
+
+// Everything the step needs from the mesh, computed on the host once.
+gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
+{
+	const int N = m->num_nodes, E = m->num_tets;
+	h->N = N;
+	h->E = E;
+	h->n = 3 * N;
+	h->tets.assign(m->tets, m->tets + 4 * (size_t)E);
+	const double* X = m->rest_positions;
+
+	// Rest precompute (Fem3DElementTetrahedron.cpp:92-216; Fem3DElementCorotationalTetrahedron.cpp:57-72).
+	std::vector<double> rest((size_t)kRestFields * E);
+	h->cmass.resize(E);
+	std::vector<double> elemMass(E);
+	for (int e = 0; e < E; ++e)
+	{
+		const int* nd = &h->tets[4 * (size_t)e];
+		for (int a = 0; a < 4; ++a)
+			for (int b = a + 1; b < 4; ++b)
+				if (nd[a] == nd[b]) return fail(h, GBFEM_INVALID_ARG, "tet " + std::to_string(e) + " repeats a node");
+		double V[4][4], Vi[4][4];
+		for (int a = 0; a < 4; ++a)
+		{
+			for (int k = 0; k < 3; ++k) V[k][a] = X[3 * (size_t)nd[a] + k];
+			V[3][a] = 1.0;
+		}
+		if (!inverse44(V, Vi))
+			return fail(h, GBFEM_DEGENERATE_ELEMENT,
+						"tet " + std::to_string(e) + ": matrix V not invertible (degenerated tetrahedron)");
+		const double* p0 = X + 3 * (size_t)nd[0];
+		const double* p1 = X + 3 * (size_t)nd[1];
+		const double* p2 = X + 3 * (size_t)nd[2];
+		const double* p3 = X + 3 * (size_t)nd[3];
+		const double vol = (det3v(p1, p2, p3) - det3v(p0, p2, p3) + det3v(p0, p1, p3) - det3v(p0, p1, p2)) / 6.0;
+		const double Ey = m->young_modulus[e], nu = m->poisson_ratio[e], rho = m->mass_density[e];
+		const double lambda = Ey * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+		const double mu = Ey / (2.0 * (1 + nu));
+		for (int a = 0; a < 4; ++a)
+			for (int k = 0; k < 3; ++k) rest[(size_t)(3 * a + k) * E + e] = Vi[a][k];
+		rest[(size_t)12 * E + e] = vol;
+		rest[(size_t)13 * E + e] = lambda * vol;
+		rest[(size_t)14 * E + e] = mu * vol;
+		rest[(size_t)15 * E + e] = vol * rho / 20.0;
+		h->cmass[e] = vol * rho / 20.0;
+		elemMass[e] = vol * rho;  // FemElement::getMass
+	}
+	// Node adjacency (the union of element node blocks, FemRepresentation.cpp:121-132).
+	std::vector<int> cnt(N + 1, 0);
+	for (int e = 0; e < E; ++e)
+		for (int a = 0; a < 4; ++a) cnt[h->tets[4 * (size_t)e + a] + 1] += 4;
+	for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+	std::vector<int> raw(cnt[N]);
+	{
+		std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+		for (int e = 0; e < E; ++e)
+			for (int a = 0; a < 4; ++a)
+				for (int b = 0; b < 4; ++b) raw[fill[h->tets[4 * (size_t)e + a]]++] = h->tets[4 * (size_t)e + b];
+	}
+	h->adjPtr.assign(N + 1, 0);
+	h->adj.clear();
+	h->adj.reserve(raw.size() / 3 + N);
+	for (int i = 0; i < N; ++i)
+	{
+		auto b = raw.begin() + cnt[i], en = raw.begin() + cnt[i + 1];
+		std::sort(b, en);
+		auto last = std::unique(b, en);
+		if (b == last) h->adj.push_back(i);  // isolated node: keep its diagonal block
+		else h->adj.insert(h->adj.end(), b, last);
+		h->adjPtr[i + 1] = (int)h->adj.size();
+	}
+	h->nb = (int)h->adj.size();
+	h->nnz = 9LL * h->nb;
+	if (h->nnz > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "pattern exceeds int32 indices");
+	// Lower blocks (I >= J) in BSR order.
+	std::vector<int> lowerOfPos(h->nb, -1);
+	std::vector<int4> lblk;
+	lblk.reserve(h->nb / 2 + N);
+	for (int I = 0; I < N; ++I)
+		for (int k = h->adjPtr[I]; k < h->adjPtr[I + 1]; ++k)
+		{
+			int J = h->adj[k];
+			if (J > I) continue;
+			lowerOfPos[k] = (int)lblk.size();
+			lblk.push_back(make_int4(I, J, k, I == J ? -1 : h->blockPos(J, I)));
+		}
+	h->nl = (int)lblk.size();
+	// Element slot -> lower block contributions, element order inside each block.
+	std::vector<int> slotLower((size_t)E * kSlots);
+	std::vector<int> cptr(h->nl + 1, 0);
+	static const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+	for (int e = 0; e < E; ++e)
+	{
+		const int* nd = &h->tets[4 * (size_t)e];
+		for (int s = 0; s < kSlots; ++s)
+		{
+			int I, J;
+			if (s < 4)
+				I = J = nd[s];
+			else
+			{
+				I = std::max(nd[pa[s - 4]], nd[pb[s - 4]]);
+				J = std::min(nd[pa[s - 4]], nd[pb[s - 4]]);
+			}
+			int L = lowerOfPos[h->blockPos(I, J)];
+			slotLower[(size_t)e * kSlots + s] = L;
+			cptr[L + 1]++;
+		}
+	}
+	for (int L = 0; L < h->nl; ++L) cptr[L + 1] += cptr[L];
+	std::vector<int> cidx((size_t)E * kSlots);
+	std::vector<double> lmass(h->nl, 0.0);
+	{
+		std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+		for (int e = 0; e < E; ++e)
+			for (int s = 0; s < kSlots; ++s)
+			{
+				int L = slotLower[(size_t)e * kSlots + s];
+				cidx[fill[L]++] = e * kSlots + s;
+				lmass[L] += h->cmass[e] * (s < 4 ? 2.0 : 1.0);
+			}
+	}
+	// Node incidences and lumped node masses (FemRepresentation.cpp:102-117).
+	std::vector<int> iptr(N + 1, 0), iidx(4 * (size_t)E);
+	for (int e = 0; e < E; ++e)
+		for (int a = 0; a < 4; ++a) iptr[h->tets[4 * (size_t)e + a] + 1]++;
+	for (int i = 0; i < N; ++i) iptr[i + 1] += iptr[i];
+	std::vector<double> nmass(N, 0.0);
+	{
+		std::vector<int> fill(iptr.begin(), iptr.end() - 1);
+		for (int e = 0; e < E; ++e)
+			for (int a = 0; a < 4; ++a)
+			{
+				int I = h->tets[4 * (size_t)e + a];
+				iidx[fill[I]++] = 4 * e + a;
+				nmass[I] += elemMass[e] / 4;
+			}
+	}
+	h->bcMask.assign(h->n, 0);
+	for (int i = 0; i < m->num_bc_dofs; ++i) h->bcMask[m->bc_dofs[i]] = 1;
+
+	cudaStream_t s = h->stream;
+	GB_CUDA(h, h->d_tets.upload(reinterpret_cast<const int4*>(h->tets.data()), E, s));
+	GB_CUDA(h, h->d_rest.upload(rest.data(), rest.size(), s));
+	GB_CUDA(h, h->d_xrest.upload(X, h->n, s));
+	GB_CUDA(h, h->d_brow.upload(h->adjPtr.data(), N + 1, s));
+	GB_CUDA(h, h->d_bcol.upload(h->adj.data(), h->adj.size(), s));
+	GB_CUDA(h, h->d_lblk.upload(lblk.data(), lblk.size(), s));
+	GB_CUDA(h, h->d_cptr.upload(cptr.data(), cptr.size(), s));
+	GB_CUDA(h, h->d_cidx.upload(cidx.data(), cidx.size(), s));
+	GB_CUDA(h, h->d_lmass.upload(lmass.data(), lmass.size(), s));
+	GB_CUDA(h, h->d_iptr.upload(iptr.data(), iptr.size(), s));
+	GB_CUDA(h, h->d_iidx.upload(iidx.data(), iidx.size(), s));
+	GB_CUDA(h, h->d_nmass.upload(nmass.data(), nmass.size(), s));
+	GB_CUDA(h, h->d_bc.upload(h->bcMask.data(), h->bcMask.size(), s));
+	GB_CUDA(h, h->d_x.upload(X, h->n, s));
+	GB_CUDA(h, h->d_v.alloc(h->n));
+	GB_CUDA(h, cudaMemsetAsync(h->d_v.p, 0, sizeof(double) * h->n, s));
+	GB_CUDA(h, h->d_kslots.alloc((size_t)E * kSlots * 9));
+	GB_CUDA(h, h->d_rhsE.alloc((size_t)E * 12));
+	GB_CUDA(h, h->d_A.alloc((size_t)h->nb * 9));
+	const size_t nv = h->n;
+	for (DevBuf<double>* b : {&h->d_invdiag, &h->d_rhs, &h->d_dv, &h->d_r, &h->d_p, &h->d_q}) GB_CUDA(h, b->alloc(nv));
+	GB_CUDA(h, h->d_part.alloc(partial_slots(h->launch().vecGrid)));
+	GB_CUDA(h, h->d_counters.alloc(4));
+	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));
+	GB_CUDA(h, h->d_ctl.alloc(1));
+	GB_CUDA(h, cudaMemsetAsync(h->d_ctl.p, 0, sizeof(CgCtl), s));
+	GB_CUDA(h, cudaMallocHost(&h->h_ctl, sizeof(CgCtl)));
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	return GBFEM_OK;
+}
+
+// Lazily built maps for exporting the full (non-mirrored) system in CSC order.
+gbfem_status ensure_system_maps(gbfem_handle h)
+{
+	if (h->d_sptr.p) return GBFEM_OK;
+	const int E = h->E;
+	const int64_t nnz = h->nnz;
+	std::vector<int> slot((size_t)E * 144);
+	std::vector<int> sptr(nnz + 1, 0);
+	for (int e = 0; e < E; ++e)
+	{
+		const int* nd = &h->tets[4 * (size_t)e];
+		for (int a = 0; a < 4; ++a)
+			for (int i = 0; i < 3; ++i)
+				for (int b = 0; b < 4; ++b)
+					for (int j = 0; j < 3; ++j)
+					{
+						int64_t k = h->cscSlot(3 * nd[a] + i, 3 * nd[b] + j);
+						slot[(size_t)e * 144 + (3 * a + i) * 12 + 3 * b + j] = (int)k;
+						sptr[k + 1]++;
+					}
+	}
+	for (int64_t k = 0; k < nnz; ++k) sptr[k + 1] += sptr[k];
+	std::vector<int> sidx((size_t)E * 144), srow(nnz), scol(nnz);
+	std::vector<double> smass(nnz, 0.0);
+	std::vector<int> fill(sptr.begin(), sptr.end() - 1);
+	for (int e = 0; e < E; ++e)
+		for (int l = 0; l < 144; ++l)
+		{
+			int k = slot[(size_t)e * 144 + l];
+			sidx[fill[k]++] = e * 144 + l;
+			int a = l / 36, i = (l / 12) % 3, b = (l % 12) / 3, j = l % 3;
+			if (i == j) smass[k] += h->cmass[e] * (a == b ? 2.0 : 1.0);
+		}
+	for (int J = 0; J < h->N; ++J)
+		for (int j = 0; j < 3; ++j)
+		{
+			int c = 3 * J + j;
+			int deg = h->adjPtr[J + 1] - h->adjPtr[J];
+			int64_t k = 9LL * h->adjPtr[J] + 3LL * j * deg;
+			for (int t = h->adjPtr[J]; t < h->adjPtr[J + 1]; ++t)
+				for (int i = 0; i < 3; ++i, ++k)
+				{
+					srow[k] = 3 * h->adj[t] + i;
+					scol[k] = c;
+				}
+		}
+	cudaStream_t s = h->stream;
+	GB_CUDA(h, h->d_sptr.upload(sptr.data(), sptr.size(), s));
+	GB_CUDA(h, h->d_sidx.upload(sidx.data(), sidx.size(), s));
+	GB_CUDA(h, h->d_srow.upload(srow.data(), srow.size(), s));
+	GB_CUDA(h, h->d_scol.upload(scol.data(), scol.size(), s));
+	GB_CUDA(h, h->d_smass.upload(smass.data(), smass.size(), s));
+	GB_CUDA(h, h->d_kfull.alloc((size_t)E * 144));
+	GB_CUDA(h, h->d_fE.alloc((size_t)E * 12));
+	GB_CUDA(h, h->d_S.alloc(nnz));
+	GB_CUDA(h, h->d_f.alloc(h->n));
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	return GBFEM_OK;
+}
+
+struct PhaseTimer
+{
+	bool on = false;
+	cudaStream_t s = nullptr;
+	cudaEvent_t ev[5] = {};
+	void init(bool enable, cudaStream_t st)
+	{
+		on = enable;
+		s = st;
+		if (on)
+			for (auto& e : ev) cudaEventCreate(&e);
+	}
+	void mark(int i)
+	{
+		if (on) cudaEventRecord(ev[i], s);
+	}
+	float ms(int a, int b)
+	{
+		float t = 0;
+		if (on) cudaEventElapsedTime(&t, ev[a], ev[b]);
+		return t;
+	}
+	~PhaseTimer()
+	{
+		if (on)
+			for (auto& e : ev) cudaEventDestroy(e);
+	}
+};
+
+// Jacobi PCG on the handle's symmetric BSR matrix; the host polls the device control block
+// between chunks of iterations (kernels after convergence return immediately).
+gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter)
+{
+	const Launch L = h->launch();
+	MatBsr3 A{h->N, h->d_brow.p, h->d_bcol.p, h->d_A.p};
+	launch_cg_init(h->n, b, h->d_invdiag.p, x, h->d_r.p, h->d_p.p, h->d_ctl.p, h->d_part.p, h->prm.cg_tolerance,
+				   maxIter, L);
+	long long launched = 0;
+	int chunk = 4;
+	for (;;)
+	{
+		for (int k = 0; k < chunk; ++k)
+		{
+			launch_cg_spmv_bsr(A, h->d_p.p, h->d_q.p, h->d_ctl.p, h->d_part.p, L);
+			launch_cg_update(h->n, h->d_invdiag.p, h->d_p.p, h->d_q.p, x, h->d_r.p, h->d_ctl.p, h->d_part.p, L);
+			launch_cg_pupdate(h->n, h->d_invdiag.p, h->d_r.p, h->d_p.p, h->d_ctl.p, L);
+		}
+		launched += chunk;
+		GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl.p, sizeof(CgCtl), cudaMemcpyDeviceToHost, h->stream));
+		GB_CUDA(h, cudaStreamSynchronize(h->stream));
+		if (h->h_ctl->done) break;
+		if (launched > (long long)maxIter + 64) return fail(h, GBFEM_CUDA_ERROR, "CG control block did not finish");
+		chunk = std::min(chunk * 2, 32);
+	}
+	return GBFEM_OK;
+}
+
+gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
+{
+	const bool keep = (flags & GBFEM_STEP_KEEP_SYSTEM) != 0;
+	if (keep)
+	{
+		gbfem_status st = ensure_system_maps(h);
+		if (st != GBFEM_OK) return st;
+	}
+	const Launch L = h->launch();
+	cudaStream_t s = h->stream;
+	const DevBody body = h->body();
+	const int newtonMax = std::max(1, (int)h->prm.newton_max_iterations);
+	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * h->n;
+	const double c1 = 1.0 / dt + h->prm.rayleigh_mass;
+	const double c2 = dt + h->prm.rayleigh_stiffness;
+	double* xt = h->d_x.p;
+	double* vt = h->d_v.p;
+	if (newtonMax > 1)
+	{
+		if (!h->d_xt.p)
+		{
+			GB_CUDA(h, h->d_xt.alloc(h->n));
+			GB_CUDA(h, h->d_vt.alloc(h->n));
+			GB_CUDA(h, h->d_dvPrev.alloc(h->n));
+		}
+		GB_CUDA(h, cudaMemcpyAsync(h->d_xt.p, h->d_x.p, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, s));
+		GB_CUDA(h, cudaMemcpyAsync(h->d_vt.p, h->d_v.p, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, s));
+		GB_CUDA(h, cudaMemsetAsync(h->d_dvPrev.p, 0, sizeof(double) * h->n, s));
+		xt = h->d_xt.p;
+		vt = h->d_vt.p;
+	}
+	PhaseTimer tm;
+	tm.init((flags & GBFEM_STEP_TIME_PHASES) != 0, s);
+	for (int it = 0; it < newtonMax; ++it)
+	{
+		tm.mark(0);
+		launch_element_fp64(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
+							h->d_kslots.p, h->d_rhsE.p, keep ? h->d_kfull.p : nullptr, keep ? h->d_fE.p : nullptr,
+							h->d_counters.p, s);
+		tm.mark(1);
+		launch_assemble_bsr(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+		launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+		if (keep)
+		{
+			launch_assemble_full_csc((int)h->nnz, h->d_sptr.p, h->d_sidx.p, h->d_srow.p, h->d_scol.p, h->d_kfull.p,
+									 h->d_smass.p, h->d_bc.p, c1, c2, h->d_S.p, s);
+			launch_rhs_gather(body, h->d_fE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_f.p, 0, s);
+		}
+		tm.mark(2);
+		GB_CUDA(h, cudaGetLastError());
+		gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter);
+		if (st != GBFEM_OK) return st;
+		tm.mark(3);
+		h->stats.cg_iterations += h->h_ctl->iter;
+		h->stats.cg_relative_residual = h->h_ctl->bb > 0 ? std::sqrt(h->h_ctl->rr / h->h_ctl->bb) : 0.0;
+		if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
+		launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, xt, h->d_x.p, h->d_v.p, dt, newtonMax > 1, h->d_ctl.p,
+							h->d_part.p, L);
+		tm.mark(4);
+		if (tm.on)
+		{
+			GB_CUDA(h, cudaStreamSynchronize(s));
+			h->stats.ms_element += tm.ms(0, 1);
+			h->stats.ms_assemble += tm.ms(1, 2);
+			h->stats.ms_solve += tm.ms(2, 3);
+			h->stats.ms_update += tm.ms(3, 4);
+		}
+		if (newtonMax > 1)
+		{
+			GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl.p, sizeof(CgCtl), cudaMemcpyDeviceToHost, s));
+			GB_CUDA(h, cudaStreamSynchronize(s));
+			if (h->h_ctl->newtonVar < h->prm.newton_epsilon) break;  // OdeSolverEulerImplicit.cpp:101-112
+		}
+	}
+	h->haveSystem = keep;
+	launch_validity(h->n, h->d_x.p, h->d_v.p, h->d_ctl.p, h->d_part.p, L);
+	GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl.p, sizeof(CgCtl), cudaMemcpyDeviceToHost, s));
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	GB_CUDA(h, cudaGetLastError());
+	h->stats.steps++;
+	if (h->h_ctl->nonfinite)
+	{
+		h->active = false;  // FemRepresentation.cpp:285-293
+		return fail(h, GBFEM_NONFINITE, "state is not finite; representation deactivated");
+	}
+	return GBFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbfem_status gbfem_params_default(gbfem_params* out)
+{
+	if (!out) return GBFEM_INVALID_ARG;
+	std::memset(out, 0, sizeof(*out));
+	out->rayleigh_mass = 0.0;
+	out->rayleigh_stiffness = 0.0;
+	out->gravity[0] = 0.0;
+	out->gravity[1] = -9.81;
+	out->gravity[2] = 0.0;
+	out->gravity_enabled = 1;
+	out->newton_max_iterations = 1;
+	out->newton_epsilon = 1e-5;
+	out->cg_tolerance = DBL_EPSILON;
+	out->cg_max_iterations = 0;
+	out->precision = GBFEM_PRECISION_FP64;
+	out->device = 0;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_create(const gbfem_mesh_desc* m, const gbfem_params* prm, gbfem_handle* out)
+{
+	if (!out) return fail(nullptr, GBFEM_INVALID_ARG, "out is NULL");
+	*out = nullptr;
+	if (!m || !prm) return fail(nullptr, GBFEM_INVALID_ARG, "mesh or params is NULL");
+	if (m->num_nodes <= 0 || m->num_tets <= 0 || !m->rest_positions || !m->tets || !m->young_modulus ||
+		!m->poisson_ratio || !m->mass_density || (m->num_bc_dofs > 0 && !m->bc_dofs) || m->num_bc_dofs < 0)
+		return fail(nullptr, GBFEM_INVALID_ARG, "empty mesh or missing arrays");
+	if (m->num_nodes > INT32_MAX / 3) return fail(nullptr, GBFEM_INVALID_ARG, "too many nodes");
+	for (int64_t i = 0; i < 4LL * m->num_tets; ++i)
+		if (m->tets[i] < 0 || m->tets[i] >= m->num_nodes)
+			return fail(nullptr, GBFEM_INVALID_ARG, "Invalid nodeId " + std::to_string(m->tets[i]));
+	for (int32_t e = 0; e < m->num_tets; ++e)
+	{
+		// FemElement::initialize material checks (FemElement.cpp:33-43).
+		const double rho = m->mass_density[e], nu = m->poisson_ratio[e], Ey = m->young_modulus[e];
+		if (!(rho > 0.0) || !(nu > 0.0 && nu < 0.5) || !(Ey > 0.0))
+			return fail(nullptr, GBFEM_INVALID_ARG, "invalid material on tet " + std::to_string(e));
+	}
+	for (int32_t i = 0; i < m->num_bc_dofs; ++i)
+		if (m->bc_dofs[i] < 0 || m->bc_dofs[i] >= 3 * m->num_nodes)
+			return fail(nullptr, GBFEM_INVALID_ARG, "Invalid boundary condition dof " + std::to_string(m->bc_dofs[i]));
+	if (!(prm->newton_max_iterations >= 1) || !(prm->newton_epsilon >= 0.0) || !(prm->cg_tolerance >= 0.0) ||
+		prm->precision < 0 || prm->precision > 1)
+		return fail(nullptr, GBFEM_INVALID_ARG, "invalid solver parameters");
+	auto* h = new gbfem_handle_s();
+	h->prm = *prm;
+	h->device = prm->device;
+	cudaError_t ce = cudaSetDevice(h->device);
+	if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+	if (ce != cudaSuccess)
+	{
+		std::string msg = std::string("CUDA unavailable: ") + cudaGetErrorString(ce);
+		delete h;
+		return fail(nullptr, GBFEM_CUDA_ERROR, msg);
+	}
+	gbfem_status st = build_body(h, m);
+	if (st != GBFEM_OK)
+	{
+		g_lastCreateError = h->err;
+		h->release();
+		delete h;
+		return st;
+	}
+	h->stats.active = 1;
+	*out = h;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_destroy(gbfem_handle h)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	cudaSetDevice(h->device);
+	if (h->stream) cudaStreamSynchronize(h->stream);
+	h->release();
+	delete h;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flags)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (!(dt > 0.0) || nsteps < 0) return fail(h, GBFEM_INVALID_ARG, "dt must be > 0 and nsteps >= 0");
+	std::memset(&h->stats, 0, sizeof(h->stats));
+	if (!h->active)
+	{
+		h->stats.active = 0;
+		return fail(h, GBFEM_INACTIVE, "representation is deactivated");
+	}
+	GB_CUDA(h, cudaSetDevice(h->device));
+	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), h->stream));
+	gbfem_status result = GBFEM_OK;
+	for (int sidx = 0; sidx < nsteps; ++sidx)
+	{
+		gbfem_status st = step_once(h, dt, flags);
+		if (st == GBFEM_NONFINITE || st == GBFEM_CUDA_ERROR || st == GBFEM_OUT_OF_MEMORY)
+		{
+			result = st;
+			break;
+		}
+	}
+	int counters[4] = {0, 0, 0, 0};
+	cudaMemcpy(counters, h->d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost);
+	h->stats.singular_g = counters[0];
+	h->stats.polar_fallbacks = counters[1];
+	h->stats.active = h->active ? 1 : 0;
+	if (result == GBFEM_OK && h->stats.cg_max_iterations_hit > 0)
+	{
+		h->err = "CG reached its maximum number of iterations";
+		result = GBFEM_CG_MAXITER;
+	}
+	return result;
+}
+
+gbfem_status gbfem_get_stats(gbfem_handle h, gbfem_stats* out)
+{
+	if (!h || !out) return GBFEM_INVALID_ARG;
+	*out = h->stats;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_get_state(gbfem_handle h, double* x, double* v)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	GB_CUDA(h, cudaSetDevice(h->device));
+	if (x) GB_CUDA(h, cudaMemcpyAsync(x, h->d_x.p, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->stream));
+	if (v) GB_CUDA(h, cudaMemcpyAsync(v, h->d_v.p, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->stream));
+	GB_CUDA(h, cudaStreamSynchronize(h->stream));
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_set_state(gbfem_handle h, const double* x, const double* v)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	GB_CUDA(h, cudaSetDevice(h->device));
+	if (x) GB_CUDA(h, cudaMemcpyAsync(h->d_x.p, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->stream));
+	if (v) GB_CUDA(h, cudaMemcpyAsync(h->d_v.p, v, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->stream));
+	GB_CUDA(h, cudaStreamSynchronize(h->stream));
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_set_velocities(gbfem_handle h, int32_t count, const int32_t* dofs, const double* values)
+{
+	if (!h || count < 0 || (count > 0 && (!dofs || !values))) return GBFEM_INVALID_ARG;
+	for (int32_t i = 0; i < count; ++i)
+		if (dofs[i] < 0 || dofs[i] >= h->n) return fail(h, GBFEM_INVALID_ARG, "dof out of range");
+	if (count == 0) return GBFEM_OK;
+	GB_CUDA(h, cudaSetDevice(h->device));
+	if (h->d_idx.n < (size_t)count)
+	{
+		GB_CUDA(h, h->d_idx.alloc(count));
+		GB_CUDA(h, h->d_vals.alloc(count));
+	}
+	GB_CUDA(h, cudaMemcpyAsync(h->d_idx.p, dofs, sizeof(int) * count, cudaMemcpyHostToDevice, h->stream));
+	GB_CUDA(h, cudaMemcpyAsync(h->d_vals.p, values, sizeof(double) * count, cudaMemcpyHostToDevice, h->stream));
+	launch_scatter_values(count, h->d_idx.p, h->d_vals.p, h->d_v.p, h->stream);
+	GB_CUDA(h, cudaStreamSynchronize(h->stream));
+	GB_CUDA(h, cudaGetLastError());
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (x) *x = h->d_x.p;
+	if (v) *v = h->d_v.p;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_stream(gbfem_handle h, void** stream)
+{
+	if (!h || !stream) return GBFEM_INVALID_ARG;
+	*stream = (void*)h->stream;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_reactivate(gbfem_handle h)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	h->active = true;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_get_sizes(gbfem_handle h, int64_t* num_dofs, int64_t* nnz)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (num_dofs) *num_dofs = h->n;
+	if (nnz) *nnz = h->nnz;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_get_pattern(gbfem_handle h, int32_t* colptr, int32_t* rowidx)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (colptr)
+	{
+		colptr[0] = 0;
+		for (int J = 0; J < h->N; ++J)
+		{
+			int deg = h->adjPtr[J + 1] - h->adjPtr[J];
+			for (int j = 0; j < 3; ++j) colptr[3 * J + j + 1] = (int32_t)(9LL * h->adjPtr[J] + 3LL * (j + 1) * deg);
+		}
+	}
+	if (rowidx)
+	{
+		int64_t k = 0;
+		for (int J = 0; J < h->N; ++J)
+			for (int j = 0; j < 3; ++j)
+				for (int t = h->adjPtr[J]; t < h->adjPtr[J + 1]; ++t)
+					for (int i = 0; i < 3; ++i) rowidx[k++] = 3 * h->adj[t] + i;
+	}
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_get_scatter(gbfem_handle h, int32_t* map)
+{
+	if (!h || !map) return GBFEM_INVALID_ARG;
+	for (int e = 0; e < h->E; ++e)
+	{
+		const int* nd = &h->tets[4 * (size_t)e];
+		for (int a = 0; a < 4; ++a)
+			for (int b = 0; b < 4; ++b)
+				for (int j = 0; j < 3; ++j)
+				{
+					int64_t first = h->cscSlot(3 * nd[a], 3 * nd[b] + j);
+					for (int i = 0; i < 3; ++i) map[(size_t)e * 144 + (3 * a + i) * 12 + 3 * b + j] = (int32_t)(first + i);
+				}
+	}
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_get_system(gbfem_handle h, double* S, double* rhs, double* f)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (!h->haveSystem) return fail(h, GBFEM_INVALID_ARG, "no system kept: step with GBFEM_STEP_KEEP_SYSTEM first");
+	GB_CUDA(h, cudaSetDevice(h->device));
+	if (S) GB_CUDA(h, cudaMemcpyAsync(S, h->d_S.p, sizeof(double) * h->nnz, cudaMemcpyDeviceToHost, h->stream));
+	if (rhs) GB_CUDA(h, cudaMemcpyAsync(rhs, h->d_rhs.p, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->stream));
+	if (f) GB_CUDA(h, cudaMemcpyAsync(f, h->d_f.p, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->stream));
+	GB_CUDA(h, cudaStreamSynchronize(h->stream));
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_last_error(gbfem_handle h, char* buf, size_t len)
+{
+	if (!buf || len == 0) return GBFEM_INVALID_ARG;
+	const std::string& s = h ? h->err : g_lastCreateError;
+	std::snprintf(buf, len, "%s", s.c_str());
+	return GBFEM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// LinearSparseSolveAndInverseCG on a caller matrix.
+// ------------------------------------------------------------------------------------------
+struct gbfem_cg_s
+{
+	int device = 0, n = 0;
+	double tol = DBL_EPSILON;
+	int maxIter = 0;
+	cudaStream_t stream = nullptr;
+	DevBuf<int> rowptr, col;
+	DevBuf<double> val, invdiag, b, x, r, p, q, part;
+	DevBuf<CgCtl> ctl;
+	CgCtl* h_ctl = nullptr;
+	void release()
+	{
+		rowptr.free();
+		col.free();
+		for (auto* d : {&val, &invdiag, &b, &x, &r, &p, &q, &part}) d->free();
+		ctl.free();
+		if (h_ctl) cudaFreeHost(h_ctl);
+		h_ctl = nullptr;
+		if (stream) cudaStreamDestroy(stream);
+		stream = nullptr;
+	}
+};
+
+extern "C" {
+
+gbfem_status gbfem_cg_create(int32_t n, const int32_t* colptr, const int32_t* rowidx, const double* values,
+							 int32_t device, gbfem_cg* out)
+{
+	if (!out || n <= 0 || !colptr || !rowidx || !values) return fail(nullptr, GBFEM_INVALID_ARG, "bad CG matrix");
+	*out = nullptr;
+	if (colptr[0] != 0) return fail(nullptr, GBFEM_INVALID_ARG, "colptr[0] must be 0");
+	for (int c = 0; c < n; ++c)
+		if (colptr[c + 1] < colptr[c]) return fail(nullptr, GBFEM_INVALID_ARG, "colptr not monotone");
+	for (int64_t k = 0; k < colptr[n]; ++k)
+		if (rowidx[k] < 0 || rowidx[k] >= n) return fail(nullptr, GBFEM_INVALID_ARG, "row index out of range");
+	// Symmetric CSR from the lower triangle (row >= col) of the CSC matrix.
+	std::vector<int> cnt(n + 1, 0);
+	std::vector<double> invd(n, 1.0);
+	for (int c = 0; c < n; ++c)
+		for (int k = colptr[c]; k < colptr[c + 1]; ++k)
+		{
+			int r = rowidx[k];
+			if (r < c) continue;
+			cnt[r + 1]++;
+			if (r != c) cnt[c + 1]++;
+			if (r == c && values[k] != 0.0) invd[r] = 1.0 / values[k];
+		}
+	for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+	std::vector<std::pair<int, double>> ent(cnt[n]);
+	{
+		std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+		for (int c = 0; c < n; ++c)
+			for (int k = colptr[c]; k < colptr[c + 1]; ++k)
+			{
+				int r = rowidx[k];
+				if (r < c) continue;
+				ent[fill[r]++] = {c, values[k]};
+				if (r != c) ent[fill[c]++] = {r, values[k]};
+			}
+	}
+	std::vector<int> colv(ent.size());
+	std::vector<double> valv(ent.size());
+	for (int i = 0; i < n; ++i)
+	{
+		std::sort(ent.begin() + cnt[i], ent.begin() + cnt[i + 1],
+				  [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
+		for (int k = cnt[i]; k < cnt[i + 1]; ++k)
+		{
+			colv[k] = ent[k].first;
+			valv[k] = ent[k].second;
+		}
+	}
+	auto* g = new gbfem_cg_s();
+	g->device = device;
+	g->n = n;
+	auto bad = [&](cudaError_t e) {
+		std::string msg = std::string("CUDA: ") + cudaGetErrorString(e);
+		g->release();
+		delete g;
+		return fail(nullptr, e == cudaErrorMemoryAllocation ? GBFEM_OUT_OF_MEMORY : GBFEM_CUDA_ERROR, msg);
+	};
+	cudaError_t e = cudaSetDevice(device);
+	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess) e = g->rowptr.upload(cnt.data(), n + 1, g->stream);
+	if (e == cudaSuccess) e = g->col.upload(colv.data(), colv.size(), g->stream);
+	if (e == cudaSuccess) e = g->val.upload(valv.data(), valv.size(), g->stream);
+	if (e == cudaSuccess) e = g->invdiag.upload(invd.data(), n, g->stream);
+	for (auto* d : {&g->b, &g->x, &g->r, &g->p, &g->q})
+		if (e == cudaSuccess) e = d->alloc(n);
+	int grid = std::max(1, std::min((n + 255) / 256, 152 * 8));
+	if (e == cudaSuccess) e = g->part.alloc(partial_slots(grid));
+	if (e == cudaSuccess) e = g->ctl.alloc(1);
+	if (e == cudaSuccess) e = cudaMemsetAsync(g->ctl.p, 0, sizeof(CgCtl), g->stream);
+	if (e == cudaSuccess) e = cudaMallocHost(&g->h_ctl, sizeof(CgCtl));
+	if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+	if (e != cudaSuccess) return bad(e);
+	*out = g;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_cg_set_tolerance(gbfem_cg cg, double tolerance)
+{
+	if (!cg || !(tolerance >= 0.0)) return GBFEM_INVALID_ARG;
+	cg->tol = tolerance;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_cg_set_max_iterations(gbfem_cg cg, int32_t max_iterations)
+{
+	if (!cg) return GBFEM_INVALID_ARG;
+	cg->maxIter = max_iterations;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_cg_solve(gbfem_cg cg, const double* b, double* x, int32_t* iterations, double* relative_residual)
+{
+	if (!cg || !b || !x) return GBFEM_INVALID_ARG;
+	auto cuda = [](cudaError_t e) { return e == cudaSuccess; };
+	if (!cuda(cudaSetDevice(cg->device))) return GBFEM_CUDA_ERROR;
+	Launch L;
+	L.stream = cg->stream;
+	L.vecGrid = std::max(1, std::min((cg->n + 255) / 256, 152 * 8));
+	const int maxIter = cg->maxIter > 0 ? cg->maxIter : 2 * cg->n;
+	if (!cuda(cudaMemcpyAsync(cg->b.p, b, sizeof(double) * cg->n, cudaMemcpyHostToDevice, cg->stream)))
+		return GBFEM_CUDA_ERROR;
+	MatCsr A{cg->n, cg->rowptr.p, cg->col.p, cg->val.p};
+	launch_cg_init(cg->n, cg->b.p, cg->invdiag.p, cg->x.p, cg->r.p, cg->p.p, cg->ctl.p, cg->part.p, cg->tol, maxIter, L);
+	long long launched = 0;
+	int chunk = 4;
+	for (;;)
+	{
+		for (int k = 0; k < chunk; ++k)
+		{
+			launch_cg_spmv_csr(A, cg->p.p, cg->q.p, cg->ctl.p, cg->part.p, L);
+			launch_cg_update(cg->n, cg->invdiag.p, cg->p.p, cg->q.p, cg->x.p, cg->r.p, cg->ctl.p, cg->part.p, L);
+			launch_cg_pupdate(cg->n, cg->invdiag.p, cg->r.p, cg->p.p, cg->ctl.p, L);
+		}
+		launched += chunk;
+		if (!cuda(cudaMemcpyAsync(cg->h_ctl, cg->ctl.p, sizeof(CgCtl), cudaMemcpyDeviceToHost, cg->stream)) ||
+			!cuda(cudaStreamSynchronize(cg->stream)))
+			return GBFEM_CUDA_ERROR;
+		if (cg->h_ctl->done) break;
+		if (launched > (long long)maxIter + 64) return GBFEM_CUDA_ERROR;
+		chunk = std::min(chunk * 2, 32);
+	}
+	if (!cuda(cudaMemcpyAsync(x, cg->x.p, sizeof(double) * cg->n, cudaMemcpyDeviceToHost, cg->stream)) ||
+		!cuda(cudaStreamSynchronize(cg->stream)) || !cuda(cudaGetLastError()))
+		return GBFEM_CUDA_ERROR;
+	if (iterations) *iterations = cg->h_ctl->iter;
+	if (relative_residual) *relative_residual = cg->h_ctl->bb > 0 ? std::sqrt(cg->h_ctl->rr / cg->h_ctl->bb) : 0.0;
+	return cg->h_ctl->converged ? GBFEM_OK : GBFEM_CG_MAXITER;
+}
+
+gbfem_status gbfem_cg_destroy(gbfem_cg cg)
+{
+	if (!cg) return GBFEM_INVALID_ARG;
+	cudaSetDevice(cg->device);
+	cg->release();
+	delete cg;
+	return GBFEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+// gbfem_internal.h -- shared declarations of the gbfem host code and kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbfem {
+
+// Per-element rest data, structure of arrays: kRest[k * E + e].
+//   k = 0..11  shape-function gradients g_a (a = 0..3, 3 components each) = rows of V^-1
+//   k = 12     rest volume V
+//   k = 13     lambda * V
+//   k = 14     mu * V
+//   k = 15     consistent-mass coefficient rho * V / 20
+constexpr int kRestFields = 16;
+// Lower-triangle blocks an element writes: 4 diagonal blocks then the 6 node pairs
+// (0,1),(0,2),(0,3),(1,2),(1,3),(2,3), each stored with the larger global node id as its row.
+constexpr int kSlots = 10;
+
+// Device view of one body.
+struct DevBody
+{
+	int N = 0, E = 0, n = 0;        // nodes, tets, dofs
+	int nb = 0, nl = 0;             // BSR blocks (full, symmetric) and lower blocks
+	const int4* tets = nullptr;
+	const double* rest = nullptr;   // kRestFields * E
+	const double* xrest = nullptr;  // 3N
+	const int* brow = nullptr;      // N+1, BSR row pointer
+	const int* bcol = nullptr;      // nb
+	const int4* lblk = nullptr;     // nl: {I, J, pos(I,J), pos(J,I) or -1}
+	const int* cptr = nullptr;      // nl+1
+	const int* cidx = nullptr;      // E*kSlots: e*kSlots + slot, element order inside a lower block
+	const double* lmass = nullptr;  // nl: consistent-mass coefficient of the lower block
+	const int* iptr = nullptr;      // N+1 node incidences
+	const int* iidx = nullptr;      // 4E: e*4 + a, element order
+	const double* nmass = nullptr;  // N lumped node mass (gravity)
+	const uint8_t* bc = nullptr;    // n boundary-condition mask
+};
+
+// Device control block of one CG solve; all scalars live on the device.
+struct CgCtl
+{
+	double bb, rz, pq, rr, threshold, alpha, beta, pad0;
+	int iter, done, converged, maxIter;
+	unsigned int ticket[4];
+	double newtonVar;   // max |dv - dv_prev| of the last Newton iteration
+	double sumX, sumV;  // OdeState::isValid sums
+	int nonfinite, pad1;
+};
+
+struct Launch
+{
+	int vecGrid = 0;   // blocks of 256 threads for the dof-wise kernels
+	cudaStream_t stream = nullptr;
+};
+
+// ---- element / assembly (FP64 plain form)
+void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
+						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
+						 double* fE, int* counters, cudaStream_t s);
+void launch_assemble_bsr(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
+						 cudaStream_t s);
+void launch_rhs_gather(const DevBody& b, const double* rhsE, const double* gravity, int gravityOn, double* rhs,
+					   int applyBc, cudaStream_t s);
+// Full (non-mirrored) system for export: CSC slots gather from full element matrices.
+void launch_assemble_full_csc(int nnz, const int* sptr, const int* sidx, const int* srow, const int* scol,
+							  const double* kfull, const double* smass, const uint8_t* bc, double c1, double c2,
+							  double* S, cudaStream_t s);
+
+// ---- CG on the mirrored symmetric matrix
+struct MatBsr3
+{
+	int rows;            // block rows
+	const int* brow;
+	const int* bcol;
+	const double* val;   // 9 per block, row-major
+};
+struct MatCsr
+{
+	int rows;
+	const int* rowptr;
+	const int* col;
+	const double* val;
+};
+void launch_cg_init(int n, const double* b, const double* invdiag, double* x, double* r, double* p, CgCtl* ctl,
+					double* part, double tol, int maxIter, const Launch& L);
+void launch_cg_spmv_bsr(const MatBsr3& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L);
+void launch_cg_spmv_csr(const MatCsr& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L);
+void launch_cg_update(int n, const double* invdiag, const double* p, const double* q, double* x, double* r,
+					  CgCtl* ctl, double* part, const Launch& L);
+void launch_cg_pupdate(int n, const double* invdiag, const double* r, double* p, CgCtl* ctl, const Launch& L);
+
+// ---- state
+void launch_state_update(int n, const double* dv, double* dvPrev, const double* xt, double* xn, double* vn,
+						 double dt, int trackNewton, CgCtl* ctl, double* part, const Launch& L);
+void launch_validity(int n, const double* x, const double* v, CgCtl* ctl, double* part, const Launch& L);
+void launch_scatter_values(int count, const int* idx, const double* vals, double* dst, cudaStream_t s);
+
+// Partial-sum buffer size needed by the reductions for a given vecGrid.
+inline int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }
+
+}  // namespace gbfem

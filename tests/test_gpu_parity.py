@@ -1,0 +1,132 @@
+"""GPU parity against the CPU oracle (restatement of the reference step), through the C ABI."""
+
+import numpy as np
+import pytest
+
+from opensurgsim_gb300 import _lib, mesh
+from opensurgsim_gb300.body import Body, CgSolver
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    d = np.linalg.norm(a - b)
+    n = np.linalg.norm(b)
+    return d / n if n > 0 else d
+
+
+def pair(scene, **kw):
+    return Body.from_scene(scene, **kw), O.OracleModel.from_scene(scene, **kw)
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 3, 4), (10, 10, 10)])
+def test_pattern_and_scatter_bit_exact(gpu_lib, dims):
+    s = mesh.scene_cube(*dims)
+    g, o = pair(s)
+    assert g.nnz == o.nnz
+    gc, gr = g.pattern()
+    oc, orr = o.pattern()
+    assert np.array_equal(gc, oc) and np.array_equal(gr, orr)
+    assert np.array_equal(g.scatter(), o.scatter())
+
+
+def test_first_step_system_matches_oracle(gpu_lib):
+    s = mesh.scene_cube(4, 3, 5)
+    g, o = pair(s)
+    # a deformed, moving start state so that rotations, damping and the dR/dx terms are exercised
+    rng = np.random.default_rng(5)
+    x0, _ = o.state()
+    x = x0 + rng.normal(0, 2e-4, x0.shape)
+    v = rng.normal(0, 1e-2, x0.shape)
+    for m in (g, o):
+        m.set_state(x, v)
+    assert g.step(1e-3, 1, _lib.STEP_KEEP_SYSTEM) == _lib.GBFEM_OK
+    assert o.step(1e-3, 1) == 0
+    gs, os_ = g.system(), o.system()
+    eS = np.abs(gs["S"] - os_["S"]).max() / np.abs(os_["S"]).max()
+    erhs = rel(gs["rhs"], os_["rhs"])
+    ef = rel(gs["f"], os_["f"])
+    print(f"S {eS:.3e} rhs {erhs:.3e} f {ef:.3e}")
+    assert eS < 1e-12
+    assert erhs < 1e-10
+    assert ef < 1e-10
+    gx, gv = g.state()
+    ox, ov = o.state()
+    assert rel(gx - x, ox - x) < 1e-8
+    assert rel(gv, ov) < 1e-8
+
+
+def test_cube_100_steps_displacement(gpu_lib):
+    s = mesh.scene_cube(10, 10, 10)
+    g, o = pair(s)
+    x0, _ = o.state()
+    errs = []
+    for k in range(10):
+        assert g.step(s.dt, 10) == _lib.GBFEM_OK
+        assert o.step(s.dt, 10) == 0
+        gx, _ = g.state()
+        ox, _ = o.state()
+        errs.append(rel(gx - x0, ox - x0))
+    print("rel disp err per 10 steps", ["%.2e" % e for e in errs])
+    assert max(errs) < 1e-8
+
+
+def test_bc_dofs_fixed_and_deterministic(gpu_lib):
+    s = mesh.scene_cube(3, 3, 3)
+    a = Body.from_scene(s)
+    b = Body.from_scene(s)
+    a.step(1e-3, 20)
+    b.step(1e-3, 20)
+    xa, va = a.state()
+    xb, vb = b.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    bc = s.mesh.bc_dofs
+    assert np.array_equal(xa[bc], s.mesh.nodes.ravel()[bc])
+    assert np.all(va[bc] == 0)
+
+
+def test_nonfinite_state_deactivates(gpu_lib):
+    s = mesh.scene_cube(2, 2, 2)
+    g = Body.from_scene(s)
+    x, v = g.state()
+    v[5] = np.nan
+    g.set_state(x, v)
+    assert g.step(1e-3, 1) == _lib.GBFEM_NONFINITE
+    assert g.stats()["active"] == 0
+    assert g.step(1e-3, 1) == _lib.GBFEM_INACTIVE
+
+
+def _cg_matrix(n=18):
+    # LinearSparseSolveAndInverseTests.cpp:57-88: dense-filled 18x18, fmod(10.3 cos(r c) + 3.24, 10),
+    # rhs fmod(-4.1 r^2 + 3.46, 5).
+    r, c = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    A = np.fmod(10.3 * np.cos((r * c).astype(float)) + 3.24, 10.0)
+    b = np.fmod(-4.1 * np.arange(n) ** 2 + 3.46, 5.0)
+    colptr = np.arange(0, n * n + 1, n, dtype=np.int32)
+    rowidx = np.tile(np.arange(n, dtype=np.int32), n)
+    vals = A.T.ravel().copy()  # column-major
+    return A, b, colptr, rowidx, vals
+
+
+def test_cg_max_iterations_behaviour(gpu_lib):
+    A, b, colptr, rowidx, vals = _cg_matrix()
+    expected = np.linalg.solve(A, b)
+
+    def approx(x, y, prec):  # Eigen isApprox
+        return np.linalg.norm(x - y) <= prec * min(np.linalg.norm(x), np.linalg.norm(y))
+
+    cg = CgSolver(colptr, rowidx, vals)
+    x, it, res, st = cg.solve(b)
+    assert approx(x, expected, 1e-5)
+    cg.set_tolerance(1e-10)
+    cg.set_max_iterations(18)
+    x, it, res, st = cg.solve(b)
+    assert approx(x, expected, 1e-5) and not approx(x, expected, 1e-10)
+    assert st == _lib.GBFEM_CG_MAXITER
+    cg.set_max_iterations(50)
+    x, it, res, st = cg.solve(b)
+    assert approx(x, expected, 1e-10)
+    ox, oit, ores, ost = O.cg_solve(colptr, rowidx, vals, b, tol=1e-10, max_iter=50)
+    assert oit == it
+    assert np.linalg.norm(x - ox) <= 1e-9 * np.linalg.norm(ox)
