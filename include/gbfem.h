@@ -99,12 +99,17 @@ typedef struct gbfem_stats
 	int32_t singular_g;             /* element updates that hit the singular-G early return */
 	int32_t polar_fallbacks;        /* element updates that took the SVD polar path */
 	int32_t active;
-	int32_t reserved[5];
+	int32_t kernel_launches;        /* kernels this call launched */
+	int32_t spmv_timed;             /* CG matrix-vector launches timed (GBFEM_STEP_TIME_KERNELS) */
+	int32_t reserved0;
+	double ms_spmv;                 /* summed device time of those launches (CUDA events) */
+	double reserved[2];
 } gbfem_stats;
 
 /* Flags for gbfem_step. */
 #define GBFEM_STEP_TIME_PHASES 1u   /* record per-phase device times (adds events) */
 #define GBFEM_STEP_KEEP_SYSTEM 2u   /* keep the full S / rhs / f of the last solve for export */
+#define GBFEM_STEP_TIME_KERNELS 4u  /* time every CG matrix-vector launch with CUDA events */
 
 GBFEM_API gbfem_status gbfem_params_default(gbfem_params* out);
 
@@ -126,6 +131,9 @@ GBFEM_API gbfem_status gbfem_set_state(gbfem_handle h, const double* x, const do
 /* v[dofs[i]] = values[i]: prescribe the velocity of (boundary-condition) dofs before a step. */
 GBFEM_API gbfem_status gbfem_set_velocities(gbfem_handle h, int32_t count, const int32_t* dofs,
 											const double* values);
+/* Same with dofs and values already in device memory of the handle's GPU (no host copy). */
+GBFEM_API gbfem_status gbfem_set_velocities_device(gbfem_handle h, int32_t count, const int32_t* dofs_dev,
+												   const double* values_dev);
 /* Device pointers of the state (FP64, 3*num_nodes each), valid until gbfem_destroy. */
 GBFEM_API gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v);
 /* The CUDA stream the handle launches on (a cudaStream_t). */

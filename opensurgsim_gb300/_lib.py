@@ -27,11 +27,12 @@ PRECISION_MIXED = 1
 
 STEP_TIME_PHASES = 1
 STEP_KEEP_SYSTEM = 2
+STEP_TIME_KERNELS = 4
 
 # Every symbol the header declares; the CPU tests check the library exports all of them.
 EXPORTED = [
     "gbfem_params_default", "gbfem_create", "gbfem_destroy", "gbfem_step", "gbfem_get_stats", "gbfem_get_state",
-    "gbfem_set_state", "gbfem_set_velocities", "gbfem_device_state", "gbfem_stream", "gbfem_reactivate",
+    "gbfem_set_state", "gbfem_set_velocities", "gbfem_set_velocities_device", "gbfem_device_state", "gbfem_stream", "gbfem_reactivate",
     "gbfem_get_sizes", "gbfem_get_pattern", "gbfem_get_scatter", "gbfem_get_system", "gbfem_last_error",
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
     "gbfem_cg_destroy",
@@ -82,11 +83,15 @@ class Stats(ctypes.Structure):
         ("singular_g", ctypes.c_int32),
         ("polar_fallbacks", ctypes.c_int32),
         ("active", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("kernel_launches", ctypes.c_int32),
+        ("spmv_timed", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("ms_spmv", ctypes.c_double),
+        ("reserved", ctypes.c_double * 2),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
 
 
 _lib = None
@@ -111,6 +116,7 @@ def load():
         "gbfem_get_state": (S, [H, D, D]),
         "gbfem_set_state": (S, [H, D, D]),
         "gbfem_set_velocities": (S, [H, ctypes.c_int32, I32, D]),
+        "gbfem_set_velocities_device": (S, [H, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]),
         "gbfem_device_state": (S, [H, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
         "gbfem_stream": (S, [H, ctypes.POINTER(ctypes.c_void_p)]),
         "gbfem_reactivate": (S, [H]),

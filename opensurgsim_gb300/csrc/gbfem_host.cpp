@@ -95,6 +95,7 @@ struct gbfem_handle_s
 	int nb = 0, nl = 0;
 	int64_t nnz = 0;
 	bool active = true;
+	int launches = 0;  // kernels launched by the current gbfem_step call
 	std::string err;
 	gbfem_stats stats{};
 
@@ -107,7 +108,8 @@ struct gbfem_handle_s
 	// device
 	DevBuf<int4> d_tets;
 	DevBuf<double> d_rest, d_xrest, d_lmass, d_nmass;
-	DevBuf<int> d_brow, d_bcol, d_cptr, d_cidx, d_iptr, d_iidx;
+	DevBuf<int> d_perm, d_off, d_sellcol, d_cptr, d_cidx, d_iptr, d_iidx;
+	int64_t sellSlots = 0;
 	DevBuf<int4> d_lblk;
 	DevBuf<uint8_t> d_bc;
 	DevBuf<double> d_x, d_v, d_xt, d_vt;
@@ -134,8 +136,6 @@ struct gbfem_handle_s
 		b.tets = d_tets.p;
 		b.rest = d_rest.p;
 		b.xrest = d_xrest.p;
-		b.brow = d_brow.p;
-		b.bcol = d_bcol.p;
 		b.lblk = d_lblk.p;
 		b.cptr = d_cptr.p;
 		b.cidx = d_cidx.p;
@@ -181,7 +181,7 @@ struct gbfem_handle_s
 								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
 								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f};
 		for (auto* b : bd) b->free();
-		DevBuf<int>* bi[] = {&d_brow, &d_bcol, &d_cptr, &d_cidx, &d_iptr, &d_iidx, &d_counters, &d_idx,
+		DevBuf<int>* bi[] = {&d_perm, &d_off, &d_sellcol, &d_cptr, &d_cidx, &d_iptr, &d_iidx, &d_counters, &d_idx,
 							 &d_sptr, &d_sidx, &d_srow, &d_scol};
 		for (auto* b : bi) b->free();
 		d_bc.free();
@@ -284,7 +284,40 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	h->nb = (int)h->adj.size();
 	h->nnz = 9LL * h->nb;
 	if (h->nnz > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "pattern exceeds int32 indices");
-	// Lower blocks (I >= J) in BSR order.
+	// SELL-32 layout of the block matrix: rows sorted by block count (descending, stable).
+	std::vector<int> perm(N), sellBase(h->nb);
+	for (int i = 0; i < N; ++i) perm[i] = i;
+	std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+		return (h->adjPtr[a + 1] - h->adjPtr[a]) > (h->adjPtr[b + 1] - h->adjPtr[b]);
+	});
+	const int nchunks = (N + 31) / 32;
+	std::vector<int> off(nchunks + 1, 0);
+	for (int c = 0; c < nchunks; ++c)
+	{
+		int w = 0;
+		for (int l = 0; l < 32 && 32 * c + l < N; ++l)
+		{
+			int I = perm[32 * c + l];
+			w = std::max(w, h->adjPtr[I + 1] - h->adjPtr[I]);
+		}
+		off[c + 1] = off[c] + w;
+	}
+	const int64_t sellSlots = 32LL * off[nchunks];
+	if (sellSlots * 9 > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "matrix exceeds int32 indices");
+	std::vector<int> scol(sellSlots, 0);
+	for (int rs = 0; rs < N; ++rs)
+	{
+		const int I = perm[rs], c = rs >> 5, lane = rs & 31;
+		const int deg = h->adjPtr[I + 1] - h->adjPtr[I];
+		for (int t = 0; t < off[c + 1] - off[c]; ++t)
+		{
+			const int k = off[c] + t;
+			scol[(size_t)k * 32 + lane] = (t < deg) ? h->adj[h->adjPtr[I] + t] : I;
+			if (t < deg) sellBase[h->adjPtr[I] + t] = k * 288 + lane;
+		}
+	}
+	h->sellSlots = sellSlots;
+	// Lower blocks (I >= J) in row order, written to the SELL positions of (I,J) and (J,I).
 	std::vector<int> lowerOfPos(h->nb, -1);
 	std::vector<int4> lblk;
 	lblk.reserve(h->nb / 2 + N);
@@ -294,7 +327,7 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 			int J = h->adj[k];
 			if (J > I) continue;
 			lowerOfPos[k] = (int)lblk.size();
-			lblk.push_back(make_int4(I, J, k, I == J ? -1 : h->blockPos(J, I)));
+			lblk.push_back(make_int4(I, J, sellBase[k], I == J ? -1 : sellBase[h->blockPos(J, I)]));
 		}
 	h->nl = (int)lblk.size();
 	// Element slot -> lower block contributions, element order inside each block.
@@ -355,8 +388,9 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	GB_CUDA(h, h->d_tets.upload(reinterpret_cast<const int4*>(h->tets.data()), E, s));
 	GB_CUDA(h, h->d_rest.upload(rest.data(), rest.size(), s));
 	GB_CUDA(h, h->d_xrest.upload(X, h->n, s));
-	GB_CUDA(h, h->d_brow.upload(h->adjPtr.data(), N + 1, s));
-	GB_CUDA(h, h->d_bcol.upload(h->adj.data(), h->adj.size(), s));
+	GB_CUDA(h, h->d_perm.upload(perm.data(), perm.size(), s));
+	GB_CUDA(h, h->d_off.upload(off.data(), off.size(), s));
+	GB_CUDA(h, h->d_sellcol.upload(scol.data(), scol.size(), s));
 	GB_CUDA(h, h->d_lblk.upload(lblk.data(), lblk.size(), s));
 	GB_CUDA(h, h->d_cptr.upload(cptr.data(), cptr.size(), s));
 	GB_CUDA(h, h->d_cidx.upload(cidx.data(), cidx.size(), s));
@@ -370,7 +404,8 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	GB_CUDA(h, cudaMemsetAsync(h->d_v.p, 0, sizeof(double) * h->n, s));
 	GB_CUDA(h, h->d_kslots.alloc((size_t)E * kSlots * 9));
 	GB_CUDA(h, h->d_rhsE.alloc((size_t)E * 12));
-	GB_CUDA(h, h->d_A.alloc((size_t)h->nb * 9));
+	GB_CUDA(h, h->d_A.alloc((size_t)sellSlots * 9));
+	GB_CUDA(h, cudaMemsetAsync(h->d_A.p, 0, sizeof(double) * sellSlots * 9, s));  // padding blocks stay 0
 	const size_t nv = h->n;
 	for (DevBuf<double>* b : {&h->d_invdiag, &h->d_rhs, &h->d_dv, &h->d_r, &h->d_p, &h->d_q}) GB_CUDA(h, b->alloc(nv));
 	GB_CUDA(h, h->d_part.alloc(partial_slots(h->launch().vecGrid)));
@@ -472,30 +507,77 @@ struct PhaseTimer
 	}
 };
 
+// CUDA events bracketing individual kernel launches (GBFEM_STEP_TIME_KERNELS).
+struct KernelTimer
+{
+	static constexpr int kPairs = 32;
+	cudaEvent_t a[kPairs] = {}, b[kPairs] = {};
+	bool ready = false;
+	bool init()
+	{
+		if (ready) return true;
+		for (int i = 0; i < kPairs; ++i)
+			if (cudaEventCreate(&a[i]) != cudaSuccess || cudaEventCreate(&b[i]) != cudaSuccess) return false;
+		ready = true;
+		return true;
+	}
+	~KernelTimer()
+	{
+		if (ready)
+			for (int i = 0; i < kPairs; ++i)
+			{
+				cudaEventDestroy(a[i]);
+				cudaEventDestroy(b[i]);
+			}
+	}
+};
+
 // Jacobi PCG on the handle's symmetric BSR matrix; the host polls the device control block
 // between chunks of iterations (kernels after convergence return immediately).
-gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter)
+gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter, bool timeSpmv)
 {
+	static thread_local KernelTimer kt;
+	if (timeSpmv && !kt.init()) return fail(h, GBFEM_CUDA_ERROR, "cudaEventCreate failed");
 	const Launch L = h->launch();
-	MatBsr3 A{h->N, h->d_brow.p, h->d_bcol.p, h->d_A.p};
+	MatSell3 A{h->N, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A.p};
 	launch_cg_init(h->n, b, h->d_invdiag.p, x, h->d_r.p, h->d_p.p, h->d_ctl.p, h->d_part.p, h->prm.cg_tolerance,
 				   maxIter, L);
+	h->launches++;
 	long long launched = 0;
 	int chunk = 4;
+	int iterBefore = 0;
 	for (;;)
 	{
 		for (int k = 0; k < chunk; ++k)
 		{
-			launch_cg_spmv_bsr(A, h->d_p.p, h->d_q.p, h->d_ctl.p, h->d_part.p, L);
+			if (timeSpmv) cudaEventRecord(kt.a[k], h->stream);
+			launch_cg_spmv_sell(A, h->d_p.p, h->d_q.p, h->d_ctl.p, h->d_part.p, L);
+			if (timeSpmv) cudaEventRecord(kt.b[k], h->stream);
 			launch_cg_update(h->n, h->d_invdiag.p, h->d_p.p, h->d_q.p, x, h->d_r.p, h->d_ctl.p, h->d_part.p, L);
 			launch_cg_pupdate(h->n, h->d_invdiag.p, h->d_r.p, h->d_p.p, h->d_ctl.p, L);
 		}
+		h->launches += 3 * chunk;
 		launched += chunk;
 		GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl.p, sizeof(CgCtl), cudaMemcpyDeviceToHost, h->stream));
 		GB_CUDA(h, cudaStreamSynchronize(h->stream));
+		if (timeSpmv)
+		{
+			// Launches that did work: one per iteration, plus the converging one.
+			const CgCtl& c = *h->h_ctl;
+			int real = c.iter - iterBefore + ((c.done && c.converged && c.bb > 0 && c.iter < c.maxIter) ? 1 : 0);
+			real = std::max(0, std::min(real, chunk));
+			for (int k = 0; k < real; ++k)
+			{
+				float ms = 0;
+				cudaEventElapsedTime(&ms, kt.a[k], kt.b[k]);
+				h->stats.ms_spmv += ms;
+				h->stats.spmv_timed++;
+			}
+			iterBefore = c.iter;
+		}
 		if (h->h_ctl->done) break;
 		if (launched > (long long)maxIter + 64) return fail(h, GBFEM_CUDA_ERROR, "CG control block did not finish");
-		chunk = std::min(chunk * 2, 32);
+		chunk = std::min(chunk * 2, KernelTimer::kPairs);
 	}
 	return GBFEM_OK;
 }
@@ -550,7 +632,8 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 		}
 		tm.mark(2);
 		GB_CUDA(h, cudaGetLastError());
-		gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter);
+		h->launches += keep ? 5 : 3;
+		gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, (flags & GBFEM_STEP_TIME_KERNELS) != 0);
 		if (st != GBFEM_OK) return st;
 		tm.mark(3);
 		h->stats.cg_iterations += h->h_ctl->iter;
@@ -558,6 +641,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 		if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
 		launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, xt, h->d_x.p, h->d_v.p, dt, newtonMax > 1, h->d_ctl.p,
 							h->d_part.p, L);
+		h->launches++;
 		tm.mark(4);
 		if (tm.on)
 		{
@@ -576,6 +660,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 	}
 	h->haveSystem = keep;
 	launch_validity(h->n, h->d_x.p, h->d_v.p, h->d_ctl.p, h->d_part.p, L);
+	h->launches++;
 	GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl.p, sizeof(CgCtl), cudaMemcpyDeviceToHost, s));
 	GB_CUDA(h, cudaStreamSynchronize(s));
 	GB_CUDA(h, cudaGetLastError());
@@ -675,6 +760,7 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	if (!h) return GBFEM_INVALID_ARG;
 	if (!(dt > 0.0) || nsteps < 0) return fail(h, GBFEM_INVALID_ARG, "dt must be > 0 and nsteps >= 0");
 	std::memset(&h->stats, 0, sizeof(h->stats));
+	h->launches = 0;
 	if (!h->active)
 	{
 		h->stats.active = 0;
@@ -697,6 +783,7 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	h->stats.singular_g = counters[0];
 	h->stats.polar_fallbacks = counters[1];
 	h->stats.active = h->active ? 1 : 0;
+	h->stats.kernel_launches = h->launches;
 	if (result == GBFEM_OK && h->stats.cg_max_iterations_hit > 0)
 	{
 		h->err = "CG reached its maximum number of iterations";
@@ -748,6 +835,17 @@ gbfem_status gbfem_set_velocities(gbfem_handle h, int32_t count, const int32_t* 
 	GB_CUDA(h, cudaMemcpyAsync(h->d_vals.p, values, sizeof(double) * count, cudaMemcpyHostToDevice, h->stream));
 	launch_scatter_values(count, h->d_idx.p, h->d_vals.p, h->d_v.p, h->stream);
 	GB_CUDA(h, cudaStreamSynchronize(h->stream));
+	GB_CUDA(h, cudaGetLastError());
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_set_velocities_device(gbfem_handle h, int32_t count, const int32_t* dofs_dev,
+										 const double* values_dev)
+{
+	if (!h || count < 0 || (count > 0 && (!dofs_dev || !values_dev))) return GBFEM_INVALID_ARG;
+	if (count == 0) return GBFEM_OK;
+	GB_CUDA(h, cudaSetDevice(h->device));
+	launch_scatter_values(count, dofs_dev, values_dev, h->d_v.p, h->stream);
 	GB_CUDA(h, cudaGetLastError());
 	return GBFEM_OK;
 }

@@ -25,9 +25,7 @@ struct DevBody
 	const int4* tets = nullptr;
 	const double* rest = nullptr;   // kRestFields * E
 	const double* xrest = nullptr;  // 3N
-	const int* brow = nullptr;      // N+1, BSR row pointer
-	const int* bcol = nullptr;      // nb
-	const int4* lblk = nullptr;     // nl: {I, J, pos(I,J), pos(J,I) or -1}
+	const int4* lblk = nullptr;     // nl: {I, J, SELL base of (I,J), SELL base of (J,I) or -1}
 	const int* cptr = nullptr;      // nl+1
 	const int* cidx = nullptr;      // E*kSlots: e*kSlots + slot, element order inside a lower block
 	const double* lmass = nullptr;  // nl: consistent-mass coefficient of the lower block
@@ -68,12 +66,18 @@ void launch_assemble_full_csc(int nnz, const int* sptr, const int* sidx, const i
 							  double* S, cudaStream_t s);
 
 // ---- CG on the mirrored symmetric matrix
-struct MatBsr3
+// Sliced-ELL storage of the 3x3-block matrix ("SELL-32"): block rows are sorted by their number
+// of blocks and cut into chunks of 32 rows; chunk c holds width[c] = off[c+1] - off[c] block
+// columns. Block column k of the chunk stores, for its 32 rows (lanes), the column node id at
+// col[k*32 + lane] and the 9 values (row-major inside the block) at val[k*288 + m*32 + lane].
+// Rows shorter than the chunk width are padded with zero blocks pointing at the row's own node.
+struct MatSell3
 {
-	int rows;            // block rows
-	const int* brow;
-	const int* bcol;
-	const double* val;   // 9 per block, row-major
+	int rows;            // block rows (nodes)
+	const int* perm;     // sorted position -> node id
+	const int* off;      // chunk offsets in block columns, nchunks + 1
+	const int* col;
+	const double* val;
 };
 struct MatCsr
 {
@@ -84,7 +88,7 @@ struct MatCsr
 };
 void launch_cg_init(int n, const double* b, const double* invdiag, double* x, double* r, double* p, CgCtl* ctl,
 					double* part, double tol, int maxIter, const Launch& L);
-void launch_cg_spmv_bsr(const MatBsr3& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L);
+void launch_cg_spmv_sell(const MatSell3& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L);
 void launch_cg_spmv_csr(const MatCsr& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L);
 void launch_cg_update(int n, const double* invdiag, const double* p, const double* q, double* x, double* r,
 					  CgCtl* ctl, double* part, const Launch& L);

@@ -549,13 +549,13 @@ __global__ void k_assemble_bsr(DevBody b, const double* __restrict__ ks, double 
 			if (b.bc[r] | b.bc[c]) blk[3 * i + j] = (r == c) ? 1.0 : 0.0;
 		}
 #pragma unroll
-	for (int m = 0; m < 9; ++m) A[(size_t)lb.z * 9 + m] = blk[m];
+	for (int m = 0; m < 9; ++m) A[(size_t)lb.z + 32 * m] = blk[m];
 	if (lb.w >= 0)
 	{
 #pragma unroll
 		for (int i = 0; i < 3; ++i)
 #pragma unroll
-			for (int j = 0; j < 3; ++j) A[(size_t)lb.w * 9 + 3 * j + i] = blk[3 * i + j];
+			for (int j = 0; j < 3; ++j) A[(size_t)lb.w + 32 * (3 * j + i)] = blk[3 * i + j];
 	}
 	if (I == J)
 	{
@@ -726,41 +726,36 @@ __global__ void k_cg_init(int n, const double* __restrict__ bvec, const double* 
 	}
 }
 
-__global__ void __launch_bounds__(256) k_cg_spmv_bsr(MatBsr3 A, const double* __restrict__ p, double* __restrict__ q,
-													  CgCtl* ctl, double* part)
+// q = A p on the SELL-32 block matrix: one thread per block row (3 scalar rows), no reductions,
+// every value and column load coalesced across the warp (a warp is one chunk).
+__global__ void __launch_bounds__(256) k_cg_spmv_sell(MatSell3 A, const double* __restrict__ p,
+													   double* __restrict__ q, CgCtl* ctl, double* part)
 {
 	if (ctl->done) return;
-	const int lane = threadIdx.x & 31;
-	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const int nwarps = (gridDim.x * blockDim.x) >> 5;
 	double v[1] = {0.0};
-	for (int row = warp; row < A.rows; row += nwarps)
+	const int stride = gridDim.x * blockDim.x;
+	const int nrowsPadded = (A.rows + 31) & ~31;
+	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < nrowsPadded; rs += stride)
 	{
-		const int v0 = A.brow[row] * 9, v1 = A.brow[row + 1] * 9;
+		const int c = rs >> 5, lane = rs & 31;
+		const int k0 = A.off[c], k1 = A.off[c + 1];
 		double a0 = 0, a1 = 0, a2 = 0;
-		for (int k = v0 + lane; k < v1; k += 32)
+		for (int k = k0; k < k1; ++k)
 		{
-			const int blk = k / 9;
-			const int m = k - blk * 9;
-			const int i = m / 3;
-			const int j = m - 3 * i;
-			const double t = A.val[k] * p[3 * A.bcol[blk] + j];
-			if (i == 0)
-				a0 += t;
-			else if (i == 1)
-				a1 += t;
-			else
-				a2 += t;
+			const int J = A.col[k * 32 + lane];
+			const double* vb = A.val + (size_t)k * 288 + lane;
+			const double p0 = p[3 * J], p1 = p[3 * J + 1], p2 = p[3 * J + 2];
+			a0 += vb[0] * p0 + vb[32] * p1 + vb[64] * p2;
+			a1 += vb[96] * p0 + vb[128] * p1 + vb[160] * p2;
+			a2 += vb[192] * p0 + vb[224] * p1 + vb[256] * p2;
 		}
-		a0 = warp_reduce<OpSum>(a0);
-		a1 = warp_reduce<OpSum>(a1);
-		a2 = warp_reduce<OpSum>(a2);
-		if (lane == 0)
+		if (rs < A.rows)
 		{
-			q[3 * row] = a0;
-			q[3 * row + 1] = a1;
-			q[3 * row + 2] = a2;
-			v[0] += p[3 * row] * a0 + p[3 * row + 1] * a1 + p[3 * row + 2] * a2;
+			const int I = A.perm[rs];
+			q[3 * I] = a0;
+			q[3 * I + 1] = a1;
+			q[3 * I + 2] = a2;
+			v[0] += p[3 * I] * a0 + p[3 * I + 1] * a1 + p[3 * I + 2] * a2;
 		}
 	}
 	double tot[1];
@@ -948,9 +943,9 @@ void launch_cg_init(int n, const double* b, const double* invdiag, double* x, do
 	k_cg_init<<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, b, invdiag, x, r, p, ctl, part, tol, maxIter);
 }
 
-void launch_cg_spmv_bsr(const MatBsr3& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L)
+void launch_cg_spmv_sell(const MatSell3& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L)
 {
-	k_cg_spmv_bsr<<<L.vecGrid, 256, 0, L.stream>>>(A, p, q, ctl, part);
+	k_cg_spmv_sell<<<L.vecGrid, 256, 0, L.stream>>>(A, p, q, ctl, part);
 }
 
 void launch_cg_spmv_csr(const MatCsr& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L)

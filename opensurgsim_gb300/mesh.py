@@ -129,10 +129,17 @@ def scene_cube(a=10, b=10, c=10, h=0.01, seed=0, young=1e5, poisson=0.45, densit
     return Scene(mesh=mesh, name=f"cube{a}x{b}x{c}", **kw)
 
 
-def scene_bar_compression(a=40, b=40, c=160, h=0.01, seed=1, steps=200, dt=1e-3, ramp_steps=50) -> Scene:
+def scene_bar_compression(a=40, b=40, c=160, h=0.004, seed=1, steps=200, dt=1e-3, ramp_steps=50,
+                          cg_max_iterations=0) -> Scene:
     """Large bar: per-tet E log-uniform in [1e4, 1e6] Pa, nu uniform in [0.40, 0.49]; z = 0 clamped;
     the z = c*h face is driven at -0.2*L/(ramp_steps*dt) along z for `ramp_steps` steps (a 20%
-    axial compression ramp), then held."""
+    axial compression ramp), then held.
+
+    The driven face moves 0.2*c/ramp_steps = 0.64 cube edges per step whatever h is, while an
+    elastic wave crosses sqrt(E/rho)*dt/h edges per step. With h = 1 cm the top layers invert within
+    three steps and the system stops being positive definite (CG never converges). With h = 4 mm
+    (a 16 x 16 x 64 cm bar) no element inverts during the 50 ramp steps (about 450 CG iterations
+    per step at tolerance 1e-10); a few elements invert after the ramp, while the bar is held."""
     nodes, tets = cube_grid(a, b, c, h=h, seed=seed)
     E = tets.shape[0]
     rng = np.random.Generator(np.random.PCG64(seed + 1000))
@@ -143,7 +150,7 @@ def scene_bar_compression(a=40, b=40, c=160, h=0.01, seed=1, steps=200, dt=1e-3,
     mesh = TetMesh(nodes, tets, young, poisson, np.full(E, 1000.0), np.concatenate([clamp, top]), (a, b, c), h)
     L = c * h
     return Scene(mesh=mesh, dt=dt, steps=steps, driven_dofs=top, driven_velocity=-0.2 * L / (ramp_steps * dt),
-                 ramp_steps=ramp_steps, name=f"bar{a}x{b}x{c}")
+                 ramp_steps=ramp_steps, name=f"bar{a}x{b}x{c}", cg_max_iterations=cg_max_iterations)
 
 
 def batch_dims(count: int, lo: float, hi: float, seed: int) -> list:

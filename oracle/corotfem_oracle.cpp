@@ -811,19 +811,26 @@ struct FemModel : Equation
 				for (int I : adj[J])
 					for (int i = 0; i < 3; ++i) pat.rowidx[k++] = 3 * I + i;
 			}
-		// Scatter map: SparseMatrix.h blockWithSearch (:178-242) resolved once per element entry.
+		// Scatter map: SparseMatrix.h blockWithSearch (:178-242) resolved once per element entry. The
+		// first row of block (n_a, n_b) in column 3 n_b + j sits at 3 * (position of n_a in adj[n_b]).
 		scatter.resize(tets.size() * 144);
 		for (size_t e = 0; e < tets.size(); ++e)
 		{
 			const Tet& t = tets[e];
-			for (int a = 0; a < 4; ++a)
-				for (int b = 0; b < 4; ++b)
+			for (int b = 0; b < 4; ++b)
+			{
+				const vector<int>& col = adj[t.n[b]];
+				for (int a = 0; a < 4; ++a)
+				{
+					int pos = (int)(std::lower_bound(col.begin(), col.end(), t.n[a]) - col.begin());
 					for (int j = 0; j < 3; ++j)
 					{
-						int64_t first = pat.find(3 * t.n[a], 3 * t.n[b] + j);
+						int64_t first = pat.colptr[3 * t.n[b] + j] + 3 * pos;
 						for (int i = 0; i < 3; ++i)
 							scatter[e * 144 + (3 * a + i) * 12 + 3 * b + j] = (int)(first + i);
 					}
+				}
+			}
 		}
 		M.assign(pat.nnz(), 0.0);
 		D.assign(pat.nnz(), 0.0);
