@@ -254,7 +254,7 @@ def run_ours(args, rank, world, local, dist):
     spmv_ms = agg["ms_spmv"] / max(1, agg["spmv_timed"])
     peak, peak_kind = load_peak()
     achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9 if spmv_ms > 0 else None
-    traffic = load_traffic(f"spmv_bsr_{args.precision}_{args.config}")
+    traffic = load_traffic(f"spmv_sell_{args.precision}_{args.config}")
     cg_per_step = agg["cg_iterations"] / max(1, args.steps)
     line = {
         "metric": METRIC,
@@ -286,7 +286,7 @@ def run_ours(args, rank, world, local, dist):
         "e2e": {"value": e2e_value, "unit": "tet-element-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {
-            "kernel": f"k_cg_spmv_bsr ({args.precision})",
+            "kernel": f"k_cg_spmv_sell ({args.precision})",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": traffic,
             "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms,

@@ -114,6 +114,12 @@ struct gbfem_handle_s
 	DevBuf<uint8_t> d_bc;
 	DevBuf<double> d_x, d_v, d_xt, d_vt;
 	DevBuf<double> d_kslots, d_rhsE, d_A, d_invdiag, d_rhs, d_dv, d_dvPrev, d_r, d_p, d_q, d_part;
+	// mixed-precision form
+	DevBuf<float> d_rest32, d_kslots32, d_rhsE32, d_A32, d_invdiag32, d_r32, d_p32, d_q32;
+	DevBuf<double> d_r64;
+	DevBuf<MixCtl> d_mix;
+	MixCtl* h_mix = nullptr;
+	bool mixed() const { return prm.precision == GBFEM_PRECISION_MIXED; }
 	DevBuf<int> d_counters;
 	DevBuf<CgCtl> d_ctl;
 	CgCtl* h_ctl = nullptr;
@@ -135,6 +141,7 @@ struct gbfem_handle_s
 		b.nl = nl;
 		b.tets = d_tets.p;
 		b.rest = d_rest.p;
+		b.rest32 = d_rest32.p;
 		b.xrest = d_xrest.p;
 		b.lblk = d_lblk.p;
 		b.cptr = d_cptr.p;
@@ -177,6 +184,12 @@ struct gbfem_handle_s
 		h_ctl = nullptr;
 		DevBuf<int4>* b4[] = {&d_tets, &d_lblk};
 		for (auto* b : b4) b->free();
+		if (h_mix) cudaFreeHost(h_mix);
+		h_mix = nullptr;
+		DevBuf<float>* bf[] = {&d_rest32, &d_kslots32, &d_rhsE32, &d_A32, &d_invdiag32, &d_r32, &d_p32, &d_q32};
+		for (auto* b : bf) b->free();
+		d_r64.free();
+		d_mix.free();
 		DevBuf<double>* bd[] = {&d_rest, &d_xrest, &d_lmass, &d_nmass, &d_x, &d_v, &d_xt, &d_vt, &d_kslots,
 								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
 								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f};
@@ -402,12 +415,32 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	GB_CUDA(h, h->d_x.upload(X, h->n, s));
 	GB_CUDA(h, h->d_v.alloc(h->n));
 	GB_CUDA(h, cudaMemsetAsync(h->d_v.p, 0, sizeof(double) * h->n, s));
-	GB_CUDA(h, h->d_kslots.alloc((size_t)E * kSlots * 9));
-	GB_CUDA(h, h->d_rhsE.alloc((size_t)E * 12));
-	GB_CUDA(h, h->d_A.alloc((size_t)sellSlots * 9));
-	GB_CUDA(h, cudaMemsetAsync(h->d_A.p, 0, sizeof(double) * sellSlots * 9, s));  // padding blocks stay 0
 	const size_t nv = h->n;
-	for (DevBuf<double>* b : {&h->d_invdiag, &h->d_rhs, &h->d_dv, &h->d_r, &h->d_p, &h->d_q}) GB_CUDA(h, b->alloc(nv));
+	if (!h->mixed())
+	{
+		GB_CUDA(h, h->d_kslots.alloc((size_t)E * kSlots * 9));
+		GB_CUDA(h, h->d_rhsE.alloc((size_t)E * 12));
+		GB_CUDA(h, h->d_A.alloc((size_t)sellSlots * 9));
+		GB_CUDA(h, cudaMemsetAsync(h->d_A.p, 0, sizeof(double) * sellSlots * 9, s));  // padding blocks stay 0
+		for (DevBuf<double>* b : {&h->d_invdiag, &h->d_r, &h->d_p, &h->d_q}) GB_CUDA(h, b->alloc(nv));
+	}
+	else
+	{
+		// FP32 copy of the FP64 rest precompute (K0 and volume stay FP64-derived).
+		std::vector<float> rest32(rest.begin(), rest.end());
+		GB_CUDA(h, h->d_rest32.upload(rest32.data(), rest32.size(), s));
+		GB_CUDA(h, cudaStreamSynchronize(s));
+		GB_CUDA(h, h->d_kslots32.alloc((size_t)E * kSlots * 9));
+		GB_CUDA(h, h->d_rhsE32.alloc((size_t)E * 12));
+		GB_CUDA(h, h->d_A32.alloc((size_t)sellSlots * 9));
+		GB_CUDA(h, cudaMemsetAsync(h->d_A32.p, 0, sizeof(float) * sellSlots * 9, s));
+		for (DevBuf<float>* b : {&h->d_invdiag32, &h->d_r32, &h->d_p32, &h->d_q32}) GB_CUDA(h, b->alloc(nv));
+		GB_CUDA(h, h->d_r64.alloc(nv));
+		GB_CUDA(h, h->d_mix.alloc(1));
+		GB_CUDA(h, cudaMemsetAsync(h->d_mix.p, 0, sizeof(MixCtl), s));
+		GB_CUDA(h, cudaMallocHost(&h->h_mix, sizeof(MixCtl)));
+	}
+	for (DevBuf<double>* b : {&h->d_rhs, &h->d_dv}) GB_CUDA(h, b->alloc(nv));
 	GB_CUDA(h, h->d_part.alloc(partial_slots(h->launch().vecGrid)));
 	GB_CUDA(h, h->d_counters.alloc(4));
 	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));
@@ -582,9 +615,67 @@ gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter, boo
 	return GBFEM_OK;
 }
 
+// Mixed-precision solve: FP32 CG iterations with reliable FP64 residual refreshes; the host polls
+// the device control block between chunks of iterations.
+gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, bool timeSpmv)
+{
+	static thread_local KernelTimer kt;
+	if (timeSpmv && !kt.init()) return fail(h, GBFEM_CUDA_ERROR, "cudaEventCreate failed");
+	const Launch L = h->launch();
+	MixBufs m;
+	m.n = h->n;
+	m.b = b;
+	m.x = x;
+	m.r64 = h->d_r64.p;
+	m.r = h->d_r32.p;
+	m.p = h->d_p32.p;
+	m.q = h->d_q32.p;
+	m.invdiag = h->d_invdiag32.p;
+	m.A = MatSellT<float>{h->N, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A32.p};
+	m.ctl = h->d_mix.p;
+	m.part = h->d_part.p;
+	// Refresh the FP64 residual whenever the FP32 residual norm has dropped ~30x (|r|^2 by 1e-3).
+	constexpr double kReliableDrop = 1e-3;
+	launch_mix_init(m, h->prm.cg_tolerance, maxIter, kReliableDrop, L);
+	h->launches += kMixInitKernels;
+	long long launched = 0;
+	int chunk = 4;
+	int spmvSoFar = 0;
+	for (;;)
+	{
+		for (int k = 0; k < chunk; ++k)
+			launch_mix_iteration(m, L, timeSpmv ? kt.a[k] : nullptr, timeSpmv ? kt.b[k] : nullptr);
+		h->launches += kMixKernelsPerIteration * chunk;
+		launched += chunk;
+		GB_CUDA(h, cudaMemcpyAsync(h->h_mix, h->d_mix.p, sizeof(MixCtl), cudaMemcpyDeviceToHost, h->stream));
+		GB_CUDA(h, cudaStreamSynchronize(h->stream));
+		const MixCtl& c = *h->h_mix;
+		if (timeSpmv)
+		{
+			// Launches that multiplied by the matrix: one per counted iteration, plus the converging one.
+			const int total = c.iter + ((c.done && c.converged && c.bb > 0) ? 1 : 0);
+			const int real = std::max(0, std::min(total - spmvSoFar, chunk));
+			spmvSoFar = total;
+			for (int k = 0; k < real; ++k)
+			{
+				float ms = 0;
+				cudaEventElapsedTime(&ms, kt.a[k], kt.b[k]);
+				h->stats.ms_spmv += ms;
+				h->stats.spmv_timed++;
+			}
+		}
+		if (c.done) break;
+		if (launched > (long long)maxIter + 64) return fail(h, GBFEM_CUDA_ERROR, "CG control block did not finish");
+		chunk = std::min(chunk * 2, KernelTimer::kPairs);
+	}
+	return GBFEM_OK;
+}
+
 gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 {
 	const bool keep = (flags & GBFEM_STEP_KEEP_SYSTEM) != 0;
+	if (keep && h->mixed())
+		return fail(h, GBFEM_INVALID_ARG, "GBFEM_STEP_KEEP_SYSTEM is available in the FP64 form only");
 	if (keep)
 	{
 		gbfem_status st = ensure_system_maps(h);
@@ -618,27 +709,50 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 	for (int it = 0; it < newtonMax; ++it)
 	{
 		tm.mark(0);
-		launch_element_fp64(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
-							h->d_kslots.p, h->d_rhsE.p, keep ? h->d_kfull.p : nullptr, keep ? h->d_fE.p : nullptr,
-							h->d_counters.p, s);
-		tm.mark(1);
-		launch_assemble_bsr(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
-		launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
-		if (keep)
+		const bool timeK = (flags & GBFEM_STEP_TIME_KERNELS) != 0;
+		if (h->mixed())
 		{
-			launch_assemble_full_csc((int)h->nnz, h->d_sptr.p, h->d_sidx.p, h->d_srow.p, h->d_scol.p, h->d_kfull.p,
-									 h->d_smass.p, h->d_bc.p, c1, c2, h->d_S.p, s);
-			launch_rhs_gather(body, h->d_fE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_f.p, 0, s);
+			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
+							   h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s);
+			tm.mark(1);
+			launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+			launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+			tm.mark(2);
+			GB_CUDA(h, cudaGetLastError());
+			h->launches += 3;
+			gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
+			if (st != GBFEM_OK) return st;
+			tm.mark(3);
+			const MixCtl& mc = *h->h_mix;
+			h->stats.cg_iterations += mc.iter;
+			h->stats.refinement_sweeps += mc.updates;
+			h->stats.cg_relative_residual = mc.bb > 0 ? std::sqrt(mc.rrTrue / mc.bb) : 0.0;
+			if (!mc.converged) h->stats.cg_max_iterations_hit++;
 		}
-		tm.mark(2);
-		GB_CUDA(h, cudaGetLastError());
-		h->launches += keep ? 5 : 3;
-		gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, (flags & GBFEM_STEP_TIME_KERNELS) != 0);
-		if (st != GBFEM_OK) return st;
-		tm.mark(3);
-		h->stats.cg_iterations += h->h_ctl->iter;
-		h->stats.cg_relative_residual = h->h_ctl->bb > 0 ? std::sqrt(h->h_ctl->rr / h->h_ctl->bb) : 0.0;
-		if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
+		else
+		{
+			launch_element_fp64(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
+								h->prm.rayleigh_stiffness, h->d_kslots.p, h->d_rhsE.p, keep ? h->d_kfull.p : nullptr,
+								keep ? h->d_fE.p : nullptr, h->d_counters.p, s);
+			tm.mark(1);
+			launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+			if (keep)
+			{
+				launch_assemble_full_csc((int)h->nnz, h->d_sptr.p, h->d_sidx.p, h->d_srow.p, h->d_scol.p,
+										 h->d_kfull.p, h->d_smass.p, h->d_bc.p, c1, c2, h->d_S.p, s);
+				launch_rhs_gather(body, h->d_fE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_f.p, 0, s);
+			}
+			tm.mark(2);
+			GB_CUDA(h, cudaGetLastError());
+			h->launches += keep ? 5 : 3;
+			gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
+			if (st != GBFEM_OK) return st;
+			tm.mark(3);
+			h->stats.cg_iterations += h->h_ctl->iter;
+			h->stats.cg_relative_residual = h->h_ctl->bb > 0 ? std::sqrt(h->h_ctl->rr / h->h_ctl->bb) : 0.0;
+			if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
+		}
 		launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, xt, h->d_x.p, h->d_v.p, dt, newtonMax > 1, h->d_ctl.p,
 							h->d_part.p, L);
 		h->launches++;

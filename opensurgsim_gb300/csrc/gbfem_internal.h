@@ -6,7 +6,8 @@
 
 namespace gbfem {
 
-// Per-element rest data, structure of arrays: kRest[k * E + e].
+// Per-element rest data, structure of arrays: rest[k * E + e] (FP64; the mixed form keeps an
+// FP32 copy with the same layout).
 //   k = 0..11  shape-function gradients g_a (a = 0..3, 3 components each) = rows of V^-1
 //   k = 12     rest volume V
 //   k = 13     lambda * V
@@ -21,9 +22,10 @@ constexpr int kSlots = 10;
 struct DevBody
 {
 	int N = 0, E = 0, n = 0;        // nodes, tets, dofs
-	int nb = 0, nl = 0;             // BSR blocks (full, symmetric) and lower blocks
+	int nb = 0, nl = 0;             // blocks of the symmetric block matrix, lower blocks
 	const int4* tets = nullptr;
 	const double* rest = nullptr;   // kRestFields * E
+	const float* rest32 = nullptr;  // FP32 copy (mixed form)
 	const double* xrest = nullptr;  // 3N
 	const int4* lblk = nullptr;     // nl: {I, J, SELL base of (I,J), SELL base of (J,I) or -1}
 	const int* cptr = nullptr;      // nl+1
@@ -35,7 +37,7 @@ struct DevBody
 	const uint8_t* bc = nullptr;    // n boundary-condition mask
 };
 
-// Device control block of one CG solve; all scalars live on the device.
+// Device control block of one FP64 CG solve; all scalars live on the device.
 struct CgCtl
 {
 	double bb, rz, pq, rr, threshold, alpha, beta, pad0;
@@ -46,39 +48,45 @@ struct CgCtl
 	int nonfinite, pad1;
 };
 
+// Control block of the mixed-precision solve: FP32 CG iterations on the FP32 matrix, the
+// solution accumulated in FP64, and the true FP64 residual b - A x recomputed ("reliable update")
+// whenever the FP32 residual has dropped by reliableDrop since the last refresh. The FP32 vectors
+// are kept normalised: r_true ~= s * r32.
+struct MixCtl
+{
+	double bb, threshold;   // |b|^2, tol^2 |b|^2
+	double s;               // residual scale
+	double rz, pq, alpha, beta;
+	double rr32, rrLast;    // |r32|^2 now and right after the last refresh
+	double rrTrue;          // |b - A x|^2 at the last refresh
+	double reliableDrop;    // refresh when rr32 < reliableDrop * rrLast
+	double sNew, ratio, rzPend;
+	int iter, done, converged, maxIter;
+	int updates, pending, nonfinite, pad;
+	unsigned int ticket[4];
+};
+
 struct Launch
 {
 	int vecGrid = 0;   // blocks of 256 threads for the dof-wise kernels
 	cudaStream_t stream = nullptr;
 };
 
-// ---- element / assembly (FP64 plain form)
-void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
-						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
-						 double* fE, int* counters, cudaStream_t s);
-void launch_assemble_bsr(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
-						 cudaStream_t s);
-void launch_rhs_gather(const DevBody& b, const double* rhsE, const double* gravity, int gravityOn, double* rhs,
-					   int applyBc, cudaStream_t s);
-// Full (non-mirrored) system for export: CSC slots gather from full element matrices.
-void launch_assemble_full_csc(int nnz, const int* sptr, const int* sidx, const int* srow, const int* scol,
-							  const double* kfull, const double* smass, const uint8_t* bc, double c1, double c2,
-							  double* S, cudaStream_t s);
-
-// ---- CG on the mirrored symmetric matrix
 // Sliced-ELL storage of the 3x3-block matrix ("SELL-32"): block rows are sorted by their number
 // of blocks and cut into chunks of 32 rows; chunk c holds width[c] = off[c+1] - off[c] block
 // columns. Block column k of the chunk stores, for its 32 rows (lanes), the column node id at
 // col[k*32 + lane] and the 9 values (row-major inside the block) at val[k*288 + m*32 + lane].
 // Rows shorter than the chunk width are padded with zero blocks pointing at the row's own node.
-struct MatSell3
+template <typename T>
+struct MatSellT
 {
 	int rows;            // block rows (nodes)
 	const int* perm;     // sorted position -> node id
 	const int* off;      // chunk offsets in block columns, nchunks + 1
 	const int* col;
-	const double* val;
+	const T* val;
 };
+using MatSell3 = MatSellT<double>;
 struct MatCsr
 {
 	int rows;
@@ -86,6 +94,28 @@ struct MatCsr
 	const int* col;
 	const double* val;
 };
+
+// ---- element / assembly
+void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
+						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
+						 double* fE, int* counters, cudaStream_t s);
+void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
+						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
+						cudaStream_t s);
+void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
+					 cudaStream_t s);
+void launch_assemble(const DevBody& b, const float* kslots, double c1, double c2, float* A, float* invdiag,
+					 cudaStream_t s);
+void launch_rhs_gather(const DevBody& b, const double* rhsE, const double* gravity, int gravityOn, double* rhs,
+					   int applyBc, cudaStream_t s);
+void launch_rhs_gather(const DevBody& b, const float* rhsE, const double* gravity, int gravityOn, double* rhs,
+					   int applyBc, cudaStream_t s);
+// Full (non-mirrored) system for export: CSC slots gather from full element matrices.
+void launch_assemble_full_csc(int nnz, const int* sptr, const int* sidx, const int* srow, const int* scol,
+							  const double* kfull, const double* smass, const uint8_t* bc, double c1, double c2,
+							  double* S, cudaStream_t s);
+
+// ---- FP64 CG on the mirrored symmetric matrix
 void launch_cg_init(int n, const double* b, const double* invdiag, double* x, double* r, double* p, CgCtl* ctl,
 					double* part, double tol, int maxIter, const Launch& L);
 void launch_cg_spmv_sell(const MatSell3& A, const double* p, double* q, CgCtl* ctl, double* part, const Launch& L);
@@ -93,6 +123,27 @@ void launch_cg_spmv_csr(const MatCsr& A, const double* p, double* q, CgCtl* ctl,
 void launch_cg_update(int n, const double* invdiag, const double* p, const double* q, double* x, double* r,
 					  CgCtl* ctl, double* part, const Launch& L);
 void launch_cg_pupdate(int n, const double* invdiag, const double* r, double* p, CgCtl* ctl, const Launch& L);
+
+// ---- mixed-precision CG with reliable FP64 updates
+struct MixBufs
+{
+	int n;
+	const double* b;      // right-hand side (FP64)
+	double* x;            // solution (FP64)
+	double* r64;          // true residual scratch (FP64)
+	float* r;             // normalised FP32 residual
+	float* p;
+	float* q;
+	const float* invdiag;
+	MatSellT<float> A;
+	MixCtl* ctl;
+	double* part;
+};
+void launch_mix_init(const MixBufs& m, double tol, int maxIter, double reliableDrop, const Launch& L);
+// One iteration: spmv, update, refresh, rescale, p update (events, if given, bracket the spmv).
+void launch_mix_iteration(const MixBufs& m, const Launch& L, cudaEvent_t evA = nullptr, cudaEvent_t evB = nullptr);
+constexpr int kMixKernelsPerIteration = 5;
+constexpr int kMixInitKernels = 2;
 
 // ---- state
 void launch_state_update(int n, const double* dv, double* dvPrev, const double* xt, double* xn, double* vn,

@@ -1,26 +1,15 @@
 // gbfem_kernels.cu -- sm_103a kernels of the corotational-tetrahedron implicit-Euler step.
 //
-// Element kernel (one element per thread): deformation gradient, polar decomposition, the
-// corotational tangent stiffness (R K0 R^T plus the dR/dx terms of
-// Fem3DElementCorotationalTetrahedron.cpp:199-286, including the reference's use of the rotated
-// stiffness in KTimesRx_x0, :276) and the element's share of the implicit-Euler right-hand side.
-// Assembly gathers element blocks through a precomputed map (deterministic, element order), the
-// right-hand side gathers per node, and the Jacobi-preconditioned CG reads the symmetric matrix
-// built from the lower triangle, as Eigen's ConjugateGradient<..., Lower> does.
-//
-// The element math is written in closed form on the shape-function gradients g_a instead of
-// 12x12 products: with h_a = R g_a and G_ab = g_a . g_b,
-//   K0_ab   = V (lambda g_a g_b^T + mu g_b g_a^T + mu G_ab I)            (= V B^T Em B)
-//   Krot_ab = V (lambda h_a h_b^T + mu h_b h_a^T + mu G_ab I)            (= R K0_ab R^T)
-//   dR/dx_(b,q) = [psi_bq]x R,  psi_bq = G^-1 (g_b x r_q),  r_q = row q of R
-//   extra(3a+i, 3b+q) = (T_a G^-1 (g_b x r_q))_i,
-//   T_a = -[R y_a]x + R (sum_c K0_ac [w_c]x) R^T,  w_c = R^T (x_c - x_0) - (x0_c - x0_0),
-//   y = Krot w  (the reference's KTimesRx_x0).
-// All quantities are formed on positions relative to node 0, which the tangent annihilates.
+// Element kernels (one element per thread; the math is in gbfem_element.cuh), deterministic
+// gather assembly into a symmetric SELL-32 block matrix built from the lower triangle (Eigen's
+// ConjugateGradient<..., Lower> reads only that triangle), the per-node right-hand-side gather,
+// the FP64 Jacobi-PCG, and the mixed-precision CG (FP32 iterations, FP64 solution and reliable
+// FP64 residual refreshes).
 
 #include <cfloat>
 #include <cstdint>
 
+#include "gbfem_element.cuh"
 #include "gbfem_internal.h"
 
 namespace gbfem {
@@ -28,508 +17,110 @@ namespace gbfem {
 namespace {
 
 constexpr int kVecThreads = 256;
+constexpr int kElemThreads = 64;
 
 // ------------------------------------------------------------------------------------------
-// Small 3x3 helpers (row-major arrays of 9).
-// ------------------------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ void cofactor3(const T* X, T* C)
-{
-	C[0] = X[4] * X[8] - X[5] * X[7];
-	C[1] = X[5] * X[6] - X[3] * X[8];
-	C[2] = X[3] * X[7] - X[4] * X[6];
-	C[3] = X[2] * X[7] - X[1] * X[8];
-	C[4] = X[0] * X[8] - X[2] * X[6];
-	C[5] = X[1] * X[6] - X[0] * X[7];
-	C[6] = X[1] * X[5] - X[2] * X[4];
-	C[7] = X[2] * X[3] - X[0] * X[5];
-	C[8] = X[0] * X[4] - X[1] * X[3];
-}
-
-template <typename T>
-__device__ __forceinline__ T det3(const T* X)
-{
-	return X[0] * (X[4] * X[8] - X[5] * X[7]) - X[1] * (X[3] * X[8] - X[5] * X[6]) + X[2] * (X[3] * X[7] - X[4] * X[6]);
-}
-
-template <typename T>
-__device__ __forceinline__ void cross3(const T* a, const T* b, T* c)
-{
-	c[0] = a[1] * b[2] - a[2] * b[1];
-	c[1] = a[2] * b[0] - a[0] * b[2];
-	c[2] = a[0] * b[1] - a[1] * b[0];
-}
-
-template <typename T>
-struct Eps;
-template <>
-struct Eps<double>
-{
-	static constexpr double eps = DBL_EPSILON;
-	static constexpr double newtonTol2 = 1e-26;  // |X_k+1 - X_k|_F^2
-};
-template <>
-struct Eps<float>
-{
-	static constexpr float eps = FLT_EPSILON;
-	static constexpr float newtonTol2 = 1e-11f;
-};
-
-// Polar factor by Newton's iteration X <- (g X + X^-T / g) / 2 (Higham), Frobenius scaling on
-// the first iterations. Valid for det F > 0, where the rotation equals the SVD-based result of
-// Transform::computeRotationScaling. Returns false (caller falls back to the SVD) otherwise or
-// when the iteration does not settle within the bound.
-template <typename T>
-__device__ bool polar_newton(const T* F, T* R)
-{
-	T X[9];
-#pragma unroll
-	for (int k = 0; k < 9; ++k) X[k] = F[k];
-	for (int it = 0; it < 20; ++it)
-	{
-		T C[9];
-		cofactor3(X, C);
-		T d = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];
-		if (!(d > T(0))) return false;
-		T gam = T(1);
-		if (it < 3)
-		{
-			T nx = 0, nc = 0;
-#pragma unroll
-			for (int k = 0; k < 9; ++k)
-			{
-				nx += X[k] * X[k];
-				nc += C[k] * C[k];
-			}
-			gam = sqrt(sqrt(nc / (nx * d * d)));
-		}
-		T a = T(0.5) * gam;
-		T b = T(0.5) / (gam * d);
-		T diff = 0;
-#pragma unroll
-		for (int k = 0; k < 9; ++k)
-		{
-			T xn = a * X[k] + b * C[k];
-			T dd = xn - X[k];
-			diff += dd * dd;
-			X[k] = xn;
-		}
-		if (diff < Eps<T>::newtonTol2 && it >= 1)
-		{
-#pragma unroll
-			for (int k = 0; k < 9; ++k) R[k] = X[k];
-			return true;
-		}
-	}
-	return false;
-}
-
-// SVD-based polar factor for any F (one-sided Jacobi, bounded sweeps), proper rotation with the
-// reflection placed on the smallest singular value.
-template <typename T>
-__device__ void polar_svd(const T* F, T* R)
-{
-	T A[9], V[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-#pragma unroll
-	for (int k = 0; k < 9; ++k) A[k] = F[k];
-	for (int sweep = 0; sweep < 40; ++sweep)
-	{
-		bool rotated = false;
-		for (int pp = 0; pp < 3; ++pp)
-		{
-			int p = (pp == 2) ? 1 : 0;
-			int q = (pp == 0) ? 1 : 2;
-			T al = 0, be = 0, ga = 0;
-			for (int k = 0; k < 3; ++k)
-			{
-				al += A[3 * k + p] * A[3 * k + p];
-				be += A[3 * k + q] * A[3 * k + q];
-				ga += A[3 * k + p] * A[3 * k + q];
-			}
-			if (ga == T(0) || fabs(ga) <= Eps<T>::eps * sqrt(al * be)) continue;
-			rotated = true;
-			T zeta = (be - al) / (T(2) * ga);
-			T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-			T c = T(1) / sqrt(T(1) + t * t);
-			T s = c * t;
-			for (int k = 0; k < 3; ++k)
-			{
-				T ap = A[3 * k + p], aq = A[3 * k + q];
-				A[3 * k + p] = c * ap - s * aq;
-				A[3 * k + q] = s * ap + c * aq;
-				T vp = V[3 * k + p], vq = V[3 * k + q];
-				V[3 * k + p] = c * vp - s * vq;
-				V[3 * k + q] = s * vp + c * vq;
-			}
-		}
-		if (!rotated) break;
-	}
-	T sv[3];
-	for (int j = 0; j < 3; ++j) sv[j] = sqrt(A[j] * A[j] + A[3 + j] * A[3 + j] + A[6 + j] * A[6 + j]);
-	int o[3] = {0, 1, 2};
-	if (sv[o[0]] < sv[o[1]]) { int tt = o[0]; o[0] = o[1]; o[1] = tt; }
-	if (sv[o[1]] < sv[o[2]]) { int tt = o[1]; o[1] = o[2]; o[2] = tt; }
-	if (sv[o[0]] < sv[o[1]]) { int tt = o[0]; o[0] = o[1]; o[1] = tt; }
-	T U[9], Vs[9];
-	for (int j = 0; j < 3; ++j)
-		for (int k = 0; k < 3; ++k) Vs[3 * k + j] = V[3 * k + o[j]];
-	T smax = sv[o[0]] > T(0) ? sv[o[0]] : T(1);
-	for (int j = 0; j < 3; ++j)
-	{
-		T s = sv[o[j]];
-		if (s > T(1e-12) * smax && s > T(0))
-		{
-			for (int k = 0; k < 3; ++k) U[3 * k + j] = A[3 * k + o[j]] / s;
-		}
-		else if (j == 2)
-		{
-			U[2] = U[3] * U[7] - U[6] * U[4];
-			U[5] = U[6] * U[1] - U[0] * U[7];
-			U[8] = U[0] * U[4] - U[3] * U[1];
-		}
-		else
-		{
-			// Rank < 2: complete with the canonical axis least aligned with column 0, orthonormalised.
-			int ax = 0;
-			T best = T(2);
-			for (int a = 0; a < 3; ++a)
-			{
-				T d = (j == 0) ? T(0) : fabs(U[3 * a]);
-				if (d < best) { best = d; ax = a; }
-			}
-			T e[3] = {T(ax == 0), T(ax == 1), T(ax == 2)};
-			if (j == 1)
-			{
-				T d = e[0] * U[0] + e[1] * U[3] + e[2] * U[6];
-				for (int k = 0; k < 3; ++k) e[k] -= d * U[3 * k];
-			}
-			T nrm = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
-			for (int k = 0; k < 3; ++k) U[3 * k + j] = e[k] / nrm;
-		}
-	}
-	T x = (det3(U) * det3(Vs) < T(0)) ? T(-1) : T(1);
-	for (int k = 0; k < 3; ++k) U[3 * k + 2] *= x;
-	for (int i = 0; i < 3; ++i)
-		for (int j = 0; j < 3; ++j) R[3 * i + j] = U[3 * i] * Vs[3 * j] + U[3 * i + 1] * Vs[3 * j + 1] + U[3 * i + 2] * Vs[3 * j + 2];
-}
-
-// (K0 u)_a = lambdaV tr(D) g_a + muV D^T g_a + muV sum_c G_ac u_c,  D = sum_c u_c g_c^T.
-template <typename T>
-__device__ __forceinline__ void k0_apply(const T (&g)[4][3], const T (&Gab)[4][4], T lamV, T muV, const T (&u)[4][3],
-										 T (&out)[4][3])
-{
-	T D[3][3];
-#pragma unroll
-	for (int i = 0; i < 3; ++i)
-#pragma unroll
-		for (int j = 0; j < 3; ++j) D[i][j] = u[0][i] * g[0][j] + u[1][i] * g[1][j] + u[2][i] * g[2][j] + u[3][i] * g[3][j];
-	T tr = D[0][0] + D[1][1] + D[2][2];
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int j = 0; j < 3; ++j)
-			out[a][j] = lamV * tr * g[a][j] + muV * (D[0][j] * g[a][0] + D[1][j] * g[a][1] + D[2][j] * g[a][2]) +
-						muV * (Gab[a][0] * u[0][j] + Gab[a][1] * u[1][j] + Gab[a][2] * u[2][j] + Gab[a][3] * u[3][j]);
-}
-
-__device__ __forceinline__ int pair_slot(int a, int b)
-{
-	// (0,1)->4 (0,2)->5 (0,3)->6 (1,2)->7 (1,3)->8 (2,3)->9 for a < b
-	return (a == 0) ? (3 + b) : (a == 1 ? (5 + b) : 9);
-}
-
-// ------------------------------------------------------------------------------------------
-// Element kernel, FP64. One element per thread.
+// Element kernels
 // ------------------------------------------------------------------------------------------
 template <bool kDebug>
-__global__ void __launch_bounds__(64) k_element_fp64(DevBody b, const double* __restrict__ xn,
-													  const double* __restrict__ vn, const double* __restrict__ xt,
-													  const double* __restrict__ vt, double dt, double alpha,
-													  double beta, double* __restrict__ kslots,
-													  double* __restrict__ rhsE, double* __restrict__ kfull,
-													  double* __restrict__ fE, int* counters)
+__global__ void __launch_bounds__(kElemThreads) k_element_fp64(DevBody b, const double* __restrict__ xn,
+																const double* __restrict__ vn,
+																const double* __restrict__ xt,
+																const double* __restrict__ vt, double dt, double alpha,
+																double beta, double* __restrict__ kslots,
+																double* __restrict__ rhsE, double* __restrict__ kfull,
+																double* __restrict__ fE, int* counters)
 {
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= b.E) return;
 	const int E = b.E;
-	const int4 t4 = b.tets[e];
-	const int nd[4] = {t4.x, t4.y, t4.z, t4.w};
+	elem::ElemIn in;
+	elem::gather(b, e, xn, vn, xt, vt, dt, alpha, beta, in);
 	double g[4][3];
 #pragma unroll
 	for (int a = 0; a < 4; ++a)
 #pragma unroll
 		for (int k = 0; k < 3; ++k) g[a][k] = b.rest[(3 * a + k) * E + e];
 	const double lamV = b.rest[13 * E + e], muV = b.rest[14 * E + e], cm = b.rest[15 * E + e];
+	const int fl = elem::compute<double, kDebug>(in, g, lamV, muV, cm, kslots + (size_t)e * (kSlots * 9), 1,
+												 rhsE + (size_t)e * 12, 1, kDebug ? kfull + (size_t)e * 144 : nullptr,
+												 kDebug ? fE + (size_t)e * 12 : nullptr);
+	if (fl & 1) atomicAdd(&counters[1], 1);
+	if (fl & 2) atomicAdd(&counters[0], 1);
+}
 
-	// Relative positions (node 0 is the origin) and the right-hand-side operands per node:
-	//   uK = -beta v_n + (x_n - x_t - dt v_n),  uM = -alpha v_n - (v_n - v_t)/dt.
-	double p[4][3], q[4][3], uK[4][3], uM[4][3], vv[4][3];
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int k = 0; k < 3; ++k)
-		{
-			const int d = 3 * nd[a] + k;
-			const double xa = xn[d], va = vn[d];
-			p[a][k] = xa - xn[3 * nd[0] + k];
-			q[a][k] = b.xrest[d] - b.xrest[3 * nd[0] + k];
-			uK[a][k] = -beta * va + ((xa - xt[d]) - dt * va);
-			uM[a][k] = -alpha * va - (va - vt[d]) / dt;
-			vv[a][k] = va;
-		}
-	// F = sum_a p_a g_a^T (linear part of P V^-1, Fem3DElementCorotationalTetrahedron.cpp:146).
-	double F[9];
-#pragma unroll
-	for (int i = 0; i < 3; ++i)
-#pragma unroll
-		for (int j = 0; j < 3; ++j) F[3 * i + j] = p[1][i] * g[1][j] + p[2][i] * g[2][j] + p[3][i] * g[3][j];
-	double R[9];
-	if (!polar_newton(F, R))
+// FP32 element kernel of the mixed form. Results are staged in shared memory and written out
+// with coalesced stores (element-major, the layout the assembly gathers).
+__global__ void __launch_bounds__(kElemThreads) k_element_f32(DevBody b, const double* __restrict__ xn,
+															   const double* __restrict__ vn,
+															   const double* __restrict__ xt,
+															   const double* __restrict__ vt, double dt, double alpha,
+															   double beta, float* __restrict__ kslots,
+															   float* __restrict__ rhsE, int* counters)
+{
+	constexpr int kV = kSlots * 9;
+	__shared__ float sks[kV][kElemThreads + 1];
+	__shared__ float srhs[12][kElemThreads + 1];
+	const int e0 = blockIdx.x * kElemThreads;
+	const int e = e0 + threadIdx.x;
+	const int E = b.E;
+	if (e < E)
 	{
-		polar_svd(F, R);
-		atomicAdd(&counters[1], 1);
+		elem::ElemIn in;
+		elem::gather(b, e, xn, vn, xt, vt, dt, alpha, beta, in);
+		float g[4][3];
+#pragma unroll
+		for (int a = 0; a < 4; ++a)
+#pragma unroll
+			for (int k = 0; k < 3; ++k) g[a][k] = b.rest32[(3 * a + k) * E + e];
+		const float lamV = b.rest32[13 * E + e], muV = b.rest32[14 * E + e], cm = b.rest32[15 * E + e];
+		const int fl = elem::compute<float, false>(in, g, lamV, muV, cm, &sks[0][threadIdx.x], kElemThreads + 1,
+												   &srhs[0][threadIdx.x], kElemThreads + 1, nullptr, nullptr);
+		if (fl & 1) atomicAdd(&counters[1], 1);
+		if (fl & 2) atomicAdd(&counters[0], 1);
 	}
-	// S = R^T F (symmetric part), G = (tr(S) I - S) R^T (:208).
-	double S[9];
-#pragma unroll
-	for (int i = 0; i < 3; ++i)
-#pragma unroll
-		for (int j = 0; j < 3; ++j) S[3 * i + j] = R[i] * F[j] + R[3 + i] * F[3 + j] + R[6 + i] * F[6 + j];
+	__syncthreads();
+	const int cnt = min(kElemThreads, E - e0);
+	float* dstK = kslots + (size_t)e0 * kV;
+	for (int idx = threadIdx.x; idx < cnt * kV; idx += kElemThreads)
 	{
-		double s01 = 0.5 * (S[1] + S[3]), s02 = 0.5 * (S[2] + S[6]), s12 = 0.5 * (S[5] + S[7]);
-		S[1] = S[3] = s01;
-		S[2] = S[6] = s02;
-		S[5] = S[7] = s12;
+		const int el = idx / kV;
+		dstK[idx] = sks[idx - el * kV][el];
 	}
-	const double trS = S[0] + S[4] + S[8];
-	double Gm[9];
-#pragma unroll
-	for (int i = 0; i < 3; ++i)
-#pragma unroll
-		for (int j = 0; j < 3; ++j)
-		{
-			double s = 0;
-#pragma unroll
-			for (int k = 0; k < 3; ++k) s += ((i == k ? trS : 0.0) - S[3 * i + k]) * R[3 * j + k];
-			Gm[3 * i + j] = s;
-		}
-	double Gi[9];
-	bool extra;
+	float* dstR = rhsE + (size_t)e0 * 12;
+	for (int idx = threadIdx.x; idx < cnt * 12; idx += kElemThreads)
 	{
-		double C[9];
-		cofactor3(Gm, C);
-		const double d = Gm[0] * C[0] + Gm[1] * C[1] + Gm[2] * C[2];
-		extra = fabs(d) > 1e-12;  // computeInverseAndDetWithCheck threshold (:210)
-		const double id = 1.0 / d;
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-#pragma unroll
-			for (int j = 0; j < 3; ++j) Gi[3 * i + j] = C[3 * j + i] * id;
-		if (!extra) atomicAdd(&counters[0], 1);
-	}
-	// w_c = R^T p_c - q_c (local frame), u~_c = R^T uK_c - w_c.
-	double w[4][3], ut[4][3], wt[4][3];
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-		{
-			w[a][i] = R[i] * p[a][0] + R[3 + i] * p[a][1] + R[6 + i] * p[a][2] - q[a][i];
-			ut[a][i] = R[i] * uK[a][0] + R[3 + i] * uK[a][1] + R[6 + i] * uK[a][2];
-		}
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-		{
-			ut[a][i] -= w[a][i];
-			wt[a][i] = R[i] * w[a][0] + R[3 + i] * w[a][1] + R[6 + i] * w[a][2];  // R^T w
-		}
-	double Gab[4][4];
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int c = 0; c < 4; ++c) Gab[a][c] = g[a][0] * g[c][0] + g[a][1] * g[c][1] + g[a][2] * g[c][2];
-	double h[4][3];
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-#pragma unroll
-		for (int i = 0; i < 3; ++i) h[a][i] = R[3 * i] * g[a][0] + R[3 * i + 1] * g[a][1] + R[3 * i + 2] * g[a][2];
-
-	// y = Krot w = R K0 (R^T w)  (KTimesRx_x0, :276); Ry_a = R y_a.
-	double tmp[4][3], Ry[4][3];
-	k0_apply(g, Gab, lamV, muV, wt, tmp);
-#pragma unroll
-	for (int a = 0; a < 4; ++a)
-	{
-		double ya[3];
-#pragma unroll
-		for (int i = 0; i < 3; ++i) ya[i] = R[3 * i] * tmp[a][0] + R[3 * i + 1] * tmp[a][1] + R[3 * i + 2] * tmp[a][2];
-#pragma unroll
-		for (int i = 0; i < 3; ++i) Ry[a][i] = R[3 * i] * ya[0] + R[3 * i + 1] * ya[1] + R[3 * i + 2] * ya[2];
-	}
-	// zeta = sum_c g_c x w_c, W[i] = sum_c g_c[i] w_c, zt = sum_c g_c x u~_c.
-	double zeta[3] = {0, 0, 0}, zt[3] = {0, 0, 0}, W[3][3];
-#pragma unroll
-	for (int c = 0; c < 4; ++c)
-	{
-		double cr[3];
-		cross3(g[c], w[c], cr);
-		zeta[0] += cr[0];
-		zeta[1] += cr[1];
-		zeta[2] += cr[2];
-		cross3(g[c], ut[c], cr);
-		zt[0] += cr[0];
-		zt[1] += cr[1];
-		zt[2] += cr[2];
-	}
-#pragma unroll
-	for (int i = 0; i < 3; ++i)
-#pragma unroll
-		for (int j = 0; j < 3; ++j) W[i][j] = g[0][i] * w[0][j] + g[1][i] * w[1][j] + g[2][i] * w[2][j] + g[3][i] * w[3][j];
-	// c_bq = g_b x r_q.
-	double cbq[4][3][3];
-#pragma unroll
-	for (int bb = 0; bb < 4; ++bb)
-#pragma unroll
-		for (int qq = 0; qq < 3; ++qq) cross3(g[bb], &R[3 * qq], cbq[bb][qq]);
-	// Right-hand side: rhs_a = R K0(u~)_a + T'_a zt + cm (uM_a + sum uM).
-	double Ku[4][3];
-	k0_apply(g, Gab, lamV, muV, ut, Ku);
-	double KW[4][3];
-	if (kDebug) k0_apply(g, Gab, lamV, muV, w, KW);
-	double sumM[3] = {uM[0][0] + uM[1][0] + uM[2][0] + uM[3][0], uM[0][1] + uM[1][1] + uM[2][1] + uM[3][1],
-					  uM[0][2] + uM[1][2] + uM[2][2] + uM[3][2]};
-	double sumV[3] = {vv[0][0] + vv[1][0] + vv[2][0] + vv[3][0], vv[0][1] + vv[1][1] + vv[2][1] + vv[3][1],
-					  vv[0][2] + vv[1][2] + vv[2][2] + vv[3][2]};
-	double* ks = kslots + (size_t)e * (kSlots * 9);
-
-#pragma unroll 1
-	for (int a = 0; a < 4; ++a)
-	{
-		// L_a = lambdaV g_a zeta^T + muV [rows: g_a x W_i] + muV [sum_c G_ac w_c]x   (local frame)
-		double L[9];
-		double sw[3];
-#pragma unroll
-		for (int k = 0; k < 3; ++k) sw[k] = Gab[a][0] * w[0][k] + Gab[a][1] * w[1][k] + Gab[a][2] * w[2][k] + Gab[a][3] * w[3][k];
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-		{
-			double cr[3];
-			cross3(g[a], W[i], cr);
-#pragma unroll
-			for (int j = 0; j < 3; ++j) L[3 * i + j] = lamV * g[a][i] * zeta[j] + muV * cr[j];
-		}
-		L[1] -= muV * sw[2];
-		L[2] += muV * sw[1];
-		L[3] += muV * sw[2];
-		L[5] -= muV * sw[0];
-		L[6] -= muV * sw[1];
-		L[7] += muV * sw[0];
-		// T_a = -[R y_a]x + R L R^T ; T'_a = T_a G^-1
-		double RL[9], T[9];
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-#pragma unroll
-			for (int j = 0; j < 3; ++j) RL[3 * i + j] = R[3 * i] * L[j] + R[3 * i + 1] * L[3 + j] + R[3 * i + 2] * L[6 + j];
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-#pragma unroll
-			for (int j = 0; j < 3; ++j) T[3 * i + j] = RL[3 * i] * R[3 * j] + RL[3 * i + 1] * R[3 * j + 1] + RL[3 * i + 2] * R[3 * j + 2];
-		T[1] += Ry[a][2];
-		T[2] -= Ry[a][1];
-		T[3] -= Ry[a][2];
-		T[5] += Ry[a][0];
-		T[6] += Ry[a][1];
-		T[7] -= Ry[a][0];
-		double Tp[9];
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-#pragma unroll
-			for (int j = 0; j < 3; ++j)
-				Tp[3 * i + j] = extra ? (T[3 * i] * Gi[j] + T[3 * i + 1] * Gi[3 + j] + T[3 * i + 2] * Gi[6 + j]) : 0.0;
-
-		// rhs block a
-		double ra[3];
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-			ra[i] = R[3 * i] * Ku[a][0] + R[3 * i + 1] * Ku[a][1] + R[3 * i + 2] * Ku[a][2] + Tp[3 * i] * zt[0] +
-					Tp[3 * i + 1] * zt[1] + Tp[3 * i + 2] * zt[2] + cm * (uM[a][i] + sumM[i]);
-#pragma unroll
-		for (int i = 0; i < 3; ++i) rhsE[(size_t)e * 12 + 3 * a + i] = ra[i];
-
-		double kv[3] = {0, 0, 0};
-#pragma unroll 1
-		for (int bb = 0; bb < 4; ++bb)
-		{
-			const bool store = (a == bb) || (nd[a] > nd[bb]);
-			if (!store && !kDebug) continue;
-			double blk[9];
-#pragma unroll
-			for (int i = 0; i < 3; ++i)
-#pragma unroll
-				for (int qq = 0; qq < 3; ++qq)
-				{
-					double v = lamV * h[a][i] * h[bb][qq] + muV * h[bb][i] * h[a][qq] +
-							   Tp[3 * i] * cbq[bb][qq][0] + Tp[3 * i + 1] * cbq[bb][qq][1] + Tp[3 * i + 2] * cbq[bb][qq][2];
-					if (i == qq) v += muV * Gab[a][bb];
-					blk[3 * i + qq] = v;
-				}
-			if (store)
-			{
-				const int slot = (a == bb) ? a : pair_slot(a < bb ? a : bb, a < bb ? bb : a);
-#pragma unroll
-				for (int k = 0; k < 9; ++k) ks[slot * 9 + k] = blk[k];
-			}
-			if (kDebug)
-			{
-#pragma unroll
-				for (int i = 0; i < 3; ++i)
-				{
-#pragma unroll
-					for (int qq = 0; qq < 3; ++qq) kfull[(size_t)e * 144 + (3 * a + i) * 12 + 3 * bb + qq] = blk[3 * i + qq];
-					kv[i] += blk[3 * i] * vv[bb][0] + blk[3 * i + 1] * vv[bb][1] + blk[3 * i + 2] * vv[bb][2];
-				}
-			}
-		}
-		if (kDebug)
-		{
-			// f_e - alpha M0 v - beta K_e v, with f_e = -(R K0(w)_a + T'_a zeta)  (:103-113).
-#pragma unroll
-			for (int i = 0; i < 3; ++i)
-			{
-				double fe = -(R[3 * i] * KW[a][0] + R[3 * i + 1] * KW[a][1] + R[3 * i + 2] * KW[a][2] +
-							  Tp[3 * i] * zeta[0] + Tp[3 * i + 1] * zeta[1] + Tp[3 * i + 2] * zeta[2]);
-				fE[(size_t)e * 12 + 3 * a + i] = fe - alpha * (cm * (vv[a][i] + sumV[i])) - beta * kv[i];
-			}
-		}
+		const int el = idx / 12;
+		dstR[idx] = srhs[idx - el * 12][el];
 	}
 }
 
 // ------------------------------------------------------------------------------------------
 // Assembly: one thread per lower block (I >= J). Sums element blocks in element order, forms
 // S = c1 M + c2 K (c1 = 1/dt + alpha, c2 = dt + beta), applies boundary conditions
-// (OdeState.cpp:197-218: zero rows and columns, diagonal 1) and writes the symmetric BSR matrix
-// that Eigen's selfadjointView<Lower> implies.
+// (OdeState.cpp:197-218: zero rows and columns, diagonal 1) and writes the symmetric matrix
+// that Eigen's selfadjointView<Lower> implies into its SELL-32 slots.
 // ------------------------------------------------------------------------------------------
-__global__ void k_assemble_bsr(DevBody b, const double* __restrict__ ks, double c1, double c2, double* __restrict__ A,
-							   double* __restrict__ invdiag)
+template <typename T>
+__global__ void k_assemble(DevBody b, const T* __restrict__ ks, double c1, double c2, T* __restrict__ A,
+						   T* __restrict__ invdiag)
 {
 	const int L = blockIdx.x * blockDim.x + threadIdx.x;
 	if (L >= b.nl) return;
 	const int4 lb = b.lblk[L];
-	double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+	T s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 	const int k1 = b.cptr[L + 1];
 	for (int k = b.cptr[L]; k < k1; ++k)
 	{
-		const double* src = ks + (size_t)b.cidx[k] * 9;
+		const T* src = ks + (size_t)b.cidx[k] * 9;
 #pragma unroll
 		for (int m = 0; m < 9; ++m) s[m] += src[m];
 	}
-	const double mm = c1 * b.lmass[L];
-	double blk[9];
+	const T mm = T(c1 * b.lmass[L]);
+	const T c2t = T(c2);
+	T blk[9];
 #pragma unroll
-	for (int m = 0; m < 9; ++m) blk[m] = c2 * s[m];
+	for (int m = 0; m < 9; ++m) blk[m] = c2t * s[m];
 	blk[0] += mm;
 	blk[4] += mm;
 	blk[8] += mm;
@@ -546,7 +137,7 @@ __global__ void k_assemble_bsr(DevBody b, const double* __restrict__ ks, double 
 		for (int j = 0; j < 3; ++j)
 		{
 			const int r = 3 * I + i, c = 3 * J + j;
-			if (b.bc[r] | b.bc[c]) blk[3 * i + j] = (r == c) ? 1.0 : 0.0;
+			if (b.bc[r] | b.bc[c]) blk[3 * i + j] = (r == c) ? T(1) : T(0);
 		}
 #pragma unroll
 	for (int m = 0; m < 9; ++m) A[(size_t)lb.z + 32 * m] = blk[m];
@@ -562,13 +153,14 @@ __global__ void k_assemble_bsr(DevBody b, const double* __restrict__ ks, double 
 #pragma unroll
 		for (int i = 0; i < 3; ++i)
 		{
-			const double d = blk[4 * i];
-			invdiag[3 * I + i] = (d != 0.0) ? 1.0 / d : 1.0;  // DiagonalPreconditioner
+			const T d = blk[4 * i];
+			invdiag[3 * I + i] = (d != T(0)) ? T(1) / d : T(1);  // DiagonalPreconditioner
 		}
 	}
 }
 
-__global__ void k_rhs_gather(DevBody b, const double* __restrict__ rhsE, double g0, double g1, double g2, int gravityOn,
+template <typename T>
+__global__ void k_rhs_gather(DevBody b, const T* __restrict__ rhsE, double g0, double g1, double g2, int gravityOn,
 							 double* __restrict__ rhs, int applyBc)
 {
 	const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -578,10 +170,10 @@ __global__ void k_rhs_gather(DevBody b, const double* __restrict__ rhsE, double 
 	for (int k = b.iptr[I]; k < k1; ++k)
 	{
 		const int c = b.iidx[k];
-		const double* src = rhsE + (size_t)(c >> 2) * 12 + 3 * (c & 3);
-		s0 += src[0];
-		s1 += src[1];
-		s2 += src[2];
+		const T* src = rhsE + (size_t)(c >> 2) * 12 + 3 * (c & 3);
+		s0 += double(src[0]);
+		s1 += double(src[1]);
+		s2 += double(src[2]);
 	}
 	if (gravityOn)  // FemRepresentation::addGravityForce (:641-662)
 	{
@@ -618,31 +210,32 @@ __global__ void k_assemble_full_csc(int nnz, const int* __restrict__ sptr, const
 
 // ------------------------------------------------------------------------------------------
 // Deterministic grid reductions: every block writes its partials, the last block to finish
-// (ticket counter) sums them in block order. Results do not depend on scheduling.
+// (ticket counter) sums them in block order. Results do not depend on scheduling. Per-thread and
+// block-level sums use the accumulation type T; the cross-block sum is FP64.
 // ------------------------------------------------------------------------------------------
 struct OpSum
 {
-	__device__ static double apply(double a, double b) { return a + b; }
-	__device__ static double identity() { return 0.0; }
+	template <typename T>
+	__device__ static T apply(T a, T b) { return a + b; }
 };
 struct OpMax
 {
-	__device__ static double apply(double a, double b) { return fmax(a, b); }
-	__device__ static double identity() { return 0.0; }
+	template <typename T>
+	__device__ static T apply(T a, T b) { return a > b ? a : b; }
 };
 
-template <typename Op>
-__device__ __forceinline__ double warp_reduce(double v)
+template <typename Op, typename T>
+__device__ __forceinline__ T warp_reduce(T v)
 {
 #pragma unroll
 	for (int o = 16; o > 0; o >>= 1) v = Op::apply(v, __shfl_xor_sync(0xffffffffu, v, o));
 	return v;
 }
 
-template <typename Op, int NV>
-__device__ __forceinline__ void block_reduce(double (&v)[NV])
+template <typename Op, int NV, typename T>
+__device__ __forceinline__ void block_reduce(T (&v)[NV])
 {
-	__shared__ double sh[NV][32];
+	__shared__ T sh[NV][32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
 	for (int k = 0; k < NV; ++k) v[k] = warp_reduce<Op>(v[k]);
@@ -654,21 +247,21 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV])
 #pragma unroll
 	for (int k = 0; k < NV; ++k)
 	{
-		double x = (lane < nw) ? sh[k][lane] : Op::identity();
+		const T x = (lane < nw) ? sh[k][lane] : T(0);
 		v[k] = warp_reduce<Op>(x);  // every warp holds the block total
 	}
 }
 
-// Returns true in every thread of the last block, with tot[] = grid totals.
-template <typename Op, int NV>
-__device__ bool grid_reduce(double (&v)[NV], double* part, unsigned int* ticket, double (&tot)[NV])
+// Returns true in every thread of the last block, with tot[] = grid totals (FP64).
+template <typename Op, int NV, typename T>
+__device__ bool grid_reduce(T (&v)[NV], double* part, unsigned int* ticket, double (&tot)[NV])
 {
 	__shared__ bool amLast;
-	block_reduce<Op, NV>(v);
+	block_reduce<Op, NV, T>(v);
 	if (threadIdx.x == 0)
 	{
 #pragma unroll
-		for (int k = 0; k < NV; ++k) part[k * gridDim.x + blockIdx.x] = v[k];
+		for (int k = 0; k < NV; ++k) part[k * gridDim.x + blockIdx.x] = double(v[k]);
 		__threadfence();
 		const unsigned int t = atomicAdd(ticket, 1u);
 		amLast = (t == gridDim.x - 1);
@@ -679,17 +272,39 @@ __device__ bool grid_reduce(double (&v)[NV], double* part, unsigned int* ticket,
 #pragma unroll
 	for (int k = 0; k < NV; ++k)
 	{
-		double s = Op::identity();
+		double s = 0.0;
 		for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s = Op::apply(s, __ldcg(&part[k * gridDim.x + i]));
 		tot[k] = s;
 	}
-	block_reduce<Op, NV>(tot);
+	block_reduce<Op, NV, double>(tot);
 	if (threadIdx.x == 0) *ticket = 0u;
 	return true;
 }
 
 // ------------------------------------------------------------------------------------------
-// Conjugate gradient (Eigen's conjugate_gradient with a Jacobi preconditioner, x0 = 0).
+// Sliced-ELL block SpMV: one thread per block row (3 scalar rows), no reductions, every value and
+// column load coalesced across the warp (a warp is one chunk of 32 rows).
+// ------------------------------------------------------------------------------------------
+template <typename T, typename Acc, typename PT>
+__device__ __forceinline__ void sell_row(const MatSellT<T>& A, const PT* __restrict__ p, int rs, Acc& a0, Acc& a1,
+										 Acc& a2)
+{
+	const int c = rs >> 5, lane = rs & 31;
+	const int k0 = A.off[c], k1 = A.off[c + 1];
+	a0 = a1 = a2 = Acc(0);
+	for (int k = k0; k < k1; ++k)
+	{
+		const int J = A.col[k * 32 + lane];
+		const T* vb = A.val + (size_t)k * 288 + lane;
+		const Acc p0 = Acc(p[3 * J]), p1 = Acc(p[3 * J + 1]), p2 = Acc(p[3 * J + 2]);
+		a0 += Acc(vb[0]) * p0 + Acc(vb[32]) * p1 + Acc(vb[64]) * p2;
+		a1 += Acc(vb[96]) * p0 + Acc(vb[128]) * p1 + Acc(vb[160]) * p2;
+		a2 += Acc(vb[192]) * p0 + Acc(vb[224]) * p1 + Acc(vb[256]) * p2;
+	}
+}
+
+// ------------------------------------------------------------------------------------------
+// FP64 conjugate gradient (Eigen's conjugate_gradient with a Jacobi preconditioner, x0 = 0).
 // ------------------------------------------------------------------------------------------
 __global__ void k_cg_init(int n, const double* __restrict__ bvec, const double* __restrict__ invdiag,
 						  double* __restrict__ x, double* __restrict__ r, double* __restrict__ p, CgCtl* ctl,
@@ -726,8 +341,6 @@ __global__ void k_cg_init(int n, const double* __restrict__ bvec, const double* 
 	}
 }
 
-// q = A p on the SELL-32 block matrix: one thread per block row (3 scalar rows), no reductions,
-// every value and column load coalesced across the warp (a warp is one chunk).
 __global__ void __launch_bounds__(256) k_cg_spmv_sell(MatSell3 A, const double* __restrict__ p,
 													   double* __restrict__ q, CgCtl* ctl, double* part)
 {
@@ -737,18 +350,8 @@ __global__ void __launch_bounds__(256) k_cg_spmv_sell(MatSell3 A, const double* 
 	const int nrowsPadded = (A.rows + 31) & ~31;
 	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < nrowsPadded; rs += stride)
 	{
-		const int c = rs >> 5, lane = rs & 31;
-		const int k0 = A.off[c], k1 = A.off[c + 1];
-		double a0 = 0, a1 = 0, a2 = 0;
-		for (int k = k0; k < k1; ++k)
-		{
-			const int J = A.col[k * 32 + lane];
-			const double* vb = A.val + (size_t)k * 288 + lane;
-			const double p0 = p[3 * J], p1 = p[3 * J + 1], p2 = p[3 * J + 2];
-			a0 += vb[0] * p0 + vb[32] * p1 + vb[64] * p2;
-			a1 += vb[96] * p0 + vb[128] * p1 + vb[160] * p2;
-			a2 += vb[192] * p0 + vb[224] * p1 + vb[256] * p2;
-		}
+		double a0, a1, a2;
+		sell_row<double, double, double>(A, p, rs, a0, a1, a2);
 		if (rs < A.rows)
 		{
 			const int I = A.perm[rs];
@@ -847,6 +450,232 @@ __global__ void k_cg_pupdate(int n, const double* __restrict__ invdiag, const do
 		p[i] = invdiag[i] * r[i] + beta * p[i];
 }
 
+// ------------------------------------------------------------------------------------------
+// Mixed-precision CG. Same recurrences as above with r, p, q and the matrix in FP32, the
+// solution x in FP64, and the residual refreshed from the FP64 product b - A x whenever the FP32
+// residual has dropped by reliableDrop (or looks converged). Convergence is decided only on the
+// refreshed FP64 residual: |b - A x|^2 < tol^2 |b|^2.
+// ------------------------------------------------------------------------------------------
+// x = 0, r64 = b; |b|^2.
+__global__ void k_mix_init0(MixBufs m, double tol, int maxIter, double drop)
+{
+	double v[1] = {0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
+	{
+		const double bi = m.b[i];
+		m.x[i] = 0.0;
+		m.r64[i] = bi;
+		v[0] += bi * bi;
+	}
+	double tot[1];
+	if (grid_reduce<OpSum, 1>(v, m.part, &m.ctl->ticket[0], tot) && threadIdx.x == 0)
+	{
+		MixCtl* c = m.ctl;
+		const double bb = tot[0];
+		c->bb = bb;
+		c->rrTrue = bb;
+		c->threshold = fmax(tol * tol * bb, DBL_MIN);
+		c->iter = 0;
+		c->maxIter = maxIter;
+		c->updates = 0;
+		c->pending = 0;
+		c->nonfinite = !isfinite(bb);
+		c->converged = (bb == 0.0 || bb < c->threshold) ? 1 : 0;
+		c->done = (c->converged || c->nonfinite) ? 1 : 0;
+		c->reliableDrop = drop;
+		c->s = sqrt(bb);
+		c->ratio = 0.0;  // no previous direction
+	}
+}
+
+// r32 = r64 / s, p32 = z32 (first direction) or p32 * ratio (rescaled), rz = r32 . z32.
+// Runs at the start (ratio = 0) and after every refresh (pending = 1).
+__device__ __forceinline__ void mix_normalise(const MixBufs& m, bool first)
+{
+	MixCtl* c = m.ctl;
+	const double inv = 1.0 / c->s;
+	const float ratio = float(c->ratio);
+	float v[2] = {0.f, 0.f};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
+	{
+		const float ri = float(m.r64[i] * inv);
+		m.r[i] = ri;
+		const float zi = m.invdiag[i] * ri;
+		m.p[i] = first ? zi : m.p[i] * ratio;
+		v[0] += ri * zi;
+		v[1] += ri * ri;
+	}
+	double tot[2];
+	if (grid_reduce<OpSum, 2>(v, m.part, &c->ticket[3], tot) && threadIdx.x == 0)
+	{
+		if (first)
+		{
+			c->rz = tot[0];
+		}
+		else
+		{
+			// beta in true units: (s_new^2 rz_new) / (s_old^2 rz_old), with p already rescaled.
+			c->beta = tot[0] / (c->rzPend * double(ratio) * double(ratio));
+			c->rz = tot[0];
+			c->iter += 1;
+			c->updates += 1;
+			c->pending = 0;
+			if (c->iter >= c->maxIter)
+			{
+				c->done = 1;
+				c->converged = 0;
+			}
+		}
+		c->rr32 = tot[1];
+		c->rrLast = tot[1];
+	}
+}
+
+__global__ void k_mix_init1(MixBufs m)
+{
+	if (m.ctl->done) return;
+	mix_normalise(m, true);
+}
+
+// q = A p (FP32), pq.
+__global__ void __launch_bounds__(256) k_mix_spmv(MixBufs m)
+{
+	MixCtl* c = m.ctl;
+	if (c->done) return;
+	float v[1] = {0.f};
+	const int stride = gridDim.x * blockDim.x;
+	const int nrowsPadded = (m.A.rows + 31) & ~31;
+	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < nrowsPadded; rs += stride)
+	{
+		float a0, a1, a2;
+		sell_row<float, float, float>(m.A, m.p, rs, a0, a1, a2);
+		if (rs < m.A.rows)
+		{
+			const int I = m.A.perm[rs];
+			m.q[3 * I] = a0;
+			m.q[3 * I + 1] = a1;
+			m.q[3 * I + 2] = a2;
+			v[0] += m.p[3 * I] * a0 + m.p[3 * I + 1] * a1 + m.p[3 * I + 2] * a2;
+		}
+	}
+	double tot[1];
+	if (grid_reduce<OpSum, 1>(v, m.part, &c->ticket[1], tot) && threadIdx.x == 0)
+	{
+		c->pq = tot[0];
+		c->alpha = c->rz / tot[0];
+	}
+}
+
+// x += alpha s p (FP64), r -= alpha q (FP32); decide whether the residual must be refreshed.
+__global__ void k_mix_update(MixBufs m)
+{
+	MixCtl* c = m.ctl;
+	if (c->done) return;
+	const float alpha = float(c->alpha);
+	const double as = c->alpha * c->s;
+	float v[2] = {0.f, 0.f};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
+	{
+		m.x[i] += as * double(m.p[i]);
+		const float ri = m.r[i] - alpha * m.q[i];
+		m.r[i] = ri;
+		v[0] += ri * ri;
+		v[1] += ri * (m.invdiag[i] * ri);
+	}
+	double tot[2];
+	if (grid_reduce<OpSum, 2>(v, m.part, &c->ticket[2], tot) && threadIdx.x == 0)
+	{
+		const double rr = tot[0];
+		c->rr32 = rr;
+		if (!isfinite(rr) || !isfinite(c->alpha))
+		{
+			c->done = 1;
+			c->converged = 0;
+			c->nonfinite = 1;
+		}
+		else if (c->s * c->s * rr < c->threshold || rr < c->reliableDrop * c->rrLast ||
+				 c->iter + 1 >= c->maxIter)
+		{
+			c->pending = 1;  // refresh before the next direction
+			c->rzPend = c->rz;
+		}
+		else
+		{
+			const double rzOld = c->rz;
+			c->rz = tot[1];
+			c->beta = tot[1] / rzOld;
+			c->iter += 1;
+		}
+	}
+}
+
+// r64 = b - A x in FP64 (FP32 matrix values, FP64 products and sums); decide convergence.
+__global__ void __launch_bounds__(256) k_mix_refresh(MixBufs m)
+{
+	MixCtl* c = m.ctl;
+	if (c->done || !c->pending) return;
+	double v[1] = {0.0};
+	const int stride = gridDim.x * blockDim.x;
+	const int nrowsPadded = (m.A.rows + 31) & ~31;
+	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < nrowsPadded; rs += stride)
+	{
+		double a0, a1, a2;
+		sell_row<float, double, double>(m.A, m.x, rs, a0, a1, a2);
+		if (rs < m.A.rows)
+		{
+			const int I = m.A.perm[rs];
+			const double r0 = m.b[3 * I] - a0, r1 = m.b[3 * I + 1] - a1, r2 = m.b[3 * I + 2] - a2;
+			m.r64[3 * I] = r0;
+			m.r64[3 * I + 1] = r1;
+			m.r64[3 * I + 2] = r2;
+			v[0] += r0 * r0 + r1 * r1 + r2 * r2;
+		}
+	}
+	double tot[1];
+	if (grid_reduce<OpSum, 1>(v, m.part, &c->ticket[1], tot) && threadIdx.x == 0)
+	{
+		const double rr = tot[0];
+		c->rrTrue = rr;
+		if (rr < c->threshold)
+		{
+			c->done = 1;  // like Eigen, the converging iteration is not counted
+			c->converged = 1;
+			c->updates += 1;
+		}
+		else if (!isfinite(rr) || c->iter + 1 >= c->maxIter)
+		{
+			c->done = 1;
+			c->converged = 0;
+			c->iter += 1;
+			if (!isfinite(rr)) c->nonfinite = 1;
+		}
+		else
+		{
+			const double sNew = sqrt(rr);
+			c->ratio = c->s / sNew;
+			c->s = sNew;
+		}
+	}
+}
+
+__global__ void k_mix_rescale(MixBufs m)
+{
+	if (m.ctl->done || !m.ctl->pending) return;
+	mix_normalise(m, false);
+}
+
+__global__ void k_mix_pupdate(MixBufs m)
+{
+	const MixCtl* c = m.ctl;
+	if (c->done) return;
+	const float beta = float(c->beta);
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
+		m.p[i] = m.invdiag[i] * m.r[i] + beta * m.p[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// State
+// ------------------------------------------------------------------------------------------
 // v_n += dv; x_n = x_t + dt v_n (OdeSolverEulerImplicit.cpp:98-99); optional Newton variation.
 __global__ void k_state_update(int n, const double* __restrict__ dv, double* __restrict__ dvPrev,
 							   const double* __restrict__ xt, double* __restrict__ xn, double* __restrict__ vn,
@@ -908,25 +737,51 @@ void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, c
 {
 	if (b.E == 0) return;
 	if (kfull)
-		k_element_fp64<true><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE, kfull, fE,
-															 counters);
+		k_element_fp64<true><<<blocks(b.E, kElemThreads), kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta,
+																				 kslots, rhsE, kfull, fE, counters);
 	else
-		k_element_fp64<false><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE, nullptr,
-															  nullptr, counters);
+		k_element_fp64<false><<<blocks(b.E, kElemThreads), kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta,
+																				  kslots, rhsE, nullptr, nullptr,
+																				  counters);
 }
 
-void launch_assemble_bsr(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
-						 cudaStream_t s)
+void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
+						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
+						cudaStream_t s)
+{
+	if (b.E == 0) return;
+	k_element_f32<<<blocks(b.E, kElemThreads), kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																	  counters);
+}
+
+void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
+					 cudaStream_t s)
 {
 	if (b.nl == 0) return;
-	k_assemble_bsr<<<blocks(b.nl, 128), 128, 0, s>>>(b, kslots, c1, c2, A, invdiag);
+	k_assemble<double><<<blocks(b.nl, 128), 128, 0, s>>>(b, kslots, c1, c2, A, invdiag);
+}
+
+void launch_assemble(const DevBody& b, const float* kslots, double c1, double c2, float* A, float* invdiag,
+					 cudaStream_t s)
+{
+	if (b.nl == 0) return;
+	k_assemble<float><<<blocks(b.nl, 128), 128, 0, s>>>(b, kslots, c1, c2, A, invdiag);
 }
 
 void launch_rhs_gather(const DevBody& b, const double* rhsE, const double* gravity, int gravityOn, double* rhs,
 					   int applyBc, cudaStream_t s)
 {
 	if (b.N == 0) return;
-	k_rhs_gather<<<blocks(b.N, 128), 128, 0, s>>>(b, rhsE, gravity[0], gravity[1], gravity[2], gravityOn, rhs, applyBc);
+	k_rhs_gather<double><<<blocks(b.N, 128), 128, 0, s>>>(b, rhsE, gravity[0], gravity[1], gravity[2], gravityOn, rhs,
+														  applyBc);
+}
+
+void launch_rhs_gather(const DevBody& b, const float* rhsE, const double* gravity, int gravityOn, double* rhs,
+					   int applyBc, cudaStream_t s)
+{
+	if (b.N == 0) return;
+	k_rhs_gather<float><<<blocks(b.N, 128), 128, 0, s>>>(b, rhsE, gravity[0], gravity[1], gravity[2], gravityOn, rhs,
+														 applyBc);
 }
 
 void launch_assemble_full_csc(int nnz, const int* sptr, const int* sidx, const int* srow, const int* scol,
@@ -962,6 +817,23 @@ void launch_cg_update(int n, const double* invdiag, const double* p, const doubl
 void launch_cg_pupdate(int n, const double* invdiag, const double* r, double* p, CgCtl* ctl, const Launch& L)
 {
 	k_cg_pupdate<<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, invdiag, r, p, ctl);
+}
+
+void launch_mix_init(const MixBufs& m, double tol, int maxIter, double reliableDrop, const Launch& L)
+{
+	k_mix_init0<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m, tol, maxIter, reliableDrop);
+	k_mix_init1<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
+}
+
+void launch_mix_iteration(const MixBufs& m, const Launch& L, cudaEvent_t evA, cudaEvent_t evB)
+{
+	if (evA) cudaEventRecord(evA, L.stream);
+	k_mix_spmv<<<L.vecGrid, 256, 0, L.stream>>>(m);
+	if (evB) cudaEventRecord(evB, L.stream);
+	k_mix_update<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
+	k_mix_refresh<<<L.vecGrid, 256, 0, L.stream>>>(m);
+	k_mix_rescale<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
+	k_mix_pupdate<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
 }
 
 void launch_state_update(int n, const double* dv, double* dvPrev, const double* xt, double* xn, double* vn,

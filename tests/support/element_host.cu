@@ -1,0 +1,106 @@
+// Test support only: the device element math of gbfem_element.cuh compiled for the host, so the
+// CPU test suite can compare it (FP64 and FP32) with the oracle element by element.
+#include <cmath>
+#include <cstring>
+
+#include "gbfem_element.cuh"
+
+namespace {
+double det33(const double m[3][3])
+{
+	return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+		   m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+}
+bool inverse44(const double a[4][4], double inv[4][4])
+{
+	double cof[4][4];
+	for (int i = 0; i < 4; ++i)
+		for (int j = 0; j < 4; ++j)
+		{
+			double m[3][3];
+			int r = 0;
+			for (int ii = 0; ii < 4; ++ii)
+			{
+				if (ii == i) continue;
+				int c = 0;
+				for (int jj = 0; jj < 4; ++jj)
+					if (jj != j) m[r][c++] = a[ii][jj];
+				++r;
+			}
+			cof[i][j] = (((i + j) & 1) ? -1.0 : 1.0) * det33(m);
+		}
+	double d = 0;
+	for (int j = 0; j < 4; ++j) d += a[0][j] * cof[0][j];
+	if (!(std::fabs(d) > 1e-12)) return false;
+	for (int i = 0; i < 4; ++i)
+		for (int j = 0; j < 4; ++j) inv[i][j] = cof[j][i] / d;
+	return true;
+}
+double det3v(const double* a, const double* b, const double* c)
+{
+	return a[0] * b[1] * c[2] + a[2] * b[0] * c[1] + a[1] * b[2] * c[0] - a[2] * b[1] * c[0] - a[1] * b[0] * c[2] -
+		   a[0] * b[2] * c[1];
+}
+
+template <typename T>
+int run(const double* x0, const double* x, const double* v, const double* xt, const double* vt, const int* nd,
+		double E, double nu, double rho, double dt, double alpha, double beta, double* K, double* rhs, double* f,
+		double* R9)
+{
+	double V[4][4], Vi[4][4];
+	for (int a = 0; a < 4; ++a)
+	{
+		for (int k = 0; k < 3; ++k) V[k][a] = x0[3 * a + k];
+		V[3][a] = 1.0;
+	}
+	if (!inverse44(V, Vi)) return -1;
+	const double vol = (det3v(x0 + 3, x0 + 6, x0 + 9) - det3v(x0, x0 + 6, x0 + 9) + det3v(x0, x0 + 3, x0 + 9) -
+						det3v(x0, x0 + 3, x0 + 6)) / 6.0;
+	const double lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+	const double mu = E / (2.0 * (1 + nu));
+	gbfem::elem::ElemIn in;
+	for (int a = 0; a < 4; ++a)
+	{
+		in.nd[a] = nd[a];
+		for (int k = 0; k < 3; ++k)
+		{
+			in.p[a][k] = x[3 * a + k] - x[k];
+			in.q[a][k] = x0[3 * a + k] - x0[k];
+			const double va = v[3 * a + k];
+			in.uK[a][k] = -beta * va + ((x[3 * a + k] - xt[3 * a + k]) - dt * va);
+			in.uM[a][k] = -alpha * va - (va - vt[3 * a + k]) / dt;
+			in.vv[a][k] = va;
+		}
+	}
+	in.alphaDbg = alpha;
+	in.betaDbg = beta;
+	T g[4][3];
+	for (int a = 0; a < 4; ++a)
+		for (int k = 0; k < 3; ++k) g[a][k] = T(Vi[a][k]);
+	T ks[90], rh[12];
+	double fd[12];
+	int fl = gbfem::elem::compute<T, true>(in, g, T(lambda * vol), T(mu * vol), T(vol * rho / 20.0), ks, 1, rh, 1, K,
+										   fd);
+	for (int i = 0; i < 12; ++i)
+	{
+		rhs[i] = double(rh[i]);
+		f[i] = fd[i];
+	}
+	// R from the Newton polar (or its fallback) on the same F
+	T F[9], Rt[9];
+	for (int i = 0; i < 3; ++i)
+		for (int j = 0; j < 3; ++j)
+			F[3 * i + j] = T(in.p[1][i]) * g[1][j] + T(in.p[2][i]) * g[2][j] + T(in.p[3][i]) * g[3][j];
+	if (!gbfem::elem::polar_newton(F, Rt)) gbfem::elem::polar_svd(F, Rt);
+	for (int k = 0; k < 9; ++k) R9[k] = double(Rt[k]);
+	return fl;
+}
+}  // namespace
+
+extern "C" int gbfem_host_element(int fp32, const double* x0, const double* x, const double* v, const double* xt,
+								  const double* vt, const int* nd, double E, double nu, double rho, double dt,
+								  double alpha, double beta, double* K144, double* rhs12, double* f12, double* R9)
+{
+	return fp32 ? run<float>(x0, x, v, xt, vt, nd, E, nu, rho, dt, alpha, beta, K144, rhs12, f12, R9)
+				: run<double>(x0, x, v, xt, vt, nd, E, nu, rho, dt, alpha, beta, K144, rhs12, f12, R9);
+}

@@ -130,3 +130,56 @@ def test_cg_max_iterations_behaviour(gpu_lib):
     ox, oit, ores, ost = O.cg_solve(colptr, rowidx, vals, b, tol=1e-10, max_iter=50)
     assert oit == it
     assert np.linalg.norm(x - ox) <= 1e-9 * np.linalg.norm(ox)
+
+
+def _run_pair(scene, steps, **kw):
+    g = Body.from_scene(scene, **kw)
+    o = O.OracleModel.from_scene(scene)
+    x0 = scene.mesh.nodes.ravel().copy()
+    errs = []
+    for k in range(steps):
+        if scene.driven_dofs is not None:
+            vals = scene.driven_values(k)
+            g.set_velocities(scene.driven_dofs, vals)
+            x, v = o.state()
+            v[scene.driven_dofs] = vals
+            o.set_state(None, v)
+        assert g.step(scene.dt, 1) == _lib.GBFEM_OK
+        assert o.step(scene.dt) == 0
+        gx, _ = g.state()
+        ox, _ = o.state()
+        errs.append(rel(gx - x0, ox - x0))
+    return errs, g
+
+
+def test_mixed_cube_displacement_error(gpu_lib):
+    """Mixed precision (FP32 element + CG, FP64 refinement) vs the FP64 oracle: <= 1e-6 rel. displacement."""
+    s = mesh.scene_cube(10, 10, 10)
+    errs, g = _run_pair(s, 100, precision=_lib.PRECISION_MIXED)
+    st = g.stats()
+    print("mixed cube: max rel disp err %.3e final %.3e sweeps %d" % (max(errs), errs[-1], st["refinement_sweeps"]))
+    assert max(errs) <= 1e-6
+
+
+def test_mixed_bar_displacement_error(gpu_lib):
+    """Driven compression bar (per-tet E and nu): mixed vs oracle over 20 steps."""
+    s = mesh.scene_bar_compression(a=6, b=6, c=24, ramp_steps=50)
+    errs, g = _run_pair(s, 20, precision=_lib.PRECISION_MIXED)
+    print("mixed bar: max rel disp err %.3e" % max(errs))
+    assert max(errs) <= 1e-6
+
+
+def test_mixed_matches_fp64_gpu_and_is_deterministic(gpu_lib):
+    s = mesh.scene_cube(6, 6, 8)
+    a = Body.from_scene(s, precision=_lib.PRECISION_MIXED)
+    b = Body.from_scene(s, precision=_lib.PRECISION_MIXED)
+    c = Body.from_scene(s)
+    for m in (a, b, c):
+        assert m.step(s.dt, 15) == _lib.GBFEM_OK
+    xa, va = a.state()
+    xb, vb = b.state()
+    xc, vc = c.state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    x0 = s.mesh.nodes.ravel()
+    assert rel(xa - x0, xc - x0) < 1e-6
+    assert a.stats()["cg_relative_residual"] < 1e-10
