@@ -168,6 +168,28 @@ GBFEM_API gbfem_status gbfem_cg_solve(gbfem_cg cg, const double* b, double* x, i
 									  double* relative_residual);
 GBFEM_API gbfem_status gbfem_cg_destroy(gbfem_cg cg);
 
+/* ---- The same Jacobi-PCG solve for callers that must not allocate memory.
+ * No counterpart in the reference. Some callers cannot call cudaMalloc once they are running: the
+ * fixed-rate physics and haptics loops of a surgical simulator (where an allocator call can block
+ * or synchronise the device at an unpredictable moment) and hosts that reserve all device memory
+ * at start-up. This entry point takes the matrix and vectors already in device memory and uses a
+ * scratch area that is part of the loaded library (a fixed array in device memory, on every GPU
+ * that loads the library, kept until the process exits), so it makes no cudaMalloc, cudaFree,
+ * pinned-memory or other allocating call.
+ *   rowptr[n+1], col[nnz], values[nnz]: the full symmetric matrix in CSR form, device pointers
+ *   b[n] (in), x[n] (out): device pointers;  stream: a cudaStream_t (NULL: default stream)
+ * The solve is the one gbfem_cg_solve runs (zero initial guess, Jacobi preconditioner, stop when
+ * |r|^2 < max(tol^2 |b|^2, DBL_MIN) or after max_iterations, <= 0 meaning 2n).
+ * Limits: n <= GBFEM_NOALLOC_MAX_DOFS, else GBFEM_INVALID_ARG (message from gbfem_last_error(NULL)).
+ * The first call on a device looks up the scratch area's device address with that device current;
+ * make that first call before any stream capture. Every call shares the one scratch area:
+ * calls that overlap on the same GPU race and must be serialised by the caller. */
+#define GBFEM_NOALLOC_MAX_DOFS 262144
+GBFEM_API gbfem_status gbfem_cg_solve_noalloc(int32_t n, const int32_t* rowptr, const int32_t* col,
+											  const double* values, const double* b, double* x, double tolerance,
+											  int32_t max_iterations, void* stream, int32_t* iterations,
+											  double* relative_residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,7 @@ EXPORTED = [
     "gbfem_set_state", "gbfem_set_velocities", "gbfem_set_velocities_device", "gbfem_device_state", "gbfem_stream", "gbfem_reactivate",
     "gbfem_get_sizes", "gbfem_get_pattern", "gbfem_get_scatter", "gbfem_get_system", "gbfem_last_error",
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
-    "gbfem_cg_destroy",
+    "gbfem_cg_destroy", "gbfem_cg_solve_noalloc",
 ]
 
 
@@ -130,6 +130,10 @@ def load():
         "gbfem_cg_set_max_iterations": (S, [H, ctypes.c_int32]),
         "gbfem_cg_solve": (S, [H, D, D, I32, D]),
         "gbfem_cg_destroy": (S, [H]),
+        "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
+                                       ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                       ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -204,6 +204,11 @@ struct gbfem_handle_s
 	}
 };
 
+namespace gbfem {
+// Message returned by gbfem_last_error(NULL, ...) (create failures, the no-allocation solve).
+void set_global_error(const std::string& msg) { g_lastCreateError = msg; }
+}  // namespace gbfem
+
 namespace {
 
 gbfem_status fail(gbfem_handle h, gbfem_status st, const std::string& msg)

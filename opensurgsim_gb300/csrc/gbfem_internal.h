@@ -152,6 +152,6 @@ void launch_validity(int n, const double* x, const double* v, CgCtl* ctl, double
 void launch_scatter_values(int count, const int* idx, const double* vals, double* dst, cudaStream_t s);
 
 // Partial-sum buffer size needed by the reductions for a given vecGrid.
-inline int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }
+constexpr int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }
 
 }  // namespace gbfem
