@@ -1,0 +1,47 @@
+"""The multi-process path of bench.py (replicas, no data-path collective) on CPU with gloo."""
+
+import os
+import socket
+
+import pytest
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import bench
+
+    r, w, lr = bench.dist_env()
+    assert (r, w, lr) == (rank, world, rank)
+    d = bench.Dist(w)
+    d.barrier()
+    mx = d.reduce(10.0 * (rank + 1), "max")
+    sm = d.reduce(100.0 + rank, "sum")
+    d.barrier()
+    d.close()
+    out.put((rank, mx, sm))
+
+
+def test_two_rank_barrier_and_reductions():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    res = sorted(q.get(timeout=10) for _ in range(2))
+    assert res == [(0, 20.0, 201.0), (1, 20.0, 201.0)]

@@ -1,0 +1,128 @@
+"""The GPU element math (gbfem_element.cuh), compiled for the host, against the oracle (CPU)."""
+
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "support", "element_host.cu")
+LIB = os.path.join(HERE, "support", "libelemhost.so")
+
+
+@pytest.fixture(scope="module")
+def elem():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    deps = [SRC, os.path.join(ROOT, "opensurgsim_gb300", "csrc", "gbfem_element.cuh")]
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(d) for d in deps):
+        subprocess.run([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                        "-I" + os.path.join(ROOT, "opensurgsim_gb300", "csrc"), "-o", LIB, SRC], check=True,
+                       capture_output=True)
+    L = ctypes.CDLL(LIB)
+    D = ctypes.POINTER(ctypes.c_double)
+    L.gbfem_host_element.argtypes = [ctypes.c_int, D, D, D, D, D, ctypes.POINTER(ctypes.c_int)] + \
+        [ctypes.c_double] * 6 + [D, D, D, D]
+    L.gbfem_host_element.restype = ctypes.c_int
+
+    def run(fp32, x0, x, v=None, E=1e6, nu=0.45, rho=1000.0, dt=1e-3, alpha=0.0, beta=0.0, nd=(0, 1, 2, 3)):
+        def d(a):
+            return np.ascontiguousarray(a, dtype=np.float64).ravel()
+        x0, x = d(x0), d(x)
+        v = np.zeros(12) if v is None else d(v)
+        K, rhs, f, R = np.zeros(144), np.zeros(12), np.zeros(12), np.zeros(9)
+        p = lambda a: a.ctypes.data_as(D)  # noqa: E731
+        fl = L.gbfem_host_element(fp32, p(x0), p(x), p(v), p(x), p(v), (ctypes.c_int * 4)(*nd), E, nu, rho, dt,
+                                  alpha, beta, p(K), p(rhs), p(f), p(R))
+        assert fl >= 0
+        return K.reshape(12, 12), f, rhs, R.reshape(3, 3), fl
+
+    return run
+
+
+def rot(angle, axis):
+    axis = np.asarray(axis, float)
+    axis = axis / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * K @ K
+
+
+X0 = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+ROT = rot(4.1415, [1.0, 0.2, -0.3])
+DELTA = np.array([[0.01, -0.02, 0.005], [-0.01, -0.01, -0.03], [0.0, -0.015, 0.03]])
+
+
+@pytest.mark.parametrize("case", ["identity", "rotation+translation", "deformed", "scale45"])
+def test_fp64_element_matches_oracle(elem, case):
+    x = {"identity": X0, "rotation+translation": (ROT @ X0.T).T + [1.2, 2.3, 3.4],
+         "deformed": (ROT @ X0.T).T + [1.2, 2.3, 3.4] + DELTA[np.arange(4) % 3],
+         "scale45": (45.3 * ROT @ X0.T).T + [1.2, 2.3, 3.4]}[case]
+    o = O.tet_compute(X0, x, 1e6, 0.45, 1000.0)
+    K, f, rhs, R, fl = elem(0, X0, x)
+    assert fl == 0
+    assert np.abs(K - o["K"]).max() <= 1e-13 * np.abs(o["K"]).max()  # includes the KTimesRx_x0 quirk
+    assert np.abs(R - o["R"]).max() < 1e-13
+    # the reference's force test uses an absolute 1e-8 (epsilonAddForce); rigid motions leave only
+    # rounding noise, which is smaller here (relative coordinates) than in the oracle
+    assert np.linalg.norm(f - o["f"]) <= max(1e-8, 1e-12 * np.linalg.norm(o["f"]))
+
+
+def test_tangent_is_not_symmetric_like_the_reference(elem):
+    x = (ROT @ X0.T).T + DELTA[np.arange(4) % 3] * 3
+    K, *_ = elem(0, X0, x)
+    o = O.tet_compute(X0, x, 1e6, 0.45, 1000.0)
+    asym = np.abs(o["K"] - o["K"].T).max() / np.abs(o["K"]).max()
+    assert asym > 1e-6  # the reference's tangent is non-symmetric (rotated stiffness in KTimesRx_x0)
+    assert np.abs((K - K.T) - (o["K"] - o["K"].T)).max() <= 1e-12 * np.abs(o["K"]).max()
+
+
+def test_rhs_combines_force_damping_and_implicit_terms(elem):
+    """rhs_e = f_e + K_e (-(beta + dt) v) + M0 (-alpha v) on the first Newton iteration."""
+    rng = np.random.default_rng(7)
+    x = X0 * 0.01 + rng.normal(0, 2e-4, (4, 3))
+    v = rng.normal(0, 0.05, 12)
+    dt, a, b = 1e-3, 0.01, 0.001
+    o = O.tet_compute(X0 * 0.01, x, 1e5, 0.45, 1000.0)
+    K, f, rhs, R, fl = elem(0, X0 * 0.01, x, v, E=1e5, dt=dt, alpha=a, beta=b)
+    expected = o["f"] + o["K"] @ (-(b + dt) * v) + o["M"] @ (-a * v)
+    assert np.linalg.norm(rhs - expected) <= 1e-10 * np.linalg.norm(expected)
+
+
+def test_fp32_element_accuracy(elem):
+    """Mixed form: FP32 tangent to ~1e-7 and FP32 force to ~1e-7 relative on realistic elements
+    (h = 4 mm, 1% strain, rotated), thanks to the FP64 Gram-difference strain."""
+    rng = np.random.default_rng(1)
+    ek, ef = [], []
+    for _ in range(100):
+        h = 0.004
+        xr = X0 * h + rng.uniform(-0.1 * h, 0.1 * h, (4, 3)) + rng.uniform(0, 0.1, 3)
+        F = np.eye(3) + 1e-2 * rng.standard_normal((3, 3))
+        Rm = rot(rng.uniform(0, 0.3), rng.standard_normal(3))
+        c = xr.mean(0)
+        x = ((Rm @ F) @ (xr - c).T).T + c
+        o = O.tet_compute(xr, x, 1e5, 0.45, 1000.0)
+        K, f, rhs, R, fl = elem(1, xr, x, E=1e5)
+        ek.append(np.abs(K - o["K"]).max() / np.abs(o["K"]).max())
+        ef.append(np.linalg.norm(f - o["f"]) / np.linalg.norm(o["f"]))
+    print("fp32 K rel err median %.2e max %.2e; f median %.2e max %.2e" % (np.median(ek), max(ek), np.median(ef),
+                                                                           max(ef)))
+    assert np.median(ek) < 5e-7 and max(ek) < 2e-6
+    assert np.median(ef) < 5e-7 and max(ef) < 1e-5
+
+
+def test_inverted_element_takes_svd_fallback(elem):
+    x = X0.copy()
+    x[3, 2] = -0.5  # node 3 pushed through the opposite face: det F < 0
+    K, f, rhs, R, fl = elem(0, X0, x)
+    assert fl & 1
+    o = O.tet_compute(X0, x, 1e6, 0.45, 1000.0)
+    assert abs(np.linalg.det(R) - 1) < 1e-12
+    assert np.abs(R - o["R"]).max() < 1e-10
+    assert np.abs(K - o["K"]).max() <= 1e-10 * np.abs(o["K"]).max()

@@ -1,0 +1,137 @@
+"""The oracle's implicit-Euler / CG semantics against the reference's own tests (CPU)."""
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from opensurgsim_gb300 import mesh
+
+
+def approx(a, b, prec):
+    return np.linalg.norm(a - b) <= prec * min(np.linalg.norm(a), np.linalg.norm(b))
+
+
+def cg_matrix(n=18):
+    # LinearSparseSolveAndInverseTests.cpp:57-88
+    r, c = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    A = np.fmod(10.3 * np.cos((r * c).astype(float)) + 3.24, 10.0)
+    b = np.fmod(-4.1 * np.arange(n) ** 2 + 3.46, 5.0)
+    colptr = np.arange(0, n * n + 1, n, dtype=np.int32)
+    rowidx = np.tile(np.arange(n, dtype=np.int32), n)
+    return A, b, colptr, rowidx, A.T.ravel().copy()
+
+
+def test_cg_max_iterations_behaviour():
+    """SparseCGMatrixComponentsTest (LinearSparseSolveAndInverseTests.cpp:162-193)."""
+    A, b, colptr, rowidx, vals = cg_matrix()
+    expected = np.linalg.solve(A, b)
+    x, it, err, st = O.cg_solve(colptr, rowidx, vals, b)  # Eigen defaults: tol = eps, maxIter = 2n
+    assert approx(x, expected, 1e-5)
+    x, it, err, st = O.cg_solve(colptr, rowidx, vals, b, tol=1e-10, max_iter=18)
+    assert approx(x, expected, 1e-5) and not approx(x, expected, 1e-10)
+    assert st == O.ORC_CG_MAXITER and it == 18
+    x, it, err, st = O.cg_solve(colptr, rowidx, vals, b, tol=1e-10, max_iter=50)
+    assert approx(x, expected, 1e-10) and st == O.ORC_OK
+
+
+def test_cg_reads_only_lower_triangle_and_zero_rhs():
+    A, b, colptr, rowidx, vals = cg_matrix(6)
+    A = A @ A.T + 6 * np.eye(6)  # SPD
+    vals = A.T.ravel().copy()
+    x_ref, *_ = O.cg_solve(colptr, rowidx, vals, b, tol=1e-14)
+    junk = vals.copy().reshape(6, 6)  # column-major: junk[c, r] = A[r, c]
+    for c in range(6):
+        for r in range(c):
+            junk[c, r] = 1e6  # upper triangle entries (r < c) must be ignored
+    x, *_ = O.cg_solve(colptr, rowidx, junk.ravel(), b, tol=1e-14)
+    assert np.allclose(x, x_ref, rtol=1e-12, atol=1e-14)
+    x, it, err, st = O.cg_solve(colptr, rowidx, vals, np.zeros(6), tol=1e-10)
+    assert np.all(x == 0) and it == 0 and st == O.ORC_OK
+
+
+@pytest.mark.parametrize("visc", [0.0, 0.1])
+def test_mass_point_backward_euler(visc):
+    """OdeSolverEulerImplicitTests.cpp:58-115 (MassPoint, mass 0.456, gravity (0,-9.81,0))."""
+    dt, m, g = 1e-3, 0.456, np.array([0.0, -9.81, 0.0])
+    x0, v0 = np.zeros(3), np.zeros(3)
+    x1, v1 = O.masspoint_step(visc, dt, x0, v0)
+    expected_v = (g * dt + v0) / (1.0 + dt * visc / m)
+    assert np.allclose(v1, expected_v, rtol=1e-12, atol=1e-15)
+    assert np.allclose(x1, v1 * dt + x0, rtol=1e-12, atol=1e-15)
+    x2, v2 = O.masspoint_step(visc, dt, x1, v1)
+    assert np.allclose(v2, (g * dt + v1) / (1.0 + dt * visc / m), rtol=1e-12)
+
+
+def test_free_fall_uniform_velocity():
+    """No boundary conditions: K annihilates translations and the consistent mass has lumped row
+    sums, so the first step is a uniform velocity g dt / (1 + alpha dt)."""
+    s = mesh.scene_cube(3, 3, 3)
+    s.mesh.bc_dofs = np.zeros(0, dtype=np.int32)
+    m = O.OracleModel(s.mesh, rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0, 0, -9.81), cg_tolerance=1e-14)
+    assert m.step(1e-3) == O.ORC_OK
+    x, v = m.state()
+    expected = -9.81 * 1e-3 / (1 + 0.01 * 1e-3)
+    assert np.allclose(v.reshape(-1, 3)[:, 2], expected, rtol=1e-9)
+    assert np.allclose(v.reshape(-1, 3)[:, :2], 0, atol=1e-12)
+
+
+def test_rigid_rotation_has_no_elastic_force():
+    s = mesh.scene_cube(2, 2, 2)
+    m = O.OracleModel(s.mesh, gravity_enabled=False, cg_tolerance=1e-14)
+    R = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    x = (R @ s.mesh.nodes.T).T.ravel() + 0.3
+    m.set_state(x, np.zeros_like(x))
+    m.step(1e-3)
+    f = m.system()["f"]
+    assert np.abs(f).max() < 1e-9 * s.mesh.young[0] * 0.01
+
+
+def test_boundary_conditions_and_pattern():
+    s = mesh.scene_cube(3, 2, 4)
+    m = O.OracleModel.from_scene(s)
+    assert m.step(s.dt, 3) == O.ORC_OK
+    x, v = m.state()
+    bc = s.mesh.bc_dofs
+    assert np.array_equal(x[bc], s.mesh.nodes.ravel()[bc]) and np.all(v[bc] == 0)
+    colptr, rowidx = m.pattern()
+    sy = m.system()
+    S = np.zeros((m.n, m.n))
+    for c in range(m.n):
+        rows = rowidx[colptr[c]:colptr[c + 1]]
+        assert np.all(np.diff(rows) > 0)  # sorted, unique
+        S[rows, c] = sy["S"][colptr[c]:colptr[c + 1]]
+    P = np.zeros_like(S, dtype=bool)
+    for c in range(m.n):
+        P[rowidx[colptr[c]:colptr[c + 1]], c] = True
+    assert np.array_equal(P, P.T)  # structurally symmetric pattern
+    for d in bc:  # OdeState::applyBoundaryConditionsToMatrix: zero row/column, diagonal 1
+        row = S[d].copy()
+        row[d] = 0
+        assert np.all(row == 0) and np.all(S[:, d][np.arange(m.n) != d] == 0) and S[d, d] == 1.0
+    assert np.all(sy["rhs"][bc] == 0)
+
+
+def test_nonfinite_state_deactivates():
+    s = mesh.scene_cube(2, 2, 2)
+    m = O.OracleModel.from_scene(s)
+    x, v = m.state()
+    v[4] = np.nan
+    m.set_state(None, v)
+    assert m.step(1e-3) == O.ORC_NONFINITE
+    assert m.step(1e-3) == O.ORC_NONFINITE
+
+
+def test_scatter_map_points_at_block_entries():
+    s = mesh.scene_cube(2, 2, 2)
+    m = O.OracleModel.from_scene(s)
+    colptr, rowidx = m.pattern()
+    sc = m.scatter().reshape(-1, 12, 12)
+    tets = s.mesh.tets
+    for e in range(tets.shape[0]):
+        for a in range(4):
+            for i in range(3):
+                for b in range(4):
+                    for j in range(3):
+                        k = sc[e, 3 * a + i, 3 * b + j]
+                        col = 3 * tets[e, b] + j
+                        assert colptr[col] <= k < colptr[col + 1] and rowidx[k] == 3 * tets[e, a] + i
