@@ -140,6 +140,21 @@ GBFEM_API gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v
 GBFEM_API gbfem_status gbfem_stream(gbfem_handle h, void** stream);
 GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
 
+/* ---- Batching: many independent meshes (each its own OpenSurgSim representation, stepped like
+ * one FreeMotion pass over them, FreeMotion.cpp:55-80) in one body. Node ids, boundary-condition
+ * dofs and states are concatenated in mesh order; every mesh keeps its own CG scalars and
+ * convergence test, and one persistent launch solves all of them. Requires
+ * GBFEM_PRECISION_MIXED. gbfem_step, gbfem_get_state, gbfem_set_velocities ... act on the batch. */
+GBFEM_API gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, const gbfem_params* params,
+										  gbfem_handle* out);
+/* Number of meshes and their node / tet offsets (count + 1 entries each) in the batch. */
+GBFEM_API gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets,
+										int32_t* tet_offsets);
+/* Per mesh, over the last gbfem_step call: CG iterations, FP64 residual refreshes, converged (all
+ * steps), worst relative residual. Arrays of `count` entries (any may be NULL). */
+GBFEM_API gbfem_status gbfem_batch_segment_stats(gbfem_handle h, int32_t* iterations, int32_t* refreshes,
+												 int32_t* converged, double* relative_residual);
+
 /* Sizes: dofs n = 3*num_nodes, scalar nonzeros of the pattern. */
 GBFEM_API gbfem_status gbfem_get_sizes(gbfem_handle h, int64_t* num_dofs, int64_t* nnz);
 /* Global pattern in CSC (Eigen ColMajor, int StorageIndex): colptr[n+1], rowidx[nnz], rows sorted.

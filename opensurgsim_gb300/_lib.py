@@ -35,7 +35,8 @@ EXPORTED = [
     "gbfem_set_state", "gbfem_set_velocities", "gbfem_set_velocities_device", "gbfem_device_state", "gbfem_stream", "gbfem_reactivate",
     "gbfem_get_sizes", "gbfem_get_pattern", "gbfem_get_scatter", "gbfem_get_system", "gbfem_last_error",
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
-    "gbfem_cg_destroy", "gbfem_cg_solve_noalloc",
+    "gbfem_cg_destroy", "gbfem_cg_solve_noalloc", "gbfem_batch_create", "gbfem_batch_info",
+    "gbfem_batch_segment_stats",
 ]
 
 
@@ -130,6 +131,10 @@ def load():
         "gbfem_cg_set_max_iterations": (S, [H, ctypes.c_int32]),
         "gbfem_cg_solve": (S, [H, D, D, I32, D]),
         "gbfem_cg_destroy": (S, [H]),
+        "gbfem_batch_create": (S, [ctypes.c_int32, ctypes.POINTER(MeshDesc), ctypes.POINTER(Params),
+                                   ctypes.POINTER(H)]),
+        "gbfem_batch_info": (S, [H, I32, I32, I32]),
+        "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),

@@ -21,23 +21,28 @@ class Body:
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5,
                  cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0):
+        """`mesh` is one TetMesh, or a list of them for a batch (mixed precision only)."""
         L = _lib.load()
-        self._nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64).ravel()
-        self._tets = np.ascontiguousarray(mesh.tets, dtype=np.int32).ravel()
-        self._E = np.ascontiguousarray(mesh.young, dtype=np.float64)
-        self._nu = np.ascontiguousarray(mesh.poisson, dtype=np.float64)
-        self._rho = np.ascontiguousarray(mesh.density, dtype=np.float64)
-        self._bc = np.ascontiguousarray(mesh.bc_dofs, dtype=np.int32)
-        d = _lib.MeshDesc()
-        d.num_nodes = self._nodes.size // 3
-        d.rest_positions = dptr(self._nodes)
-        d.num_tets = self._tets.size // 4
-        d.tets = iptr(self._tets)
-        d.young_modulus = dptr(self._E)
-        d.poisson_ratio = dptr(self._nu)
-        d.mass_density = dptr(self._rho)
-        d.num_bc_dofs = self._bc.size
-        d.bc_dofs = iptr(self._bc) if self._bc.size else None
+        meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
+        self._keep = []
+        descs = (_lib.MeshDesc * len(meshes))()
+        for k, m in enumerate(meshes):
+            arrs = [np.ascontiguousarray(m.nodes, dtype=np.float64).ravel(),
+                    np.ascontiguousarray(m.tets, dtype=np.int32).ravel(),
+                    np.ascontiguousarray(m.young, dtype=np.float64), np.ascontiguousarray(m.poisson, dtype=np.float64),
+                    np.ascontiguousarray(m.density, dtype=np.float64),
+                    np.ascontiguousarray(m.bc_dofs, dtype=np.int32)]
+            self._keep.append(arrs)
+            d = descs[k]
+            d.num_nodes = arrs[0].size // 3
+            d.rest_positions = dptr(arrs[0])
+            d.num_tets = arrs[1].size // 4
+            d.tets = iptr(arrs[1])
+            d.young_modulus = dptr(arrs[2])
+            d.poisson_ratio = dptr(arrs[3])
+            d.mass_density = dptr(arrs[4])
+            d.num_bc_dofs = arrs[5].size
+            d.bc_dofs = iptr(arrs[5]) if arrs[5].size else None
         p = _lib.Params()
         L.gbfem_params_default(ctypes.byref(p))
         p.rayleigh_mass = rayleigh_mass
@@ -52,17 +57,32 @@ class Body:
         p.device = device
         self.params = p
         h = ctypes.c_void_p()
-        st = L.gbfem_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
+        if len(meshes) == 1 and not isinstance(mesh, (list, tuple)):
+            st = L.gbfem_create(ctypes.byref(descs[0]), ctypes.byref(p), ctypes.byref(h))
+        else:
+            st = L.gbfem_batch_create(len(meshes), descs, ctypes.byref(p), ctypes.byref(h))
         if st != _lib.GBFEM_OK:
             raise GbfemError(st, _lib.last_error(None))
         self._h = h
-        self.num_nodes = d.num_nodes
-        self.num_tets = d.num_tets
+        self.num_meshes = len(meshes)
+        self.num_nodes = sum(d.num_nodes for d in descs)
+        self.num_tets = sum(d.num_tets for d in descs)
         n, nnz = ctypes.c_int64(), ctypes.c_int64()
         L.gbfem_get_sizes(h, ctypes.byref(n), ctypes.byref(nnz))
         self.n = n.value
         self.nnz = nnz.value
+        self.node_offsets = np.zeros(self.num_meshes + 1, dtype=np.int32)
+        self.tet_offsets = np.zeros(self.num_meshes + 1, dtype=np.int32)
+        L.gbfem_batch_info(h, None, iptr(self.node_offsets), iptr(self.tet_offsets))
         self.last_status = _lib.GBFEM_OK
+
+    def segment_stats(self):
+        """Per mesh over the last step call: iterations, refreshes, converged, worst relative residual."""
+        k = self.num_meshes
+        it, rf, cv = (np.zeros(k, dtype=np.int32) for _ in range(3))
+        res = np.zeros(k)
+        _lib.load().gbfem_batch_segment_stats(self._h, iptr(it), iptr(rf), iptr(cv), dptr(res))
+        return dict(iterations=it, refreshes=rf, converged=cv, relative_residual=res)
 
     @classmethod
     def from_scene(cls, scene, **over):

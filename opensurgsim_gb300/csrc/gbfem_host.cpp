@@ -6,11 +6,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/gbfem.h"
 #include "gbfem_internal.h"
+#include "gbfem_pcg.h"
 
 using namespace gbfem;
 
@@ -115,10 +117,20 @@ struct gbfem_handle_s
 	DevBuf<double> d_x, d_v, d_xt, d_vt;
 	DevBuf<double> d_kslots, d_rhsE, d_A, d_invdiag, d_rhs, d_dv, d_dvPrev, d_r, d_p, d_q, d_part;
 	// mixed-precision form
-	DevBuf<float> d_rest32, d_kslots32, d_rhsE32, d_A32, d_invdiag32, d_r32, d_p32, d_q32;
-	DevBuf<double> d_r64;
-	DevBuf<MixCtl> d_mix;
-	MixCtl* h_mix = nullptr;
+	DevBuf<float> d_rest32, d_kslots32, d_rhsE32, d_A32, d_invdiag32, d_xd, d_invd, d_r32, d_pA, d_pB, d_q32;
+	DevBuf<double> d_brs, d_r64, d_x64;
+	DevBuf<int> d_rcol, d_segChunk, d_cumW;  // row-space columns, chunk range per segment, chunk weights
+	DevBuf<double> d_slots;                  // cross-CTA partials of the persistent solve
+	int maxChunksPerCta = 0;
+	size_t pcgSmem = 0;
+	DevBuf<SegCtl> d_seg;
+	DevBuf<PcgGlobal> d_pcgGlobal;
+	SegCtl* h_seg = nullptr;
+	int pcgGrid = 0;
+	// segments (meshes of a batch): node and tet ranges, chunk ranges
+	std::vector<int> segNode{0}, segTet{0};
+	std::vector<double> segStats;  // per segment over the last gbfem_step: iterations, refreshes, converged, residual
+	int nrows = 0, nchunks = 0;
 	bool mixed() const { return prm.precision == GBFEM_PRECISION_MIXED; }
 	DevBuf<int> d_counters;
 	DevBuf<CgCtl> d_ctl;
@@ -184,12 +196,16 @@ struct gbfem_handle_s
 		h_ctl = nullptr;
 		DevBuf<int4>* b4[] = {&d_tets, &d_lblk};
 		for (auto* b : b4) b->free();
-		if (h_mix) cudaFreeHost(h_mix);
-		h_mix = nullptr;
-		DevBuf<float>* bf[] = {&d_rest32, &d_kslots32, &d_rhsE32, &d_A32, &d_invdiag32, &d_r32, &d_p32, &d_q32};
+		if (h_seg) cudaFreeHost(h_seg);
+		h_seg = nullptr;
+		DevBuf<float>* bf[] = {&d_rest32, &d_kslots32, &d_rhsE32, &d_A32, &d_invdiag32, &d_xd, &d_invd, &d_r32,
+							   &d_pA, &d_pB, &d_q32};
 		for (auto* b : bf) b->free();
-		d_r64.free();
-		d_mix.free();
+		for (auto* b : {&d_brs, &d_r64, &d_x64}) b->free();
+		for (auto* b : {&d_rcol, &d_segChunk, &d_cumW}) b->free();
+		d_slots.free();
+		d_seg.free();
+		d_pcgGlobal.free();
 		DevBuf<double>* bd[] = {&d_rest, &d_xrest, &d_lmass, &d_nmass, &d_x, &d_v, &d_xt, &d_vt, &d_kslots,
 								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
 								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f};
@@ -228,6 +244,19 @@ gbfem_status fail(gbfem_handle h, gbfem_status st, const std::string& msg)
 			return fail(h, e_ == cudaErrorMemoryAllocation ? GBFEM_OUT_OF_MEMORY : GBFEM_CUDA_ERROR,     \
 						std::string(#call) + ": " + cudaGetErrorString(e_));                            \
 	} while (0)
+
+// The persistent solve's dynamic shared memory limit is a process-wide attribute of the kernel:
+// only ever raised, so a launch sized for one handle never breaks another's.
+cudaError_t raise_pcg_smem_limit(size_t bytes)
+{
+	static std::mutex mu;
+	static size_t current = 48 * 1024;
+	std::lock_guard<std::mutex> lock(mu);
+	if (bytes <= current) return cudaSuccess;
+	const cudaError_t e = cudaFuncSetAttribute(k_pcg_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+	if (e == cudaSuccess) current = bytes;
+	return e;
+}
 
 // Everything the step needs from the mesh, computed on the host once.
 gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
@@ -302,39 +331,63 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	h->nb = (int)h->adj.size();
 	h->nnz = 9LL * h->nb;
 	if (h->nnz > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "pattern exceeds int32 indices");
-	// SELL-32 layout of the block matrix: rows sorted by block count (descending, stable).
-	std::vector<int> perm(N), sellBase(h->nb);
-	for (int i = 0; i < N; ++i) perm[i] = i;
-	std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
-		return (h->adjPtr[a + 1] - h->adjPtr[a]) > (h->adjPtr[b + 1] - h->adjPtr[b]);
-	});
-	const int nchunks = (N + 31) / 32;
-	std::vector<int> off(nchunks + 1, 0);
+	// SELL-32 layout of the block matrix. Inside each segment (mesh of a batch) rows are sorted by
+	// block count (descending, stable); each segment is padded to a multiple of 32 rows so that a
+	// chunk of 32 rows never straddles two segments. perm[row] = node id, -1 on padding rows.
+	const int nseg = (int)h->segNode.size() - 1;
+	std::vector<int> perm, chunkSeg, segChunk(nseg + 1, 0);
+	for (int sg = 0; sg < nseg; ++sg)
+	{
+		const int n0 = h->segNode[sg], n1 = h->segNode[sg + 1];
+		std::vector<int> rows(n1 - n0);
+		for (int i = n0; i < n1; ++i) rows[i - n0] = i;
+		std::stable_sort(rows.begin(), rows.end(), [&](int a, int b) {
+			return (h->adjPtr[a + 1] - h->adjPtr[a]) > (h->adjPtr[b + 1] - h->adjPtr[b]);
+		});
+		rows.resize((rows.size() + 31) / 32 * 32, -1);
+		perm.insert(perm.end(), rows.begin(), rows.end());
+		for (size_t c = 0; c < rows.size() / 32; ++c) chunkSeg.push_back(sg);
+		segChunk[sg + 1] = (int)chunkSeg.size();
+	}
+	const int nrows = (int)perm.size();
+	const int nchunks = nrows / 32;
+	std::vector<int> off(nchunks + 1, 0), iperm(N, -1), sellBase(h->nb);
+	for (int rs = 0; rs < nrows; ++rs)
+		if (perm[rs] >= 0) iperm[perm[rs]] = rs;
 	for (int c = 0; c < nchunks; ++c)
 	{
 		int w = 0;
-		for (int l = 0; l < 32 && 32 * c + l < N; ++l)
+		for (int l = 0; l < 32; ++l)
 		{
-			int I = perm[32 * c + l];
-			w = std::max(w, h->adjPtr[I + 1] - h->adjPtr[I]);
+			const int I = perm[32 * c + l];
+			if (I >= 0) w = std::max(w, h->adjPtr[I + 1] - h->adjPtr[I]);
 		}
 		off[c + 1] = off[c] + w;
 	}
 	const int64_t sellSlots = 32LL * off[nchunks];
 	if (sellSlots * 9 > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "matrix exceeds int32 indices");
-	std::vector<int> scol(sellSlots, 0);
-	for (int rs = 0; rs < N; ++rs)
+	// Column of each slot as a node id (FP64 form, dof-space vectors) and as a row position (mixed
+	// form, row-space vectors). Padding slots point at the row itself with zero values.
+	std::vector<int> scol(sellSlots, 0), rcol(sellSlots, 0);
+	for (int rs = 0; rs < nrows; ++rs)
 	{
 		const int I = perm[rs], c = rs >> 5, lane = rs & 31;
-		const int deg = h->adjPtr[I + 1] - h->adjPtr[I];
+		const int deg = (I >= 0) ? h->adjPtr[I + 1] - h->adjPtr[I] : 0;
 		for (int t = 0; t < off[c + 1] - off[c]; ++t)
 		{
 			const int k = off[c] + t;
-			scol[(size_t)k * 32 + lane] = (t < deg) ? h->adj[h->adjPtr[I] + t] : I;
+			const int J = (t < deg) ? h->adj[h->adjPtr[I] + t] : (I >= 0 ? I : perm[32 * c]);
+			scol[(size_t)k * 32 + lane] = J;
+			rcol[(size_t)k * 32 + lane] = (t < deg) ? iperm[J] : rs;
 			if (t < deg) sellBase[h->adjPtr[I] + t] = k * 288 + lane;
 		}
 	}
+	for (int64_t k = 0; k < sellSlots; ++k)  // host-side bounds check of every index the kernels follow
+		if (scol[k] < 0 || scol[k] >= N || rcol[k] < 0 || rcol[k] >= nrows)
+			return fail(h, GBFEM_CUDA_ERROR, "internal error: SELL index out of range");
 	h->sellSlots = sellSlots;
+	h->nrows = nrows;
+	h->nchunks = nchunks;
 	// Lower blocks (I >= J) in row order, written to the SELL positions of (I,J) and (J,I).
 	std::vector<int> lowerOfPos(h->nb, -1);
 	std::vector<int4> lblk;
@@ -409,6 +462,11 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	GB_CUDA(h, h->d_perm.upload(perm.data(), perm.size(), s));
 	GB_CUDA(h, h->d_off.upload(off.data(), off.size(), s));
 	GB_CUDA(h, h->d_sellcol.upload(scol.data(), scol.size(), s));
+	if (h->mixed())
+	{
+		GB_CUDA(h, h->d_rcol.upload(rcol.data(), rcol.size(), s));
+		GB_CUDA(h, h->d_segChunk.upload(segChunk.data(), segChunk.size(), s));
+	}
 	GB_CUDA(h, h->d_lblk.upload(lblk.data(), lblk.size(), s));
 	GB_CUDA(h, h->d_cptr.upload(cptr.data(), cptr.size(), s));
 	GB_CUDA(h, h->d_cidx.upload(cidx.data(), cidx.size(), s));
@@ -439,11 +497,51 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		GB_CUDA(h, h->d_rhsE32.alloc((size_t)E * 12));
 		GB_CUDA(h, h->d_A32.alloc((size_t)sellSlots * 9));
 		GB_CUDA(h, cudaMemsetAsync(h->d_A32.p, 0, sizeof(float) * sellSlots * 9, s));
-		for (DevBuf<float>* b : {&h->d_invdiag32, &h->d_r32, &h->d_p32, &h->d_q32}) GB_CUDA(h, b->alloc(nv));
-		GB_CUDA(h, h->d_r64.alloc(nv));
-		GB_CUDA(h, h->d_mix.alloc(1));
-		GB_CUDA(h, cudaMemsetAsync(h->d_mix.p, 0, sizeof(MixCtl), s));
-		GB_CUDA(h, cudaMallocHost(&h->h_mix, sizeof(MixCtl)));
+		GB_CUDA(h, h->d_invdiag32.alloc(nv));
+		const size_t nr = 3 * (size_t)nrows;  // row-space vectors of the persistent solve
+		for (DevBuf<float>* b : {&h->d_xd, &h->d_invd, &h->d_r32, &h->d_q32}) GB_CUDA(h, b->alloc(nr));
+		// z and p of each row packed in one 32-byte record (one sector per neighbour gather)
+		for (DevBuf<float>* b : {&h->d_pA, &h->d_pB}) GB_CUDA(h, b->alloc(8 * (size_t)nrows));
+		for (DevBuf<double>* b : {&h->d_brs, &h->d_r64, &h->d_x64}) GB_CUDA(h, b->alloc(nr));
+		GB_CUDA(h, h->d_seg.alloc(nseg));
+		GB_CUDA(h, h->d_pcgGlobal.alloc(1));
+		GB_CUDA(h, cudaMallocHost(&h->h_seg, sizeof(SegCtl) * nseg));
+		// Persistent grid: as many co-resident CTAs as fit, at most 4 per SM. The kernel splits the
+		// chunks of the segments still iterating over the CTAs itself; the host bounds the largest
+		// share (shared-memory partials) from the chunk weights.
+		std::vector<int> cumW(nchunks + 1, 0);
+		int wmin = INT32_MAX;
+		for (int c = 0; c < nchunks; ++c)
+		{
+			const int w = off[c + 1] - off[c] + kPcgChunkWeight;
+			wmin = std::min(wmin, w);
+			if ((int64_t)cumW[c] + w > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "matrix too large for the persistent solve");
+			cumW[c + 1] = cumW[c] + w;
+		}
+		int perSM = 0, sms = 0;
+		GB_CUDA(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+		int G = std::max(1, std::min(4 * sms, nchunks));
+		size_t smem = 0;
+		for (int attempt = 0; attempt < 2; ++attempt)
+		{
+			// A weighted share holds fewer than tot / (G wmin) + 1 chunks, a counted one at most ceil(n / G).
+			const int64_t mW = (int64_t)cumW[nchunks] / ((int64_t)G * wmin) + 2;
+			const int64_t mC = (int64_t)nchunks / G + 2;
+			h->maxChunksPerCta = (int)std::max(mW, mC);
+			smem = pcg_smem_bytes(nseg, h->maxChunksPerCta);
+			if (smem > 160 * 1024) return fail(h, GBFEM_INVALID_ARG, "batch too large for the persistent solve");
+			GB_CUDA(h, raise_pcg_smem_limit(smem));
+			GB_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_pcg_persistent, kPcgThreads, smem));
+			if (perSM < 1) return fail(h, GBFEM_INVALID_ARG, "persistent solve does not fit on an SM");
+			const int G2 = std::max(1, std::min(std::min(perSM, 4) * sms, nchunks));
+			if (G2 == G) break;
+			G = G2;  // fewer CTAs: larger shares, recompute the bound once
+		}
+		h->pcgGrid = G;
+		h->pcgSmem = smem;
+		GB_CUDA(h, h->d_cumW.upload(cumW.data(), cumW.size(), s));
+		GB_CUDA(h, h->d_slots.alloc(4 * (size_t)G));
+		GB_CUDA(h, cudaStreamSynchronize(s));
 	}
 	for (DevBuf<double>* b : {&h->d_rhs, &h->d_dv}) GB_CUDA(h, b->alloc(nv));
 	GB_CUDA(h, h->d_part.alloc(partial_slots(h->launch().vecGrid)));
@@ -577,7 +675,7 @@ gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter, boo
 	static thread_local KernelTimer kt;
 	if (timeSpmv && !kt.init()) return fail(h, GBFEM_CUDA_ERROR, "cudaEventCreate failed");
 	const Launch L = h->launch();
-	MatSell3 A{h->N, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A.p};
+	MatSell3 A{h->nrows, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A.p};
 	launch_cg_init(h->n, b, h->d_invdiag.p, x, h->d_r.p, h->d_p.p, h->d_ctl.p, h->d_part.p, h->prm.cg_tolerance,
 				   maxIter, L);
 	h->launches++;
@@ -622,56 +720,61 @@ gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter, boo
 
 // Mixed-precision solve: FP32 CG iterations with reliable FP64 residual refreshes; the host polls
 // the device control block between chunks of iterations.
-gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, bool timeSpmv)
+gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, bool timeSolve)
 {
+	const int nseg = (int)h->segNode.size() - 1;
+	cudaStream_t st = h->stream;
+	GB_CUDA(h, cudaMemsetAsync(h->d_seg.p, 0, sizeof(SegCtl) * nseg, st));
+	GB_CUDA(h, cudaMemsetAsync(h->d_pcgGlobal.p, 0, sizeof(PcgGlobal), st));
+	PcgArgs a;
+	a.nchunks = h->nchunks;
+	a.nsegs = nseg;
+	a.maxIter = maxIter;
+	a.tol = h->prm.cg_tolerance;
+	a.drop = 1e-3;  // refresh when |r|^2 has dropped 1000x (the residual norm ~30x) since the last refresh
+	a.off = h->d_off.p;
+	a.col = h->d_rcol.p;
+	a.val = h->d_A32.p;
+	a.perm = h->d_perm.p;
+	a.segChunk = h->d_segChunk.p;
+	a.b = b;
+	a.invdiag = h->d_invdiag32.p;
+	a.x = x;
+	a.brs = h->d_brs.p;
+	a.r64 = h->d_r64.p;
+	a.x64 = h->d_x64.p;
+	a.xd = h->d_xd.p;
+	a.invd = h->d_invd.p;
+	a.r = h->d_r32.p;
+	a.pA = h->d_pA.p;
+	a.pB = h->d_pB.p;
+	a.q = h->d_q32.p;
+	a.cumW = h->d_cumW.p;
+	a.slots = h->d_slots.p;
+	a.maxChunksPerCta = h->maxChunksPerCta;
+	a.seg = h->d_seg.p;
+	a.g = h->d_pcgGlobal.p;
 	static thread_local KernelTimer kt;
-	if (timeSpmv && !kt.init()) return fail(h, GBFEM_CUDA_ERROR, "cudaEventCreate failed");
-	const Launch L = h->launch();
-	MixBufs m;
-	m.n = h->n;
-	m.b = b;
-	m.x = x;
-	m.r64 = h->d_r64.p;
-	m.r = h->d_r32.p;
-	m.p = h->d_p32.p;
-	m.q = h->d_q32.p;
-	m.invdiag = h->d_invdiag32.p;
-	m.A = MatSellT<float>{h->N, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A32.p};
-	m.ctl = h->d_mix.p;
-	m.part = h->d_part.p;
-	// Refresh the FP64 residual whenever the FP32 residual norm has dropped ~30x (|r|^2 by 1e-3).
-	constexpr double kReliableDrop = 1e-3;
-	launch_mix_init(m, h->prm.cg_tolerance, maxIter, kReliableDrop, L);
-	h->launches += kMixInitKernels;
-	long long launched = 0;
-	int chunk = 4;
-	int spmvSoFar = 0;
-	for (;;)
+	if (timeSolve && !kt.init()) return fail(h, GBFEM_CUDA_ERROR, "cudaEventCreate failed");
+	if (timeSolve) cudaEventRecord(kt.a[0], st);
+	void* args[] = {&a};
+	GB_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_pcg_persistent, dim3(h->pcgGrid), dim3(kPcgThreads), args,
+										   h->pcgSmem, st));
+	if (timeSolve) cudaEventRecord(kt.b[0], st);
+	h->launches += 1;
+	PcgGlobal g;
+	GB_CUDA(h, cudaMemcpyAsync(h->h_seg, h->d_seg.p, sizeof(SegCtl) * nseg, cudaMemcpyDeviceToHost, st));
+	GB_CUDA(h, cudaMemcpyAsync(&g, h->d_pcgGlobal.p, sizeof(PcgGlobal), cudaMemcpyDeviceToHost, st));
+	GB_CUDA(h, cudaStreamSynchronize(st));
+	if (g.err)
+		return fail(h, GBFEM_CUDA_ERROR, g.err == 1 ? "persistent CG: grid barrier timed out"
+												  : "persistent CG: work share exceeded its shared-memory bound");
+	if (timeSolve)
 	{
-		for (int k = 0; k < chunk; ++k)
-			launch_mix_iteration(m, L, timeSpmv ? kt.a[k] : nullptr, timeSpmv ? kt.b[k] : nullptr);
-		h->launches += kMixKernelsPerIteration * chunk;
-		launched += chunk;
-		GB_CUDA(h, cudaMemcpyAsync(h->h_mix, h->d_mix.p, sizeof(MixCtl), cudaMemcpyDeviceToHost, h->stream));
-		GB_CUDA(h, cudaStreamSynchronize(h->stream));
-		const MixCtl& c = *h->h_mix;
-		if (timeSpmv)
-		{
-			// Launches that multiplied by the matrix: one per counted iteration, plus the converging one.
-			const int total = c.iter + ((c.done && c.converged && c.bb > 0) ? 1 : 0);
-			const int real = std::max(0, std::min(total - spmvSoFar, chunk));
-			spmvSoFar = total;
-			for (int k = 0; k < real; ++k)
-			{
-				float ms = 0;
-				cudaEventElapsedTime(&ms, kt.a[k], kt.b[k]);
-				h->stats.ms_spmv += ms;
-				h->stats.spmv_timed++;
-			}
-		}
-		if (c.done) break;
-		if (launched > (long long)maxIter + 64) return fail(h, GBFEM_CUDA_ERROR, "CG control block did not finish");
-		chunk = std::min(chunk * 2, KernelTimer::kPairs);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, kt.a[0], kt.b[0]);
+		h->stats.ms_spmv += ms;  // the whole persistent solve: one launch
+		h->stats.spmv_timed += 1;
 	}
 	return GBFEM_OK;
 }
@@ -728,11 +831,22 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 			gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
-			const MixCtl& mc = *h->h_mix;
-			h->stats.cg_iterations += mc.iter;
-			h->stats.refinement_sweeps += mc.updates;
-			h->stats.cg_relative_residual = mc.bb > 0 ? std::sqrt(mc.rrTrue / mc.bb) : 0.0;
-			if (!mc.converged) h->stats.cg_max_iterations_hit++;
+			double worst = 0.0;
+			for (int sg = 0; sg + 1 < (int)h->segNode.size(); ++sg)
+			{
+				const SegCtl& c = h->h_seg[sg];
+				const double res = c.bb > 0 ? std::sqrt(c.rrTrue / c.bb) : 0.0;
+				h->stats.cg_iterations += c.iter;
+				h->stats.refinement_sweeps += c.updates;
+				worst = std::max(worst, res);
+				if (!c.converged) h->stats.cg_max_iterations_hit++;
+				double* ss = &h->segStats[4 * (size_t)sg];
+				ss[0] += c.iter;
+				ss[1] += c.updates;
+				ss[2] = std::min(ss[2], (double)c.converged);
+				ss[3] = std::max(ss[3], res);
+			}
+			h->stats.cg_relative_residual = worst;
 		}
 		else
 		{
@@ -757,6 +871,9 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 			h->stats.cg_iterations += h->h_ctl->iter;
 			h->stats.cg_relative_residual = h->h_ctl->bb > 0 ? std::sqrt(h->h_ctl->rr / h->h_ctl->bb) : 0.0;
 			if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
+			h->segStats[0] += h->h_ctl->iter;
+			h->segStats[2] = std::min(h->segStats[2], (double)h->h_ctl->converged);
+			h->segStats[3] = std::max(h->segStats[3], h->stats.cg_relative_residual);
 		}
 		launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, xt, h->d_x.p, h->d_v.p, dt, newtonMax > 1, h->d_ctl.p,
 							h->d_part.p, L);
@@ -815,34 +932,97 @@ gbfem_status gbfem_params_default(gbfem_params* out)
 	return GBFEM_OK;
 }
 
-gbfem_status gbfem_create(const gbfem_mesh_desc* m, const gbfem_params* prm, gbfem_handle* out)
+}  // extern "C"
+
+namespace {
+
+// Checks one mesh description (Fem3DRepresentation / FemElement / OdeState input checks).
+gbfem_status validate_mesh(const gbfem_mesh_desc* m, int index)
 {
-	if (!out) return fail(nullptr, GBFEM_INVALID_ARG, "out is NULL");
-	*out = nullptr;
-	if (!m || !prm) return fail(nullptr, GBFEM_INVALID_ARG, "mesh or params is NULL");
+	const std::string where = index >= 0 ? "mesh " + std::to_string(index) + ": " : std::string();
+	if (!m) return fail(nullptr, GBFEM_INVALID_ARG, where + "mesh is NULL");
 	if (m->num_nodes <= 0 || m->num_tets <= 0 || !m->rest_positions || !m->tets || !m->young_modulus ||
 		!m->poisson_ratio || !m->mass_density || (m->num_bc_dofs > 0 && !m->bc_dofs) || m->num_bc_dofs < 0)
-		return fail(nullptr, GBFEM_INVALID_ARG, "empty mesh or missing arrays");
-	if (m->num_nodes > INT32_MAX / 3) return fail(nullptr, GBFEM_INVALID_ARG, "too many nodes");
+		return fail(nullptr, GBFEM_INVALID_ARG, where + "empty mesh or missing arrays");
+	if (m->num_nodes > INT32_MAX / 3) return fail(nullptr, GBFEM_INVALID_ARG, where + "too many nodes");
 	for (int64_t i = 0; i < 4LL * m->num_tets; ++i)
 		if (m->tets[i] < 0 || m->tets[i] >= m->num_nodes)
-			return fail(nullptr, GBFEM_INVALID_ARG, "Invalid nodeId " + std::to_string(m->tets[i]));
+			return fail(nullptr, GBFEM_INVALID_ARG, where + "Invalid nodeId " + std::to_string(m->tets[i]));
 	for (int32_t e = 0; e < m->num_tets; ++e)
 	{
 		// FemElement::initialize material checks (FemElement.cpp:33-43).
 		const double rho = m->mass_density[e], nu = m->poisson_ratio[e], Ey = m->young_modulus[e];
 		if (!(rho > 0.0) || !(nu > 0.0 && nu < 0.5) || !(Ey > 0.0))
-			return fail(nullptr, GBFEM_INVALID_ARG, "invalid material on tet " + std::to_string(e));
+			return fail(nullptr, GBFEM_INVALID_ARG, where + "invalid material on tet " + std::to_string(e));
 	}
 	for (int32_t i = 0; i < m->num_bc_dofs; ++i)
 		if (m->bc_dofs[i] < 0 || m->bc_dofs[i] >= 3 * m->num_nodes)
-			return fail(nullptr, GBFEM_INVALID_ARG, "Invalid boundary condition dof " + std::to_string(m->bc_dofs[i]));
+			return fail(nullptr, GBFEM_INVALID_ARG,
+						where + "Invalid boundary condition dof " + std::to_string(m->bc_dofs[i]));
+	return GBFEM_OK;
+}
+
+gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbfem_params* prm, gbfem_handle* out)
+{
+	if (!out) return fail(nullptr, GBFEM_INVALID_ARG, "out is NULL");
+	*out = nullptr;
+	if (!meshes || !prm || count <= 0) return fail(nullptr, GBFEM_INVALID_ARG, "mesh or params is NULL");
+	for (int32_t k = 0; k < count; ++k)
+	{
+		gbfem_status st = validate_mesh(&meshes[k], count > 1 ? k : -1);
+		if (st != GBFEM_OK) return st;
+	}
 	if (!(prm->newton_max_iterations >= 1) || !(prm->newton_epsilon >= 0.0) || !(prm->cg_tolerance >= 0.0) ||
 		prm->precision < 0 || prm->precision > 1)
 		return fail(nullptr, GBFEM_INVALID_ARG, "invalid solver parameters");
+	if (count > 1 && prm->precision != GBFEM_PRECISION_MIXED)
+		return fail(nullptr, GBFEM_INVALID_ARG, "a batch of meshes is stepped in the mixed-precision form");
+	// Concatenate the meshes (node ids, boundary-condition dofs shifted by the node offsets).
+	int64_t N = 0, E = 0, B = 0;
+	for (int32_t k = 0; k < count; ++k)
+	{
+		N += meshes[k].num_nodes;
+		E += meshes[k].num_tets;
+		B += meshes[k].num_bc_dofs;
+	}
+	if (N > INT32_MAX / 3 || E > INT32_MAX / kSlots) return fail(nullptr, GBFEM_INVALID_ARG, "batch too large");
+	std::vector<double> X, Ey, Nu, Rho;
+	std::vector<int32_t> T, Bc;
+	std::vector<int> segNode{0}, segTet{0};
+	if (count > 1)
+	{
+		X.reserve(3 * N);
+		T.reserve(4 * E);
+		Ey.reserve(E);
+		Nu.reserve(E);
+		Rho.reserve(E);
+		Bc.reserve(B);
+	}
+	for (int32_t k = 0; k < count; ++k)
+	{
+		const gbfem_mesh_desc& m = meshes[k];
+		const int32_t n0 = segNode.back();
+		if (count > 1)
+		{
+			X.insert(X.end(), m.rest_positions, m.rest_positions + 3 * (size_t)m.num_nodes);
+			for (int64_t i = 0; i < 4LL * m.num_tets; ++i) T.push_back(m.tets[i] + n0);
+			Ey.insert(Ey.end(), m.young_modulus, m.young_modulus + m.num_tets);
+			Nu.insert(Nu.end(), m.poisson_ratio, m.poisson_ratio + m.num_tets);
+			Rho.insert(Rho.end(), m.mass_density, m.mass_density + m.num_tets);
+			for (int32_t i = 0; i < m.num_bc_dofs; ++i) Bc.push_back(m.bc_dofs[i] + 3 * n0);
+		}
+		segNode.push_back(n0 + m.num_nodes);
+		segTet.push_back(segTet.back() + m.num_tets);
+	}
+	gbfem_mesh_desc merged = meshes[0];
+	if (count > 1)
+		merged = gbfem_mesh_desc{(int32_t)N, X.data(), (int32_t)E, T.data(), Ey.data(), Nu.data(), Rho.data(),
+								 (int32_t)B, Bc.data()};
 	auto* h = new gbfem_handle_s();
 	h->prm = *prm;
 	h->device = prm->device;
+	h->segNode = segNode;
+	h->segTet = segTet;
 	cudaError_t ce = cudaSetDevice(h->device);
 	if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
 	if (ce != cudaSuccess)
@@ -851,7 +1031,7 @@ gbfem_status gbfem_create(const gbfem_mesh_desc* m, const gbfem_params* prm, gbf
 		delete h;
 		return fail(nullptr, GBFEM_CUDA_ERROR, msg);
 	}
-	gbfem_status st = build_body(h, m);
+	gbfem_status st = build_body(h, &merged);
 	if (st != GBFEM_OK)
 	{
 		g_lastCreateError = h->err;
@@ -860,7 +1040,48 @@ gbfem_status gbfem_create(const gbfem_mesh_desc* m, const gbfem_params* prm, gbf
 		return st;
 	}
 	h->stats.active = 1;
+	h->segStats.assign(4 * (size_t)count, 0.0);
 	*out = h;
+	return GBFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbfem_status gbfem_create(const gbfem_mesh_desc* m, const gbfem_params* prm, gbfem_handle* out)
+{
+	return create_impl(m, 1, prm, out);
+}
+
+gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, const gbfem_params* params,
+								gbfem_handle* out)
+{
+	return create_impl(meshes, count, params, out);
+}
+
+gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	const int nseg = (int)h->segNode.size() - 1;
+	if (count) *count = nseg;
+	if (node_offsets) std::copy(h->segNode.begin(), h->segNode.end(), node_offsets);
+	if (tet_offsets) std::copy(h->segTet.begin(), h->segTet.end(), tet_offsets);
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_batch_segment_stats(gbfem_handle h, int32_t* iterations, int32_t* refreshes, int32_t* converged,
+									   double* relative_residual)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	const size_t nseg = h->segNode.size() - 1;
+	for (size_t k = 0; k < nseg; ++k)
+	{
+		if (iterations) iterations[k] = (int32_t)h->segStats[4 * k];
+		if (refreshes) refreshes[k] = (int32_t)h->segStats[4 * k + 1];
+		if (converged) converged[k] = (int32_t)h->segStats[4 * k + 2];
+		if (relative_residual) relative_residual[k] = h->segStats[4 * k + 3];
+	}
 	return GBFEM_OK;
 }
 
@@ -880,6 +1101,11 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	if (!(dt > 0.0) || nsteps < 0) return fail(h, GBFEM_INVALID_ARG, "dt must be > 0 and nsteps >= 0");
 	std::memset(&h->stats, 0, sizeof(h->stats));
 	h->launches = 0;
+	for (size_t k = 0; k < h->segStats.size(); k += 4)
+	{
+		h->segStats[k] = h->segStats[k + 1] = h->segStats[k + 3] = 0.0;
+		h->segStats[k + 2] = 1.0;
+	}
 	if (!h->active)
 	{
 		h->stats.active = 0;

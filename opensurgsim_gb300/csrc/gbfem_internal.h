@@ -48,24 +48,6 @@ struct CgCtl
 	int nonfinite, pad1;
 };
 
-// Control block of the mixed-precision solve: FP32 CG iterations on the FP32 matrix, the
-// solution accumulated in FP64, and the true FP64 residual b - A x recomputed ("reliable update")
-// whenever the FP32 residual has dropped by reliableDrop since the last refresh. The FP32 vectors
-// are kept normalised: r_true ~= s * r32.
-struct MixCtl
-{
-	double bb, threshold;   // |b|^2, tol^2 |b|^2
-	double s;               // residual scale
-	double rz, pq, alpha, beta;
-	double rr32, rrLast;    // |r32|^2 now and right after the last refresh
-	double rrTrue;          // |b - A x|^2 at the last refresh
-	double reliableDrop;    // refresh when rr32 < reliableDrop * rrLast
-	double sNew, ratio, rzPend;
-	int iter, done, converged, maxIter;
-	int updates, pending, nonfinite, pad;
-	unsigned int ticket[4];
-};
-
 struct Launch
 {
 	int vecGrid = 0;   // blocks of 256 threads for the dof-wise kernels
@@ -80,8 +62,8 @@ struct Launch
 template <typename T>
 struct MatSellT
 {
-	int rows;            // block rows (nodes)
-	const int* perm;     // sorted position -> node id
+	int rows;            // block rows incl. padding (a multiple of 32)
+	const int* perm;     // sorted position -> node id, -1 on padding rows
 	const int* off;      // chunk offsets in block columns, nchunks + 1
 	const int* col;
 	const T* val;
@@ -123,27 +105,6 @@ void launch_cg_spmv_csr(const MatCsr& A, const double* p, double* q, CgCtl* ctl,
 void launch_cg_update(int n, const double* invdiag, const double* p, const double* q, double* x, double* r,
 					  CgCtl* ctl, double* part, const Launch& L);
 void launch_cg_pupdate(int n, const double* invdiag, const double* r, double* p, CgCtl* ctl, const Launch& L);
-
-// ---- mixed-precision CG with reliable FP64 updates
-struct MixBufs
-{
-	int n;
-	const double* b;      // right-hand side (FP64)
-	double* x;            // solution (FP64)
-	double* r64;          // true residual scratch (FP64)
-	float* r;             // normalised FP32 residual
-	float* p;
-	float* q;
-	const float* invdiag;
-	MatSellT<float> A;
-	MixCtl* ctl;
-	double* part;
-};
-void launch_mix_init(const MixBufs& m, double tol, int maxIter, double reliableDrop, const Launch& L);
-// One iteration: spmv, update, refresh, rescale, p update (events, if given, bracket the spmv).
-void launch_mix_iteration(const MixBufs& m, const Launch& L, cudaEvent_t evA = nullptr, cudaEvent_t evB = nullptr);
-constexpr int kMixKernelsPerIteration = 5;
-constexpr int kMixInitKernels = 2;
 
 // ---- state
 void launch_state_update(int n, const double* dv, double* dvPrev, const double* xt, double* xn, double* vn,

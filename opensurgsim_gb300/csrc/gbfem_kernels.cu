@@ -3,8 +3,7 @@
 // Element kernels (one element per thread; the math is in gbfem_element.cuh), deterministic
 // gather assembly into a symmetric SELL-32 block matrix built from the lower triangle (Eigen's
 // ConjugateGradient<..., Lower> reads only that triangle), the per-node right-hand-side gather,
-// the FP64 Jacobi-PCG, and the mixed-precision CG (FP32 iterations, FP64 solution and reliable
-// FP64 residual refreshes).
+// the FP64 Jacobi-PCG. The mixed-precision solve is the persistent kernel of gbfem_pcg.cu.
 
 #include <cfloat>
 #include <cstdint>
@@ -352,9 +351,9 @@ __global__ void __launch_bounds__(256) k_cg_spmv_sell(MatSell3 A, const double* 
 	{
 		double a0, a1, a2;
 		sell_row<double, double, double>(A, p, rs, a0, a1, a2);
-		if (rs < A.rows)
+		const int I = A.perm[rs];
+		if (I >= 0)
 		{
-			const int I = A.perm[rs];
 			q[3 * I] = a0;
 			q[3 * I + 1] = a1;
 			q[3 * I + 2] = a2;
@@ -448,229 +447,6 @@ __global__ void k_cg_pupdate(int n, const double* __restrict__ invdiag, const do
 	const double beta = ctl->beta;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 		p[i] = invdiag[i] * r[i] + beta * p[i];
-}
-
-// ------------------------------------------------------------------------------------------
-// Mixed-precision CG. Same recurrences as above with r, p, q and the matrix in FP32, the
-// solution x in FP64, and the residual refreshed from the FP64 product b - A x whenever the FP32
-// residual has dropped by reliableDrop (or looks converged). Convergence is decided only on the
-// refreshed FP64 residual: |b - A x|^2 < tol^2 |b|^2.
-// ------------------------------------------------------------------------------------------
-// x = 0, r64 = b; |b|^2.
-__global__ void k_mix_init0(MixBufs m, double tol, int maxIter, double drop)
-{
-	double v[1] = {0.0};
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
-	{
-		const double bi = m.b[i];
-		m.x[i] = 0.0;
-		m.r64[i] = bi;
-		v[0] += bi * bi;
-	}
-	double tot[1];
-	if (grid_reduce<OpSum, 1>(v, m.part, &m.ctl->ticket[0], tot) && threadIdx.x == 0)
-	{
-		MixCtl* c = m.ctl;
-		const double bb = tot[0];
-		c->bb = bb;
-		c->rrTrue = bb;
-		c->threshold = fmax(tol * tol * bb, DBL_MIN);
-		c->iter = 0;
-		c->maxIter = maxIter;
-		c->updates = 0;
-		c->pending = 0;
-		c->nonfinite = !isfinite(bb);
-		c->converged = (bb == 0.0 || bb < c->threshold) ? 1 : 0;
-		c->done = (c->converged || c->nonfinite) ? 1 : 0;
-		c->reliableDrop = drop;
-		c->s = sqrt(bb);
-		c->ratio = 0.0;  // no previous direction
-	}
-}
-
-// r32 = r64 / s, p32 = z32 (first direction) or p32 * ratio (rescaled), rz = r32 . z32.
-// Runs at the start (ratio = 0) and after every refresh (pending = 1).
-__device__ __forceinline__ void mix_normalise(const MixBufs& m, bool first)
-{
-	MixCtl* c = m.ctl;
-	const double inv = 1.0 / c->s;
-	const float ratio = float(c->ratio);
-	float v[2] = {0.f, 0.f};
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
-	{
-		const float ri = float(m.r64[i] * inv);
-		m.r[i] = ri;
-		const float zi = m.invdiag[i] * ri;
-		m.p[i] = first ? zi : m.p[i] * ratio;
-		v[0] += ri * zi;
-		v[1] += ri * ri;
-	}
-	double tot[2];
-	if (grid_reduce<OpSum, 2>(v, m.part, &c->ticket[3], tot) && threadIdx.x == 0)
-	{
-		if (first)
-		{
-			c->rz = tot[0];
-		}
-		else
-		{
-			// beta in true units: (s_new^2 rz_new) / (s_old^2 rz_old), with p already rescaled.
-			c->beta = tot[0] / (c->rzPend * double(ratio) * double(ratio));
-			c->rz = tot[0];
-			c->iter += 1;
-			c->updates += 1;
-			c->pending = 0;
-			if (c->iter >= c->maxIter)
-			{
-				c->done = 1;
-				c->converged = 0;
-			}
-		}
-		c->rr32 = tot[1];
-		c->rrLast = tot[1];
-	}
-}
-
-__global__ void k_mix_init1(MixBufs m)
-{
-	if (m.ctl->done) return;
-	mix_normalise(m, true);
-}
-
-// q = A p (FP32), pq.
-__global__ void __launch_bounds__(256) k_mix_spmv(MixBufs m)
-{
-	MixCtl* c = m.ctl;
-	if (c->done) return;
-	float v[1] = {0.f};
-	const int stride = gridDim.x * blockDim.x;
-	const int nrowsPadded = (m.A.rows + 31) & ~31;
-	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < nrowsPadded; rs += stride)
-	{
-		float a0, a1, a2;
-		sell_row<float, float, float>(m.A, m.p, rs, a0, a1, a2);
-		if (rs < m.A.rows)
-		{
-			const int I = m.A.perm[rs];
-			m.q[3 * I] = a0;
-			m.q[3 * I + 1] = a1;
-			m.q[3 * I + 2] = a2;
-			v[0] += m.p[3 * I] * a0 + m.p[3 * I + 1] * a1 + m.p[3 * I + 2] * a2;
-		}
-	}
-	double tot[1];
-	if (grid_reduce<OpSum, 1>(v, m.part, &c->ticket[1], tot) && threadIdx.x == 0)
-	{
-		c->pq = tot[0];
-		c->alpha = c->rz / tot[0];
-	}
-}
-
-// x += alpha s p (FP64), r -= alpha q (FP32); decide whether the residual must be refreshed.
-__global__ void k_mix_update(MixBufs m)
-{
-	MixCtl* c = m.ctl;
-	if (c->done) return;
-	const float alpha = float(c->alpha);
-	const double as = c->alpha * c->s;
-	float v[2] = {0.f, 0.f};
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
-	{
-		m.x[i] += as * double(m.p[i]);
-		const float ri = m.r[i] - alpha * m.q[i];
-		m.r[i] = ri;
-		v[0] += ri * ri;
-		v[1] += ri * (m.invdiag[i] * ri);
-	}
-	double tot[2];
-	if (grid_reduce<OpSum, 2>(v, m.part, &c->ticket[2], tot) && threadIdx.x == 0)
-	{
-		const double rr = tot[0];
-		c->rr32 = rr;
-		if (!isfinite(rr) || !isfinite(c->alpha))
-		{
-			c->done = 1;
-			c->converged = 0;
-			c->nonfinite = 1;
-		}
-		else if (c->s * c->s * rr < c->threshold || rr < c->reliableDrop * c->rrLast ||
-				 c->iter + 1 >= c->maxIter)
-		{
-			c->pending = 1;  // refresh before the next direction
-			c->rzPend = c->rz;
-		}
-		else
-		{
-			const double rzOld = c->rz;
-			c->rz = tot[1];
-			c->beta = tot[1] / rzOld;
-			c->iter += 1;
-		}
-	}
-}
-
-// r64 = b - A x in FP64 (FP32 matrix values, FP64 products and sums); decide convergence.
-__global__ void __launch_bounds__(256) k_mix_refresh(MixBufs m)
-{
-	MixCtl* c = m.ctl;
-	if (c->done || !c->pending) return;
-	double v[1] = {0.0};
-	const int stride = gridDim.x * blockDim.x;
-	const int nrowsPadded = (m.A.rows + 31) & ~31;
-	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < nrowsPadded; rs += stride)
-	{
-		double a0, a1, a2;
-		sell_row<float, double, double>(m.A, m.x, rs, a0, a1, a2);
-		if (rs < m.A.rows)
-		{
-			const int I = m.A.perm[rs];
-			const double r0 = m.b[3 * I] - a0, r1 = m.b[3 * I + 1] - a1, r2 = m.b[3 * I + 2] - a2;
-			m.r64[3 * I] = r0;
-			m.r64[3 * I + 1] = r1;
-			m.r64[3 * I + 2] = r2;
-			v[0] += r0 * r0 + r1 * r1 + r2 * r2;
-		}
-	}
-	double tot[1];
-	if (grid_reduce<OpSum, 1>(v, m.part, &c->ticket[1], tot) && threadIdx.x == 0)
-	{
-		const double rr = tot[0];
-		c->rrTrue = rr;
-		if (rr < c->threshold)
-		{
-			c->done = 1;  // like Eigen, the converging iteration is not counted
-			c->converged = 1;
-			c->updates += 1;
-		}
-		else if (!isfinite(rr) || c->iter + 1 >= c->maxIter)
-		{
-			c->done = 1;
-			c->converged = 0;
-			c->iter += 1;
-			if (!isfinite(rr)) c->nonfinite = 1;
-		}
-		else
-		{
-			const double sNew = sqrt(rr);
-			c->ratio = c->s / sNew;
-			c->s = sNew;
-		}
-	}
-}
-
-__global__ void k_mix_rescale(MixBufs m)
-{
-	if (m.ctl->done || !m.ctl->pending) return;
-	mix_normalise(m, false);
-}
-
-__global__ void k_mix_pupdate(MixBufs m)
-{
-	const MixCtl* c = m.ctl;
-	if (c->done) return;
-	const float beta = float(c->beta);
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.n; i += gridDim.x * blockDim.x)
-		m.p[i] = m.invdiag[i] * m.r[i] + beta * m.p[i];
 }
 
 // ------------------------------------------------------------------------------------------
@@ -817,23 +593,6 @@ void launch_cg_update(int n, const double* invdiag, const double* p, const doubl
 void launch_cg_pupdate(int n, const double* invdiag, const double* r, double* p, CgCtl* ctl, const Launch& L)
 {
 	k_cg_pupdate<<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, invdiag, r, p, ctl);
-}
-
-void launch_mix_init(const MixBufs& m, double tol, int maxIter, double reliableDrop, const Launch& L)
-{
-	k_mix_init0<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m, tol, maxIter, reliableDrop);
-	k_mix_init1<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
-}
-
-void launch_mix_iteration(const MixBufs& m, const Launch& L, cudaEvent_t evA, cudaEvent_t evB)
-{
-	if (evA) cudaEventRecord(evA, L.stream);
-	k_mix_spmv<<<L.vecGrid, 256, 0, L.stream>>>(m);
-	if (evB) cudaEventRecord(evB, L.stream);
-	k_mix_update<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
-	k_mix_refresh<<<L.vecGrid, 256, 0, L.stream>>>(m);
-	k_mix_rescale<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
-	k_mix_pupdate<<<L.vecGrid, kVecThreads, 0, L.stream>>>(m);
 }
 
 void launch_state_update(int n, const double* dv, double* dvPrev, const double* xt, double* xn, double* vn,

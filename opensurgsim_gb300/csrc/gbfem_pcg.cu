@@ -1,0 +1,688 @@
+// gbfem_pcg.cu -- persistent mixed-precision CG over a batch of independent systems (segments).
+//
+// One cooperative launch runs a whole solve for every segment (mesh) of a batch: FP32 CG
+// iterations on the FP32 SELL-32 matrix with per-segment scalars, the solution accumulated in
+// FP64 (FP32 deltas folded at each refresh), and per-segment "reliable updates": when a
+// segment's FP32 residual has dropped by `drop` since its last refresh (or looks converged), its
+// true FP64 residual b - A x is recomputed and convergence is decided on it, at the same
+// |r|^2 < tol^2 |b|^2 rule as the FP64 form (Eigen's ConjugateGradient).
+//
+// Work is cut into chunks of 32 matrix rows (one node row per lane); segments own contiguous
+// chunk ranges. Every iteration has two phases separated by grid barriers: phase 1 is the SpMV
+// (or, for a segment due for a refresh, the FP64 residual), phase 2 the row-local update (or the
+// rescale after a refresh). Each phase walks only the chunks of the segments still iterating
+// (the active set), split over the CTAs by exact integer arithmetic on cumulative weights: the
+// SpMV phase balances block columns, the row-local phase chunk counts. Every CTA recomputes
+// its own range whenever the active set changes, so no CTA idles on finished meshes.
+//
+// Per-segment sums are deterministic: each CTA sums its chunk partials of a segment in chunk
+// order; a segment spread over CTAs bf..bl is completed by the last of them to arrive (ticket
+// counter), which adds the CTAs' partials in CTA order. Grid barriers spin with an iteration
+// limit: on timeout the kernel records an error and returns (the host reports GBFEM_CUDA_ERROR).
+
+#include <cfloat>
+#include <cstdint>
+
+#include "gbfem_pcg.h"
+
+namespace gbfem {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr long long kSpinLimit = 50000000LL;  // ~seconds; the barrier never waits that long when co-resident
+constexpr int kWarps = kPcgThreads / 32;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+	unsigned v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ int ldi(const int* p) { return *(const volatile int*)p; }
+__device__ __forceinline__ double ldd(const double* p) { return *(const volatile double*)p; }
+
+// Grid-wide barrier ending phase `ph` (all blocks co-resident: cooperative launch). The last
+// block to arrive clears the finished-segment counter that phase ph + 1 will count into.
+// Returns false on timeout.
+__device__ bool grid_barrier(PcgGlobal* g, int ph)
+{
+	__syncthreads();
+	__shared__ int ok;
+	if (threadIdx.x == 0)
+	{
+		ok = 1;
+		const unsigned gen = ld_acquire(&g->barGen);
+		__threadfence();
+		if (atomicAdd(&g->barCount, 1u) == gridDim.x - 1)
+		{
+			g->finishedIn[(ph + 1) & 1] = 0;
+			g->barCount = 0;
+			__threadfence();
+			atomicAdd(&g->barGen, 1u);
+		}
+		else
+		{
+			long long spins = 0;
+			while (ld_acquire(&g->barGen) == gen)
+			{
+				if (++spins > kSpinLimit)
+				{
+					atomicExch(&g->err, 1);
+					ok = 0;
+					break;
+				}
+				__nanosleep(32);
+			}
+		}
+		// Acquire side: the other blocks' writes of the finished phase become visible to this block
+		// (the next phase reads the vectors with plain, L1-cached loads).
+		__threadfence();
+	}
+	__syncthreads();
+	return ok && !*(volatile int*)&g->err;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+	return v;
+}
+
+// Largest s in [0, nseg) with Cp[s] <= t (for t < Cp[nseg] that segment is non-empty).
+__device__ __forceinline__ int seg_of(const int* Cp, int nseg, int t)
+{
+	int lo = 0, hi = nseg - 1;
+	while (lo < hi)
+	{
+		const int mid = (lo + hi + 1) >> 1;
+		if (Cp[mid] <= t)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	return lo;
+}
+
+// Warp-collective lower bound: smallest i in [L, R) with arr[i] >= key, or R. Same result in
+// every lane. Each round probes 32 evenly spaced entries.
+__device__ int lower_bound_warp(const int* __restrict__ arr, int L, int R, int key)
+{
+	const int lane = threadIdx.x & 31;
+	while (R - L > 32)
+	{
+		const int step = (R - L + 31) / 32;
+		const int i = L + (lane + 1) * step - 1;
+		const bool pred = (i < R) ? (__ldg(&arr[i]) >= key) : true;
+		const unsigned m = __ballot_sync(kFull, pred);
+		const int k = __ffs(m) - 1;  // m != 0: the last probe is at or past R - 1
+		const int iPrev = L + k * step - 1;
+		const int iK = L + (k + 1) * step - 1;
+		L = (k == 0) ? L : iPrev + 1;
+		R = (iK < R) ? iK : R;
+	}
+	const int i = L + lane;
+	const bool pred = (i < R) && (__ldg(&arr[i]) >= key);
+	const unsigned m = __ballot_sync(kFull, pred);
+	return m ? L + __ffs(m) - 1 : R;
+}
+
+// Per-CTA view of a set of segments: chunk-count prefix Cp and weight prefix Wp over the
+// segments (inactive segments count zero), and the partition range of this CTA.
+struct SetView
+{
+	const int* Cp;
+	const int* Wp;   // null for chunk-count partitions
+	int lo, hi;      // this CTA's positions
+	int n;           // total positions
+	long long tot;   // total weight (== n for chunk-count partitions)
+};
+
+// First position of CTA b in a block-column-weighted partition: the smallest t with
+// Wc(t) * G >= tot * b, where Wc(t) is the weight of positions [0, t). Warp-collective.
+__device__ int weighted_start(const PcgArgs& a, const int* Cp, const int* Wp, const int* sc, int nseg, int b, int G)
+{
+	const long long tot = Wp[nseg];
+	if (b <= 0 || tot == 0) return 0;
+	if (b >= G) return Cp[nseg];
+	const long long X = tot * b;
+	int lo = 0, hi = nseg - 1;  // largest s with Wp[s] * G < X
+	while (lo < hi)
+	{
+		const int mid = (lo + hi + 1) >> 1;
+		if ((long long)Wp[mid] * G < X)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	const int s = lo;
+	const long long need = (X - (long long)Wp[s] * G + G - 1) / G;  // >= 1
+	const int c0 = sc[s], ns = sc[s + 1] - sc[s];
+	const int key = __ldg(&a.cumW[c0]) + (int)need;
+	int j = lower_bound_warp(a.cumW, c0 + 1, c0 + ns + 1, key) - c0;
+	j = min(j, ns);
+	return Cp[s] + j;
+}
+
+// The CTA holding a position of cumulative weight w: floor(w * G / tot), capped.
+__device__ __forceinline__ int cta_of(long long w, long long tot, int G)
+{
+	return (int)min((long long)(G - 1), (w * G) / tot);
+}
+
+// First and last CTA holding positions of non-empty segment s in view V.
+__device__ __forceinline__ int2 seg_ctas(const PcgArgs& a, const SetView& V, const int* sc, int s)
+{
+	const int G = gridDim.x;
+	if (!V.Wp) return make_int2(cta_of(V.Cp[s], V.n, G), cta_of(V.Cp[s + 1] - 1, V.n, G));
+	const int cl = sc[s + 1] - 1;
+	const long long wl = (long long)V.Wp[s + 1] - (__ldg(&a.cumW[cl + 1]) - __ldg(&a.cumW[cl]));
+	return make_int2(cta_of(V.Wp[s], V.tot, G), cta_of(wl, V.tot, G));
+}
+
+// Calls f(slot, s, c) for this warp's share of the CTA's positions: slot = t - lo, s the
+// segment and c the chunk of position t.
+template <typename F>
+__device__ __forceinline__ void for_chunks(const SetView& V, const int* sc, int nseg, F f)
+{
+	int t = V.lo + (threadIdx.x >> 5);
+	if (t >= V.hi) return;
+	int s = seg_of(V.Cp, nseg, t);
+	for (; t < V.hi; t += kWarps)
+	{
+		while (V.Cp[s + 1] <= t) ++s;
+		f(t - V.lo, s, sc[s] + (t - V.Cp[s]));
+	}
+}
+
+// Reduce this CTA's chunk partials per segment (sp[k * M + slot]) and complete segments across
+// CTAs; fin(s, totals) runs once per segment in lane 0 of warp 0 of the completing CTA.
+template <int NV, typename Fin>
+__device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* sc, const double* sp, Fin fin)
+{
+	__syncthreads();
+	if ((threadIdx.x >> 5) != 0) return;
+	const int lane = threadIdx.x & 31;
+	const int nseg = a.nsegs, G = gridDim.x, B = blockIdx.x, M = a.maxChunksPerCta;
+	auto arrive = [&](int s, int2 fl, const double* v) {
+		const int which = (B > fl.x) ? 0 : 1;  // 0: first slot (CTAs after bf), 1: last slot (bf)
+		unsigned tk = 0;
+		if (lane == 0)
+		{
+#pragma unroll
+			for (int k = 0; k < NV; ++k) a.slots[(size_t)(2 * k + which) * G + B] = v[k];
+			__threadfence();
+			tk = atomicAdd(&a.seg[s].ticket, 1u);
+		}
+		tk = __shfl_sync(kFull, tk, 0);
+		if (tk != (unsigned)(fl.y - fl.x)) return;
+		__threadfence();
+		double tot[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+		{
+			double u = (lane == 0) ? __ldcg(&a.slots[(size_t)(2 * k + 1) * G + fl.x]) : 0.0;
+			for (int b = fl.x + 1 + lane; b <= fl.y; b += 32) u += __ldcg(&a.slots[(size_t)(2 * k) * G + b]);
+			tot[k] = warp_sum(u);
+		}
+		if (lane == 0)
+		{
+			a.seg[s].ticket = 0u;
+			fin(s, tot);
+		}
+	};
+	if (V.lo < V.hi)
+	{
+		for (int s = seg_of(V.Cp, nseg, V.lo); s < nseg && V.Cp[s] < V.hi; ++s)
+		{
+			if (V.Cp[s + 1] == V.Cp[s]) continue;
+			const int t0 = max(V.lo, V.Cp[s]), t1 = min(V.hi, V.Cp[s + 1]);
+			double v[NV];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+			{
+				double u = 0.0;
+				for (int t = t0 + lane; t < t1; t += 32) u += sp[k * M + (t - V.lo)];
+				v[k] = warp_sum(u);
+			}
+			const int2 fl = seg_ctas(a, V, sc, s);
+			if (fl.x == fl.y)
+			{
+				if (lane == 0) fin(s, v);
+			}
+			else
+				arrive(s, fl, v);
+		}
+	}
+	else if (V.lo < V.n)
+	{
+		// An empty range strictly inside a segment still counts among that segment's CTAs.
+		const int s = seg_of(V.Cp, nseg, V.lo);
+		if (V.lo > V.Cp[s])
+		{
+			double v[NV];
+#pragma unroll
+			for (int k = 0; k < NV; ++k) v[k] = 0.0;
+			arrive(s, seg_ctas(a, V, sc, s), v);
+		}
+	}
+}
+
+// q[row] (3 floats) = sum over the chunk's SELL slots of A_block * p(J), with p(J) = z(J) + beta p_old(J)
+// formed on the fly from the packed records; four slots' loads are issued before any is used.
+__device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __restrict__ zp, int c, int lane,
+											float beta, float& a0, float& a1, float& a2)
+{
+	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
+	int k = k0;
+	for (; k + 4 <= k1; k += 4)
+	{
+		int J[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) J[u] = __ldg(&a.col[(k + u) * 32 + lane]);
+		float4 zj[4], pj[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			zj[u] = zp[2 * J[u]];
+			pj[u] = zp[2 * J[u] + 1];
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			const float* vb = a.val + (size_t)(k + u) * 288 + lane;
+			const float p0 = zj[u].x + beta * pj[u].x, p1 = zj[u].y + beta * pj[u].y, p2 = zj[u].z + beta * pj[u].z;
+			a0 += __ldg(vb) * p0 + __ldg(vb + 32) * p1 + __ldg(vb + 64) * p2;
+			a1 += __ldg(vb + 96) * p0 + __ldg(vb + 128) * p1 + __ldg(vb + 160) * p2;
+			a2 += __ldg(vb + 192) * p0 + __ldg(vb + 224) * p1 + __ldg(vb + 256) * p2;
+		}
+	}
+	for (; k < k1; ++k)
+	{
+		const int J = __ldg(&a.col[k * 32 + lane]);
+		const float* vb = a.val + (size_t)k * 288 + lane;
+		const float4 zj = zp[2 * J], pj = zp[2 * J + 1];
+		const float p0 = zj.x + beta * pj.x, p1 = zj.y + beta * pj.y, p2 = zj.z + beta * pj.z;
+		a0 += __ldg(vb) * p0 + __ldg(vb + 32) * p1 + __ldg(vb + 64) * p2;
+		a1 += __ldg(vb + 96) * p0 + __ldg(vb + 128) * p1 + __ldg(vb + 160) * p2;
+		a2 += __ldg(vb + 192) * p0 + __ldg(vb + 224) * p1 + __ldg(vb + 256) * p2;
+	}
+}
+
+// FP64 residual rows of chunk c: r64 = b - A (x64 + x_delta); returns the lane's |r|^2 share.
+__device__ __forceinline__ double residual_row(const PcgArgs& a, int c, int rs, int lane)
+{
+	double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
+	for (int k = k0; k < k1; ++k)
+	{
+		const int J = __ldg(&a.col[k * 32 + lane]);
+		const float* vp = a.val + (size_t)k * 288 + lane;
+		const double x0 = a.x64[3 * J] + double(a.xd[3 * J]);
+		const double x1 = a.x64[3 * J + 1] + double(a.xd[3 * J + 1]);
+		const double x2 = a.x64[3 * J + 2] + double(a.xd[3 * J + 2]);
+		a0 += double(__ldg(vp)) * x0 + double(__ldg(vp + 32)) * x1 + double(__ldg(vp + 64)) * x2;
+		a1 += double(__ldg(vp + 96)) * x0 + double(__ldg(vp + 128)) * x1 + double(__ldg(vp + 160)) * x2;
+		a2 += double(__ldg(vp + 192)) * x0 + double(__ldg(vp + 224)) * x1 + double(__ldg(vp + 256)) * x2;
+	}
+	const double aa[3] = {a0, a1, a2};
+	double rr = 0.0;
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		const double ri = a.brs[3 * rs + i] - aa[i];
+		a.r64[3 * rs + i] = ri;
+		rr += ri * ri;
+	}
+	return rr;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
+{
+	extern __shared__ double dsm[];
+	const int lane = threadIdx.x & 31;
+	const int warp = threadIdx.x >> 5;
+	const int nseg = a.nsegs, M = a.maxChunksPerCta, G = gridDim.x, B = blockIdx.x;
+	double* sp = dsm;                                  // [2][M] chunk partials of this CTA
+	int* sc = reinterpret_cast<int*>(dsm + 2 * M);     // segChunk copy (chunk prefix of all segments)
+	int* Cp = sc + (nseg + 1);                         // active set: chunk prefix
+	int* Wp = Cp + (nseg + 1);                         // active set: weight prefix
+	__shared__ int shRange[4];
+	__shared__ int shFinished;
+	for (int i = threadIdx.x; i <= nseg; i += blockDim.x) sc[i] = a.segChunk[i];
+	__syncthreads();
+
+	// zp records: float4 pair per row, .x/.y/.z used: [2*rs] = z = invdiag * r, [2*rs + 1] = p.
+	float4* zpOld = reinterpret_cast<float4*>(a.pA);
+	float4* zpNew = reinterpret_cast<float4*>(a.pB);
+
+	int ph = 0;  // phase id, the same in every CTA; segments finished in phase ph are stamped ph + 1
+	auto finish = [&](SegCtl& S) {
+		S.done = ph + 1;
+		atomicAdd(&a.g->finishedIn[ph & 1], 1);
+		atomicAdd(&a.g->finishedSegs, 1);
+	};
+	// All chunks, chunk-count partition (positions are chunk ids).
+	SetView all;
+	all.Cp = sc;
+	all.Wp = nullptr;
+	all.n = a.nchunks;
+	all.tot = a.nchunks;
+	all.lo = (int)(((long long)all.n * B + G - 1) / G);
+	all.hi = (int)(((long long)all.n * (B + 1) + G - 1) / G);
+	SetView actW, actC;  // active set: block-column-weighted and chunk-count partitions
+	actW.Cp = actC.Cp = Cp;
+	actW.Wp = Wp;
+	actC.Wp = nullptr;
+	// Rebuild the active-set prefixes and this CTA's ranges (segments stamped before phase ph are out).
+	auto rebuild = [&]() {
+		if (warp == 0)
+		{
+			int carryC = 0, carryW = 0;
+			if (lane == 0) Cp[0] = Wp[0] = 0;
+			for (int base = 0; base < nseg; base += 32)
+			{
+				const int s = base + lane;
+				int c = 0, w = 0;
+				if (s < nseg)
+				{
+					const int d = ldi(&a.seg[s].done);
+					if (d == 0 || d > ph)
+					{
+						c = sc[s + 1] - sc[s];
+						w = __ldg(&a.cumW[sc[s + 1]]) - __ldg(&a.cumW[sc[s]]);
+					}
+				}
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1)
+				{
+					const int tc = __shfl_up_sync(kFull, c, o), tw = __shfl_up_sync(kFull, w, o);
+					if (lane >= o)
+					{
+						c += tc;
+						w += tw;
+					}
+				}
+				if (s < nseg)
+				{
+					Cp[s + 1] = carryC + c;
+					Wp[s + 1] = carryW + w;
+				}
+				carryC += __shfl_sync(kFull, c, 31);
+				carryW += __shfl_sync(kFull, w, 31);
+			}
+			__syncwarp();
+			const int lo = weighted_start(a, Cp, Wp, sc, nseg, B, G);
+			const int hi = weighted_start(a, Cp, Wp, sc, nseg, B + 1, G);
+			if (lane == 0)
+			{
+				const long long n = Cp[nseg];
+				shRange[0] = lo;
+				shRange[1] = hi;
+				shRange[2] = (int)((n * B + G - 1) / G);
+				shRange[3] = (int)((n * (B + 1) + G - 1) / G);
+			}
+		}
+		__syncthreads();
+		actW.lo = shRange[0];
+		actW.hi = shRange[1];
+		actC.lo = shRange[2];
+		actC.hi = shRange[3];
+		if (actW.hi - actW.lo > M || actC.hi - actC.lo > M)
+		{
+			// Cannot happen with the host's bound on M; clamp so shared memory stays in range.
+			if (threadIdx.x == 0) atomicExch(&a.g->err, 2);
+			actW.hi = min(actW.hi, actW.lo + M);
+			actC.hi = min(actC.hi, actC.lo + M);
+		}
+		actW.n = actC.n = Cp[nseg];
+		actW.tot = Wp[nseg];
+		actC.tot = actC.n;
+	};
+	int finished = 0;  // segments finished before the current phase (same in every CTA)
+	// Phase start: count the segments finished in the previous phase and rebuild if any.
+	auto phase_start = [&](bool force) {
+		if (threadIdx.x == 0) shFinished = ldi(&a.g->finishedIn[(ph - 1) & 1]);
+		__syncthreads();
+		const int nf = shFinished;
+		finished += nf;
+		if (nf > 0 || force) rebuild();
+	};
+	auto barrier = [&]() {
+		const bool ok = grid_barrier(a.g, ph);
+		++ph;
+		return ok;
+	};
+
+	// ---- I1: gather b, invdiag into row space; x = 0; p = 0; |b|^2 per segment.
+	for_chunks(all, sc, nseg, [&](int slot, int, int c) {
+		const int rs = 32 * c + lane;
+		const int I = a.perm[rs];
+		double bb = 0.0;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			const double bi = (I >= 0) ? a.b[3 * I + k] : 0.0;
+			a.brs[3 * rs + k] = bi;
+			a.r64[3 * rs + k] = bi;
+			a.invd[3 * rs + k] = (I >= 0) ? a.invdiag[3 * I + k] : 0.f;
+			a.x64[3 * rs + k] = 0.0;
+			a.xd[3 * rs + k] = 0.f;
+			bb += bi * bi;
+		}
+		zpOld[2 * rs + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+		bb = warp_sum(bb);
+		if (lane == 0) sp[slot] = bb;
+	});
+	reduce_segments<1>(a, all, sc, sp, [&](int s, const double* tot) {
+		SegCtl& S = a.seg[s];
+		S.bb = tot[0];
+		S.rrTrue = tot[0];
+		S.threshold = fmax(a.tol * a.tol * tot[0], DBL_MIN);
+		S.s = sqrt(tot[0]);
+		S.iter = 0;
+		S.updates = 0;
+		S.mode = 0;
+		S.beta = 0.0;
+		S.converged = (tot[0] == 0.0 || tot[0] < S.threshold) ? 1 : 0;
+		S.nonfinite = !isfinite(tot[0]);
+		if (S.converged || S.nonfinite) finish(S);
+	});
+	if (!barrier()) return;
+
+	// ---- I2: r = b / s (FP32), z = invdiag r, rz, |r|^2.
+	phase_start(true);
+	for_chunks(actC, sc, nseg, [&](int slot, int s, int c) {
+		const int rs = 32 * c + lane;
+		const double inv = 1.0 / ldd(&a.seg[s].s);
+		float rz = 0.f, rr = 0.f, z[3];
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			const float ri = float(a.brs[3 * rs + k] * inv);
+			a.r[3 * rs + k] = ri;
+			z[k] = a.invd[3 * rs + k] * ri;
+			rz += ri * z[k];
+			rr += ri * ri;
+		}
+		zpOld[2 * rs] = make_float4(z[0], z[1], z[2], 0.f);
+		rz = warp_sum(rz);
+		rr = warp_sum(rr);
+		if (lane == 0)
+		{
+			sp[slot] = rz;
+			sp[M + slot] = rr;
+		}
+	});
+	reduce_segments<2>(a, actC, sc, sp, [&](int s, const double* tot) {
+		a.seg[s].rz = tot[0];
+		a.seg[s].rr32 = tot[1];
+		a.seg[s].rrLast = tot[1];
+	});
+	if (!barrier()) return;
+
+	const int maxLoop = 2 * a.maxIter + 8;  // a refresh takes one extra iteration slot
+	for (int it = 0; it < maxLoop; ++it)
+	{
+		// ---- Phase 1. mode 0: p_new = z + beta p_old (own rows, and on the fly for gathered rows);
+		// q = A p_new; pq. mode 1: r64 = b - A (x64 + x_delta) in FP64.
+		phase_start(false);
+		if (finished >= nseg) break;
+		for_chunks(actW, sc, nseg, [&](int slot, int s, int c) {
+			const int rs = 32 * c + lane;
+			double part;
+			if (ldi(&a.seg[s].mode) == 0)
+			{
+				const float beta = float(ldd(&a.seg[s].beta));
+				float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+				spmv_row_zp(a, zpOld, c, lane, beta, a0, a1, a2);
+				const float4 zi = zpOld[2 * rs], pi = zpOld[2 * rs + 1];
+				const float4 pn = make_float4(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z, 0.f);
+				zpNew[2 * rs + 1] = pn;
+				a.q[3 * rs] = a0;
+				a.q[3 * rs + 1] = a1;
+				a.q[3 * rs + 2] = a2;
+				part = warp_sum(pn.x * a0 + pn.y * a1 + pn.z * a2);
+			}
+			else
+				part = warp_sum(residual_row(a, c, rs, lane));
+			if (lane == 0) sp[slot] = part;
+		});
+		reduce_segments<1>(a, actW, sc, sp, [&](int s, const double* tot) {
+			SegCtl& S = a.seg[s];
+			if (S.mode == 0)
+			{
+				S.pq = tot[0];
+				S.alpha = S.rz / tot[0];
+				return;
+			}
+			S.rrTrue = tot[0];
+			S.updates += 1;
+			if (tot[0] < S.threshold)
+			{
+				S.converged = 1;  // like Eigen, the converging iteration is not counted
+				finish(S);
+			}
+			else if (!isfinite(tot[0]) || S.iter + 1 >= a.maxIter)
+			{
+				S.converged = 0;
+				S.nonfinite = !isfinite(tot[0]);
+				S.iter += 1;
+				finish(S);
+			}
+			else
+			{
+				const double sNew = sqrt(tot[0]);
+				S.ratio = S.s / sNew;
+				S.s = sNew;
+				S.mode = 2;
+			}
+		});
+		if (!barrier()) return;
+
+		// ---- Phase 2. mode 0: x_delta += alpha s p, r -= alpha q, z = invdiag r; |r|^2, r.z; decide
+		// on a refresh. mode 2: fold x, r = r64 / s, z = invdiag r, p *= ratio; |r|^2, r.z.
+		phase_start(false);
+		for_chunks(actC, sc, nseg, [&](int slot, int s, int c) {
+			const int rs = 32 * c + lane;
+			float s0 = 0.f, s1 = 0.f, z[3];
+			if (ldi(&a.seg[s].mode) == 0)
+			{
+				const double alphaD = ldd(&a.seg[s].alpha);
+				const float alpha = float(alphaD);
+				const float as = float(alphaD * ldd(&a.seg[s].s));
+				const float4 pn = zpNew[2 * rs + 1];
+				const float pv[3] = {pn.x, pn.y, pn.z};
+#pragma unroll
+				for (int i = 0; i < 3; ++i)
+				{
+					const int d = 3 * rs + i;
+					a.xd[d] += as * pv[i];
+					const float ri = a.r[d] - alpha * a.q[d];
+					a.r[d] = ri;
+					z[i] = a.invd[d] * ri;
+					s0 += ri * ri;
+					s1 += ri * z[i];
+				}
+			}
+			else
+			{
+				const double inv = 1.0 / ldd(&a.seg[s].s);
+				const float ratio = float(ldd(&a.seg[s].ratio));
+#pragma unroll
+				for (int i = 0; i < 3; ++i)
+				{
+					const int d = 3 * rs + i;
+					a.x64[d] += double(a.xd[d]);
+					a.xd[d] = 0.f;
+					const float ri = float(a.r64[d] * inv);
+					a.r[d] = ri;
+					z[i] = a.invd[d] * ri;
+					s0 += ri * ri;
+					s1 += ri * z[i];
+				}
+				const float4 po = zpOld[2 * rs + 1];
+				zpNew[2 * rs + 1] = make_float4(po.x * ratio, po.y * ratio, po.z * ratio, 0.f);
+			}
+			zpNew[2 * rs] = make_float4(z[0], z[1], z[2], 0.f);
+			s0 = warp_sum(s0);
+			s1 = warp_sum(s1);
+			if (lane == 0)
+			{
+				sp[slot] = s0;
+				sp[M + slot] = s1;
+			}
+		});
+		reduce_segments<2>(a, actC, sc, sp, [&](int s, const double* tot) {
+			SegCtl& S = a.seg[s];
+			if (S.mode == 2)
+			{
+				S.beta = tot[1] / (S.rzPend * S.ratio * S.ratio);
+				S.rz = tot[1];
+				S.rr32 = tot[0];
+				S.rrLast = tot[0];
+				S.iter += 1;
+				S.mode = 0;
+				return;
+			}
+			S.rr32 = tot[0];
+			if (!isfinite(tot[0]) || !isfinite(S.alpha))
+			{
+				S.converged = 0;
+				S.nonfinite = 1;
+				finish(S);
+			}
+			else if (S.s * S.s * tot[0] < S.threshold || tot[0] < a.drop * S.rrLast || S.iter + 1 >= a.maxIter)
+			{
+				S.mode = 1;  // FP64 residual before the next direction
+				S.rzPend = S.rz;
+			}
+			else
+			{
+				const double rzOld = S.rz;
+				S.rz = tot[1];
+				S.beta = tot[1] / rzOld;
+				S.iter += 1;
+			}
+		});
+		if (!barrier()) return;
+		float4* t = zpOld;
+		zpOld = zpNew;
+		zpNew = t;
+	}
+
+	// ---- Out: x (dof space) = x64 + x_delta.
+	for_chunks(all, sc, nseg, [&](int, int, int c) {
+		const int rs = 32 * c + lane;
+		const int I = a.perm[rs];
+		if (I < 0) return;
+#pragma unroll
+		for (int k = 0; k < 3; ++k) a.x[3 * I + k] = a.x64[3 * rs + k] + double(a.xd[3 * rs + k]);
+	});
+}
+
+}  // namespace gbfem

@@ -1,0 +1,77 @@
+// gbfem_pcg.h -- persistent mixed-precision CG over a batch of segments (declarations).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace gbfem {
+
+constexpr int kPcgThreads = 256;
+constexpr int kPcgChunkWeight = 2;  // per-chunk constant added to the block-column count (SpMV work)
+
+// Per-segment (per-mesh) CG state, in device memory. Written by the CTA that completes a
+// segment's reduction, read by every CTA after the next grid barrier.
+struct SegCtl
+{
+	double bb, threshold;   // |b|^2, tol^2 |b|^2
+	double s;               // residual scale: r_true ~= s * r32
+	double rz, pq, alpha, beta;
+	double rr32, rrLast;    // |r32|^2 now and right after the last refresh
+	double rrTrue;          // |b - A x|^2 at the last refresh
+	double ratio, rzPend;
+	int iter, updates, done, converged;
+	int mode;               // 0: CG step; 1: FP64 residual next; 2: rescale next
+	int nonfinite;
+	unsigned int ticket;
+	int pad;
+};
+
+// Grid-wide control of one persistent launch.
+struct PcgGlobal
+{
+	unsigned int barCount, barGen;
+	int finishedSegs;    // total, for diagnostics
+	int finishedIn[2];   // segments finished in the current / previous phase (by phase parity)
+	int err, pad[2];
+};
+
+struct PcgArgs
+{
+	int nchunks, nsegs, maxIter, maxChunksPerCta;
+	double tol, drop;
+	// SELL-32 matrix in row space (column = neighbour row position), FP32 values
+	const int* off;        // nchunks + 1
+	const int* col;
+	const float* val;
+	const int* perm;       // row position -> node id, -1 for padding rows
+	const int* segChunk;   // nsegs + 1: first chunk of each segment (segments own contiguous chunks)
+	const int* cumW;       // nchunks + 1: prefix of (block columns + kPcgChunkWeight) per chunk
+	double* slots;         // 4 * grid cross-CTA partials: [value k][first/last][cta]
+	// in / out (dof space, FP64)
+	const double* b;
+	const float* invdiag;
+	double* x;
+	// row-space work vectors
+	double* brs;
+	double* r64;
+	double* x64;
+	float* xd;
+	float* invd;
+	float* r;
+	float* pA;             // 8 floats per row: z (3), pad, p (3), pad; 32-byte aligned
+	float* pB;
+	float* q;
+	SegCtl* seg;
+	PcgGlobal* g;
+};
+
+// Dynamic shared memory of one CTA: the active-set prefix arrays and the chunk partials.
+inline size_t pcg_smem_bytes(int nsegs, int maxChunksPerCta)
+{
+	return 2 * sizeof(double) * (size_t)maxChunksPerCta + 3 * sizeof(int) * (size_t)(nsegs + 1);
+}
+
+__global__ void k_pcg_persistent(PcgArgs a);
+
+}  // namespace gbfem

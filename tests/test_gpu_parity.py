@@ -183,3 +183,34 @@ def test_mixed_matches_fp64_gpu_and_is_deterministic(gpu_lib):
     x0 = s.mesh.nodes.ravel()
     assert rel(xa - x0, xc - x0) < 1e-6
     assert a.stats()["cg_relative_residual"] < 1e-10
+
+
+def test_batch_of_uneven_meshes_matches_individual_oracles(gpu_lib):
+    """Batched mixed form: every mesh of a batch steps like its own FP64 oracle (<= 1e-6)."""
+    rng = np.random.default_rng(11)
+    scenes = [mesh.scene_cube(a, b, c, seed=k, young=float(E))
+              for k, (a, b, c, E) in enumerate([(2, 2, 3, 1e4), (4, 3, 2, 1e5), (1, 1, 1, 3e5), (5, 5, 6, 1e6),
+                                                 (3, 6, 2, 2e4), (7, 7, 7, 8e4)])]
+    batch = Body([s.mesh for s in scenes], rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0, 0, -9.81),
+                 cg_tolerance=1e-10, precision=_lib.PRECISION_MIXED)
+    assert batch.num_meshes == len(scenes)
+    oracles = [O.OracleModel.from_scene(s) for s in scenes]
+    v0 = rng.normal(0, 0.01, batch.n)
+    batch.set_state(None, v0)
+    for k, o in enumerate(oracles):
+        n0, n1 = batch.node_offsets[k], batch.node_offsets[k + 1]
+        o.set_state(None, v0[3 * n0:3 * n1])
+    for step in range(12):
+        assert batch.step(1e-3) == _lib.GBFEM_OK
+        for o in oracles:
+            assert o.step(1e-3) == 0
+    x, _ = batch.state()
+    st = batch.segment_stats()
+    assert np.all(st["converged"] == 1) and np.all(st["relative_residual"] < 1e-10)
+    for k, (s, o) in enumerate(zip(scenes, oracles)):
+        n0, n1 = batch.node_offsets[k], batch.node_offsets[k + 1]
+        ox, _ = o.state()
+        x0 = s.mesh.nodes.ravel()
+        err = rel(x[3 * n0:3 * n1] - x0, ox - x0)
+        print(f"mesh {k}: {s.mesh.num_tets} tets, rel disp err {err:.2e}, iterations {st['iterations'][k]}")
+        assert err <= 1e-6
