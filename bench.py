@@ -1,15 +1,22 @@
 #!/usr/bin/env python
 """Benchmark: tet-element-steps/s of the corotational-tet implicit-Euler step on one GB300.
 
-Workload (default): the 40x40x160 cube-grid bar of edge h = 4 mm, 5 tets per cube (1,280,000 tets,
-270,641 nodes, 811,923 dofs), per-tet E log-uniform in [1e4, 1e6] Pa and nu uniform in [0.40, 0.49], z = 0
-clamped, the z = 160h face driven by a 20% compression ramp over 50 steps, gravity, dt = 1e-3,
-CG tolerance 1e-10. A step is one FemRepresentation::update(dt). Inputs are synthetic (seeded).
+Default workload (--config batch): 256 independent cube-grid meshes of edge 1 cm, 5 tets per cube,
+node counts log-uniform in [500, 50000] (11,543,720 tets, 2,613,280 nodes from seed 3), per-mesh E
+log-uniform in [1e4, 1e6] Pa, nu 0.45, rho 1000, bottom faces fixed, gravity -9.81 z, Rayleigh
+alpha 0.01 / beta 0.001, dt 1e-3, CG tolerance 1e-10, one Newton iteration. A step is one
+FemRepresentation::update(dt) of every mesh. The measured form is the batched mixed-precision step
+(FP32 element / assembly / CG, FP64 residual refreshes, all meshes in one persistent launch); the
+same meshes are also stepped through the plain FP64 GPU path one mesh at a time, and the line
+carries that path's throughput, the speed-up over it and the mixed-vs-FP64 displacement error.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config batch|bar|cube]
+                    [--precision fp64|mixed] [--impl reference]
 
-One JSON line on rank 0. Under torchrun every rank steps its own replica of the bar on its own GPU
-(replicas only: a single mesh does not shard without a halo exchange) and the job value is the sum.
+--config bar is the 40x40x160 compression bar (h 4 mm, 1.28M tets), --config cube the 10x10x10 cube
+(5,000 tets); both take --precision. Inputs are synthetic (seeded). One JSON line on rank 0. Under
+torchrun every rank steps its own copy of the workload on its own GPU (independent meshes shard
+with no data-path collective; weak scaling) and the job value is the sum over ranks.
 """
 
 from __future__ import annotations
@@ -22,16 +29,19 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "tet-element-steps/s"
+METRIC = "tet-element-steps/s, mixed+batched vs plain FP64 GPU path at <=1e-6 rel disp err"
+UNIT = "tet-element-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 CG_CAP = 10000
+BATCH = dict(count=256, lo=500, hi=50000, seed=3)
+BATCH_PARAMS = dict(rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0.0, 0.0, -9.81), cg_tolerance=1e-10)
+COMPARE_STEPS = 4  # steps of the FP64-path comparison (1 untimed + 3 timed) and of the error check
 
 
 def log(msg):
@@ -146,21 +156,219 @@ def load_traffic(kernel_key):
         return None
 
 
-def build_scene(args):
+def host_threads():
+    return max(1, math.ceil(0.5 * (os.cpu_count() or 1)))
+
+
+# ------------------------------------------------------------------------------------------------
+# Algorithmic bytes (HBM) of the solve, per CG iteration and per FP64 residual refresh, for one
+# mesh with scalar non-zeros nnz, N nodes and n = 3N dofs; s = bytes per matrix value. Block
+# sparse storage reads one 4-byte column index per 3x3 block (nnz / 9 of them) and one offset per
+# block row; ten vector passes per iteration; a refresh reads x, b and writes r in FP64.
+
+def bytes_per_iteration(nnz, N, s):
+    return nnz * s + (nnz // 9) * 4 + 4 * (N + 1) + 10 * s * 3 * N
+
+
+def bytes_per_refresh(nnz, N, s):
+    return nnz * s + (nnz // 9) * 4 + 4 * (N + 1) + 3 * 8 * 3 * N
+
+
+# ------------------------------------------------------------------------------------------------
+# Batched workload
+
+def batch_scenes():
+    from opensurgsim_gb300 import mesh
+
+    return mesh.scenes_batch(**BATCH)
+
+
+def batch_body(meshes, precision, device):
+    from opensurgsim_gb300 import _lib
+    from opensurgsim_gb300.body import Body
+
+    return Body(meshes, precision=precision, device=device, **BATCH_PARAMS)
+
+
+def rel_disp_err(x_mixed, x64, rest):
+    import numpy as np
+
+    d64 = x64 - rest
+    return float(np.linalg.norm((x_mixed - rest) - d64) / max(np.linalg.norm(d64), 1e-300))
+
+
+def fp64_path_comparison(meshes, local):
+    """The plain FP64 GPU path on the same meshes, one handle per mesh stepped in turn (the
+    reference steps representations one by one): COMPARE_STEPS steps, the last ones timed; and the
+    batched mixed step over the same steps for the displacement error."""
+    import numpy as np
+    import torch
+
+    from opensurgsim_gb300 import _lib
+    from opensurgsim_gb300.body import Body
+
+    bodies = [Body(m, precision=_lib.PRECISION_FP64, device=local, cg_max_iterations=0, **BATCH_PARAMS)
+              for m in meshes]
+    for b in bodies:
+        b.step(1e-3, 1)
+    torch.cuda.synchronize(local)
+    t0 = time.perf_counter()
+    its = 0
+    for _ in range(COMPARE_STEPS - 1):
+        for b in bodies:
+            b.step(1e-3, 1)
+            its += b.stats()["cg_iterations"]
+    torch.cuda.synchronize(local)
+    sec = (time.perf_counter() - t0) / (COMPARE_STEPS - 1)
+    tets = sum(m.num_tets for m in meshes)
+    x64 = [b.state()[0] for b in bodies]
+    for b in bodies:
+        b.close()
+    mixed = batch_body(meshes, _lib.PRECISION_MIXED, local)
+    mixed.step(1e-3, COMPARE_STEPS)
+    xm, _ = mixed.state()
+    errs = []
+    for k, m in enumerate(meshes):
+        n0, n1 = mixed.node_offsets[k], mixed.node_offsets[k + 1]
+        errs.append(rel_disp_err(xm[3 * n0:3 * n1], x64[k], m.nodes.ravel()))
+    mixed.close()
+    return {"value": tets / sec, "unit": UNIT, "ms_per_step": 1e3 * sec,
+            "cg_iterations_per_step": its / (COMPARE_STEPS - 1),
+            "how": (f"plain FP64 form, one handle per mesh stepped in turn; steps 2-{COMPARE_STEPS} timed "
+                    "(host clock around device-synchronised steps)")}, {
+        "max": max(errs), "median": float(np.median(errs)), "after_steps": COMPARE_STEPS,
+        "definition": "||u_mixed - u_fp64|| / ||u_fp64|| per mesh, u = x - x_rest"}
+
+
+def run_batch(args, rank, world, local, dist):
+    import numpy as np
+    import torch
+
+    from opensurgsim_gb300 import _lib, build
+
+    build.build()
+    torch.cuda.set_device(local)
+    scenes = batch_scenes()
+    meshes = [s.mesh for s in scenes]
+    tets = sum(m.num_tets for m in meshes)
+    nodes = sum(m.num_nodes for m in meshes)
+    log(f"batch: {len(meshes)} meshes, {tets} tets, {nodes} nodes")
+    body = batch_body(meshes, _lib.PRECISION_MIXED, local)
+    stream = torch.cuda.ExternalStream(body.stream(), device=local)
+    flags = _lib.STEP_TIME_KERNELS
+    for _ in range(args.warmup):
+        body.step(1e-3, 1, flags)
+    torch.cuda.synchronize(local)
+    dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches, solve_ms, statuses = 0, 0.0, []
+    alg_bytes = 0.0
+    nnz = body.nnz_per_mesh
+    nn = np.diff(body.node_offsets)
+    it_bytes = np.array([bytes_per_iteration(int(z), int(N), 4) for z, N in zip(nnz, nn)], dtype=np.float64)
+    rf_bytes = np.array([bytes_per_refresh(int(z), int(N), 4) for z, N in zip(nnz, nn)], dtype=np.float64)
+    io_bytes = float(np.sum(16 * 3 * nn))  # b in, x out (FP64)
+    iters_total = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        statuses.append(body.step(1e-3, 1, flags))
+        s = body.stats()
+        launches += s["kernel_launches"]
+        solve_ms += s["ms_spmv"]
+        ss = body.segment_stats()
+        alg_bytes += float(np.dot(ss["iterations"], it_bytes) + np.dot(ss["refreshes"], rf_bytes)) + io_bytes
+        iters_total += int(ss["iterations"].max())
+    ev1.record(stream)
+    torch.cuda.synchronize(local)
+    clocks = sampler.stop()
+    dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = dist.reduce(ms, "max")
+    value = dist.reduce(tets * args.steps, "sum") / (ms_max / 1e3)
+    log(f"timed region: {args.steps} steps in {ms:.1f} ms ({tets * args.steps / ms * 1e3 / 1e6:.1f} M tet-steps/s)")
+
+    # End to end through the public API with host buffers: every step the state of all meshes is
+    # copied in from pinned host memory (gbfem_set_state), stepped, and read back (gbfem_get_state).
+    h_x = torch.empty(body.n, dtype=torch.float64).pin_memory().numpy()
+    h_v = torch.empty(body.n, dtype=torch.float64).pin_memory().numpy()
+    body_lib = _lib.load()
+    body_lib.gbfem_get_state(body.handle, _lib.dptr(h_x), _lib.dptr(h_v))
+    torch.cuda.synchronize(local)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        body_lib.gbfem_set_state(body.handle, _lib.dptr(h_x), _lib.dptr(h_v))
+        body.step(1e-3, 1, 0)
+        body_lib.gbfem_get_state(body.handle, _lib.dptr(h_x), _lib.dptr(h_v))
+    torch.cuda.synchronize(local)
+    e2e_s = dist.reduce(time.perf_counter() - t0, "max")
+    e2e_value = dist.reduce(tets * args.steps, "sum") / e2e_s
+    log(f"e2e region: {args.steps} steps in {e2e_s:.3f} s")
+    body.close()
+
+    peak, peak_kind = load_peak()
+    launch_ms = solve_ms / max(1, args.steps)
+    per_launch = alg_bytes / max(1, args.steps)
+    achieved = per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else None
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded cube-grid meshes)",
+        "config": {
+            "workload": ("batch256: 256 cube-grid meshes (h 1 cm, 5 tets per cube, nodes log-U[500,50000], seed 3), "
+                         f"{tets} tets, {nodes} nodes, E log-U[1e4,1e6] per mesh, nu 0.45, bottom faces fixed, "
+                         "gravity, alpha 0.01, beta 0.001, dt 1e-3, CG tol 1e-10; batched mixed precision, one "
+                         "persistent solve launch per step"),
+            "meshes": len(meshes), "tets": tets, "nodes": nodes, "precision": "mixed",
+            "l2": "working set (~2 GB) larger than L2: no flush needed",
+            "parallelism": f"independent meshes, one batch per rank x{world}",
+        },
+        "gpu_launches": int(launches),
+        "cg_iterations_per_step": iters_total / max(1, args.steps),
+        "step_status": sorted(set(int(s) for s in statuses)),
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * body.n * 8,
+                "d2h_bytes_per_step": 2 * body.n * 8},
+        "roofline": {
+            "kernel": "k_pcg_persistent (whole batched mixed-precision solve, one launch per step)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "traffic": load_traffic("pcg_persistent_batch256"),
+            "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": launch_ms,
+            "peak_source": f"{peak_kind} (hbm_gbs)",
+            "bytes_model": ("per mesh: CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*3N) + refreshes x "
+                            "(nnz*4 + nnz/9*4 + 4(N+1) + 3*8*3N) + 16*3N"),
+        },
+    }
+    return line, scenes
+
+
+# ------------------------------------------------------------------------------------------------
+# Single-mesh workloads (bar, cube)
+
+def build_scene(config):
     from opensurgsim_gb300 import mesh
 
     # The explicit CG iteration cap only bounds the run if a solve ever stagnates; at the
     # benchmark's states CG converges in a few hundred iterations, far below it.
-    if args.config == "bar":
+    if config == "bar":
         return mesh.scene_bar_compression(cg_max_iterations=CG_CAP)
     return mesh.scene_cube(10, 10, 10, cg_max_iterations=CG_CAP)
 
 
-def scenario_velocities(scene, step):
-    return scene.driven_values(step) if scene.driven_dofs is not None else None
-
-
-def run_ours(args, rank, world, local, dist):
+def run_single(args, rank, world, local, dist):
     import numpy as np
     import torch
 
@@ -169,7 +377,7 @@ def run_ours(args, rank, world, local, dist):
 
     build.build()
     torch.cuda.set_device(local)
-    scene = build_scene(args)
+    scene = build_scene(args.config)
     m = scene.mesh
     log(f"scene {scene.name}: {m.num_tets} tets, {m.num_nodes} nodes")
     prec = _lib.PRECISION_MIXED if args.precision == "mixed" else _lib.PRECISION_FP64
@@ -177,6 +385,7 @@ def run_ours(args, rank, world, local, dist):
     stream = torch.cuda.ExternalStream(body.stream(), device=local)
     dt = scene.dt
     driven = scene.driven_dofs is not None
+    body_lib = _lib.load()
     if driven:
         d_dofs = torch.from_numpy(scene.driven_dofs.astype(np.int32)).cuda(local)
         ramp = torch.from_numpy(scene.driven_values(0)).cuda(local)
@@ -187,23 +396,19 @@ def run_ours(args, rank, world, local, dist):
             vals = ramp if step < scene.ramp_steps else hold
             body_lib.gbfem_set_velocities_device(body.handle, d_dofs.numel(), d_dofs.data_ptr(), vals.data_ptr())
 
-    body_lib = _lib.load()
     flags = _lib.STEP_TIME_KERNELS
-    log(f"body created: nnz {body.nnz}")
     step = 0
     for _ in range(args.warmup):
         set_driven(step)
         body.step(dt, 1, flags)
         step += 1
     torch.cuda.synchronize(local)
-    log(f"warm-up done ({args.warmup} steps)")
     dist.barrier()
     sampler = ClockSampler(local)
     sampler.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    agg = dict(cg_iterations=0, kernel_launches=0, ms_spmv=0.0, spmv_timed=0, refinement_sweeps=0,
-               polar_fallbacks=0, cg_max_iterations_hit=0)
+    agg = dict(cg_iterations=0, kernel_launches=0, ms_spmv=0.0, spmv_timed=0, refinement_sweeps=0)
     statuses = []
     ev0.record(stream)
     for _ in range(args.steps):
@@ -242,24 +447,31 @@ def run_ours(args, rank, world, local, dist):
         step += 1
     torch.cuda.synchronize(local)
     e2e_s = dist.reduce(time.perf_counter() - t0, "max")
-    log(f"e2e region: {args.steps} steps in {e2e_s:.3f} s")
     e2e_value = total_units / e2e_s
     h2d = (scene.driven_dofs.size * (4 + 8)) if driven else 0
     d2h = 2 * body.n * 8
-
-    # Roofline of the dominant kernel: the CG matrix-vector product on the symmetric BSR matrix.
-    nb = body.nnz // 9
-    val_bytes = 8 if prec == _lib.PRECISION_FP64 else 4
-    spmv_bytes = body.nnz * val_bytes + nb * 4 + (body.num_nodes + 1) * 4 + 2 * body.n * val_bytes
-    spmv_ms = agg["ms_spmv"] / max(1, agg["spmv_timed"])
     peak, peak_kind = load_peak()
-    achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9 if spmv_ms > 0 else None
-    traffic = load_traffic(f"spmv_sell_{args.precision}_{args.config}")
     cg_per_step = agg["cg_iterations"] / max(1, args.steps)
+    if prec == _lib.PRECISION_FP64:
+        # Dominant kernel: the CG SpMV on the SELL-32 block matrix, timed per launch.
+        spmv_bytes = body.nnz * 8 + (body.nnz // 9) * 4 + (body.num_nodes + 1) * 4 + 2 * body.n * 8
+        launch_ms = agg["ms_spmv"] / max(1, agg["spmv_timed"])
+        kernel, per_launch, key = "k_cg_spmv_sell (fp64)", spmv_bytes, f"spmv_sell_fp64_{args.config}"
+        model = "nnz*8 + nnz/9*4 + 4(N+1) + 2*8*n per SpMV"
+    else:
+        # Dominant kernel: the persistent mixed-precision solve, one launch per step.
+        launch_ms = agg["ms_spmv"] / max(1, args.steps)
+        iters = agg["cg_iterations"] / max(1, args.steps)
+        sweeps = agg["refinement_sweeps"] / max(1, args.steps)
+        per_launch = (iters * bytes_per_iteration(body.nnz, body.num_nodes, 4)
+                      + sweeps * bytes_per_refresh(body.nnz, body.num_nodes, 4) + 16 * body.n)
+        kernel, key = "k_pcg_persistent (mixed)", f"pcg_persistent_{args.config}"
+        model = "CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*n) + refreshes x (nnz*4 + nnz/9*4 + 4(N+1) + 3*8*n) + 16n"
+    achieved = per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else None
     line = {
         "metric": METRIC,
         "value": value,
-        "unit": "tet-element-steps/s",
+        "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -283,23 +495,41 @@ def run_ours(args, rank, world, local, dist):
         "cg_iterations_per_step": cg_per_step,
         "step_status": sorted(set(int(s) for s in statuses)),
         "clocks": clocks,
-        "e2e": {"value": e2e_value, "unit": "tet-element-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {
-            "kernel": f"k_cg_spmv_sell ({args.precision})",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-            "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms,
-            "launches_timed": agg["spmv_timed"], "peak_source": f"{peak_kind} (hbm_gbs)",
+            "kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": load_traffic(key),
+            "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": launch_ms,
+            "peak_source": f"{peak_kind} (hbm_gbs)", "bytes_model": model,
         },
     }
     body.close()
     return line, scene
 
 
-def cpu_baseline(scene, steps=1):
-    """The oracle (FP64 C++ restatement of the reference step) on the host: `steps` steps of the
-    same scene from the same start state, one thread (a representation is single-threaded)."""
+# ------------------------------------------------------------------------------------------------
+# CPU side: the oracle (FP64 C++ restatement of the reference step), the only CPU implementation
+# of the path that runs here (the reference needs Eigen and Boost).
+
+def batch_cpu_sample(scenes):
+    """Every 4th mesh of the batch (a bounded, size-representative sample)."""
+    return scenes[::4]
+
+
+def cpu_batch_steps(scenes, steps):
+    """`steps` steps of every sampled mesh, one mesh per task on ceil(0.5 * cores) host threads."""
+    from oracle import oracle as O
+
+    models = [O.OracleModel.from_scene(s) for s in scenes]
+    threads = host_threads()
+    t0 = time.perf_counter()
+    O.step_many(models, 1e-3, steps, threads)
+    sec = time.perf_counter() - t0
+    tets = sum(s.mesh.num_tets for s in scenes)
+    return tets * steps / sec, sec, threads
+
+
+def cpu_single_steps(scene, steps):
     from oracle import oracle as O
 
     model = O.OracleModel.from_scene(scene)
@@ -316,49 +546,67 @@ def cpu_baseline(scene, steps=1):
 
 
 def run_reference(args, rank, world):
-    """Reference arm: the CPU implementation of the path (the oracle restatement; the reference
-    itself cannot be built without Eigen/Boost) on the host, bounded in wall time."""
-    from opensurgsim_gb300 import mesh  # noqa: F401
+    """Reference arm: the CPU implementation of the path on the host cores, bounded samples."""
     from oracle import oracle as O
 
     if rank != 0:
         return None
     O.build()
-    scene = build_scene(args)
-    model = O.OracleModel.from_scene(scene)
-    budget_s = float(os.environ.get("GBFEM_REFERENCE_BUDGET_S", "150"))
-    step = 0
+    if args.config == "batch":
+        scenes = batch_cpu_sample(batch_scenes())
+        from oracle import oracle as O2
 
-    def one():
-        nonlocal step
-        if scene.driven_dofs is not None:
-            x, v = model.state()
-            v[scene.driven_dofs] = scene.driven_values(step)
-            model.set_state(None, v)
-        t0 = time.perf_counter()
-        model.step(scene.dt)
-        step += 1
-        return time.perf_counter() - t0
+        models = [O2.OracleModel.from_scene(s) for s in scenes]
+        threads = host_threads()
+        tets = sum(s.mesh.num_tets for s in scenes)
+        O2.step_many(models, 1e-3, max(0, min(args.warmup, 1)), threads)
+        times = []
+        budget_s = float(os.environ.get("GBFEM_REFERENCE_BUDGET_S", "150"))
+        while len(times) < args.steps and sum(times) < budget_s:
+            t0 = time.perf_counter()
+            O2.step_many(models, 1e-3, 1, threads)
+            times.append(time.perf_counter() - t0)
+        value = tets * len(times) / sum(times)
+        sample = (f"every 4th mesh of the 256-mesh batch ({len(scenes)} meshes, {tets} tets), {len(times)} timed "
+                  f"step(s), one mesh per task on {threads} host threads; oracle FP64 C++ restatement, -O3")
+        cores, workload = threads, "batch256 (every 4th mesh)"
+        ms = 1e3 * sum(times) / len(times)
+    else:
+        scene = build_scene(args.config)
+        model = O.OracleModel.from_scene(scene)
+        budget_s = float(os.environ.get("GBFEM_REFERENCE_BUDGET_S", "150"))
+        step = 0
 
-    t_warm = one() if args.warmup > 0 else 0.0
-    times = []
-    while len(times) < args.steps and (sum(times) + t_warm) < budget_s:
-        times.append(one())
-    value = scene.mesh.num_tets * len(times) / sum(times)
-    sample = (f"{len(times)} timed step(s) (+{min(args.warmup, 1)} warm-up) of the same scene, capped at "
-              f"{budget_s:.0f} s of CPU time; oracle FP64 C++ restatement, -O3, 1 thread")
-    line = {
-        "metric": METRIC, "value": value, "unit": "tet-element-steps/s", "n_gpus": world, "steps": len(times),
-        "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cube-grid meshes)",
-        "config": {"workload": "bar40x40x160 compression" if args.config == "bar" else "cube10x10x10",
-                   "tets": scene.mesh.num_tets, "precision": "fp64"},
+        def one():
+            nonlocal step
+            if scene.driven_dofs is not None:
+                x, v = model.state()
+                v[scene.driven_dofs] = scene.driven_values(step)
+                model.set_state(None, v)
+            t0 = time.perf_counter()
+            model.step(scene.dt)
+            step += 1
+            return time.perf_counter() - t0
+
+        if args.warmup > 0:
+            one()
+        times = []
+        while len(times) < args.steps and sum(times) < budget_s:
+            times.append(one())
+        value = scene.mesh.num_tets * len(times) / sum(times)
+        sample = (f"{len(times)} timed step(s) of the same scene, capped at {budget_s:.0f} s; oracle FP64 C++ "
+                  "restatement, -O3, 1 thread (a representation is single-threaded)")
+        cores, workload = 1, args.config
+        ms = 1e3 * sum(times) / len(times)
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(times),
+        "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cube-grid meshes)",
+        "config": {"workload": workload, "precision": "fp64"},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "tet-element-steps/s", "cores": 1, "kind": "port",
-                         "sample": sample},
-        "e2e": {"value": value, "unit": "tet-element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    return line
 
 
 def main():
@@ -367,9 +615,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--config", default="bar", choices=["bar", "cube"])
+    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="bar and cube only; the batch is always mixed precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 path comparison (batch)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -378,18 +628,38 @@ def main():
             print(json.dumps(line), flush=True)
         return
     dist = Dist(world)
-    line, scene = run_ours(args, rank, world, local, dist)
+    if args.config == "batch":
+        line, scenes = run_batch(args, rank, world, local, dist)
+    else:
+        line, scene = run_single(args, rank, world, local, dist)
     if rank == 0:
+        if args.config == "batch" and not args.no_compare:
+            log("plain FP64 path on the same meshes")
+            fp64, err = fp64_path_comparison([s.mesh for s in scenes], local)
+            line["fp64_path"] = fp64
+            line["speedup_vs_fp64_path"] = line["value"] / (fp64["value"] * world)
+            line["rel_disp_err_vs_fp64"] = err
+            log(f"fp64 path {fp64['value'] / 1e6:.1f} M tet-steps/s, speed-up {line['speedup_vs_fp64_path']:.2f}, "
+                f"max rel disp err {err['max']:.2e}")
         if world == 1 and not args.no_cpu_baseline:
             from oracle import oracle as O
 
             O.build()
             log("cpu baseline: oracle on the host")
-            v, t = cpu_baseline(scene, 1)
-            log(f"cpu baseline: 1 step in {t:.1f} s")
-            line["cpu_baseline"] = {"value": v, "unit": "tet-element-steps/s", "cores": 1, "kind": "port",
-                                    "sample": f"1 step of the same scene on the host ({t:.1f} s), oracle FP64 "
-                                              "C++ restatement, -O3, 1 thread"}
+            if args.config == "batch":
+                sample = batch_cpu_sample(scenes)
+                v, t, threads = cpu_batch_steps(sample, 1)
+                line["cpu_baseline"] = {
+                    "value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                    "sample": (f"1 step of every 4th mesh of the batch ({len(sample)} meshes, "
+                               f"{sum(s.mesh.num_tets for s in sample)} tets) in {t:.1f} s, one mesh per task on "
+                               f"{threads} host threads; oracle FP64 C++ restatement, -O3")}
+            else:
+                v, t = cpu_single_steps(scene, 1)
+                line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                                        "sample": f"1 step of the same scene on the host ({t:.1f} s), oracle FP64 "
+                                                  "C++ restatement, -O3, 1 thread"}
+            log(f"cpu baseline: {v / 1e3:.1f} k tet-steps/s")
         print(json.dumps(line), flush=True)
     dist.close()
 

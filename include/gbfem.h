@@ -147,9 +147,10 @@ GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
  * GBFEM_PRECISION_MIXED. gbfem_step, gbfem_get_state, gbfem_set_velocities ... act on the batch. */
 GBFEM_API gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, const gbfem_params* params,
 										  gbfem_handle* out);
-/* Number of meshes and their node / tet offsets (count + 1 entries each) in the batch. */
+/* Number of meshes, their node / tet offsets (count + 1 entries each) and the scalar non-zeros of
+ * each mesh's system matrix (count entries) in the batch. Any pointer may be NULL. */
 GBFEM_API gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets,
-										int32_t* tet_offsets);
+										int32_t* tet_offsets, int64_t* nnz_per_mesh);
 /* Per mesh, over the last gbfem_step call: CG iterations, FP64 residual refreshes, converged (all
  * steps), worst relative residual. Arrays of `count` entries (any may be NULL). */
 GBFEM_API gbfem_status gbfem_batch_segment_stats(gbfem_handle h, int32_t* iterations, int32_t* refreshes,

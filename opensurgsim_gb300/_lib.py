@@ -133,7 +133,7 @@ def load():
         "gbfem_cg_destroy": (S, [H]),
         "gbfem_batch_create": (S, [ctypes.c_int32, ctypes.POINTER(MeshDesc), ctypes.POINTER(Params),
                                    ctypes.POINTER(H)]),
-        "gbfem_batch_info": (S, [H, I32, I32, I32]),
+        "gbfem_batch_info": (S, [H, I32, I32, I32, ctypes.POINTER(ctypes.c_int64)]),
         "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,

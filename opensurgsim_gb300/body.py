@@ -73,7 +73,9 @@ class Body:
         self.nnz = nnz.value
         self.node_offsets = np.zeros(self.num_meshes + 1, dtype=np.int32)
         self.tet_offsets = np.zeros(self.num_meshes + 1, dtype=np.int32)
-        L.gbfem_batch_info(h, None, iptr(self.node_offsets), iptr(self.tet_offsets))
+        self.nnz_per_mesh = np.zeros(self.num_meshes, dtype=np.int64)
+        L.gbfem_batch_info(h, None, iptr(self.node_offsets), iptr(self.tet_offsets),
+                           self.nnz_per_mesh.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
         self.last_status = _lib.GBFEM_OK
 
     def segment_stats(self):

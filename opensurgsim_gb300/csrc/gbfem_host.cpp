@@ -524,8 +524,9 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		size_t smem = 0;
 		for (int attempt = 0; attempt < 2; ++attempt)
 		{
-			// A weighted share holds fewer than tot / (G wmin) + 1 chunks, a counted one at most ceil(n / G).
-			const int64_t mW = (int64_t)cumW[nchunks] / ((int64_t)G * wmin) + 2;
+			// A weighted share holds fewer than tot / (G wmin) + 1 chunks (tot at most kRefreshWeight
+			// times the plain total), a counted one at most ceil(n / G).
+			const int64_t mW = (int64_t)kRefreshWeight * cumW[nchunks] / ((int64_t)G * wmin) + 2;
 			const int64_t mC = (int64_t)nchunks / G + 2;
 			h->maxChunksPerCta = (int)std::max(mW, mC);
 			smem = pcg_smem_bytes(nseg, h->maxChunksPerCta);
@@ -1060,13 +1061,17 @@ gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, co
 	return create_impl(meshes, count, params, out);
 }
 
-gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets)
+gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets,
+							  int64_t* nnz_per_mesh)
 {
 	if (!h) return GBFEM_INVALID_ARG;
 	const int nseg = (int)h->segNode.size() - 1;
 	if (count) *count = nseg;
 	if (node_offsets) std::copy(h->segNode.begin(), h->segNode.end(), node_offsets);
 	if (tet_offsets) std::copy(h->segTet.begin(), h->segTet.end(), tet_offsets);
+	if (nnz_per_mesh)
+		for (int k = 0; k < nseg; ++k)
+			nnz_per_mesh[k] = 9LL * (h->adjPtr[h->segNode[k + 1]] - h->adjPtr[h->segNode[k]]);
 	return GBFEM_OK;
 }
 

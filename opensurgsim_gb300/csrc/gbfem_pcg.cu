@@ -41,9 +41,22 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 
 __device__ __forceinline__ int ldi(const int* p) { return *(const volatile int*)p; }
 __device__ __forceinline__ double ldd(const double* p) { return *(const volatile double*)p; }
+__device__ __forceinline__ double2 ldv2(const double* p)  // 16-byte aligned
+{
+	double2 v;
+	asm volatile("ld.volatile.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+	return v;
+}
+// {beta, mode} of a segment in one load.
+__device__ __forceinline__ void load_beta_mode(const SegCtl* S, double& beta, int& mode)
+{
+	const double2 v = ldv2(&S->beta);
+	beta = v.x;
+	mode = (int)(unsigned)(__double_as_longlong(v.y) & 0xffffffffLL);
+}
 
 // Grid-wide barrier ending phase `ph` (all blocks co-resident: cooperative launch). The last
-// block to arrive clears the finished-segment counter that phase ph + 1 will count into.
+// block to arrive clears the event counters that phase ph + 1 will count into.
 // Returns false on timeout.
 __device__ bool grid_barrier(PcgGlobal* g, int ph)
 {
@@ -57,6 +70,7 @@ __device__ bool grid_barrier(PcgGlobal* g, int ph)
 		if (atomicAdd(&g->barCount, 1u) == gridDim.x - 1)
 		{
 			g->finishedIn[(ph + 1) & 1] = 0;
+			g->refreshIn[(ph + 1) & 1] = 0;
 			g->barCount = 0;
 			__threadfence();
 			atomicAdd(&g->barGen, 1u);
@@ -158,9 +172,11 @@ __device__ int weighted_start(const PcgArgs& a, const int* Cp, const int* Wp, co
 			hi = mid - 1;
 	}
 	const int s = lo;
-	const long long need = (X - (long long)Wp[s] * G + G - 1) / G;  // >= 1
 	const int c0 = sc[s], ns = sc[s + 1] - sc[s];
-	const int key = __ldg(&a.cumW[c0]) + (int)need;
+	const long long base = __ldg(&a.cumW[c0]);
+	const long long mult = (Wp[s + 1] - Wp[s]) / (__ldg(&a.cumW[c0 + ns]) - base);  // segment weight multiplier
+	const long long need = (X - (long long)Wp[s] * G + G * mult - 1) / (G * mult);  // >= 1
+	const int key = (int)(base + need);
 	int j = lower_bound_warp(a.cumW, c0 + 1, c0 + ns + 1, key) - c0;
 	j = min(j, ns);
 	return Cp[s] + j;
@@ -177,8 +193,9 @@ __device__ __forceinline__ int2 seg_ctas(const PcgArgs& a, const SetView& V, con
 {
 	const int G = gridDim.x;
 	if (!V.Wp) return make_int2(cta_of(V.Cp[s], V.n, G), cta_of(V.Cp[s + 1] - 1, V.n, G));
-	const int cl = sc[s + 1] - 1;
-	const long long wl = (long long)V.Wp[s + 1] - (__ldg(&a.cumW[cl + 1]) - __ldg(&a.cumW[cl]));
+	const int c0 = sc[s], cl = sc[s + 1] - 1;
+	const long long mult = (V.Wp[s + 1] - V.Wp[s]) / (__ldg(&a.cumW[cl + 1]) - __ldg(&a.cumW[c0]));
+	const long long wl = (long long)V.Wp[s + 1] - mult * (__ldg(&a.cumW[cl + 1]) - __ldg(&a.cumW[cl]));
 	return make_int2(cta_of(V.Wp[s], V.tot, G), cta_of(wl, V.tot, G));
 }
 
@@ -378,11 +395,14 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	actW.Cp = actC.Cp = Cp;
 	actW.Wp = Wp;
 	actC.Wp = nullptr;
-	// Rebuild the active-set prefixes and this CTA's ranges (segments stamped before phase ph are out).
-	auto rebuild = [&]() {
+	// Rebuild the active-set prefixes and this CTA's ranges (segments stamped before phase ph are
+	// out). In phase 1 a segment switched to its FP64 residual in the phase before weighs
+	// kRefreshWeight times its block columns. Returns whether any segment was so weighted.
+	__shared__ int shWeighted;
+	auto rebuild = [&](bool phase1) {
 		if (warp == 0)
 		{
-			int carryC = 0, carryW = 0;
+			int carryC = 0, carryW = 0, weighted = 0;
 			if (lane == 0) Cp[0] = Wp[0] = 0;
 			for (int base = 0; base < nseg; base += 32)
 			{
@@ -395,6 +415,11 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 					{
 						c = sc[s + 1] - sc[s];
 						w = __ldg(&a.cumW[sc[s + 1]]) - __ldg(&a.cumW[sc[s]]);
+						if (phase1 && ldi(&a.seg[s].refreshAt) == ph - 1)
+						{
+							w *= kRefreshWeight;
+							weighted = 1;
+						}
 					}
 				}
 #pragma unroll
@@ -415,6 +440,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				carryC += __shfl_sync(kFull, c, 31);
 				carryW += __shfl_sync(kFull, w, 31);
 			}
+			weighted = __any_sync(kFull, weighted);
 			__syncwarp();
 			const int lo = weighted_start(a, Cp, Wp, sc, nseg, B, G);
 			const int hi = weighted_start(a, Cp, Wp, sc, nseg, B + 1, G);
@@ -425,6 +451,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				shRange[1] = hi;
 				shRange[2] = (int)((n * B + G - 1) / G);
 				shRange[3] = (int)((n * (B + 1) + G - 1) / G);
+				shWeighted = weighted;
 			}
 		}
 		__syncthreads();
@@ -442,15 +469,23 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		actW.n = actC.n = Cp[nseg];
 		actW.tot = Wp[nseg];
 		actC.tot = actC.n;
+		return shWeighted != 0;
 	};
-	int finished = 0;  // segments finished before the current phase (same in every CTA)
-	// Phase start: count the segments finished in the previous phase and rebuild if any.
-	auto phase_start = [&](bool force) {
-		if (threadIdx.x == 0) shFinished = ldi(&a.g->finishedIn[(ph - 1) & 1]);
+	int finished = 0;        // segments finished before the current phase (same in every CTA)
+	bool weighted = false;   // the current partition weighs refreshing segments
+	__shared__ int shRefresh;
+	// Phase start: count the segments finished (and, before phase 1, switched to a refresh) in the
+	// previous phase; rebuild the partition when the active set or the weights change.
+	auto phase_start = [&](bool phase1, bool force) {
+		if (threadIdx.x == 0)
+		{
+			shFinished = ldi(&a.g->finishedIn[(ph - 1) & 1]);
+			shRefresh = ldi(&a.g->refreshIn[(ph - 1) & 1]);
+		}
 		__syncthreads();
 		const int nf = shFinished;
 		finished += nf;
-		if (nf > 0 || force) rebuild();
+		if (force || nf > 0 || (phase1 && (shRefresh > 0 || weighted))) weighted = rebuild(phase1);
 	};
 	auto barrier = [&]() {
 		const bool ok = grid_barrier(a.g, ph);
@@ -487,6 +522,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		S.iter = 0;
 		S.updates = 0;
 		S.mode = 0;
+		S.refreshAt = -8;
 		S.beta = 0.0;
 		S.converged = (tot[0] == 0.0 || tot[0] < S.threshold) ? 1 : 0;
 		S.nonfinite = !isfinite(tot[0]);
@@ -495,7 +531,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	if (!barrier()) return;
 
 	// ---- I2: r = b / s (FP32), z = invdiag r, rz, |r|^2.
-	phase_start(true);
+	phase_start(false, true);
 	for_chunks(actC, sc, nseg, [&](int slot, int s, int c) {
 		const int rs = 32 * c + lane;
 		const double inv = 1.0 / ldd(&a.seg[s].s);
@@ -530,14 +566,16 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	{
 		// ---- Phase 1. mode 0: p_new = z + beta p_old (own rows, and on the fly for gathered rows);
 		// q = A p_new; pq. mode 1: r64 = b - A (x64 + x_delta) in FP64.
-		phase_start(false);
+		phase_start(true, false);
 		if (finished >= nseg) break;
 		for_chunks(actW, sc, nseg, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
-			double part;
-			if (ldi(&a.seg[s].mode) == 0)
+			double part, betaD;
+			int mode;
+			load_beta_mode(&a.seg[s], betaD, mode);
+			if (mode == 0)
 			{
-				const float beta = float(ldd(&a.seg[s].beta));
+				const float beta = float(betaD);
 				float a0 = 0.f, a1 = 0.f, a2 = 0.f;
 				spmv_row_zp(a, zpOld, c, lane, beta, a0, a1, a2);
 				const float4 zi = zpOld[2 * rs], pi = zpOld[2 * rs + 1];
@@ -586,15 +624,19 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 
 		// ---- Phase 2. mode 0: x_delta += alpha s p, r -= alpha q, z = invdiag r; |r|^2, r.z; decide
 		// on a refresh. mode 2: fold x, r = r64 / s, z = invdiag r, p *= ratio; |r|^2, r.z.
-		phase_start(false);
+		phase_start(false, false);
 		for_chunks(actC, sc, nseg, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
 			float s0 = 0.f, s1 = 0.f, z[3];
-			if (ldi(&a.seg[s].mode) == 0)
+			double betaD;
+			int mode;
+			load_beta_mode(&a.seg[s], betaD, mode);
+			const double2 as2 = ldv2(&a.seg[s].alpha);  // {alpha, s}
+			if (mode == 0)
 			{
-				const double alphaD = ldd(&a.seg[s].alpha);
+				const double alphaD = as2.x;
 				const float alpha = float(alphaD);
-				const float as = float(alphaD * ldd(&a.seg[s].s));
+				const float as = float(alphaD * as2.y);
 				const float4 pn = zpNew[2 * rs + 1];
 				const float pv[3] = {pn.x, pn.y, pn.z};
 #pragma unroll
@@ -611,7 +653,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			}
 			else
 			{
-				const double inv = 1.0 / ldd(&a.seg[s].s);
+				const double inv = 1.0 / as2.y;
 				const float ratio = float(ldd(&a.seg[s].ratio));
 #pragma unroll
 				for (int i = 0; i < 3; ++i)
@@ -659,7 +701,9 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			else if (S.s * S.s * tot[0] < S.threshold || tot[0] < a.drop * S.rrLast || S.iter + 1 >= a.maxIter)
 			{
 				S.mode = 1;  // FP64 residual before the next direction
+				S.refreshAt = ph;
 				S.rzPend = S.rz;
+				atomicAdd(&a.g->refreshIn[ph & 1], 1);
 			}
 			else
 			{

@@ -12,19 +12,22 @@ constexpr int kPcgChunkWeight = 2;  // per-chunk constant added to the block-col
 
 // Per-segment (per-mesh) CG state, in device memory. Written by the CTA that completes a
 // segment's reduction, read by every CTA after the next grid barrier.
-struct SegCtl
+struct alignas(16) SegCtl
 {
+	double beta;            // phase 1 reads {beta, mode, refreshAt} with one 16-byte load
+	int mode;               // 0: CG step; 1: FP64 residual next; 2: rescale next
+	int refreshAt;          // phase id at which mode 1 was last set
+	double alpha, s;        // phase 2 reads {alpha, s} with one 16-byte load; r_true ~= s * r32
+	double ratio;
 	double bb, threshold;   // |b|^2, tol^2 |b|^2
-	double s;               // residual scale: r_true ~= s * r32
-	double rz, pq, alpha, beta;
+	double rz, pq;
 	double rr32, rrLast;    // |r32|^2 now and right after the last refresh
 	double rrTrue;          // |b - A x|^2 at the last refresh
-	double ratio, rzPend;
+	double rzPend;
 	int iter, updates, done, converged;
-	int mode;               // 0: CG step; 1: FP64 residual next; 2: rescale next
 	int nonfinite;
 	unsigned int ticket;
-	int pad;
+	int pad[2];
 };
 
 // Grid-wide control of one persistent launch.
@@ -32,9 +35,13 @@ struct PcgGlobal
 {
 	unsigned int barCount, barGen;
 	int finishedSegs;    // total, for diagnostics
-	int finishedIn[2];   // segments finished in the current / previous phase (by phase parity)
-	int err, pad[2];
+	int err;
+	int finishedIn[2];   // segments finished in a phase, by phase parity
+	int refreshIn[2];    // segments switched to an FP64 residual in a phase, by phase parity
 };
+
+// Weight of a chunk of a segment doing its FP64 residual (phase 1), relative to an FP32 SpMV chunk.
+constexpr int kRefreshWeight = 4;
 
 struct PcgArgs
 {
