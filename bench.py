@@ -177,10 +177,11 @@ def bytes_per_refresh(nnz, N, s):
 # ------------------------------------------------------------------------------------------------
 # Batched workload
 
-def batch_scenes():
+def batch_scenes(count=BATCH["count"]):
+    """The batch workload; a smaller `count` takes the first meshes of the same seeded sequence."""
     from opensurgsim_gb300 import mesh
 
-    return mesh.scenes_batch(**BATCH)
+    return mesh.scenes_batch(**dict(BATCH, count=count))
 
 
 def batch_body(meshes, precision, device):
@@ -248,7 +249,7 @@ def run_batch(args, rank, world, local, dist):
 
     build.build()
     torch.cuda.set_device(local)
-    scenes = batch_scenes()
+    scenes = batch_scenes(args.meshes)
     meshes = [s.mesh for s in scenes]
     tets = sum(m.num_tets for m in meshes)
     nodes = sum(m.num_nodes for m in meshes)
@@ -327,8 +328,8 @@ def run_batch(args, rank, world, local, dist):
         "dtype": "f32+f64",
         "data": "synthetic (seeded cube-grid meshes)",
         "config": {
-            "workload": ("batch256: 256 cube-grid meshes (h 1 cm, 5 tets per cube, nodes log-U[500,50000], seed 3), "
-                         f"{tets} tets, {nodes} nodes, E log-U[1e4,1e6] per mesh, nu 0.45, bottom faces fixed, "
+            "workload": (f"batch{len(meshes)}: {len(meshes)} cube-grid meshes (h 1 cm, 5 tets per cube, nodes "
+                         f"log-U[500,50000], seed 3), {tets} tets, {nodes} nodes, E log-U[1e4,1e6] per mesh, nu 0.45, bottom faces fixed, "
                          "gravity, alpha 0.01, beta 0.001, dt 1e-3, CG tol 1e-10; batched mixed precision, one "
                          "persistent solve launch per step"),
             "meshes": len(meshes), "tets": tets, "nodes": nodes, "precision": "mixed",
@@ -345,7 +346,7 @@ def run_batch(args, rank, world, local, dist):
             "kernel": "k_pcg_persistent (whole batched mixed-precision solve, one launch per step)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None,
-            "traffic": load_traffic("pcg_persistent_batch256"),
+            "traffic": load_traffic(f"pcg_persistent_batch{len(meshes)}"),
             "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": launch_ms,
             "peak_source": f"{peak_kind} (hbm_gbs)",
             "bytes_model": ("per mesh: CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*3N) + refreshes x "
@@ -553,7 +554,7 @@ def run_reference(args, rank, world):
         return None
     O.build()
     if args.config == "batch":
-        scenes = batch_cpu_sample(batch_scenes())
+        scenes = batch_cpu_sample(batch_scenes(args.meshes))
         from oracle import oracle as O2
 
         models = [O2.OracleModel.from_scene(s) for s in scenes]
@@ -620,6 +621,7 @@ def main():
                     help="bar and cube only; the batch is always mixed precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 path comparison (batch)")
+    ap.add_argument("--meshes", type=int, default=BATCH["count"], help="batch size (smaller cases for profiling)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

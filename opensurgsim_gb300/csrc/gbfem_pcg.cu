@@ -39,6 +39,18 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 	return v;
 }
 
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v)
+{
+	unsigned old;
+	asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+	return old;
+}
+
+__device__ __forceinline__ void red_add_release(unsigned* p, unsigned v)
+{
+	asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ int ldi(const int* p) { return *(const volatile int*)p; }
 __device__ __forceinline__ double ldd(const double* p) { return *(const volatile double*)p; }
 __device__ __forceinline__ double2 ldv2(const double* p)  // 16-byte aligned
@@ -66,14 +78,14 @@ __device__ bool grid_barrier(PcgGlobal* g, int ph)
 	{
 		ok = 1;
 		const unsigned gen = ld_acquire(&g->barGen);
-		__threadfence();
-		if (atomicAdd(&g->barCount, 1u) == gridDim.x - 1)
+		// Arrival releases this block's writes (ordered before by __syncthreads) and, for the last
+		// block, acquires everyone else's before it releases the next generation.
+		if (atom_add_acq_rel(&g->barCount, 1u) == gridDim.x - 1)
 		{
 			g->finishedIn[(ph + 1) & 1] = 0;
 			g->refreshIn[(ph + 1) & 1] = 0;
 			g->barCount = 0;
-			__threadfence();
-			atomicAdd(&g->barGen, 1u);
+			red_add_release(&g->barGen, 1u);
 		}
 		else
 		{
@@ -89,9 +101,8 @@ __device__ bool grid_barrier(PcgGlobal* g, int ph)
 				__nanosleep(32);
 			}
 		}
-		// Acquire side: the other blocks' writes of the finished phase become visible to this block
-		// (the next phase reads the vectors with plain, L1-cached loads).
-		__threadfence();
+		// Acquire side (the spin's ld.acquire): the other blocks' writes of the finished phase are
+		// visible to this block, whose next phase reads the vectors with plain, L1-cached loads.
 	}
 	__syncthreads();
 	return ok && !*(volatile int*)&g->err;
@@ -230,12 +241,11 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 		{
 #pragma unroll
 			for (int k = 0; k < NV; ++k) a.slots[(size_t)(2 * k + which) * G + B] = v[k];
-			__threadfence();
-			tk = atomicAdd(&a.seg[s].ticket, 1u);
+			tk = atom_add_acq_rel(&a.seg[s].ticket, 1u);  // releases the slot, acquires the others'
 		}
 		tk = __shfl_sync(kFull, tk, 0);
 		if (tk != (unsigned)(fl.y - fl.x)) return;
-		__threadfence();
+		__syncwarp();
 		double tot[NV];
 #pragma unroll
 		for (int k = 0; k < NV; ++k)

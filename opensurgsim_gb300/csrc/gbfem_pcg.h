@@ -41,7 +41,7 @@ struct PcgGlobal
 };
 
 // Weight of a chunk of a segment doing its FP64 residual (phase 1), relative to an FP32 SpMV chunk.
-constexpr int kRefreshWeight = 4;
+constexpr int kRefreshWeight = 6;
 
 struct PcgArgs
 {
