@@ -140,6 +140,26 @@ GBFEM_API gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v
 GBFEM_API gbfem_status gbfem_stream(gbfem_handle h, void** stream);
 GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
 
+/* ---- Differentiation form. No counterpart in the reference (it has no adjoint); these serve
+ * gradient-based identification on the same step (opensurgsim_gb300.autograd).
+ *
+ * Per-element moduli from device arrays (E_e, and nu_e or NULL to keep each element's current nu):
+ * the reference sets them per element through Fem3DElementTetrahedron::setYoungModulus /
+ * setPoissonRatio before initialize (Fem3DElementTetrahedron.h); here they can change between
+ * steps. */
+GBFEM_API gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, const double* poisson);
+/* Reverse-mode derivative of one gbfem_step(h, dt, 1, 0) taken from state (x, v) with velocity
+ * increment dv = v' - v: given lx = dL/dx' and lv = dL/dv', writes lx_out = dL/dx and
+ * lv_out = dL/dv (may alias lx / lv) and adds dL/d(log E_e) and dL/d(nu_e) into grad_log_young and
+ * grad_poisson (either may be NULL). One Newton iteration (the reference default). All pointers are
+ * device arrays of n (state) or num_tets (gradients) doubles. Rebuilds the step's system at (x, v)
+ * and solves it transposed with the handle's CG (the FP64 or the mixed solver); the element
+ * derivatives are FP64. Does not change the handle's state. Returns GBFEM_CG_MAXITER if the
+ * transposed solve did not converge (the outputs are still written). */
+GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,
+										  const double* lx, const double* lv, double* lx_out, double* lv_out,
+										  double* grad_log_young, double* grad_poisson);
+
 /* ---- Batching: many independent meshes (each its own OpenSurgSim representation, stepped like
  * one FreeMotion pass over them, FreeMotion.cpp:55-80) in one body. Node ids, boundary-condition
  * dofs and states are concatenated in mesh order; every mesh keeps its own CG scalars and

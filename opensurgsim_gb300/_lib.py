@@ -36,7 +36,7 @@ EXPORTED = [
     "gbfem_get_sizes", "gbfem_get_pattern", "gbfem_get_scatter", "gbfem_get_system", "gbfem_last_error",
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
     "gbfem_cg_destroy", "gbfem_cg_solve_noalloc", "gbfem_batch_create", "gbfem_batch_info",
-    "gbfem_batch_segment_stats",
+    "gbfem_batch_segment_stats", "gbfem_set_materials_device", "gbfem_adjoint_step",
 ]
 
 
@@ -135,6 +135,8 @@ def load():
                                    ctypes.POINTER(H)]),
         "gbfem_batch_info": (S, [H, I32, I32, I32, ctypes.POINTER(ctypes.c_int64)]),
         "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
+        "gbfem_set_materials_device": (S, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),

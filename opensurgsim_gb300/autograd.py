@@ -1,0 +1,125 @@
+"""Differentiation form: a multi-step implicit-Euler rollout as a ``torch.autograd.Function``.
+
+Forward: set per-element Young's moduli E = exp(log_young) (``gbfem_set_materials_device``), start
+from (x0, v0) and take ``nsteps`` steps of ``dt`` with the body's own step (FP64 or mixed form),
+keeping the state every ``checkpoint_every`` steps. Backward: for each checkpoint segment, last
+first, re-run the segment's steps to recover its states, then walk them back with
+``gbfem_adjoint_step`` (the transposed solve and the per-element derivative kernels), which
+accumulates dL/d(log E) and carries (dL/dx, dL/dv) to the segment's start. Gradients flow to
+``log_young``, ``x0`` and ``v0``.
+
+The reference has no adjoint; the forward steps are the reference's Fem3DRepresentation::update
+semantics (one Newton iteration). All tensors are float64 on the body's device.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import GbfemError
+
+
+class _CudaArray:
+    """A device buffer of the library exposed to torch without a copy (__cuda_array_interface__)."""
+
+    def __init__(self, ptr: int, n: int):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3,
+                                         "strides": None}
+
+
+def state_views(body):
+    """(x, v) of the body as float64 torch tensors aliasing the library's device buffers."""
+    xp, vp = body.device_state()
+    return (torch.as_tensor(_CudaArray(xp, body.n), device=f"cuda:{body.params.device}"),
+            torch.as_tensor(_CudaArray(vp, body.n), device=f"cuda:{body.params.device}"))
+
+
+def _check(body, st, allow=(_lib.GBFEM_OK,)):
+    if st not in allow:
+        raise GbfemError(st, _lib.last_error(body.handle))
+
+
+def set_young(body, log_young: torch.Tensor):
+    young = torch.exp(log_young.detach().to(torch.float64)).contiguous()
+    torch.cuda.synchronize(young.device)
+    _check(body, _lib.load().gbfem_set_materials_device(body.handle, ctypes.c_void_p(young.data_ptr()), None))
+
+
+def rollout_states(body, x0, v0, dt, nsteps, keep=None):
+    """Step from (x0, v0); returns the final (x, v) and, if ``keep`` is a list, appends every
+    intermediate state (including the first) to it."""
+    xv, vv = state_views(body)
+    torch.cuda.synchronize(xv.device)
+    xv.copy_(x0)
+    vv.copy_(v0)
+    torch.cuda.synchronize(xv.device)
+    if keep is not None:
+        keep.append((xv.clone(), vv.clone()))
+    for _ in range(nsteps):
+        st = body.step(dt, 1)
+        _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+        if keep is not None:
+            keep.append((xv.clone(), vv.clone()))
+    return xv.clone(), vv.clone()
+
+
+class ImplicitRollout(torch.autograd.Function):
+    """(x_T, v_T) = rollout(log_young, x0, v0); see the module docstring."""
+
+    @staticmethod
+    def forward(ctx, log_young, x0, v0, body, dt, nsteps, checkpoint_every):
+        set_young(body, log_young)
+        k = max(1, int(checkpoint_every))
+        checkpoints = []
+        xv, vv = state_views(body)
+        torch.cuda.synchronize(xv.device)
+        xv.copy_(x0.detach())
+        vv.copy_(v0.detach())
+        torch.cuda.synchronize(xv.device)
+        checkpoints.append((xv.clone(), vv.clone()))
+        for t in range(nsteps):
+            st = body.step(dt, 1)
+            _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+            if (t + 1) % k == 0 and t + 1 < nsteps:
+                checkpoints.append((xv.clone(), vv.clone()))
+        ctx.body, ctx.dt, ctx.nsteps, ctx.k = body, dt, nsteps, k
+        ctx.checkpoints = checkpoints
+        ctx.save_for_backward(log_young)
+        return xv.clone(), vv.clone()
+
+    @staticmethod
+    def backward(ctx, gx, gv):
+        (log_young,) = ctx.saved_tensors
+        body, dt, nsteps, k = ctx.body, ctx.dt, ctx.nsteps, ctx.k
+        dev = log_young.device
+        n = body.n
+        lx = (gx if gx is not None else torch.zeros(n, dtype=torch.float64, device=dev)).to(torch.float64).contiguous().clone()
+        lv = (gv if gv is not None else torch.zeros(n, dtype=torch.float64, device=dev)).to(torch.float64).contiguous().clone()
+        glog = torch.zeros(body.num_tets, dtype=torch.float64, device=dev)
+        L = _lib.load()
+        set_young(body, log_young)
+        starts = list(range(0, nsteps, k))
+        for seg in reversed(range(len(starts))):
+            t0 = starts[seg]
+            t1 = min(t0 + k, nsteps)
+            x0s, v0s = ctx.checkpoints[seg]
+            states = []
+            rollout_states(body, x0s, v0s, dt, t1 - t0, keep=states)
+            torch.cuda.synchronize(dev)
+            for t in reversed(range(t1 - t0)):
+                xt, vt = states[t]
+                dv = (states[t + 1][1] - vt).contiguous()
+                torch.cuda.synchronize(dev)
+                st = L.gbfem_adjoint_step(body.handle, float(dt), *[ctypes.c_void_p(a.data_ptr()) for a in
+                                                                     (xt, vt, dv, lx, lv, lx, lv, glog)], None)
+                _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+        torch.cuda.synchronize(dev)
+        return glog, lx, lv, None, None, None, None
+
+
+def rollout(body, log_young, x0, v0, dt, nsteps, checkpoint_every=10):
+    """Differentiable rollout: returns (x_T, v_T) with gradients to log_young, x0 and v0."""
+    return ImplicitRollout.apply(log_young, x0, v0, body, dt, nsteps, checkpoint_every)

@@ -1,5 +1,6 @@
 // gbfem_element.cuh -- per-element corotational-tetrahedron math, templated on the arithmetic
-// type of the bulk work (double for the plain form, float for the mixed form).
+// type of the bulk work (double for the plain form, float for the mixed form, Dual for the
+// element derivatives of the adjoint).
 //
 // Closed form on the shape-function gradients g_a (rows of V^-1) instead of 12x12 products.
 // With h_a = R g_a and G_ab = g_a . g_b:
@@ -18,7 +19,9 @@
 
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
+#include "gbfem_dual.cuh"
 #include "gbfem_internal.h"
 
 namespace gbfem {
@@ -65,6 +68,12 @@ struct Eps<float>
 {
 	static constexpr float eps = FLT_EPSILON;
 	static constexpr float newtonTol2 = 1e-11f;
+};
+template <>
+struct Eps<Dual>
+{
+	static constexpr double eps = DBL_EPSILON;
+	static constexpr double newtonTol2 = 1e-26;
 };
 
 // Polar factor by Newton's iteration X <- (g X + X^-T / g) / 2 (Higham), Frobenius scaling on the
@@ -235,17 +244,20 @@ __host__ __device__ __forceinline__ int pair_slot(int a, int b)
 	return (a == 0) ? (3 + b) : (a == 1 ? (5 + b) : 9);
 }
 
-// Per-element inputs gathered by the kernels (node 0 is the origin of p and q).
-struct ElemIn
+// Per-element inputs gathered by the kernels (node 0 is the origin of p and q), with scalar type P
+// (double, or Dual when the adjoint seeds a derivative direction in them).
+template <typename P>
+struct ElemInT
 {
 	int nd[4];
-	double p[4][3];    // x_n,a - x_n,0
-	double q[4][3];    // x0_a - x0_0
-	double uK[4][3];   // -beta v_n + (x_n - x_t - dt v_n)
-	double uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
-	double vv[4][3];   // v_n (debug force only)
+	P p[4][3];    // x_n,a - x_n,0
+	P q[4][3];    // x0_a - x0_0
+	P uK[4][3];   // -beta v_n + (x_n - x_t - dt v_n)
+	P uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
+	P vv[4][3];   // v_n (debug force only)
 	double alphaDbg, betaDbg;  // Rayleigh coefficients (debug force only)
 };
+using ElemIn = ElemInT<double>;
 
 __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __restrict__ xn,
 									   const double* __restrict__ vn, const double* __restrict__ xt,
@@ -287,8 +299,8 @@ __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __
 //   damping force of FemRepresentation.cpp:565-629 folded in).
 // Debug outputs (double only): kfull[144] the full tangent, fdbg[12] = f_e - alpha M0 v - beta K_e v.
 // Returns a bitmask: 1 = polar fallback to the FP64 SVD, 2 = singular G (extra terms skipped).
-template <typename T, bool kDebug>
-__host__ __device__ int compute(const ElemIn& in, const T (&g)[4][3], T lamV, T muV, T cm, T* ks, int ksStride, T* rhs,
+template <typename T, bool kDebug, typename In = ElemIn>
+__host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV, T cm, T* ks, int ksStride, T* rhs,
 					   int rhsStride, double* kfull, double* fdbg)
 {
 	int flags = 0;
@@ -302,16 +314,22 @@ __host__ __device__ int compute(const ElemIn& in, const T (&g)[4][3], T lamV, T 
 	T R[9];
 	if (!polar_newton(F, R))
 	{
-		// Near-inverted or degenerate element: FP64 SVD path (the reference's computeRotationScaling).
-		double Fd[9], Rd[9];
+		// Near-inverted or degenerate element: SVD path (the reference's computeRotationScaling),
+		// always at least FP64.
+		if constexpr (std::is_same<T, float>::value)
+		{
+			double Fd[9], Rd[9];
 #pragma unroll
-		for (int i = 0; i < 3; ++i)
+			for (int i = 0; i < 3; ++i)
 #pragma unroll
-			for (int j = 0; j < 3; ++j)
-				Fd[3 * i + j] = in.p[1][i] * double(g[1][j]) + in.p[2][i] * double(g[2][j]) + in.p[3][i] * double(g[3][j]);
-		polar_svd(Fd, Rd);
+				for (int j = 0; j < 3; ++j)
+					Fd[3 * i + j] = in.p[1][i] * double(g[1][j]) + in.p[2][i] * double(g[2][j]) + in.p[3][i] * double(g[3][j]);
+			polar_svd(Fd, Rd);
 #pragma unroll
-		for (int k = 0; k < 9; ++k) R[k] = T(Rd[k]);
+			for (int k = 0; k < 9; ++k) R[k] = T(Rd[k]);
+		}
+		else
+			polar_svd(F, R);
 		flags |= 1;
 	}
 	// S = sym(R^T F), G = (tr(S) I - S) R^T (:208), G^-1 with the |det| > 1e-12 check (:210).
@@ -354,15 +372,14 @@ __host__ __device__ int compute(const ElemIn& in, const T (&g)[4][3], T lamV, T 
 	}
 	// Corotated strain displacement w_c = R^T p_c - q_c and u~_c = R^T uK_c - w_c.
 	T w[4][3], ut[4][3], wt[4][3];
-	if (sizeof(T) == sizeof(double))
+	if constexpr (!std::is_same<T, float>::value)
 	{
 #pragma unroll
 		for (int a = 0; a < 4; ++a)
 #pragma unroll
 			for (int i = 0; i < 3; ++i)
 			{
-				w[a][i] = T(double(R[i]) * in.p[a][0] + double(R[3 + i]) * in.p[a][1] + double(R[6 + i]) * in.p[a][2] -
-							in.q[a][i]);
+				w[a][i] = R[i] * T(in.p[a][0]) + R[3 + i] * T(in.p[a][1]) + R[6 + i] * T(in.p[a][2]) - T(in.q[a][i]);
 				ut[a][i] = R[i] * T(in.uK[a][0]) + R[3 + i] * T(in.uK[a][1]) + R[6 + i] * T(in.uK[a][2]) - w[a][i];
 			}
 	}

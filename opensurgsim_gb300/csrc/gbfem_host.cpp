@@ -115,6 +115,7 @@ struct gbfem_handle_s
 	DevBuf<int4> d_lblk;
 	DevBuf<uint8_t> d_bc;
 	DevBuf<double> d_x, d_v, d_xt, d_vt;
+	DevBuf<double> d_mu, d_adjG, d_gx, d_gv;  // differentiation form (allocated on first use)
 	DevBuf<double> d_kslots, d_rhsE, d_A, d_invdiag, d_rhs, d_dv, d_dvPrev, d_r, d_p, d_q, d_part;
 	// mixed-precision form
 	DevBuf<float> d_rest32, d_kslots32, d_rhsE32, d_A32, d_invdiag32, d_xd, d_invd, d_r32, d_pA, d_pB, d_q32;
@@ -206,6 +207,7 @@ struct gbfem_handle_s
 		d_slots.free();
 		d_seg.free();
 		d_pcgGlobal.free();
+		for (auto* b : {&d_mu, &d_adjG, &d_gx, &d_gv}) b->free();
 		DevBuf<double>* bd[] = {&d_rest, &d_xrest, &d_lmass, &d_nmass, &d_x, &d_v, &d_xt, &d_vt, &d_kslots,
 								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
 								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f};
@@ -1059,6 +1061,72 @@ gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, co
 								gbfem_handle* out)
 {
 	return create_impl(meshes, count, params, out);
+}
+
+gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, const double* poisson)
+{
+	if (!h || !young) return GBFEM_INVALID_ARG;
+	launch_set_materials(h->E, young, poisson, h->d_rest.p, h->mixed() ? h->d_rest32.p : nullptr, h->stream);
+	GB_CUDA(h, cudaGetLastError());
+	GB_CUDA(h, cudaStreamSynchronize(h->stream));
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,
+								const double* lx, const double* lv, double* lx_out, double* lv_out,
+								double* grad_log_young, double* grad_poisson)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (!x || !v || !dv || !lx || !lv || !lx_out || !lv_out || !(dt > 0.0))
+		return fail(h, GBFEM_INVALID_ARG, "gbfem_adjoint_step: null array or dt <= 0");
+	cudaStream_t s = h->stream;
+	const DevBody body = h->body();
+	const int n = h->n;
+	if (!h->d_mu.p)
+	{
+		GB_CUDA(h, h->d_mu.alloc(n));
+		GB_CUDA(h, h->d_adjG.alloc(n));
+		GB_CUDA(h, h->d_gx.alloc(12 * (size_t)h->E));
+		GB_CUDA(h, h->d_gv.alloc(12 * (size_t)h->E));
+	}
+	const double alpha = h->prm.rayleigh_mass, beta = h->prm.rayleigh_stiffness;
+	const double c1 = 1.0 / dt + alpha, c2 = dt + beta;
+	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * n;
+	// The step's system at (x, v), as the first Newton iteration of step_once builds it.
+	if (h->mixed())
+	{
+		launch_element_f32(body, x, v, x, v, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s);
+		launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+	}
+	else
+	{
+		launch_element_fp64(body, x, v, x, v, dt, alpha, beta, h->d_kslots.p, h->d_rhsE.p, nullptr, nullptr,
+							h->d_counters.p, s);
+		launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+	}
+	launch_adjoint_rhs(n, h->d_bc.p, lx, lv, dt, h->d_adjG.p, s);
+	GB_CUDA(h, cudaGetLastError());
+	h->launches += 3;
+	bool converged = true;
+	if (h->mixed())
+	{
+		gbfem_status st = run_mixed(h, h->d_adjG.p, h->d_mu.p, maxIter, false);
+		if (st != GBFEM_OK) return st;
+		for (size_t k = 0; k + 1 < h->segNode.size(); ++k) converged = converged && h->h_seg[k].converged;
+	}
+	else
+	{
+		gbfem_status st = run_cg(h, h->d_adjG.p, h->d_mu.p, maxIter, false);
+		if (st != GBFEM_OK) return st;
+		converged = h->h_ctl->converged != 0;
+	}
+	launch_element_adjoint(body, x, v, h->d_mu.p, dv, dt, alpha, beta, h->d_gx.p, h->d_gv.p, grad_log_young,
+						   grad_poisson, s);
+	launch_adjoint_gather(body, h->d_gx.p, h->d_gv.p, lx, lv, dt, lx_out, lv_out, s);
+	GB_CUDA(h, cudaGetLastError());
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	h->launches += 2;
+	return converged ? GBFEM_OK : fail(h, GBFEM_CG_MAXITER, "adjoint solve did not converge");
 }
 
 gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets,

@@ -111,6 +111,16 @@ void launch_state_update(int n, const double* dv, double* dvPrev, const double* 
 						 double dt, int trackNewton, CgCtl* ctl, double* part, const Launch& L);
 void launch_validity(int n, const double* x, const double* v, CgCtl* ctl, double* part, const Launch& L);
 void launch_scatter_values(int count, const int* idx, const double* vals, double* dst, cudaStream_t s);
+// Differentiation form (gbfem_adjoint.cu).
+void launch_element_adjoint(const DevBody& b, const double* x, const double* v, const double* mu, const double* dv,
+							double dt, double alpha, double beta, double* gx, double* gv, double* gLogE, double* gNu,
+							cudaStream_t s);
+void launch_adjoint_gather(const DevBody& b, const double* gx, const double* gv, const double* lx, const double* lv,
+						   double dt, double* lxOut, double* lvOut, cudaStream_t s);
+void launch_adjoint_rhs(int n, const uint8_t* bc, const double* lx, const double* lv, double dt, double* g,
+						cudaStream_t s);
+void launch_set_materials(int E, const double* young, const double* poisson, double* rest, float* rest32,
+						  cudaStream_t s);
 
 // Partial-sum buffer size needed by the reductions for a given vecGrid.
 constexpr int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }

@@ -1,8 +1,10 @@
-// Test support only: the device element math of gbfem_element.cuh compiled for the host, so the
-// CPU test suite can compare it (FP64 and FP32) with the oracle element by element.
+// Test support only: the device element math of gbfem_element.cuh (and the element adjoint of
+// gbfem_adjoint.cuh) compiled for the host, so the CPU test suite can compare it (FP64 and FP32)
+// with the oracle element by element, and the adjoint with finite differences.
 #include <cmath>
 #include <cstring>
 
+#include "gbfem_adjoint.cuh"
 #include "gbfem_element.cuh"
 
 namespace {
@@ -103,4 +105,50 @@ extern "C" int gbfem_host_element(int fp32, const double* x0, const double* x, c
 {
 	return fp32 ? run<float>(x0, x, v, xt, vt, nd, E, nu, rho, dt, alpha, beta, K144, rhs12, f12, R9)
 				: run<double>(x0, x, v, xt, vt, nd, E, nu, rho, dt, alpha, beta, K144, rhs12, f12, R9);
+}
+
+// psi_e and its derivatives for one element (x, v absolute positions / velocities of the 4 nodes,
+// mu and dv the adjoint and velocity increment at its 12 dofs). Returns -1 for a degenerate rest tet.
+extern "C" int gbfem_host_adjoint_element(const double* x0, const double* x, const double* v, const int* nd, double E,
+										  double nu, double rho, double dt, double alpha, double beta, const double* mu,
+										  const double* dv, double* psi, double* gx, double* gv, double* pLam,
+										  double* pMu)
+{
+	double V[4][4], Vi[4][4];
+	for (int a = 0; a < 4; ++a)
+	{
+		for (int k = 0; k < 3; ++k) V[k][a] = x0[3 * a + k];
+		V[3][a] = 1.0;
+	}
+	if (!inverse44(V, Vi)) return -1;
+	const double vol = (det3v(x0 + 3, x0 + 6, x0 + 9) - det3v(x0, x0 + 6, x0 + 9) + det3v(x0, x0 + 3, x0 + 9) -
+						det3v(x0, x0 + 3, x0 + 6)) / 6.0;
+	const double lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+	const double mu_ = E / (2.0 * (1 + nu));
+	int ndv[4];
+	double X[4][3], R0[4][3], Vel[4][3], MU[12], DV[12], g[4][3];
+	for (int a = 0; a < 4; ++a)
+	{
+		ndv[a] = nd[a];
+		for (int k = 0; k < 3; ++k)
+		{
+			X[a][k] = x[3 * a + k];
+			R0[a][k] = x0[3 * a + k];
+			Vel[a][k] = v[3 * a + k];
+			g[a][k] = Vi[a][k];
+		}
+	}
+	for (int j = 0; j < 12; ++j)
+	{
+		MU[j] = mu[j];
+		DV[j] = dv[j];
+	}
+	const double lamV = lambda * vol, muV = mu_ * vol, cm = vol * rho / 20.0;
+	gbfem::elem::ElemIn in;
+	gbfem::adj::fill_input(in, ndv, X, R0, Vel, dt, alpha, beta, -1, -1);
+	double ks[90], rh[12];
+	gbfem::elem::compute<double, false>(in, g, lamV, muV, cm, ks, 1, rh, 1, nullptr, nullptr);
+	*psi = gbfem::adj::element_psi(ndv, ks, rh, MU, DV, dt + beta);
+	gbfem::adj::adjoint_element(ndv, X, R0, Vel, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
+	return 0;
 }

@@ -21,7 +21,8 @@ def elem():
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    deps = [SRC, os.path.join(ROOT, "opensurgsim_gb300", "csrc", "gbfem_element.cuh")]
+    deps = [SRC] + [os.path.join(ROOT, "opensurgsim_gb300", "csrc", f)
+                    for f in ("gbfem_element.cuh", "gbfem_adjoint.cuh", "gbfem_dual.cuh")]
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(d) for d in deps):
         subprocess.run([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
                         "-I" + os.path.join(ROOT, "opensurgsim_gb300", "csrc"), "-o", LIB, SRC], check=True,
@@ -31,6 +32,9 @@ def elem():
     L.gbfem_host_element.argtypes = [ctypes.c_int, D, D, D, D, D, ctypes.POINTER(ctypes.c_int)] + \
         [ctypes.c_double] * 6 + [D, D, D, D]
     L.gbfem_host_element.restype = ctypes.c_int
+    L.gbfem_host_adjoint_element.argtypes = [D, D, D, ctypes.POINTER(ctypes.c_int)] + [ctypes.c_double] * 6 + \
+        [D] * 7
+    L.gbfem_host_adjoint_element.restype = ctypes.c_int
 
     def run(fp32, x0, x, v=None, E=1e6, nu=0.45, rho=1000.0, dt=1e-3, alpha=0.0, beta=0.0, nd=(0, 1, 2, 3)):
         def d(a):
@@ -44,6 +48,20 @@ def elem():
         assert fl >= 0
         return K.reshape(12, 12), f, rhs, R.reshape(3, 3), fl
 
+    def adjoint(x0, x, v, mu, dv, E=1e5, nu=0.45, rho=1000.0, dt=1e-3, alpha=0.01, beta=0.001, nd=(0, 1, 2, 3)):
+        def d(a):
+            return np.ascontiguousarray(a, dtype=np.float64).ravel()
+        x0, x, v, mu, dv = d(x0), d(x), d(v), d(mu), d(dv)
+        psi, pl, pm = (ctypes.c_double() for _ in range(3))
+        gx, gv = np.zeros(12), np.zeros(12)
+        p = lambda a: a.ctypes.data_as(D)  # noqa: E731
+        r = L.gbfem_host_adjoint_element(p(x0), p(x), p(v), (ctypes.c_int * 4)(*nd), E, nu, rho, dt, alpha, beta,
+                                         p(mu), p(dv), ctypes.byref(psi), p(gx), p(gv), ctypes.byref(pl),
+                                         ctypes.byref(pm))
+        assert r == 0
+        return psi.value, gx, gv, pl.value, pm.value
+
+    run.adjoint = adjoint
     return run
 
 
@@ -126,3 +144,55 @@ def test_inverted_element_takes_svd_fallback(elem):
     assert abs(np.linalg.det(R) - 1) < 1e-12
     assert np.abs(R - o["R"]).max() < 1e-10
     assert np.abs(K - o["K"]).max() <= 1e-10 * np.abs(o["K"]).max()
+
+
+def _adjoint_case(seed):
+    rng = np.random.default_rng(seed)
+    x0 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float) * 0.01 + rng.uniform(-1e-3, 1e-3, (4, 3))
+    R = rot(0.7, [1.0, 2.0, 0.5])
+    x = (x0 @ R.T) * 1.05 + rng.uniform(-5e-4, 5e-4, (4, 3)) + 0.02
+    v = rng.normal(0, 0.05, (4, 3))
+    mu = rng.normal(0, 1.0, 12)
+    dv = rng.normal(0, 0.01, 12)
+    nd = tuple(int(i) for i in rng.permutation([3, 7, 11, 19]))
+    return x0, x, v, mu, dv, nd
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_element_adjoint_position_gradient_matches_central_differences(elem, seed):
+    """d psi_e / d x_e from the dual-number passes vs central differences of psi_e (the element
+    share of mu.rhs - mu.S dv that the step's adjoint differentiates)."""
+    x0, x, v, mu, dv, nd = _adjoint_case(seed)
+    _, gx, _, _, _ = elem.adjoint(x0, x, v, mu, dv, nd=nd)
+    h = 1e-7
+    fd = np.zeros(12)
+    for j in range(12):
+        xp, xm = x.copy().ravel(), x.copy().ravel()
+        xp[j] += h
+        xm[j] -= h
+        fd[j] = (elem.adjoint(x0, xp, v, mu, dv, nd=nd)[0] - elem.adjoint(x0, xm, v, mu, dv, nd=nd)[0]) / (2 * h)
+    assert np.linalg.norm(gx - fd) <= 1e-6 * np.linalg.norm(fd)
+
+
+@pytest.mark.parametrize("seed", [0, 3])
+def test_element_adjoint_velocity_and_modulus_gradients(elem, seed):
+    x0, x, v, mu, dv, nd = _adjoint_case(seed)
+    E, nu = 2.5e5, 0.42
+    psi, _, gv, pl, pm = elem.adjoint(x0, x, v, mu, dv, E=E, nu=nu, nd=nd)
+    h = 1e-6
+    fd = np.zeros(12)
+    for j in range(12):
+        vp, vm = v.copy().ravel(), v.copy().ravel()
+        vp[j] += h
+        vm[j] -= h
+        fd[j] = (elem.adjoint(x0, x, vp, mu, dv, E=E, nu=nu, nd=nd)[0] -
+                 elem.adjoint(x0, x, vm, mu, dv, E=E, nu=nu, nd=nd)[0]) / (2 * h)
+    assert np.linalg.norm(gv - fd) <= 1e-8 * np.linalg.norm(fd)
+    # log E: psi's elastic part is homogeneous of degree one in (lambda V, mu V).
+    vol = abs(np.linalg.det(np.c_[x0[1:] - x0[0]])) / 6
+    lamV = E * nu / ((1 + nu) * (1 - 2 * nu)) * vol
+    muV = E / (2 * (1 + nu)) * vol
+    hE = 1e-6
+    fdE = (elem.adjoint(x0, x, v, mu, dv, E=E * np.exp(hE), nu=nu, nd=nd)[0] -
+           elem.adjoint(x0, x, v, mu, dv, E=E * np.exp(-hE), nu=nu, nd=nd)[0]) / (2 * hE)
+    assert abs(lamV * pl + muV * pm - fdE) <= 1e-7 * abs(fdE)

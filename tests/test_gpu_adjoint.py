@@ -1,0 +1,110 @@
+"""Differentiation form on the GPU: gradients of a multi-step rollout (gbfem_adjoint_step behind
+torch.autograd) against central finite differences of the forward rollout, FP64 and mixed."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _setup(precision, nx=3, ny=3, nz=4, tol=1e-13, seed=0):
+    from opensurgsim_gb300 import _lib, mesh
+    from opensurgsim_gb300.body import Body
+
+    scene = mesh.scene_cube(nx, ny, nz, seed=seed)
+    prec = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
+    body = Body.from_scene(scene, precision=prec, cg_tolerance=tol)
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(seed + 11)
+    m = scene.mesh
+    theta = torch.tensor(np.log(m.young) + rng.normal(0, 0.3, m.num_tets), dtype=torch.float64, device=dev)
+    x0 = torch.tensor(m.nodes.ravel(), dtype=torch.float64, device=dev)
+    v0 = torch.tensor(rng.normal(0, 0.01, body.n), dtype=torch.float64, device=dev)
+    v0[torch.tensor(m.bc_dofs, dtype=torch.long, device=dev)] = 0.0
+    wx = torch.tensor(rng.normal(0, 1, body.n), dtype=torch.float64, device=dev)
+    wv = torch.tensor(rng.normal(0, 1e-3, body.n), dtype=torch.float64, device=dev)
+    return scene, body, theta, x0, v0, wx, wv
+
+
+def _loss(body, theta, x0, v0, wx, wv, dt, steps, every=4):
+    from opensurgsim_gb300.autograd import rollout
+
+    xT, vT = rollout(body, theta, x0, v0, dt, steps, checkpoint_every=every)
+    return (wx * (xT - x0)).sum() + (wv * vT).sum()
+
+
+def _loss_value(body, theta, x0, v0, wx, wv, dt, steps):
+    with torch.no_grad():
+        return float(_loss(body, theta, x0, v0, wx, wv, dt, steps))
+
+
+@pytest.mark.parametrize("steps,every", [(6, 4), (5, 10)])
+def test_fp64_log_young_gradient_matches_central_differences(gpu_lib, steps, every):
+    scene, body, theta, x0, v0, wx, wv = _setup("fp64")
+    th = theta.clone().requires_grad_(True)
+    L = _loss(body, th, x0, v0, wx, wv, scene.dt, steps, every)
+    L.backward()
+    g = th.grad.detach().cpu().numpy()
+    h = 1e-5
+    fd = np.zeros_like(g)
+    for e in range(g.size):
+        tp, tm = theta.clone(), theta.clone()
+        tp[e] += h
+        tm[e] -= h
+        fd[e] = (_loss_value(body, tp, x0, v0, wx, wv, scene.dt, steps) -
+                 _loss_value(body, tm, x0, v0, wx, wv, scene.dt, steps)) / (2 * h)
+    err = np.linalg.norm(g - fd) / np.linalg.norm(fd)
+    assert err <= 1e-4, err
+    big = np.abs(fd) > 0.1 * np.abs(fd).max()
+    assert np.max(np.abs(g[big] - fd[big]) / np.abs(fd[big])) <= 1e-3
+
+
+def test_fp64_initial_state_gradients_match_directional_differences(gpu_lib):
+    scene, body, theta, x0, v0, wx, wv = _setup("fp64", seed=4)
+    from opensurgsim_gb300.autograd import rollout
+
+    x0g = x0.clone().requires_grad_(True)
+    v0g = v0.clone().requires_grad_(True)
+    xT, vT = rollout(body, theta, x0g, v0g, scene.dt, 5, checkpoint_every=2)
+    L = (wx * xT).sum() + (wv * vT).sum()
+    L.backward()
+    rng = np.random.default_rng(7)
+    bc = torch.tensor(scene.mesh.bc_dofs, dtype=torch.long, device=x0.device)
+    for which, base, grad in (("v", v0, v0g.grad), ("x", x0, x0g.grad)):
+        d = torch.tensor(rng.normal(0, 1, body.n), dtype=torch.float64, device=x0.device)
+        d[bc] = 0.0
+        h = 1e-6 if which == "v" else 1e-8
+
+        def val(delta):
+            with torch.no_grad():
+                xa = x0 + delta * d if which == "x" else x0
+                va = v0 + delta * d if which == "v" else v0
+                xT_, vT_ = rollout(body, theta, xa, va, scene.dt, 5, checkpoint_every=2)
+                return float((wx * xT_).sum() + (wv * vT_).sum())
+
+        fd = (val(h) - val(-h)) / (2 * h)
+        ad = float((grad * d).sum())
+        assert abs(ad - fd) <= 1e-5 * abs(fd), (which, ad, fd)
+
+
+def test_mixed_adjoint_agrees_with_fp64_adjoint(gpu_lib):
+    grads = {}
+    for prec in ("fp64", "mixed"):
+        scene, body, theta, x0, v0, wx, wv = _setup(prec, tol=1e-12, seed=2)
+        th = theta.clone().requires_grad_(True)
+        _loss(body, th, x0, v0, wx, wv, scene.dt, 6).backward()
+        grads[prec] = th.grad.detach().cpu().numpy()
+    err = np.linalg.norm(grads["mixed"] - grads["fp64"]) / np.linalg.norm(grads["fp64"])
+    assert err <= 1e-4, err
+
+
+def test_adjoint_is_deterministic(gpu_lib):
+    out = []
+    for _ in range(2):
+        scene, body, theta, x0, v0, wx, wv = _setup("fp64", seed=5)
+        th = theta.clone().requires_grad_(True)
+        _loss(body, th, x0, v0, wx, wv, scene.dt, 4).backward()
+        out.append(th.grad.detach().cpu().numpy())
+    assert np.array_equal(out[0], out[1])
