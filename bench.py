@@ -509,6 +509,139 @@ def run_single(args, rank, world, local, dist):
 
 
 # ------------------------------------------------------------------------------------------------
+# Differentiation workload (--config adjoint): identification of per-element log E on a 20x20x40
+# cube grid (80,000 tets) from 64 marker positions after 50 steps.
+
+ADJ_STEPS, ADJ_CHECKPOINT, ADJ_MARKERS, ADJ_FD_ELEMENTS, ADJ_FD_H = 50, 10, 64, 32, 1e-6
+
+
+def adjoint_problem(seed=5):
+    """theta_e = ln(1e5) + N(0, 0.3), v0 ~ N(0, 0.01) m/s per free dof, 64 seeded marker nodes, targets
+    from a second (ground-truth) theta field after 50 steps; bottom face fixed, gravity, alpha 0.01,
+    beta 0.001, dt 1e-3; CG tolerance 1e-12 (finite differences at h = 1e-6 need tight solves)."""
+    import numpy as np
+
+    from opensurgsim_gb300 import mesh
+
+    scene = mesh.scene_cube(20, 20, 40, seed=seed, cg_tolerance=1e-12)
+    m = scene.mesh
+    rng = np.random.default_rng(seed)
+    theta = math.log(1e5) + rng.normal(0, 0.3, m.num_tets)
+    theta_true = math.log(1e5) + rng.normal(0, 0.3, m.num_tets)
+    v0 = rng.normal(0, 0.01, 3 * m.num_nodes)
+    v0[m.bc_dofs] = 0.0
+    bc_nodes = set((m.bc_dofs // 3).tolist())
+    free = np.array([i for i in range(m.num_nodes) if i not in bc_nodes])
+    markers = np.sort(rng.choice(free, ADJ_MARKERS, replace=False))
+    return scene, theta, theta_true, v0, markers
+
+
+def run_adjoint(args, local):
+    """Forward + backward throughput of the 50-step rollout (FP64 and mixed), the gradient against
+    central finite differences on 32 random elements, and the mixed gradient against the FP64 one."""
+    import numpy as np
+    import torch
+
+    from opensurgsim_gb300 import _lib, build
+    from opensurgsim_gb300.autograd import rollout
+    from opensurgsim_gb300.body import Body
+
+    build.build()
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    scene, theta_np, theta_true_np, v0_np, markers = adjoint_problem()
+    m = scene.mesh
+    x0 = torch.tensor(m.nodes.ravel(), dtype=torch.float64, device=dev)
+    v0 = torch.tensor(v0_np, dtype=torch.float64, device=dev)
+    theta = torch.tensor(theta_np, dtype=torch.float64, device=dev)
+    mk = torch.tensor(np.stack([3 * markers, 3 * markers + 1, 3 * markers + 2], 1).ravel(), dtype=torch.long,
+                      device=dev)
+    bodies = {p: Body.from_scene(scene, precision=(_lib.PRECISION_MIXED if p == "mixed" else _lib.PRECISION_FP64),
+                                 device=local) for p in ("fp64", "mixed")}
+    with torch.no_grad():
+        xT, _ = rollout(bodies["fp64"], torch.tensor(theta_true_np, dtype=torch.float64, device=dev), x0, v0,
+                        scene.dt, ADJ_STEPS, ADJ_CHECKPOINT)
+        target = xT[mk].clone()
+
+    def loss(body, th, flags=0):
+        xT_, _ = rollout(body, th, x0, v0, scene.dt, ADJ_STEPS, ADJ_CHECKPOINT, flags)
+        return ((xT_[mk] - target) ** 2).sum()
+
+    results = {}
+    for p, body in bodies.items():
+        def fwd_bwd():
+            th = theta.clone().requires_grad_(True)
+            L = loss(body, th)
+            L.backward()
+            return float(L.detach()), th.grad.detach().clone()
+        fwd_bwd()  # warm-up
+        torch.cuda.synchronize(dev)
+        reps = 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            Lval, g = fwd_bwd()
+        torch.cuda.synchronize(dev)
+        sec = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        with torch.no_grad():
+            loss(body, theta)
+        torch.cuda.synchronize(dev)
+        sec_fwd = time.perf_counter() - t0
+        # Phase split of the adjoint steps of the last (first-in-time) checkpoint segment: the stats
+        # restart at every forward step, so they hold that segment's adjoint steps.
+        th = theta.clone().requires_grad_(True)
+        loss(body, th, _lib.STEP_TIME_PHASES).backward()
+        st = body.stats()
+        nadj = min(ADJ_CHECKPOINT, ADJ_STEPS)
+        split = {"system_ms": st["ms_element"] / nadj, "transposed_solve_ms": st["ms_solve"] / nadj,
+                 "element_derivatives_ms": st["ms_update"] / nadj}
+        results[p] = {"loss": Lval, "grad": g, "sec": sec, "sec_forward": sec_fwd, "split": split}
+        log(f"adjoint {p}: forward+backward {sec:.3f} s, forward {sec_fwd:.3f} s, loss {Lval:.6e}, split {split}")
+    # Central finite differences in log E on 32 random elements (FP64 form).
+    rng = np.random.default_rng(17)
+    els = np.sort(rng.choice(m.num_tets, ADJ_FD_ELEMENTS, replace=False))
+    g64 = results["fp64"]["grad"].cpu().numpy()
+    fd = np.zeros(len(els))
+    with torch.no_grad():
+        for i, e in enumerate(els):
+            tp, tm = theta.clone(), theta.clone()
+            tp[e] += ADJ_FD_H
+            tm[e] -= ADJ_FD_H
+            fd[i] = (float(loss(bodies["fp64"], tp)) - float(loss(bodies["fp64"], tm))) / (2 * ADJ_FD_H)
+    diff = np.abs(g64[els] - fd)
+    gm = results["mixed"]["grad"].cpu().numpy()
+    mixed_err = float(np.linalg.norm(gm - g64) / np.linalg.norm(g64))
+    E = m.num_tets
+    line = {
+        "metric": "tet-element-steps/s (forward + backward of a 50-step rollout, adjoint form)",
+        "value": E * ADJ_STEPS / results["fp64"]["sec"],
+        "unit": UNIT,
+        "n_gpus": 1, "steps": 2, "warmup": 1,
+        "ms_per_step": 1e3 * results["fp64"]["sec"] / ADJ_STEPS,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded cube-grid mesh, seeded parameters)",
+        "config": {"workload": ("adjoint20x20x40: 80,000 tets, log E = ln 1e5 + N(0, 0.3), v0 ~ N(0, 0.01), 64 "
+                                "markers, targets from a ground-truth log E field, 50 steps, checkpoints every "
+                                "10, CG tol 1e-12"), "tets": E, "nodes": m.num_nodes},
+        "adjoint_step_split_ms": results["fp64"]["split"],
+        "mixed": {"value": E * ADJ_STEPS / results["mixed"]["sec"],
+                  "ms_per_step": 1e3 * results["mixed"]["sec"] / ADJ_STEPS,
+                  "grad_rel_err_vs_fp64": mixed_err, "adjoint_step_split_ms": results["mixed"]["split"]},
+        "forward_only": {"fp64": E * ADJ_STEPS / results["fp64"]["sec_forward"],
+                         "mixed": E * ADJ_STEPS / results["mixed"]["sec_forward"]},
+        "fd_check": {"elements": ADJ_FD_ELEMENTS, "h": ADJ_FD_H,
+                     "norm_rel_err": float(np.linalg.norm(g64[els] - fd) / np.linalg.norm(fd)),
+                     "max_err_rel_to_max_grad": float(diff.max() / np.abs(fd).max()),
+                     "median_rel_err": float(np.median(diff / np.abs(fd))), "gate": 1e-4},
+        "loss": results["fp64"]["loss"],
+        "timing": "host clock around device-synchronised forward+backward (2 repetitions after 1 warm-up)",
+    }
+    for b in bodies.values():
+        b.close()
+    return line
+
+
+# ------------------------------------------------------------------------------------------------
 # CPU side: the oracle (FP64 C++ restatement of the reference step), the only CPU implementation
 # of the path that runs here (the reference needs Eigen and Boost).
 
@@ -616,7 +749,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube"])
+    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube", "adjoint"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="bar and cube only; the batch is always mixed precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -628,6 +761,10 @@ def main():
         line = run_reference(args, rank, world)
         if rank == 0:
             print(json.dumps(line), flush=True)
+        return
+    if args.config == "adjoint":
+        if rank == 0:
+            print(json.dumps(run_adjoint(args, local)), flush=True)
         return
     dist = Dist(world)
     if args.config == "batch":

@@ -155,10 +155,12 @@ GBFEM_API gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* 
  * device arrays of n (state) or num_tets (gradients) doubles. Rebuilds the step's system at (x, v)
  * and solves it transposed with the handle's CG (the FP64 or the mixed solver); the element
  * derivatives are FP64. Does not change the handle's state. Returns GBFEM_CG_MAXITER if the
- * transposed solve did not converge (the outputs are still written). */
+ * transposed solve did not converge (the outputs are still written). With GBFEM_STEP_TIME_PHASES in
+ * flags the call adds its device times to the stats: ms_element (system rebuild), ms_solve
+ * (transposed solve), ms_update (element derivatives and the node gather). */
 GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,
 										  const double* lx, const double* lv, double* lx_out, double* lv_out,
-										  double* grad_log_young, double* grad_poisson);
+										  double* grad_log_young, double* grad_poisson, uint32_t flags);
 
 /* ---- Batching: many independent meshes (each its own OpenSurgSim representation, stepped like
  * one FreeMotion pass over them, FreeMotion.cpp:55-80) in one body. Node ids, boundary-condition

@@ -136,7 +136,7 @@ def load():
         "gbfem_batch_info": (S, [H, I32, I32, I32, ctypes.POINTER(ctypes.c_int64)]),
         "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
         "gbfem_set_materials_device": (S, [H, ctypes.c_void_p, ctypes.c_void_p]),
-        "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9),
+        "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9 + [ctypes.c_uint32]),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),

@@ -70,7 +70,7 @@ class ImplicitRollout(torch.autograd.Function):
     """(x_T, v_T) = rollout(log_young, x0, v0); see the module docstring."""
 
     @staticmethod
-    def forward(ctx, log_young, x0, v0, body, dt, nsteps, checkpoint_every):
+    def forward(ctx, log_young, x0, v0, body, dt, nsteps, checkpoint_every, flags=0):
         set_young(body, log_young)
         k = max(1, int(checkpoint_every))
         checkpoints = []
@@ -85,7 +85,7 @@ class ImplicitRollout(torch.autograd.Function):
             _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
             if (t + 1) % k == 0 and t + 1 < nsteps:
                 checkpoints.append((xv.clone(), vv.clone()))
-        ctx.body, ctx.dt, ctx.nsteps, ctx.k = body, dt, nsteps, k
+        ctx.body, ctx.dt, ctx.nsteps, ctx.k, ctx.flags = body, dt, nsteps, k, int(flags)
         ctx.checkpoints = checkpoints
         ctx.save_for_backward(log_young)
         return xv.clone(), vv.clone()
@@ -114,12 +114,14 @@ class ImplicitRollout(torch.autograd.Function):
                 dv = (states[t + 1][1] - vt).contiguous()
                 torch.cuda.synchronize(dev)
                 st = L.gbfem_adjoint_step(body.handle, float(dt), *[ctypes.c_void_p(a.data_ptr()) for a in
-                                                                     (xt, vt, dv, lx, lv, lx, lv, glog)], None)
+                                                                     (xt, vt, dv, lx, lv, lx, lv, glog)], None,
+                                          ctx.flags)
                 _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
         torch.cuda.synchronize(dev)
-        return glog, lx, lv, None, None, None, None
+        return glog, lx, lv, None, None, None, None, None
 
 
-def rollout(body, log_young, x0, v0, dt, nsteps, checkpoint_every=10):
-    """Differentiable rollout: returns (x_T, v_T) with gradients to log_young, x0 and v0."""
-    return ImplicitRollout.apply(log_young, x0, v0, body, dt, nsteps, checkpoint_every)
+def rollout(body, log_young, x0, v0, dt, nsteps, checkpoint_every=10, flags=0):
+    """Differentiable rollout: returns (x_T, v_T) with gradients to log_young, x0 and v0. ``flags``
+    (e.g. STEP_TIME_PHASES) go to every adjoint step."""
+    return ImplicitRollout.apply(log_young, x0, v0, body, dt, nsteps, checkpoint_every, flags)

@@ -10,7 +10,7 @@
 // where psi(x, v, theta) = mu . rhs - mu . S dv (mu and dv held fixed; BC entries of both are zero,
 // which removes the BC rows and columns the forward replaces by constants). psi is a sum of
 // element terms psi_e, so the per-element kernels below produce d psi_e / d(x_e, v_e, E_e, nu_e):
-//   - x: forward-mode dual numbers through the same element code (12 seeded passes), which
+//   - x: forward-mode dual numbers through the same element code (9 seeded passes), which
 //     differentiates the rotation, the corotated tangent (its dR/dx terms) and the force exactly;
 //   - v: psi is linear in v, d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e;
 //   - E, nu: psi_e is linear in (lambda V, mu V), so two evaluations with unit moduli give both.
@@ -23,6 +23,9 @@ namespace {
 
 constexpr int kAdjThreads = 64;
 
+// One thread per element, its eleven passes in turn (splitting them over threads was measured
+// slower: every pass needs the same large per-thread state, so more threads only add local-memory
+// traffic). gx[e*12 + 3..11], gv[e*12 + 0..11]; gLogE[e], gNu[e] accumulate.
 __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, const double* __restrict__ x,
 																 const double* __restrict__ v,
 																 const double* __restrict__ mu,
@@ -55,10 +58,12 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 #pragma unroll
 		for (int k = 0; k < 3; ++k) g[a][k] = b.rest[(3 * a + k) * E + e];
 	const double lamV = b.rest[13 * E + e], muV = b.rest[14 * E + e], cm = b.rest[15 * E + e];
+	const bool moduli = gLogE || gNu;
 	double pl = 0.0, pm = 0.0;
-	const bool wantModuli = gLogE || gNu;
-	adj::adjoint_element(nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
-						 gv + (size_t)e * 12, wantModuli ? &pl : nullptr, wantModuli ? &pm : nullptr);
+	for (int item = 0; item < (moduli ? adj::kAdjItems : adj::kAdjItems - 1); ++item)
+		adj::adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
+						  gv + (size_t)e * 12, &pl, &pm);
+	if (!moduli) return;
 	// lambda V = V E nu / ((1 + nu)(1 - 2 nu)), mu V = V E / (2 (1 + nu)): d/d log E scales both by
 	// one; nu = lambda / (2 (lambda + mu)).
 	if (gLogE) gLogE[e] += lamV * pl + muV * pm;
@@ -73,7 +78,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 }
 
 // dL/dx_t = lx + sum_e gx, dL/dv_t = dt lx + lv + sum_e gv, summed over each node's incidences in
-// element order (deterministic).
+// element order (deterministic); an element's node 0 takes minus the sum of its nodes 1..3.
 __global__ void k_adjoint_gather(DevBody b, const double* __restrict__ gx, const double* __restrict__ gv,
 								 const double* __restrict__ lx, const double* __restrict__ lv, double dt,
 								 double* __restrict__ lxOut, double* __restrict__ lvOut)
@@ -85,12 +90,13 @@ __global__ void k_adjoint_gather(DevBody b, const double* __restrict__ gx, const
 	for (int k = b.iptr[I]; k < k1; ++k)
 	{
 		const int c = b.iidx[k];
-		const size_t o = (size_t)(c >> 2) * 12 + 3 * (c & 3);
+		const size_t o = (size_t)(c >> 2) * 12;
+		const int a = c & 3;
 #pragma unroll
 		for (int j = 0; j < 3; ++j)
 		{
-			sx[j] += gx[o + j];
-			sv[j] += gv[o + j];
+			sx[j] += (a == 0) ? -(gx[o + 3 + j] + gx[o + 6 + j] + gx[o + 9 + j]) : gx[o + 3 * a + j];
+			sv[j] += gv[o + 3 * a + j];
 		}
 	}
 #pragma unroll

@@ -3,7 +3,7 @@
 // psi_e(x_e, v_e, lambda V, mu V) = mu_e . rhs_e - c2 <lower-triangle blocks of K_e, (mu, dv)> is the
 // element's share of psi = mu . rhs - mu . S dv, the scalar whose gradients give the step's adjoint
 // (see gbfem_adjoint.cu). adjoint_element() returns d psi_e / d x_e (12, forward-mode dual
-// numbers through the element code), d psi_e / d v_e (12) and d psi_e / d(lambda V), d(mu V).
+// numbers through the element code, nine passes), d psi_e / d v_e (12) and d psi_e / d(lambda V), d(mu V).
 #pragma once
 
 #include "gbfem_element.cuh"
@@ -77,31 +77,36 @@ __host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], co
 	in.betaDbg = beta;
 }
 
-// One element: X, R0, V positions / rest positions / velocities of its nodes, MU and DV the adjoint
-// and the step's velocity increment at its dofs (zero on BC dofs).
-__host__ __device__ inline void adjoint_element(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
-												const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],
-												const double (&g)[4][3], double lamV, double muV, double cm, double dt,
-												double alpha, double beta, double* gx, double* gv, double* pLam,
-												double* pMu)
+// Work items of one element, each an independent pass through the element code: items 0..8 are the
+// dual passes seeded on x_(1 + item/3, item%3) (psi_e depends on the positions only through
+// p_a = x_a - x_0, so d/dx_0 = -sum_a d/dx_a needs no pass of its own), item 9 the velocity
+// gradient, item 10 the two unit-modulus evaluations.
+constexpr int kAdjItems = 11;
+
+// One item of one element: X, R0, V positions / rest positions / velocities of its nodes, MU and DV
+// the adjoint and the step's velocity increment at its dofs (zero on BC dofs). Writes gx[3 + item]
+// (items 0..8), gv[0..11] (item 9) or *pLam, *pMu (item 10).
+__host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const double (&X)[4][3],
+											 const double (&R0)[4][3], const double (&V)[4][3], const double (&MU)[12],
+											 const double (&DV)[12], const double (&g)[4][3], double lamV, double muV,
+											 double cm, double dt, double alpha, double beta, double* gx, double* gv,
+											 double* pLam, double* pMu)
 {
 	const double c2 = dt + beta;
-	if (gx)
+	if (item < 9)
 	{
 		Dual gD[4][3];
 		for (int a = 0; a < 4; ++a)
 			for (int k = 0; k < 3; ++k) gD[a][k] = Dual(g[a][k]);
-		for (int s = 0; s < 12; ++s)
-		{
-			elem::ElemInT<Dual> in;
-			fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3);
-			Dual ks[kSlots * 9], rhs[12];
-			elem::compute<Dual, false, elem::ElemInT<Dual>>(in, gD, Dual(lamV), Dual(muV), Dual(cm), ks, 1, rhs, 1,
-															 nullptr, nullptr);
-			gx[s] = element_psi(nd, ks, rhs, MU, DV, c2).d;
-		}
+		const int s = 3 + item;
+		elem::ElemInT<Dual> in;
+		fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3);
+		Dual ks[kSlots * 9], rhs[12];
+		elem::compute<Dual, false, elem::ElemInT<Dual>>(in, gD, Dual(lamV), Dual(muV), Dual(cm), ks, 1, rhs, 1,
+														 nullptr, nullptr);
+		gx[s] = element_psi(nd, ks, rhs, MU, DV, c2).d;
 	}
-	if (gv)
+	else if (item == 9)
 	{
 		// d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (K_e: the full element tangent).
 		elem::ElemIn in;
@@ -118,17 +123,29 @@ __host__ __device__ inline void adjoint_element(const int (&nd)[4], const double
 			gv[c] = -c2 * t - alpha * cm * (MU[c] + sm[c % 3]);
 		}
 	}
-	if (pLam || pMu)
+	else
 	{
 		// psi_e's elastic part is linear in (lambda V, mu V): evaluate it with unit moduli.
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
 		double ks[kSlots * 9], rhs[12];
 		elem::compute<double, false>(in, g, 1.0, 0.0, 0.0, ks, 1, rhs, 1, nullptr, nullptr);
-		if (pLam) *pLam = element_psi(nd, ks, rhs, MU, DV, c2);
+		*pLam = element_psi(nd, ks, rhs, MU, DV, c2);
 		elem::compute<double, false>(in, g, 0.0, 1.0, 0.0, ks, 1, rhs, 1, nullptr, nullptr);
-		if (pMu) *pMu = element_psi(nd, ks, rhs, MU, DV, c2);
+		*pMu = element_psi(nd, ks, rhs, MU, DV, c2);
 	}
+}
+
+// All items of one element in one call (gx[0..2] completed from translation invariance).
+__host__ __device__ inline void adjoint_element(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
+												const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],
+												const double (&g)[4][3], double lamV, double muV, double cm, double dt,
+												double alpha, double beta, double* gx, double* gv, double* pLam,
+												double* pMu)
+{
+	for (int item = 0; item < kAdjItems; ++item)
+		adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
+	for (int k = 0; k < 3; ++k) gx[k] = -(gx[3 + k] + gx[6 + k] + gx[9 + k]);
 }
 
 }  // namespace adj

@@ -1074,7 +1074,7 @@ gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, con
 
 gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,
 								const double* lx, const double* lv, double* lx_out, double* lv_out,
-								double* grad_log_young, double* grad_poisson)
+								double* grad_log_young, double* grad_poisson, uint32_t flags)
 {
 	if (!h) return GBFEM_INVALID_ARG;
 	if (!x || !v || !dv || !lx || !lv || !lx_out || !lv_out || !(dt > 0.0))
@@ -1092,6 +1092,9 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	const double alpha = h->prm.rayleigh_mass, beta = h->prm.rayleigh_stiffness;
 	const double c1 = 1.0 / dt + alpha, c2 = dt + beta;
 	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * n;
+	PhaseTimer tm;
+	tm.init((flags & GBFEM_STEP_TIME_PHASES) != 0, s);
+	tm.mark(0);
 	// The step's system at (x, v), as the first Newton iteration of step_once builds it.
 	if (h->mixed())
 	{
@@ -1107,6 +1110,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	launch_adjoint_rhs(n, h->d_bc.p, lx, lv, dt, h->d_adjG.p, s);
 	GB_CUDA(h, cudaGetLastError());
 	h->launches += 3;
+	tm.mark(1);
 	bool converged = true;
 	if (h->mixed())
 	{
@@ -1120,12 +1124,20 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 		if (st != GBFEM_OK) return st;
 		converged = h->h_ctl->converged != 0;
 	}
+	tm.mark(2);
 	launch_element_adjoint(body, x, v, h->d_mu.p, dv, dt, alpha, beta, h->d_gx.p, h->d_gv.p, grad_log_young,
 						   grad_poisson, s);
 	launch_adjoint_gather(body, h->d_gx.p, h->d_gv.p, lx, lv, dt, lx_out, lv_out, s);
+	tm.mark(3);
 	GB_CUDA(h, cudaGetLastError());
 	GB_CUDA(h, cudaStreamSynchronize(s));
 	h->launches += 2;
+	if (tm.on)
+	{
+		h->stats.ms_element += tm.ms(0, 1);
+		h->stats.ms_solve += tm.ms(1, 2);
+		h->stats.ms_update += tm.ms(2, 3);
+	}
 	return converged ? GBFEM_OK : fail(h, GBFEM_CG_MAXITER, "adjoint solve did not converge");
 }
 
