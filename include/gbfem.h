@@ -84,7 +84,8 @@ typedef struct gbfem_params
 	int32_t cg_max_iterations;      /* setMaxIterations; <= 0 selects Eigen's default 2n */
 	int32_t precision;              /* gbfem_precision */
 	int32_t device;                 /* CUDA device ordinal */
-	int32_t reserved[7];
+	int32_t autotune;               /* mixed form: tune block sizes and the solve schedule on the first step */
+	int32_t reserved[6];
 } gbfem_params;
 
 /* Per-call statistics of the last gbfem_step. */
@@ -110,6 +111,10 @@ typedef struct gbfem_stats
 #define GBFEM_STEP_TIME_PHASES 1u   /* record per-phase device times (adds events) */
 #define GBFEM_STEP_KEEP_SYSTEM 2u   /* keep the full S / rhs / f of the last solve for export */
 #define GBFEM_STEP_TIME_KERNELS 4u  /* time every CG matrix-vector launch with CUDA events */
+#define GBFEM_STEP_GRAPH 8u         /* mixed form, one Newton iteration: capture the step into a CUDA graph
+                                       once and launch it nsteps times with no host round trip between
+                                       steps (statistics and the finiteness check are read at the end,
+                                       so a non-finite state is reported after the last step) */
 
 GBFEM_API gbfem_status gbfem_params_default(gbfem_params* out);
 
@@ -139,6 +144,16 @@ GBFEM_API gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v
 /* The CUDA stream the handle launches on (a cudaStream_t). */
 GBFEM_API gbfem_status gbfem_stream(gbfem_handle h, void** stream);
 GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
+
+/* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
+ * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
+ * CTAs per SM and refresh weights 4, 6, 8 on its own system, and keeps the fastest. The solve's
+ * partition sets the rounding of its sums, so a run that must repeat another bit for bit reads the
+ * choice with gbfem_get_tuning and pins it with gbfem_set_tuning (which also disables autotune). */
+GBFEM_API gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm,
+										int32_t* refresh_weight);
+GBFEM_API gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t ctas_per_sm,
+										int32_t refresh_weight);
 
 /* ---- Differentiation form. No counterpart in the reference (it has no adjoint); these serve
  * gradient-based identification on the same step (opensurgsim_gb300.autograd).

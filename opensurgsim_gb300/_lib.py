@@ -28,6 +28,7 @@ PRECISION_MIXED = 1
 STEP_TIME_PHASES = 1
 STEP_KEEP_SYSTEM = 2
 STEP_TIME_KERNELS = 4
+STEP_GRAPH = 8
 
 # Every symbol the header declares; the CPU tests check the library exports all of them.
 EXPORTED = [
@@ -36,7 +37,8 @@ EXPORTED = [
     "gbfem_get_sizes", "gbfem_get_pattern", "gbfem_get_scatter", "gbfem_get_system", "gbfem_last_error",
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
     "gbfem_cg_destroy", "gbfem_cg_solve_noalloc", "gbfem_batch_create", "gbfem_batch_info",
-    "gbfem_batch_segment_stats", "gbfem_set_materials_device", "gbfem_adjoint_step",
+    "gbfem_batch_segment_stats", "gbfem_set_materials_device", "gbfem_adjoint_step", "gbfem_get_tuning",
+    "gbfem_set_tuning",
 ]
 
 
@@ -66,7 +68,8 @@ class Params(ctypes.Structure):
         ("cg_max_iterations", ctypes.c_int32),
         ("precision", ctypes.c_int32),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("autotune", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -136,6 +139,8 @@ def load():
         "gbfem_batch_info": (S, [H, I32, I32, I32, ctypes.POINTER(ctypes.c_int64)]),
         "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
         "gbfem_set_materials_device": (S, [H, ctypes.c_void_p, ctypes.c_void_p]),
+        "gbfem_get_tuning": (S, [H, I32, I32, I32]),
+        "gbfem_set_tuning": (S, [H, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
         "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9 + [ctypes.c_uint32]),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,

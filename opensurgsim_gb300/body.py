@@ -20,7 +20,8 @@ class Body:
 
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5,
-                 cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0):
+                 cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0,
+                 autotune=False):
         """`mesh` is one TetMesh, or a list of them for a batch (mixed precision only)."""
         L = _lib.load()
         meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
@@ -55,6 +56,7 @@ class Body:
         p.cg_max_iterations = cg_max_iterations
         p.precision = precision
         p.device = device
+        p.autotune = 1 if autotune else 0
         self.params = p
         h = ctypes.c_void_p()
         if len(meshes) == 1 and not isinstance(mesh, (list, tuple)):
@@ -85,6 +87,15 @@ class Body:
         res = np.zeros(k)
         _lib.load().gbfem_batch_segment_stats(self._h, iptr(it), iptr(rf), iptr(cv), dptr(res))
         return dict(iterations=it, refreshes=rf, converged=cv, relative_residual=res)
+
+    def tuning(self):
+        """(elements per block, CTAs per SM, refresh weight) of the mixed form's kernels."""
+        e, c, r = (ctypes.c_int32() for _ in range(3))
+        self._check(_lib.load().gbfem_get_tuning(self._h, ctypes.byref(e), ctypes.byref(c), ctypes.byref(r)))
+        return e.value, c.value, r.value
+
+    def set_tuning(self, elems_per_block, ctas_per_sm, refresh_weight):
+        self._check(_lib.load().gbfem_set_tuning(self._h, int(elems_per_block), int(ctas_per_sm), int(refresh_weight)))
 
     @classmethod
     def from_scene(cls, scene, **over):

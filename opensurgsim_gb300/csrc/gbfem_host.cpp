@@ -124,6 +124,20 @@ struct gbfem_handle_s
 	DevBuf<double> d_slots;                  // cross-CTA partials of the persistent solve
 	int maxChunksPerCta = 0;
 	size_t pcgSmem = 0;
+	// Tuning of the mixed form (picked by the autotuner or set by gbfem_set_tuning).
+	int smCount = 0, chunkWeightMin = 1;
+	int64_t chunkWeightTotal = 0;
+	int ctasPerSM = 4, refreshWeight = kRefreshWeightDefault, elemsPerBlock = 64;
+	bool tuned = false;
+	int tuneVersion = 0;
+	// CUDA graph of one mixed-form step (GBFEM_STEP_GRAPH), rebuilt when dt, the timing flag or the
+	// tuning changes.
+	cudaGraphExec_t graphExec = nullptr;
+	double graphDt = 0.0;
+	bool graphTimed = false;
+	int graphVersion = -1;
+	DevBuf<double> d_acc;                    // per-segment statistics of graph-launched steps
+	cudaEvent_t graphEv[2] = {nullptr, nullptr};
 	DevBuf<SegCtl> d_seg;
 	DevBuf<PcgGlobal> d_pcgGlobal;
 	SegCtl* h_seg = nullptr;
@@ -205,6 +219,11 @@ struct gbfem_handle_s
 		for (auto* b : {&d_brs, &d_r64, &d_x64}) b->free();
 		for (auto* b : {&d_rcol, &d_segChunk, &d_cumW}) b->free();
 		d_slots.free();
+		d_acc.free();
+		if (graphExec) cudaGraphExecDestroy(graphExec);
+		graphExec = nullptr;
+		for (auto& e : graphEv)
+			if (e) cudaEventDestroy(e);
 		d_seg.free();
 		d_pcgGlobal.free();
 		for (auto* b : {&d_mu, &d_adjG, &d_gx, &d_gv}) b->free();
@@ -258,6 +277,31 @@ cudaError_t raise_pcg_smem_limit(size_t bytes)
 	const cudaError_t e = cudaFuncSetAttribute(k_pcg_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 	if (e == cudaSuccess) current = bytes;
 	return e;
+}
+
+// Grid of the persistent solve for `cps` CTAs per SM: G = min(cps * SMs, chunks); the largest share
+// of a CTA in chunks (its shared-memory partials) is bounded from the chunk weights: a weighted share
+// holds fewer than tot / (G wmin) + 1 chunks (tot at most kRefreshWeightMax times the plain total), a
+// counted one at most ceil(n / G). Fails if that many CTAs do not fit on an SM.
+gbfem_status configure_pcg(gbfem_handle h, int cps)
+{
+	const int nseg = (int)h->segNode.size() - 1;
+	const int G = std::max(1, std::min(cps * h->smCount, h->nchunks));
+	const int64_t mW = (int64_t)kRefreshWeightMax * h->chunkWeightTotal / ((int64_t)G * h->chunkWeightMin) + 2;
+	const int64_t mC = (int64_t)h->nchunks / G + 2;
+	const int M = (int)std::max(mW, mC);
+	const size_t smem = pcg_smem_bytes(nseg, M);
+	if (smem > 160 * 1024) return fail(h, GBFEM_INVALID_ARG, "batch too large for the persistent solve");
+	GB_CUDA(h, raise_pcg_smem_limit(smem));
+	int perSM = 0;
+	GB_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_pcg_persistent, kPcgThreads, smem));
+	if (perSM < std::min(cps, (G + h->smCount - 1) / h->smCount))
+		return fail(h, GBFEM_INVALID_ARG, "persistent solve: " + std::to_string(cps) + " CTAs per SM do not fit");
+	h->pcgGrid = G;
+	h->maxChunksPerCta = M;
+	h->pcgSmem = smem;
+	h->ctasPerSM = cps;
+	return GBFEM_OK;
 }
 
 // Everything the step needs from the mesh, computed on the host once.
@@ -520,30 +564,15 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 			if ((int64_t)cumW[c] + w > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "matrix too large for the persistent solve");
 			cumW[c + 1] = cumW[c] + w;
 		}
-		int perSM = 0, sms = 0;
-		GB_CUDA(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-		int G = std::max(1, std::min(4 * sms, nchunks));
-		size_t smem = 0;
-		for (int attempt = 0; attempt < 2; ++attempt)
-		{
-			// A weighted share holds fewer than tot / (G wmin) + 1 chunks (tot at most kRefreshWeight
-			// times the plain total), a counted one at most ceil(n / G).
-			const int64_t mW = (int64_t)kRefreshWeight * cumW[nchunks] / ((int64_t)G * wmin) + 2;
-			const int64_t mC = (int64_t)nchunks / G + 2;
-			h->maxChunksPerCta = (int)std::max(mW, mC);
-			smem = pcg_smem_bytes(nseg, h->maxChunksPerCta);
-			if (smem > 160 * 1024) return fail(h, GBFEM_INVALID_ARG, "batch too large for the persistent solve");
-			GB_CUDA(h, raise_pcg_smem_limit(smem));
-			GB_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_pcg_persistent, kPcgThreads, smem));
-			if (perSM < 1) return fail(h, GBFEM_INVALID_ARG, "persistent solve does not fit on an SM");
-			const int G2 = std::max(1, std::min(std::min(perSM, 4) * sms, nchunks));
-			if (G2 == G) break;
-			G = G2;  // fewer CTAs: larger shares, recompute the bound once
-		}
-		h->pcgGrid = G;
-		h->pcgSmem = smem;
+		GB_CUDA(h, cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, h->device));
+		h->chunkWeightTotal = cumW[nchunks];
+		h->chunkWeightMin = std::max(1, wmin);
+		gbfem_status cst = GBFEM_INVALID_ARG;
+		for (int cps = 4; cps >= 1 && cst != GBFEM_OK; --cps) cst = configure_pcg(h, cps);
+		if (cst != GBFEM_OK) return cst;
 		GB_CUDA(h, h->d_cumW.upload(cumW.data(), cumW.size(), s));
-		GB_CUDA(h, h->d_slots.alloc(4 * (size_t)G));
+		GB_CUDA(h, h->d_slots.alloc(4 * 4 * (size_t)h->smCount));  // any grid of up to 4 CTAs per SM
+		GB_CUDA(h, h->d_acc.alloc(4 * (size_t)nseg + 2));
 		GB_CUDA(h, cudaStreamSynchronize(s));
 	}
 	for (DevBuf<double>* b : {&h->d_rhs, &h->d_dv}) GB_CUDA(h, b->alloc(nv));
@@ -723,7 +752,8 @@ gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter, boo
 
 // Mixed-precision solve: FP32 CG iterations with reliable FP64 residual refreshes; the host polls
 // the device control block between chunks of iterations.
-gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, bool timeSolve)
+// Enqueue one persistent solve on the handle's stream (no host synchronisation; capturable).
+gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIter, cudaEvent_t ev0, cudaEvent_t ev1)
 {
 	const int nseg = (int)h->segNode.size() - 1;
 	cudaStream_t st = h->stream;
@@ -755,16 +785,36 @@ gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, 
 	a.cumW = h->d_cumW.p;
 	a.slots = h->d_slots.p;
 	a.maxChunksPerCta = h->maxChunksPerCta;
+	a.refreshWeight = h->refreshWeight;
+	a.pad = 0;
 	a.seg = h->d_seg.p;
 	a.g = h->d_pcgGlobal.p;
+	if (ev0) GB_CUDA(h, cudaEventRecord(ev0, st));
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(h->pcgGrid);
+	cfg.blockDim = dim3(kPcgThreads);
+	cfg.dynamicSmemBytes = h->pcgSmem;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeCooperative;  // all blocks co-resident (the grid barrier needs it)
+	attr[0].val.cooperative = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	GB_CUDA(h, cudaLaunchKernelEx(&cfg, k_pcg_persistent, a));
+	if (ev1) GB_CUDA(h, cudaEventRecord(ev1, st));
+	h->launches += 1;
+	return GBFEM_OK;
+}
+
+// Mixed-precision solve: one persistent launch, then its per-segment results are read back.
+gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, bool timeSolve)
+{
+	const int nseg = (int)h->segNode.size() - 1;
+	cudaStream_t st = h->stream;
 	static thread_local KernelTimer kt;
 	if (timeSolve && !kt.init()) return fail(h, GBFEM_CUDA_ERROR, "cudaEventCreate failed");
-	if (timeSolve) cudaEventRecord(kt.a[0], st);
-	void* args[] = {&a};
-	GB_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_pcg_persistent, dim3(h->pcgGrid), dim3(kPcgThreads), args,
-										   h->pcgSmem, st));
-	if (timeSolve) cudaEventRecord(kt.b[0], st);
-	h->launches += 1;
+	gbfem_status es = enqueue_mixed(h, b, x, maxIter, timeSolve ? kt.a[0] : nullptr, timeSolve ? kt.b[0] : nullptr);
+	if (es != GBFEM_OK) return es;
 	PcgGlobal g;
 	GB_CUDA(h, cudaMemcpyAsync(h->h_seg, h->d_seg.p, sizeof(SegCtl) * nseg, cudaMemcpyDeviceToHost, st));
 	GB_CUDA(h, cudaMemcpyAsync(&g, h->d_pcgGlobal.p, sizeof(PcgGlobal), cudaMemcpyDeviceToHost, st));
@@ -778,6 +828,200 @@ gbfem_status run_mixed(gbfem_handle h, const double* b, double* x, int maxIter, 
 		cudaEventElapsedTime(&ms, kt.a[0], kt.b[0]);
 		h->stats.ms_spmv += ms;  // the whole persistent solve: one launch
 		h->stats.spmv_timed += 1;
+	}
+	return GBFEM_OK;
+}
+
+// Reads the persistent solve's error flag after a synchronising point.
+gbfem_status check_pcg_error(gbfem_handle h)
+{
+	PcgGlobal g;
+	GB_CUDA(h, cudaMemcpy(&g, h->d_pcgGlobal.p, sizeof(PcgGlobal), cudaMemcpyDeviceToHost));
+	if (g.err)
+		return fail(h, GBFEM_CUDA_ERROR, g.err == 1 ? "persistent CG: grid barrier timed out"
+												  : "persistent CG: work share exceeded its shared-memory bound");
+	return GBFEM_OK;
+}
+
+// Autotuner of the mixed form, run on the first step's own system: times the element kernel at 32
+// and 64 elements per block, then the persistent solve for 2, 3 and 4 CTAs per SM and refresh
+// weights 4, 6 and 8, and keeps the fastest of each. The element kernel's results do not depend on
+// its block size; the solve's partition does change its rounding (not its convergence test), so a
+// run that must reproduce another bit for bit pins the choice with gbfem_set_tuning.
+gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, double dt, double c1, double c2,
+						int maxIter)
+{
+	const DevBody body = h->body();
+	cudaStream_t s = h->stream;
+	const double alpha = h->prm.rayleigh_mass, beta = h->prm.rayleigh_stiffness;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	GB_CUDA(h, cudaEventCreate(&e0));
+	GB_CUDA(h, cudaEventCreate(&e1));
+	auto elapsed = [&]() -> float {
+		float ms = 0.f;
+		cudaEventSynchronize(e1);
+		cudaEventElapsedTime(&ms, e0, e1);
+		return ms;
+	};
+	float bestE = 1e30f;
+	int eBest = 64;
+	for (int rep = 0; rep < 2; ++rep)
+		for (int ept : {32, 64})
+		{
+			cudaEventRecord(e0, s);
+			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
+							   h->d_counters.p, s, ept);
+			cudaEventRecord(e1, s);
+			const float t = elapsed();
+			if (rep == 1 && t < bestE)
+			{
+				bestE = t;
+				eBest = ept;
+			}
+		}
+	h->elemsPerBlock = eBest;
+	launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
+					   h->d_counters.p, s, eBest);
+	launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+	GB_CUDA(h, cudaGetLastError());
+	float bestS = 1e30f;
+	int cBest = h->ctasPerSM, rBest = h->refreshWeight;
+	for (int cps : {2, 3, 4})
+	{
+		if (configure_pcg(h, cps) != GBFEM_OK) continue;
+		for (int rw : {4, 6, 8})
+		{
+			h->refreshWeight = rw;
+			gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, e0, e1);
+			if (st != GBFEM_OK) return st;
+			const float t = elapsed();
+			st = check_pcg_error(h);
+			if (st != GBFEM_OK) return st;
+			if (t < bestS)
+			{
+				bestS = t;
+				cBest = cps;
+				rBest = rw;
+			}
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	gbfem_status st = configure_pcg(h, cBest);
+	if (st != GBFEM_OK) return st;
+	h->refreshWeight = rBest;
+	h->tuned = true;
+	h->tuneVersion++;
+	h->err.clear();
+	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));  // count the real step only
+	return GBFEM_OK;
+}
+
+// One mixed-form step (first Newton iteration) enqueued without host synchronisation, then the
+// per-segment statistics accumulated on the device: the body of the captured step graph.
+gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
+{
+	const DevBody body = h->body();
+	cudaStream_t s = h->stream;
+	const Launch L = h->launch();
+	const int nseg = (int)h->segNode.size() - 1;
+	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * h->n;
+	const double c1 = 1.0 / dt + h->prm.rayleigh_mass, c2 = dt + h->prm.rayleigh_stiffness;
+	launch_element_f32(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
+					   h->prm.rayleigh_stiffness, h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock);
+	launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+	gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timed ? h->graphEv[0] : nullptr,
+									timed ? h->graphEv[1] : nullptr);
+	if (st != GBFEM_OK) return st;
+	launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, h->d_x.p, h->d_x.p, h->d_v.p, dt, 0, h->d_ctl.p, h->d_part.p, L);
+	launch_validity(h->n, h->d_x.p, h->d_v.p, h->d_ctl.p, h->d_part.p, L);
+	launch_step_accumulate(h->d_seg.p, nseg, &h->d_ctl.p->nonfinite, &h->d_pcgGlobal.p->err, h->d_acc.p, s);
+	GB_CUDA(h, cudaGetLastError());
+	return GBFEM_OK;
+}
+
+// GBFEM_STEP_GRAPH: the step is captured once into a CUDA graph (per dt, timing flag and tuning)
+// and the graph is launched nsteps times with no host round trip between steps; statistics and the
+// finiteness check are accumulated on the device and read once at the end.
+gbfem_status step_graph(gbfem_handle h, double dt, int nsteps, uint32_t flags)
+{
+	if (!h->mixed() || h->prm.newton_max_iterations > 1 || (flags & GBFEM_STEP_KEEP_SYSTEM))
+		return fail(h, GBFEM_INVALID_ARG,
+					"GBFEM_STEP_GRAPH needs the mixed form, one Newton iteration and no GBFEM_STEP_KEEP_SYSTEM");
+	cudaStream_t s = h->stream;
+	const int nseg = (int)h->segNode.size() - 1;
+	const bool timed = (flags & GBFEM_STEP_TIME_KERNELS) != 0;
+	if (!h->graphExec || h->graphDt != dt || h->graphTimed != timed || h->graphVersion != h->tuneVersion)
+	{
+		if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
+		h->graphExec = nullptr;
+		if (timed && !h->graphEv[0])
+		{
+			GB_CUDA(h, cudaEventCreate(&h->graphEv[0]));
+			GB_CUDA(h, cudaEventCreate(&h->graphEv[1]));
+		}
+		GB_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		const int launchesBefore = h->launches;
+		gbfem_status st = enqueue_step_mixed(h, dt, timed);
+		h->launches = launchesBefore;
+		cudaGraph_t graph = nullptr;
+		const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+		if (st != GBFEM_OK)
+		{
+			if (graph) cudaGraphDestroy(graph);
+			return st;
+		}
+		GB_CUDA(h, ce);
+		const cudaError_t ie = cudaGraphInstantiate(&h->graphExec, graph, 0);
+		cudaGraphDestroy(graph);
+		GB_CUDA(h, ie);
+		h->graphDt = dt;
+		h->graphTimed = timed;
+		h->graphVersion = h->tuneVersion;
+	}
+	std::vector<double> acc(4 * (size_t)nseg + 2, 0.0);
+	for (int k = 0; k < nseg; ++k) acc[4 * (size_t)k + 2] = 1.0;
+	GB_CUDA(h, cudaMemcpyAsync(h->d_acc.p, acc.data(), sizeof(double) * acc.size(), cudaMemcpyHostToDevice, s));
+	GB_CUDA(h, cudaMemsetAsync(h->d_pcgGlobal.p, 0, sizeof(PcgGlobal), s));
+	for (int i = 0; i < nsteps; ++i)
+	{
+		GB_CUDA(h, cudaGraphLaunch(h->graphExec, s));
+		h->launches += 7;  // element, assembly, rhs, solve, state update, validity, accumulate
+		if (timed)
+		{
+			GB_CUDA(h, cudaStreamSynchronize(s));
+			float ms = 0.f;
+			cudaEventElapsedTime(&ms, h->graphEv[0], h->graphEv[1]);
+			h->stats.ms_spmv += ms;
+			h->stats.spmv_timed += 1;
+		}
+	}
+	GB_CUDA(h, cudaMemcpyAsync(acc.data(), h->d_acc.p, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, s));
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	GB_CUDA(h, cudaGetLastError());
+	double worst = 0.0;
+	for (int k = 0; k < nseg; ++k)
+	{
+		const double* a = &acc[4 * (size_t)k];
+		h->stats.cg_iterations += (int)a[0];
+		h->stats.refinement_sweeps += (int)a[1];
+		if (a[2] < 1.0) h->stats.cg_max_iterations_hit++;
+		worst = std::max(worst, a[3]);
+		double* ss = &h->segStats[4 * (size_t)k];
+		ss[0] += a[0];
+		ss[1] += a[1];
+		ss[2] = std::min(ss[2], a[2]);
+		ss[3] = std::max(ss[3], a[3]);
+	}
+	h->stats.cg_relative_residual = worst;
+	h->stats.steps += nsteps;
+	if (acc[4 * (size_t)nseg + 1] != 0.0) return fail(h, GBFEM_CUDA_ERROR, "persistent CG: grid barrier timed out");
+	if (acc[4 * (size_t)nseg] != 0.0)
+	{
+		h->active = false;  // FemRepresentation.cpp:285-293
+		return fail(h, GBFEM_NONFINITE, "state is not finite after a graph-launched step; representation deactivated");
 	}
 	return GBFEM_OK;
 }
@@ -823,8 +1067,13 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 		const bool timeK = (flags & GBFEM_STEP_TIME_KERNELS) != 0;
 		if (h->mixed())
 		{
+			if (h->prm.autotune && !h->tuned)
+			{
+				gbfem_status tst = tune_mixed(h, xt, vt, dt, c1, c2, maxIter);
+				if (tst != GBFEM_OK) return tst;
+			}
 			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
-							   h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s);
+							   h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock);
 			tm.mark(1);
 			launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 			launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
@@ -1063,6 +1312,32 @@ gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, co
 	return create_impl(meshes, count, params, out);
 }
 
+gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm, int32_t* refresh_weight)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (elems_per_block) *elems_per_block = h->elemsPerBlock;
+	if (ctas_per_sm) *ctas_per_sm = h->ctasPerSM;
+	if (refresh_weight) *refresh_weight = h->refreshWeight;
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t ctas_per_sm, int32_t refresh_weight)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (!h->mixed()) return fail(h, GBFEM_INVALID_ARG, "tuning applies to the mixed form");
+	if ((elems_per_block != 32 && elems_per_block != 64) || ctas_per_sm < 1 || ctas_per_sm > 4 || refresh_weight < 1 ||
+		refresh_weight > kRefreshWeightMax)
+		return fail(h, GBFEM_INVALID_ARG, "tuning: elems_per_block 32|64, ctas_per_sm 1..4, refresh_weight 1..8");
+	GB_CUDA(h, cudaSetDevice(h->device));
+	gbfem_status st = configure_pcg(h, ctas_per_sm);
+	if (st != GBFEM_OK) return st;
+	h->elemsPerBlock = elems_per_block;
+	h->refreshWeight = refresh_weight;
+	h->tuned = true;
+	h->tuneVersion++;
+	return GBFEM_OK;
+}
+
 gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, const double* poisson)
 {
 	if (!h || !young) return GBFEM_INVALID_ARG;
@@ -1199,10 +1474,23 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	GB_CUDA(h, cudaSetDevice(h->device));
 	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), h->stream));
 	gbfem_status result = GBFEM_OK;
-	for (int sidx = 0; sidx < nsteps; ++sidx)
+	int sidx = 0;
+	if ((flags & GBFEM_STEP_GRAPH) && h->prm.autotune && !h->tuned && nsteps > 0)
+	{
+		result = step_once(h, dt, flags & ~GBFEM_STEP_GRAPH);  // the first step tunes, outside any graph
+		sidx = 1;
+	}
+	if ((flags & GBFEM_STEP_GRAPH) && sidx < nsteps &&
+		!(result == GBFEM_NONFINITE || result == GBFEM_CUDA_ERROR || result == GBFEM_OUT_OF_MEMORY))
+	{
+		gbfem_status st = step_graph(h, dt, nsteps - sidx, flags);
+		if (st != GBFEM_OK) result = st;
+		sidx = nsteps;
+	}
+	for (; sidx < nsteps; ++sidx)
 	{
 		gbfem_status st = step_once(h, dt, flags);
-		if (st == GBFEM_NONFINITE || st == GBFEM_CUDA_ERROR || st == GBFEM_OUT_OF_MEMORY)
+		if (st == GBFEM_NONFINITE || st == GBFEM_CUDA_ERROR || st == GBFEM_OUT_OF_MEMORY || st == GBFEM_INVALID_ARG)
 		{
 			result = st;
 			break;

@@ -81,9 +81,10 @@ struct MatCsr
 void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
 						 double* fE, int* counters, cudaStream_t s);
+// elemsPerBlock: 32 or 64 (a tuning choice; results do not depend on it).
 void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
-						cudaStream_t s);
+						cudaStream_t s, int elemsPerBlock = 64);
 void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
 					 cudaStream_t s);
 void launch_assemble(const DevBody& b, const float* kslots, double c1, double c2, float* A, float* invdiag,

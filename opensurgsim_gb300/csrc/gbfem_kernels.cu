@@ -48,9 +48,11 @@ __global__ void __launch_bounds__(kElemThreads) k_element_fp64(DevBody b, const 
 	if (fl & 2) atomicAdd(&counters[0], 1);
 }
 
-// FP32 element kernel of the mixed form. Results are staged in shared memory and written out
-// with coalesced stores (element-major, the layout the assembly gathers).
-__global__ void __launch_bounds__(kElemThreads) k_element_f32(DevBody b, const double* __restrict__ xn,
+// FP32 element kernel of the mixed form, kT elements per block (a tuning choice). Results are
+// staged in shared memory and written out with coalesced stores (element-major, the layout the
+// assembly gathers).
+template <int kT>
+__global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __restrict__ xn,
 															   const double* __restrict__ vn,
 															   const double* __restrict__ xt,
 															   const double* __restrict__ vt, double dt, double alpha,
@@ -58,9 +60,9 @@ __global__ void __launch_bounds__(kElemThreads) k_element_f32(DevBody b, const d
 															   float* __restrict__ rhsE, int* counters)
 {
 	constexpr int kV = kSlots * 9;
-	__shared__ float sks[kV][kElemThreads + 1];
-	__shared__ float srhs[12][kElemThreads + 1];
-	const int e0 = blockIdx.x * kElemThreads;
+	__shared__ float sks[kV][kT + 1];
+	__shared__ float srhs[12][kT + 1];
+	const int e0 = blockIdx.x * kT;
 	const int e = e0 + threadIdx.x;
 	const int E = b.E;
 	if (e < E)
@@ -73,21 +75,21 @@ __global__ void __launch_bounds__(kElemThreads) k_element_f32(DevBody b, const d
 #pragma unroll
 			for (int k = 0; k < 3; ++k) g[a][k] = b.rest32[(3 * a + k) * E + e];
 		const float lamV = b.rest32[13 * E + e], muV = b.rest32[14 * E + e], cm = b.rest32[15 * E + e];
-		const int fl = elem::compute<float, false>(in, g, lamV, muV, cm, &sks[0][threadIdx.x], kElemThreads + 1,
-												   &srhs[0][threadIdx.x], kElemThreads + 1, nullptr, nullptr);
+		const int fl = elem::compute<float, false>(in, g, lamV, muV, cm, &sks[0][threadIdx.x], kT + 1,
+												   &srhs[0][threadIdx.x], kT + 1, nullptr, nullptr);
 		if (fl & 1) atomicAdd(&counters[1], 1);
 		if (fl & 2) atomicAdd(&counters[0], 1);
 	}
 	__syncthreads();
-	const int cnt = min(kElemThreads, E - e0);
+	const int cnt = min(kT, E - e0);
 	float* dstK = kslots + (size_t)e0 * kV;
-	for (int idx = threadIdx.x; idx < cnt * kV; idx += kElemThreads)
+	for (int idx = threadIdx.x; idx < cnt * kV; idx += kT)
 	{
 		const int el = idx / kV;
 		dstK[idx] = sks[idx - el * kV][el];
 	}
 	float* dstR = rhsE + (size_t)e0 * 12;
-	for (int idx = threadIdx.x; idx < cnt * 12; idx += kElemThreads)
+	for (int idx = threadIdx.x; idx < cnt * 12; idx += kT)
 	{
 		const int el = idx / 12;
 		dstR[idx] = srhs[idx - el * 12][el];
@@ -523,11 +525,13 @@ void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, c
 
 void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
-						cudaStream_t s)
+						cudaStream_t s, int elemsPerBlock)
 {
 	if (b.E == 0) return;
-	k_element_f32<<<blocks(b.E, kElemThreads), kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
-																	  counters);
+	if (elemsPerBlock == 32)
+		k_element_f32<32><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE, counters);
+	else
+		k_element_f32<64><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE, counters);
 }
 
 void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,

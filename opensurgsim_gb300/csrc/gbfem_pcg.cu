@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	actC.Wp = nullptr;
 	// Rebuild the active-set prefixes and this CTA's ranges (segments stamped before phase ph are
 	// out). In phase 1 a segment switched to its FP64 residual in the phase before weighs
-	// kRefreshWeight times its block columns. Returns whether any segment was so weighted.
+	// refreshWeight times its block columns. Returns whether any segment was so weighted.
 	__shared__ int shWeighted;
 	auto rebuild = [&](bool phase1) {
 		if (warp == 0)
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 						w = __ldg(&a.cumW[sc[s + 1]]) - __ldg(&a.cumW[sc[s]]);
 						if (phase1 && ldi(&a.seg[s].refreshAt) == ph - 1)
 						{
-							w *= kRefreshWeight;
+							w *= a.refreshWeight;
 							weighted = 1;
 						}
 					}
@@ -737,6 +737,35 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 #pragma unroll
 		for (int k = 0; k < 3; ++k) a.x[3 * I + k] = a.x64[3 * rs + k] + double(a.xd[3 * rs + k]);
 	});
+}
+
+namespace {
+
+__global__ void k_step_accumulate(const SegCtl* __restrict__ seg, int nseg, const int* __restrict__ ctlNonfinite,
+								  const int* __restrict__ pcgErr, double* __restrict__ acc)
+{
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nseg; k += gridDim.x * blockDim.x)
+	{
+		const SegCtl& c = seg[k];
+		const double res = c.bb > 0 ? sqrt(c.rrTrue / c.bb) : 0.0;
+		acc[4 * k] += c.iter;
+		acc[4 * k + 1] += c.updates;
+		acc[4 * k + 2] = fmin(acc[4 * k + 2], (double)c.converged);
+		acc[4 * k + 3] = fmax(acc[4 * k + 3], res);
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0)
+	{
+		if (*ctlNonfinite) acc[4 * nseg] = 1.0;
+		if (*pcgErr) acc[4 * nseg + 1] = 1.0;
+	}
+}
+
+}  // namespace
+
+void launch_step_accumulate(const SegCtl* seg, int nseg, const int* ctlNonfinite, const int* pcgErr, double* acc,
+							cudaStream_t s)
+{
+	k_step_accumulate<<<(nseg + 127) / 128, 128, 0, s>>>(seg, nseg, ctlNonfinite, pcgErr, acc);
 }
 
 }  // namespace gbfem

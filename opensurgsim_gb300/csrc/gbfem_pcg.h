@@ -40,12 +40,15 @@ struct PcgGlobal
 	int refreshIn[2];    // segments switched to an FP64 residual in a phase, by phase parity
 };
 
-// Weight of a chunk of a segment doing its FP64 residual (phase 1), relative to an FP32 SpMV chunk.
-constexpr int kRefreshWeight = 6;
+// Weight of a chunk of a segment doing its FP64 residual (phase 1), relative to an FP32 SpMV chunk:
+// a tuning choice (PcgArgs::refreshWeight), at most kRefreshWeightMax.
+constexpr int kRefreshWeightDefault = 6;
+constexpr int kRefreshWeightMax = 8;
 
 struct PcgArgs
 {
 	int nchunks, nsegs, maxIter, maxChunksPerCta;
+	int refreshWeight, pad;
 	double tol, drop;
 	// SELL-32 matrix in row space (column = neighbour row position), FP32 values
 	const int* off;        // nchunks + 1
@@ -80,5 +83,12 @@ inline size_t pcg_smem_bytes(int nsegs, int maxChunksPerCta)
 }
 
 __global__ void k_pcg_persistent(PcgArgs a);
+
+// Per-step statistics kept on the device (graph-launched steps): acc[4*s + 0/1/2/3] += iterations,
+// += refreshes, min= converged, max= relative residual of segment s; acc[4*nseg] = 1 once a step's
+// state was not finite (ctlNonfinite points at the validity kernel's flag), acc[4*nseg + 1] = 1 once
+// a solve reported an error (pcgErr).
+void launch_step_accumulate(const SegCtl* seg, int nseg, const int* ctlNonfinite, const int* pcgErr, double* acc,
+							cudaStream_t s);
 
 }  // namespace gbfem

@@ -1,0 +1,91 @@
+"""Batched form on the GPU: steps launched as a CUDA graph and the autotuner."""
+
+import numpy as np
+import pytest
+
+from opensurgsim_gb300 import _lib, mesh
+
+pytestmark = pytest.mark.gpu
+
+DIMS = [(2, 2, 3, 1e4), (4, 3, 2, 1e5), (1, 1, 1, 3e5), (5, 5, 6, 1e6), (3, 6, 2, 2e4)]
+
+
+def _batch(**kw):
+    from opensurgsim_gb300.body import Body
+
+    scenes = [mesh.scene_cube(a, b, c, seed=k, young=float(E)) for k, (a, b, c, E) in enumerate(DIMS)]
+    b = Body([s.mesh for s in scenes], rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0, 0, -9.81),
+             cg_tolerance=1e-10, precision=_lib.PRECISION_MIXED, **kw)
+    v0 = np.random.default_rng(3).normal(0, 0.01, b.n)
+    b.set_state(None, v0)
+    return scenes, b
+
+
+def test_graph_steps_equal_regular_steps_bit_for_bit(gpu_lib):
+    _, a = _batch()
+    _, g = _batch()
+    g.set_tuning(*a.tuning())
+    assert a.step(1e-3, 6) == _lib.GBFEM_OK
+    assert g.step(1e-3, 2, _lib.STEP_GRAPH) == _lib.GBFEM_OK   # captures the graph
+    assert g.step(1e-3, 4, _lib.STEP_GRAPH) == _lib.GBFEM_OK   # relaunches it
+    xa, va = a.state()
+    xg, vg = g.state()
+    assert np.array_equal(xa, xg) and np.array_equal(va, vg)
+    sg = g.segment_stats()
+    assert np.all(sg["converged"] == 1) and np.all(sg["iterations"] > 0)
+    assert g.stats()["kernel_launches"] == 4 * 7
+
+
+def test_graph_is_recaptured_when_dt_changes(gpu_lib):
+    _, a = _batch()
+    _, g = _batch()
+    g.set_tuning(*a.tuning())
+    for dt in (1e-3, 5e-4, 1e-3):
+        assert a.step(dt, 2) == _lib.GBFEM_OK
+        assert g.step(dt, 2, _lib.STEP_GRAPH) == _lib.GBFEM_OK
+    assert np.array_equal(a.state()[0], g.state()[0])
+
+
+def test_graph_step_reports_a_nonfinite_state(gpu_lib):
+    _, g = _batch()
+    x, v = g.state()
+    v[7] = np.nan
+    g.set_state(None, v)
+    assert g.step(1e-3, 3, _lib.STEP_GRAPH) == _lib.GBFEM_NONFINITE
+    assert g.step(1e-3, 1, _lib.STEP_GRAPH) == _lib.GBFEM_INACTIVE
+
+
+def test_autotune_picks_a_candidate_and_pinning_reproduces_it(gpu_lib):
+    scenes, t = _batch(autotune=True)
+    _, ref = _batch()
+    assert t.step(1e-3, 3) == _lib.GBFEM_OK
+    assert ref.step(1e-3, 3) == _lib.GBFEM_OK
+    e, c, r = t.tuning()
+    assert e in (32, 64) and c in (2, 3, 4) and r in (4, 6, 8)
+    xt, _ = t.state()
+    xr, _ = ref.state()
+    for k, s in enumerate(scenes):
+        n0, n1 = t.node_offsets[k], t.node_offsets[k + 1]
+        x0 = s.mesh.nodes.ravel()
+        d = xr[3 * n0:3 * n1] - x0
+        assert np.linalg.norm(xt[3 * n0:3 * n1] - x0 - d) <= 1e-6 * np.linalg.norm(d)
+    # A second body pinned to the tuned choice repeats the tuned run bit for bit.
+    _, p = _batch()
+    p.set_tuning(e, c, r)
+    assert p.step(1e-3, 3) == _lib.GBFEM_OK
+    assert np.array_equal(p.state()[0], xt)
+
+
+def test_autotune_with_graph_steps(gpu_lib):
+    _, t = _batch(autotune=True)
+    assert t.step(1e-3, 4, _lib.STEP_GRAPH) == _lib.GBFEM_OK
+    assert t.stats()["steps"] == 4
+    assert np.all(t.segment_stats()["converged"] == 1)
+
+
+def test_set_tuning_rejects_bad_values(gpu_lib):
+    _, b = _batch()
+    with pytest.raises(_lib.GbfemError):
+        b.set_tuning(48, 2, 6)
+    with pytest.raises(_lib.GbfemError):
+        b.set_tuning(64, 5, 6)
