@@ -185,11 +185,10 @@ def batch_scenes(count=BATCH["count"]):
     return mesh.scenes_batch(**dict(BATCH, count=count))
 
 
-def batch_body(meshes, precision, device):
-    from opensurgsim_gb300 import _lib
+def batch_body(meshes, precision, device, autotune=False):
     from opensurgsim_gb300.body import Body
 
-    return Body(meshes, precision=precision, device=device, **BATCH_PARAMS)
+    return Body(meshes, precision=precision, device=device, autotune=autotune, **BATCH_PARAMS)
 
 
 def rel_disp_err(x_mixed, x64, rest):
@@ -264,12 +263,15 @@ def run_batch(args, rank, world, local, dist):
     tets = sum(m.num_tets for m in meshes)
     nodes = sum(m.num_nodes for m in meshes)
     log(f"batch: rank {rank}/{world} steps {len(meshes)} of {len(all_scenes)} meshes, {tets} tets, {nodes} nodes")
-    body = batch_body(meshes, _lib.PRECISION_MIXED, local)
+    body = batch_body(meshes, _lib.PRECISION_MIXED, local, autotune=True)
     stream = torch.cuda.ExternalStream(body.stream(), device=local)
-    flags = _lib.STEP_TIME_KERNELS
+    # Steps run as a captured CUDA graph; the first warm-up step autotunes (outside the graph).
+    flags = _lib.STEP_TIME_KERNELS | _lib.STEP_GRAPH
     for _ in range(args.warmup):
         body.step(1e-3, 1, flags)
     torch.cuda.synchronize(local)
+    tuning = body.tuning()
+    log(f"tuning: {tuning[0]} elements per block, {tuning[1]} CTAs per SM, refresh weight {tuning[2]}")
     dist.barrier()
     sampler = ClockSampler(local)
     sampler.start()
@@ -282,17 +284,15 @@ def run_batch(args, rank, world, local, dist):
     it_bytes = np.array([bytes_per_iteration(int(z), int(N), 4) for z, N in zip(nnz, nn)], dtype=np.float64)
     rf_bytes = np.array([bytes_per_refresh(int(z), int(N), 4) for z, N in zip(nnz, nn)], dtype=np.float64)
     io_bytes = float(np.sum(16 * 3 * nn))  # b in, x out (FP64)
-    iters_total = 0
     ev0.record(stream)
-    for _ in range(args.steps):
-        statuses.append(body.step(1e-3, 1, flags))
-        s = body.stats()
-        launches += s["kernel_launches"]
-        solve_ms += s["ms_spmv"]
-        ss = body.segment_stats()
-        alg_bytes += float(np.dot(ss["iterations"], it_bytes) + np.dot(ss["refreshes"], rf_bytes)) + io_bytes
-        iters_total += int(ss["iterations"].max())
+    statuses.append(body.step(1e-3, args.steps, flags))
     ev1.record(stream)
+    s = body.stats()
+    launches = s["kernel_launches"]
+    solve_ms = s["ms_spmv"]
+    ss = body.segment_stats()  # summed over the call's steps
+    alg_bytes = float(np.dot(ss["iterations"], it_bytes) + np.dot(ss["refreshes"], rf_bytes)) + io_bytes * args.steps
+    iters_total = int(ss["iterations"].max())
     torch.cuda.synchronize(local)
     clocks = sampler.stop()
     dist.barrier()
@@ -312,7 +312,7 @@ def run_batch(args, rank, world, local, dist):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         body_lib.gbfem_set_state(body.handle, _lib.dptr(h_x), _lib.dptr(h_v))
-        body.step(1e-3, 1, 0)
+        body.step(1e-3, 1, _lib.STEP_GRAPH)
         body_lib.gbfem_get_state(body.handle, _lib.dptr(h_x), _lib.dptr(h_v))
     torch.cuda.synchronize(local)
     e2e_s = dist.reduce(time.perf_counter() - t0, "max")
@@ -342,14 +342,16 @@ def run_batch(args, rank, world, local, dist):
                          f"nodes log-U[500,50000], seed 3), {total_tets} tets, {total_nodes} nodes, E log-U[1e4,1e6] "
                          "per mesh, nu 0.45, bottom faces fixed, "
                          "gravity, alpha 0.01, beta 0.001, dt 1e-3, CG tol 1e-10; batched mixed precision, one "
-                         "persistent solve launch per step"),
+                         "persistent solve launch per step, steps launched as a CUDA graph"),
+            "tuning": {"elements_per_block": tuning[0], "ctas_per_sm": tuning[1], "refresh_weight": tuning[2],
+                       "how": "autotuned on the first warm-up step"},
             "meshes": len(all_scenes), "tets": total_tets, "nodes": total_nodes, "precision": "mixed",
             "l2": "working set (~2 GB) larger than L2: no flush needed",
             "parallelism": (f"meshes sharded over {world} ranks by greedy bin-packing (opensurgsim_gb300.shard), "
                             "no data-path collective" if world > 1 else "one GPU, all meshes in one batch"),
         },
         "gpu_launches": int(launches),
-        "cg_iterations_per_step": iters_total / max(1, args.steps),
+        "cg_iterations_per_step": iters_total / max(1, args.steps),  # the slowest mesh
         "step_status": sorted(set(int(s) for s in statuses)),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * body.n * 8,
@@ -394,7 +396,7 @@ def run_single(args, rank, world, local, dist):
     m = scene.mesh
     log(f"scene {scene.name}: {m.num_tets} tets, {m.num_nodes} nodes")
     prec = _lib.PRECISION_MIXED if args.precision == "mixed" else _lib.PRECISION_FP64
-    body = Body.from_scene(scene, precision=prec, device=local)
+    body = Body.from_scene(scene, precision=prec, device=local, autotune=(prec == _lib.PRECISION_MIXED))
     stream = torch.cuda.ExternalStream(body.stream(), device=local)
     dt = scene.dt
     driven = scene.driven_dofs is not None
@@ -409,7 +411,10 @@ def run_single(args, rank, world, local, dist):
             vals = ramp if step < scene.ramp_steps else hold
             body_lib.gbfem_set_velocities_device(body.handle, d_dofs.numel(), d_dofs.data_ptr(), vals.data_ptr())
 
-    flags = _lib.STEP_TIME_KERNELS
+    # The mixed form's steps run as a captured CUDA graph (the prescribed velocities are written into
+    # the state between graph launches); the first warm-up step autotunes.
+    graph = _lib.STEP_GRAPH if prec == _lib.PRECISION_MIXED else 0
+    flags = _lib.STEP_TIME_KERNELS | graph
     step = 0
     for _ in range(args.warmup):
         set_driven(step)
@@ -455,7 +460,7 @@ def run_single(args, rank, world, local, dist):
         if driven:
             h_vals.numpy()[:] = scene.driven_values(step)
             body.set_velocities(h_dofs.numpy(), h_vals.numpy())
-        body.step(dt, 1, 0)
+        body.step(dt, 1, graph)
         body_lib.gbfem_get_state(body.handle, _lib.dptr(h_x), _lib.dptr(h_v))
         step += 1
     torch.cuda.synchronize(local)

@@ -753,7 +753,10 @@ gbfem_status run_cg(gbfem_handle h, const double* b, double* x, int maxIter, boo
 // Mixed-precision solve: FP32 CG iterations with reliable FP64 residual refreshes; the host polls
 // the device control block between chunks of iterations.
 // Enqueue one persistent solve on the handle's stream (no host synchronisation; capturable).
-gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIter, cudaEvent_t ev0, cudaEvent_t ev1)
+// ev0/ev1 (optional) bracket the solve; inside a stream capture they are recorded as external event
+// nodes (a plain record there would only become a dependency edge and never record the event).
+gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIter, cudaEvent_t ev0, cudaEvent_t ev1,
+						   bool capturing = false)
 {
 	const int nseg = (int)h->segNode.size() - 1;
 	cudaStream_t st = h->stream;
@@ -789,7 +792,8 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	a.pad = 0;
 	a.seg = h->d_seg.p;
 	a.g = h->d_pcgGlobal.p;
-	if (ev0) GB_CUDA(h, cudaEventRecord(ev0, st));
+	const unsigned evFlags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+	if (ev0) GB_CUDA(h, cudaEventRecordWithFlags(ev0, st, evFlags));
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(h->pcgGrid);
 	cfg.blockDim = dim3(kPcgThreads);
@@ -801,7 +805,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
 	GB_CUDA(h, cudaLaunchKernelEx(&cfg, k_pcg_persistent, a));
-	if (ev1) GB_CUDA(h, cudaEventRecord(ev1, st));
+	if (ev1) GB_CUDA(h, cudaEventRecordWithFlags(ev1, st, evFlags));
 	h->launches += 1;
 	return GBFEM_OK;
 }
@@ -857,22 +861,23 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
 	GB_CUDA(h, cudaEventCreate(&e0));
 	GB_CUDA(h, cudaEventCreate(&e1));
-	auto elapsed = [&]() -> float {
-		float ms = 0.f;
-		cudaEventSynchronize(e1);
-		cudaEventElapsedTime(&ms, e0, e1);
-		return ms;
+	float t = 0.f;
+	auto elapsed = [&]() -> cudaError_t {
+		cudaError_t e = cudaEventSynchronize(e1);
+		if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+		return e;
 	};
 	float bestE = 1e30f;
 	int eBest = 64;
 	for (int rep = 0; rep < 2; ++rep)
 		for (int ept : {32, 64})
 		{
-			cudaEventRecord(e0, s);
+			GB_CUDA(h, cudaEventRecord(e0, s));
 			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
 							   h->d_counters.p, s, ept);
-			cudaEventRecord(e1, s);
-			const float t = elapsed();
+			GB_CUDA(h, cudaGetLastError());
+			GB_CUDA(h, cudaEventRecord(e1, s));
+			GB_CUDA(h, elapsed());
 			if (rep == 1 && t < bestE)
 			{
 				bestE = t;
@@ -889,13 +894,17 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 	int cBest = h->ctasPerSM, rBest = h->refreshWeight;
 	for (int cps : {2, 3, 4})
 	{
-		if (configure_pcg(h, cps) != GBFEM_OK) continue;
+		if (configure_pcg(h, cps) != GBFEM_OK)
+		{
+			(void)cudaGetLastError();  // an infeasible candidate is skipped; clear any error it left
+			continue;
+		}
 		for (int rw : {4, 6, 8})
 		{
 			h->refreshWeight = rw;
 			gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, e0, e1);
 			if (st != GBFEM_OK) return st;
-			const float t = elapsed();
+			GB_CUDA(h, elapsed());
 			st = check_pcg_error(h);
 			if (st != GBFEM_OK) return st;
 			if (t < bestS)
@@ -933,7 +942,7 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 	gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timed ? h->graphEv[0] : nullptr,
-									timed ? h->graphEv[1] : nullptr);
+									timed ? h->graphEv[1] : nullptr, /*capturing=*/true);
 	if (st != GBFEM_OK) return st;
 	launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, h->d_x.p, h->d_x.p, h->d_v.p, dt, 0, h->d_ctl.p, h->d_part.p, L);
 	launch_validity(h->n, h->d_x.p, h->d_v.p, h->d_ctl.p, h->d_part.p, L);
@@ -993,7 +1002,7 @@ gbfem_status step_graph(gbfem_handle h, double dt, int nsteps, uint32_t flags)
 		{
 			GB_CUDA(h, cudaStreamSynchronize(s));
 			float ms = 0.f;
-			cudaEventElapsedTime(&ms, h->graphEv[0], h->graphEv[1]);
+			GB_CUDA(h, cudaEventElapsedTime(&ms, h->graphEv[0], h->graphEv[1]));
 			h->stats.ms_spmv += ms;
 			h->stats.spmv_timed += 1;
 		}

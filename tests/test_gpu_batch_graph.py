@@ -89,3 +89,14 @@ def test_set_tuning_rejects_bad_values(gpu_lib):
         b.set_tuning(48, 2, 6)
     with pytest.raises(_lib.GbfemError):
         b.set_tuning(64, 5, 6)
+
+
+def test_timed_graph_steps_report_the_solve_time(gpu_lib):
+    _, a = _batch()
+    _, g = _batch()
+    g.set_tuning(*a.tuning())
+    assert a.step(1e-3, 3) == _lib.GBFEM_OK
+    assert g.step(1e-3, 3, _lib.STEP_GRAPH | _lib.STEP_TIME_KERNELS) == _lib.GBFEM_OK
+    st = g.stats()
+    assert st["spmv_timed"] == 3 and st["ms_spmv"] > 0.0
+    assert np.array_equal(a.state()[0], g.state()[0])
