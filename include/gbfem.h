@@ -85,7 +85,8 @@ typedef struct gbfem_params
 	int32_t precision;              /* gbfem_precision */
 	int32_t device;                 /* CUDA device ordinal */
 	int32_t autotune;               /* mixed form: tune block sizes and the solve schedule on the first step */
-	int32_t reserved[6];
+	int32_t element_type;           /* GBFEM_ELEMENT_COROTATIONAL_TET (default) or GBFEM_ELEMENT_LINEAR_TET */
+	int32_t reserved[5];
 } gbfem_params;
 
 /* Per-call statistics of the last gbfem_step. */
@@ -106,6 +107,18 @@ typedef struct gbfem_stats
 	double ms_spmv;                 /* summed device time of those launches (CUDA events) */
 	double reserved[2];
 } gbfem_stats;
+
+/* Element types (gbfem_params.element_type).
+ *  COROTATIONAL_TET: Fem3DElementCorotationalTetrahedron (Fem3DElementCorotationalTetrahedron.cpp:77-288)
+ *                    stepped by OdeSolverEulerImplicit.
+ *  LINEAR_TET:       Fem3DElementTetrahedron (Fem3DElementTetrahedron.cpp:77-90: K_e = K0,
+ *                    f_e = -K0 (x - x0)) stepped by OdeSolverLinearEulerImplicit
+ *                    (OdeSolverLinearEulerImplicit.cpp:43-64): the first step assembles and solves the
+ *                    full system; later steps (same dt and materials) update only the right-hand side
+ *                    and solve with the stored system matrix. The dense compliance matrix the reference
+ *                    forms on the first step is not formed (every solve is a CG solve). */
+#define GBFEM_ELEMENT_COROTATIONAL_TET 0
+#define GBFEM_ELEMENT_LINEAR_TET 1
 
 /* Flags for gbfem_step. */
 #define GBFEM_STEP_TIME_PHASES 1u   /* record per-phase device times (adds events) */
@@ -170,7 +183,7 @@ GBFEM_API gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* 
  * device arrays of n (state) or num_tets (gradients) doubles. Rebuilds the step's system at (x, v)
  * and solves it transposed with the handle's CG (the FP64 or the mixed solver); the element
  * derivatives are FP64. Does not change the handle's state. Returns GBFEM_CG_MAXITER if the
- * transposed solve did not converge (the outputs are still written). With GBFEM_STEP_TIME_PHASES in
+ * transposed solve did not converge (the outputs are still written). Corotational elements only. With GBFEM_STEP_TIME_PHASES in
  * flags the call adds its device times to the stats: ms_element (system rebuild), ms_solve
  * (transposed solve), ms_update (element derivatives and the node gather). */
 GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,

@@ -25,6 +25,9 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "DEGENERATE_ELEMENT", 3: "CG_MAXIT
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
+ELEMENT_COROTATIONAL_TET = 0
+ELEMENT_LINEAR_TET = 1
+
 STEP_TIME_PHASES = 1
 STEP_KEEP_SYSTEM = 2
 STEP_TIME_KERNELS = 4
@@ -69,7 +72,8 @@ class Params(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("device", ctypes.c_int32),
         ("autotune", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("element_type", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
 

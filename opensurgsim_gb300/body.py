@@ -21,7 +21,7 @@ class Body:
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5,
                  cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0,
-                 autotune=False):
+                 autotune=False, element_type=_lib.ELEMENT_COROTATIONAL_TET):
         """`mesh` is one TetMesh, or a list of them for a batch (mixed precision only)."""
         L = _lib.load()
         meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
@@ -57,6 +57,7 @@ class Body:
         p.precision = precision
         p.device = device
         p.autotune = 1 if autotune else 0
+        p.element_type = element_type
         self.params = p
         h = ctypes.c_void_p()
         if len(meshes) == 1 and not isinstance(mesh, (list, tuple)):

@@ -298,8 +298,11 @@ __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __
 //   implicit-Euler right-hand side, OdeSolverEulerImplicit.cpp:155-158, with the Rayleigh
 //   damping force of FemRepresentation.cpp:565-629 folded in).
 // Debug outputs (double only): kfull[144] the full tangent, fdbg[12] = f_e - alpha M0 v - beta K_e v.
+// ks may be null (right-hand side only). kLinear: the linear tetrahedron of
+// Fem3DElementTetrahedron::doUpdateFMDK (Fem3DElementTetrahedron.cpp:77-90): R = I, K_e = K0,
+// f_e = -K0 (x - x0), no rotation terms.
 // Returns a bitmask: 1 = polar fallback to the FP64 SVD, 2 = singular G (extra terms skipped).
-template <typename T, bool kDebug, typename In = ElemIn>
+template <typename T, bool kDebug, typename In = ElemIn, bool kLinear = false>
 __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV, T cm, T* ks, int ksStride, T* rhs,
 					   int rhsStride, double* kfull, double* fdbg)
 {
@@ -312,7 +315,12 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 		for (int j = 0; j < 3; ++j)
 			F[3 * i + j] = T(in.p[1][i]) * g[1][j] + T(in.p[2][i]) * g[2][j] + T(in.p[3][i]) * g[3][j];
 	T R[9];
-	if (!polar_newton(F, R))
+	if constexpr (kLinear)
+	{
+#pragma unroll
+		for (int k = 0; k < 9; ++k) R[k] = (k % 4 == 0) ? T(1) : T(0);
+	}
+	else if (!polar_newton(F, R))
 	{
 		// Near-inverted or degenerate element: SVD path (the reference's computeRotationScaling),
 		// always at least FP64.
@@ -357,7 +365,8 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			Gm[3 * i + j] = s;
 		}
 	T Gi[9];
-	bool extra;
+	bool extra = false;
+	if constexpr (!kLinear)
 	{
 		T C[9];
 		cofactor3(Gm, C);
@@ -372,7 +381,19 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 	}
 	// Corotated strain displacement w_c = R^T p_c - q_c and u~_c = R^T uK_c - w_c.
 	T w[4][3], ut[4][3], wt[4][3];
-	if constexpr (!std::is_same<T, float>::value)
+	if constexpr (kLinear)
+	{
+		// u = x - x0 relative to node 0 (K0 annihilates translations), formed in the input precision.
+#pragma unroll
+		for (int a = 0; a < 4; ++a)
+#pragma unroll
+			for (int i = 0; i < 3; ++i)
+			{
+				w[a][i] = T(in.p[a][i] - in.q[a][i]);
+				ut[a][i] = T(in.uK[a][i]) - w[a][i];
+			}
+	}
+	else if constexpr (!std::is_same<T, float>::value)
 	{
 #pragma unroll
 		for (int a = 0; a < 4; ++a)
@@ -550,7 +571,7 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 #pragma unroll
 		for (int bb = 0; bb < 4; ++bb)
 		{
-			const bool store = (a == bb) || (in.nd[a] > in.nd[bb]);
+			const bool store = ((a == bb) || (in.nd[a] > in.nd[bb])) && ks != nullptr;
 			if (!store && !kDebug) continue;
 			T blk[9];
 #pragma unroll

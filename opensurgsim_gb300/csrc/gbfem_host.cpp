@@ -147,6 +147,11 @@ struct gbfem_handle_s
 	std::vector<double> segStats;  // per segment over the last gbfem_step: iterations, refreshes, converged, residual
 	int nrows = 0, nchunks = 0;
 	bool mixed() const { return prm.precision == GBFEM_PRECISION_MIXED; }
+	bool linear() const { return prm.element_type == GBFEM_ELEMENT_LINEAR_TET; }
+	// Linear elements: the system matrix assembled for linearDt stays valid until dt or a material
+	// changes (OdeSolverLinearEulerImplicit keeps its first step's system).
+	bool linearReady = false;
+	double linearDt = 0.0;
 	DevBuf<int> d_counters;
 	DevBuf<CgCtl> d_ctl;
 	CgCtl* h_ctl = nullptr;
@@ -874,7 +879,7 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 		{
 			GB_CUDA(h, cudaEventRecord(e0, s));
 			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
-							   h->d_counters.p, s, ept);
+							   h->d_counters.p, s, ept, h->linear());
 			GB_CUDA(h, cudaGetLastError());
 			GB_CUDA(h, cudaEventRecord(e1, s));
 			GB_CUDA(h, elapsed());
@@ -886,7 +891,7 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 		}
 	h->elemsPerBlock = eBest;
 	launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
-					   h->d_counters.p, s, eBest);
+					   h->d_counters.p, s, eBest, h->linear());
 	launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 	GB_CUDA(h, cudaGetLastError());
@@ -937,9 +942,11 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	const int nseg = (int)h->segNode.size() - 1;
 	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * h->n;
 	const double c1 = 1.0 / dt + h->prm.rayleigh_mass, c2 = dt + h->prm.rayleigh_stiffness;
+	const bool reuse = h->linear() && h->linearReady && h->linearDt == dt;
 	launch_element_f32(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
-					   h->prm.rayleigh_stiffness, h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock);
-	launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+					   h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s,
+					   h->elemsPerBlock, h->linear());
+	if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 	gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timed ? h->graphEv[0] : nullptr,
 									timed ? h->graphEv[1] : nullptr, /*capturing=*/true);
@@ -1081,14 +1088,22 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 				gbfem_status tst = tune_mixed(h, xt, vt, dt, c1, c2, maxIter);
 				if (tst != GBFEM_OK) return tst;
 			}
+			const bool reuse = h->linear() && h->linearReady && h->linearDt == dt;
 			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
-							   h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock);
+							   reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock,
+							   h->linear());
 			tm.mark(1);
-			launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+			if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+			if (h->linear() && !reuse)
+			{
+				h->linearReady = true;
+				h->linearDt = dt;
+				h->tuneVersion++;  // a captured step graph must be rebuilt (right-hand side only from now on)
+			}
 			launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 			tm.mark(2);
 			GB_CUDA(h, cudaGetLastError());
-			h->launches += 3;
+			h->launches += reuse ? 2 : 3;
 			gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
@@ -1111,11 +1126,18 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 		}
 		else
 		{
+			const bool reuse = h->linear() && h->linearReady && h->linearDt == dt && !keep;
 			launch_element_fp64(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
-								h->prm.rayleigh_stiffness, h->d_kslots.p, h->d_rhsE.p, keep ? h->d_kfull.p : nullptr,
-								keep ? h->d_fE.p : nullptr, h->d_counters.p, s);
+								h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots.p, h->d_rhsE.p,
+								keep ? h->d_kfull.p : nullptr, keep ? h->d_fE.p : nullptr, h->d_counters.p, s,
+								h->linear());
 			tm.mark(1);
-			launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			if (!reuse) launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			if (h->linear() && !reuse)
+			{
+				h->linearReady = true;
+				h->linearDt = dt;
+			}
 			launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 			if (keep)
 			{
@@ -1125,7 +1147,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 			}
 			tm.mark(2);
 			GB_CUDA(h, cudaGetLastError());
-			h->launches += keep ? 5 : 3;
+			h->launches += keep ? 5 : (reuse ? 2 : 3);
 			gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
@@ -1234,7 +1256,7 @@ gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbf
 		if (st != GBFEM_OK) return st;
 	}
 	if (!(prm->newton_max_iterations >= 1) || !(prm->newton_epsilon >= 0.0) || !(prm->cg_tolerance >= 0.0) ||
-		prm->precision < 0 || prm->precision > 1)
+		prm->precision < 0 || prm->precision > 1 || prm->element_type < 0 || prm->element_type > 1)
 		return fail(nullptr, GBFEM_INVALID_ARG, "invalid solver parameters");
 	if (count > 1 && prm->precision != GBFEM_PRECISION_MIXED)
 		return fail(nullptr, GBFEM_INVALID_ARG, "a batch of meshes is stepped in the mixed-precision form");
@@ -1351,6 +1373,7 @@ gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, con
 {
 	if (!h || !young) return GBFEM_INVALID_ARG;
 	launch_set_materials(h->E, young, poisson, h->d_rest.p, h->mixed() ? h->d_rest32.p : nullptr, h->stream);
+	h->linearReady = false;  // the stored linear system no longer matches
 	GB_CUDA(h, cudaGetLastError());
 	GB_CUDA(h, cudaStreamSynchronize(h->stream));
 	return GBFEM_OK;
@@ -1363,6 +1386,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	if (!h) return GBFEM_INVALID_ARG;
 	if (!x || !v || !dv || !lx || !lv || !lx_out || !lv_out || !(dt > 0.0))
 		return fail(h, GBFEM_INVALID_ARG, "gbfem_adjoint_step: null array or dt <= 0");
+	if (h->linear()) return fail(h, GBFEM_INVALID_ARG, "gbfem_adjoint_step: corotational elements only");
 	cudaStream_t s = h->stream;
 	const DevBody body = h->body();
 	const int n = h->n;
@@ -1484,7 +1508,8 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), h->stream));
 	gbfem_status result = GBFEM_OK;
 	int sidx = 0;
-	if ((flags & GBFEM_STEP_GRAPH) && h->prm.autotune && !h->tuned && nsteps > 0)
+	const bool needPlainStep = (h->prm.autotune && !h->tuned) || (h->linear() && !(h->linearReady && h->linearDt == dt));
+	if ((flags & GBFEM_STEP_GRAPH) && needPlainStep && nsteps > 0)
 	{
 		result = step_once(h, dt, flags & ~GBFEM_STEP_GRAPH);  // the first step tunes, outside any graph
 		sidx = 1;

@@ -78,13 +78,14 @@ struct MatCsr
 };
 
 // ---- element / assembly
+// kslots may be null (right-hand side only); linear: the linear tetrahedron (K_e = K0, no rotation).
 void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
-						 double* fE, int* counters, cudaStream_t s);
+						 double* fE, int* counters, cudaStream_t s, bool linear = false);
 // elemsPerBlock: 32 or 64 (a tuning choice; results do not depend on it).
 void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
-						cudaStream_t s, int elemsPerBlock = 64);
+						cudaStream_t s, int elemsPerBlock = 64, bool linear = false);
 void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
 					 cudaStream_t s);
 void launch_assemble(const DevBody& b, const float* kslots, double c1, double c2, float* A, float* invdiag,

@@ -21,7 +21,7 @@ constexpr int kElemThreads = 64;
 // ------------------------------------------------------------------------------------------
 // Element kernels
 // ------------------------------------------------------------------------------------------
-template <bool kDebug>
+template <bool kDebug, bool kLinear>
 __global__ void __launch_bounds__(kElemThreads) k_element_fp64(DevBody b, const double* __restrict__ xn,
 																const double* __restrict__ vn,
 																const double* __restrict__ xt,
@@ -41,9 +41,9 @@ __global__ void __launch_bounds__(kElemThreads) k_element_fp64(DevBody b, const 
 #pragma unroll
 		for (int k = 0; k < 3; ++k) g[a][k] = b.rest[(3 * a + k) * E + e];
 	const double lamV = b.rest[13 * E + e], muV = b.rest[14 * E + e], cm = b.rest[15 * E + e];
-	const int fl = elem::compute<double, kDebug>(in, g, lamV, muV, cm, kslots + (size_t)e * (kSlots * 9), 1,
-												 rhsE + (size_t)e * 12, 1, kDebug ? kfull + (size_t)e * 144 : nullptr,
-												 kDebug ? fE + (size_t)e * 12 : nullptr);
+	const int fl = elem::compute<double, kDebug, elem::ElemIn, kLinear>(
+		in, g, lamV, muV, cm, kslots ? kslots + (size_t)e * (kSlots * 9) : nullptr, 1, rhsE + (size_t)e * 12, 1,
+		kDebug ? kfull + (size_t)e * 144 : nullptr, kDebug ? fE + (size_t)e * 12 : nullptr);
 	if (fl & 1) atomicAdd(&counters[1], 1);
 	if (fl & 2) atomicAdd(&counters[0], 1);
 }
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kElemThreads) k_element_fp64(DevBody b, const 
 // FP32 element kernel of the mixed form, kT elements per block (a tuning choice). Results are
 // staged in shared memory and written out with coalesced stores (element-major, the layout the
 // assembly gathers).
-template <int kT>
+template <int kT, bool kLinear>
 __global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __restrict__ xn,
 															   const double* __restrict__ vn,
 															   const double* __restrict__ xt,
@@ -75,18 +75,22 @@ __global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __r
 #pragma unroll
 			for (int k = 0; k < 3; ++k) g[a][k] = b.rest32[(3 * a + k) * E + e];
 		const float lamV = b.rest32[13 * E + e], muV = b.rest32[14 * E + e], cm = b.rest32[15 * E + e];
-		const int fl = elem::compute<float, false>(in, g, lamV, muV, cm, &sks[0][threadIdx.x], kT + 1,
-												   &srhs[0][threadIdx.x], kT + 1, nullptr, nullptr);
+		const int fl = elem::compute<float, false, elem::ElemIn, kLinear>(
+			in, g, lamV, muV, cm, kslots ? &sks[0][threadIdx.x] : nullptr, kT + 1, &srhs[0][threadIdx.x], kT + 1,
+			nullptr, nullptr);
 		if (fl & 1) atomicAdd(&counters[1], 1);
 		if (fl & 2) atomicAdd(&counters[0], 1);
 	}
 	__syncthreads();
 	const int cnt = min(kT, E - e0);
-	float* dstK = kslots + (size_t)e0 * kV;
-	for (int idx = threadIdx.x; idx < cnt * kV; idx += kT)
+	if (kslots)
 	{
-		const int el = idx / kV;
-		dstK[idx] = sks[idx - el * kV][el];
+		float* dstK = kslots + (size_t)e0 * kV;
+		for (int idx = threadIdx.x; idx < cnt * kV; idx += kT)
+		{
+			const int el = idx / kV;
+			dstK[idx] = sks[idx - el * kV][el];
+		}
 	}
 	float* dstR = rhsE + (size_t)e0 * 12;
 	for (int idx = threadIdx.x; idx < cnt * 12; idx += kT)
@@ -511,27 +515,47 @@ inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 // ------------------------------------------------------------------------------------------
 void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
-						 double* fE, int* counters, cudaStream_t s)
+						 double* fE, int* counters, cudaStream_t s, bool linear)
 {
 	if (b.E == 0) return;
+	const int nb = blocks(b.E, kElemThreads);
 	if (kfull)
-		k_element_fp64<true><<<blocks(b.E, kElemThreads), kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta,
-																				 kslots, rhsE, kfull, fE, counters);
+	{
+		if (linear)
+			k_element_fp64<true, true><<<nb, kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																	kfull, fE, counters);
+		else
+			k_element_fp64<true, false><<<nb, kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																	 kfull, fE, counters);
+	}
+	else if (linear)
+		k_element_fp64<false, true><<<nb, kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																 nullptr, nullptr, counters);
 	else
-		k_element_fp64<false><<<blocks(b.E, kElemThreads), kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta,
-																				  kslots, rhsE, nullptr, nullptr,
-																				  counters);
+		k_element_fp64<false, false><<<nb, kElemThreads, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																  nullptr, nullptr, counters);
 }
 
 void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
-						cudaStream_t s, int elemsPerBlock)
+						cudaStream_t s, int elemsPerBlock, bool linear)
 {
 	if (b.E == 0) return;
 	if (elemsPerBlock == 32)
-		k_element_f32<32><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE, counters);
+	{
+		if (linear)
+			k_element_f32<32, true><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																	counters);
+		else
+			k_element_f32<32, false><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																	 counters);
+	}
+	else if (linear)
+		k_element_f32<64, true><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																counters);
 	else
-		k_element_f32<64><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE, counters);
+		k_element_f32<64, false><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+																 counters);
 }
 
 void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,

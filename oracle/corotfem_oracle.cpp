@@ -236,6 +236,7 @@ struct Tet
 	double M[12][12], K[12][12];
 	double f[12];
 	bool orientationWarning = false;
+	bool linear = false;   // Fem3DElementTetrahedron instead of the corotational element
 	int singularG = 0;     // count of updates that hit the singular-G early return
 	int invalidRotation = 0;  // count of updates that hit the |det R - 1| > 1e-8 early return
 };
@@ -382,12 +383,33 @@ void computeRotationMassAndStiffness(Tet& t, const double* x /*12*/, bool wantM,
 	}
 }
 
-// Fem3DElementCorotationalTetrahedron::doUpdateFMDK, :77-114 (options = FMDK).
+// Fem3DElementCorotationalTetrahedron::doUpdateFMDK, :77-114 (options = FMDK); with `linear`,
+// Fem3DElementTetrahedron::doUpdateFMDK (Fem3DElementTetrahedron.cpp:77-90): M = M0, K = K0,
+// f = -K0 (x - x0).
 void tetUpdateFMDK(Tet& t, const double* X /*global positions*/)
 {
+	const bool linear = t.linear;
 	double x[12];
 	for (int a = 0; a < 4; ++a)
 		for (int k = 0; k < 3; ++k) x[3 * a + k] = X[3 * t.n[a] + k];
+	if (linear)
+	{
+		for (int i = 0; i < 12; ++i)
+			for (int j = 0; j < 12; ++j)
+			{
+				t.M[i][j] = t.M0[i][j];
+				t.K[i][j] = t.K0[i][j];
+			}
+		for (int i = 0; i < 3; ++i)
+			for (int j = 0; j < 3; ++j) t.R[i][j] = (i == j) ? 1.0 : 0.0;
+		for (int i = 0; i < 12; ++i)
+		{
+			double s = 0;
+			for (int k = 0; k < 12; ++k) s += t.K0[i][k] * (x[k] - t.x0[k]);
+			t.f[i] = -s;
+		}
+		return;
+	}
 	computeRotationMassAndStiffness(t, x, true, true);
 	double Rx0[12];
 	for (int a = 0; a < 4; ++a)
@@ -958,6 +980,7 @@ struct orc_params
 	double newton_epsilon;
 	double cg_tolerance;
 	int32_t cg_max_iterations;  // <= 0: Eigen default 2n
+	int32_t element_type;       // 0: corotational tetrahedron, 1: linear tetrahedron
 };
 
 struct orc_stats
@@ -991,6 +1014,7 @@ void* orc_create(int32_t numNodes, const double* x, int32_t numTets, const int32
 		m->tets[e].E = E[e];
 		m->tets[e].nu = nu[e];
 		m->tets[e].rho = rho[e];
+		m->tets[e].linear = prm->element_type == 1;
 	}
 	std::vector<char> seen(3 * (size_t)numNodes, 0);
 	for (int i = 0; i < numBc; ++i)

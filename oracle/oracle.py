@@ -30,6 +30,7 @@ class OrcParams(ctypes.Structure):
         ("newton_epsilon", ctypes.c_double),
         ("cg_tolerance", ctypes.c_double),
         ("cg_max_iterations", ctypes.c_int32),
+        ("element_type", ctypes.c_int32),   # 0 corotational tetrahedron, 1 linear tetrahedron
     ]
 
 
@@ -107,11 +108,13 @@ class OracleError(RuntimeError):
 
 
 class OracleModel:
-    """An OpenSurgSim-style Fem3DRepresentation (corotational tets, implicit Euler, CG) on the CPU."""
+    """An OpenSurgSim-style Fem3DRepresentation (corotational or linear tets, implicit Euler, CG) on
+    the CPU. element_type 1 selects Fem3DElementTetrahedron; its linear implicit Euler
+    (OdeSolverLinearEulerImplicit) takes the same steps, the system matrix being constant."""
 
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5, cg_tolerance=1e-10,
-                 cg_max_iterations=0):
+                 cg_max_iterations=0, element_type=0):
         L = lib()
         self._nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64).ravel()
         self._tets = np.ascontiguousarray(mesh.tets, dtype=np.int32).ravel()
@@ -128,6 +131,7 @@ class OracleModel:
         p.newton_epsilon = newton_epsilon
         p.cg_tolerance = cg_tolerance
         p.cg_max_iterations = cg_max_iterations
+        p.element_type = element_type
         st = ctypes.c_int32(0)
         self.num_nodes = mesh.nodes.shape[0]
         self.num_tets = mesh.tets.shape[0]

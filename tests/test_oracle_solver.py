@@ -135,3 +135,41 @@ def test_scatter_map_points_at_block_entries():
                         k = sc[e, 3 * a + i, 3 * b + j]
                         col = 3 * tets[e, b] + j
                         assert colptr[col] <= k < colptr[col + 1] and rowidx[k] == 3 * tets[e, a] + i
+
+
+def _csc_matvec(colptr, rowidx, vals, v):
+    out = np.zeros_like(v)
+    for c in range(len(colptr) - 1):
+        sl = slice(colptr[c], colptr[c + 1])
+        out[rowidx[sl]] += vals[sl] * v[c]
+    return out
+
+
+def test_linear_tetrahedron_force_and_constant_stiffness():
+    """Fem3DElementTetrahedron::doUpdateFMDK (Fem3DElementTetrahedron.cpp:77-90): K does not depend on
+    the state and f = -K (x - x0) + gravity - alpha M v - beta K v (FemRepresentation.cpp:479-545)."""
+    s = mesh.scene_cube(2, 2, 3)
+    alpha, beta = 0.01, 0.001
+    m = O.OracleModel(s.mesh, rayleigh_mass=alpha, rayleigh_stiffness=beta, gravity=(0, 0, -9.81),
+                      cg_tolerance=1e-14, element_type=1)
+    colptr, rowidx = m.pattern()
+    rng = np.random.default_rng(4)
+    x0 = s.mesh.nodes.ravel()
+    Ks = []
+    for trial in range(2):
+        R = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]]) if trial else np.eye(3)
+        x = (R @ s.mesh.nodes.T).T.ravel() + rng.normal(0, 1e-4, x0.size)
+        v = rng.normal(0, 0.01, x0.size)
+        m.set_state(x, v)
+        m.step(1e-3)
+        sys_ = m.system()
+        Ks.append(sys_["K"].copy())
+        K, M = sys_["K"], sys_["M"]
+        g = np.zeros_like(x0)
+        g[2::3] = -9.81 * m.mass_per_node()
+        expect = (-_csc_matvec(colptr, rowidx, K, x - x0) + g - alpha * _csc_matvec(colptr, rowidx, M, v)
+                  - beta * _csc_matvec(colptr, rowidx, K, v))
+        assert np.linalg.norm(sys_["f"] - expect) <= 1e-10 * np.linalg.norm(expect)
+    assert np.array_equal(Ks[0], Ks[1])
+    # A rigid rotation is not force-free for the linear element (it is for the corotational one).
+    assert np.abs(sys_["f"] - g).max() > 1e-3
