@@ -158,6 +158,23 @@ GBFEM_API gbfem_status gbfem_device_state(gbfem_handle h, double** x, double** v
 GBFEM_API gbfem_status gbfem_stream(gbfem_handle h, void** stream);
 GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
 
+/* ---- Compliance (DeformableRepresentation::applyCompliance, DeformableRepresentation.cpp:175-191;
+ * with warping, FemRepresentation::applyCompliance, FemRepresentation.cpp:329-340, and the node
+ * rotations of Fem3DCorotationalTetrahedronRepresentation.cpp:85-143). For each of the ncols columns of b
+ * (host, column-major n x ncols, e.g. constraint directions): zero the boundary-condition rows, solve
+ * with the system matrix of the last step, zero the boundary-condition rows of the solution, write the
+ * column of x. The columns are solved together, eight at a time, by a multi-right-hand-side CG that
+ * reads the matrix once per iteration for all of them; each column has its own Eigen-style
+ * convergence test (tolerance and maximum iterations of the handle). Replaces the dense inverse the
+ * reference forms for getComplianceMatrix(); the dense matrix is this call on the identity's
+ * columns. GBFEM_COMPLIANCE_WARPING: x = W S^-1 W^T b with W the per-node slerp average of the element
+ * rotations at the positions the last step started from (corotational element only). iterations
+ * (may be NULL) receives the CG iterations summed over columns. Returns GBFEM_CG_MAXITER if a column
+ * did not converge. */
+#define GBFEM_COMPLIANCE_WARPING 1u
+GBFEM_API gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, const double* b, double* x, uint32_t flags,
+											  int32_t* iterations);
+
 /* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
  * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
  * CTAs per SM and refresh weights 4, 6, 8 on its own system, and keeps the fastest. The solve's

@@ -32,6 +32,7 @@ STEP_TIME_PHASES = 1
 STEP_KEEP_SYSTEM = 2
 STEP_TIME_KERNELS = 4
 STEP_GRAPH = 8
+COMPLIANCE_WARPING = 1
 
 # Every symbol the header declares; the CPU tests check the library exports all of them.
 EXPORTED = [
@@ -41,7 +42,7 @@ EXPORTED = [
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
     "gbfem_cg_destroy", "gbfem_cg_solve_noalloc", "gbfem_batch_create", "gbfem_batch_info",
     "gbfem_batch_segment_stats", "gbfem_set_materials_device", "gbfem_adjoint_step", "gbfem_get_tuning",
-    "gbfem_set_tuning",
+    "gbfem_set_tuning", "gbfem_apply_compliance",
 ]
 
 
@@ -144,6 +145,7 @@ def load():
         "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
         "gbfem_set_materials_device": (S, [H, ctypes.c_void_p, ctypes.c_void_p]),
         "gbfem_get_tuning": (S, [H, I32, I32, I32]),
+        "gbfem_apply_compliance": (S, [H, ctypes.c_int32, D, D, ctypes.c_uint32, I32]),
         "gbfem_set_tuning": (S, [H, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
         "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9 + [ctypes.c_uint32]),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

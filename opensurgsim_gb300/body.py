@@ -89,6 +89,19 @@ class Body:
         _lib.load().gbfem_batch_segment_stats(self._h, iptr(it), iptr(rf), iptr(cv), dptr(res))
         return dict(iterations=it, refreshes=rf, converged=cv, relative_residual=res)
 
+    def apply_compliance(self, B, warping=False):
+        """Solve the last step's system for the columns of B (n x k): applyCompliance semantics (BC rows
+        zeroed in and out), optionally with compliance warping. Returns (X, status, iterations)."""
+        B = np.asfortranarray(np.asarray(B, dtype=np.float64).reshape(self.n, -1))
+        X = np.zeros_like(B, order="F")
+        it = ctypes.c_int32(0)
+        st = _lib.load().gbfem_apply_compliance(self._h, B.shape[1], B.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                X.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                _lib.COMPLIANCE_WARPING if warping else 0, ctypes.byref(it))
+        if st not in (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER):
+            raise GbfemError(st, _lib.last_error(self._h))
+        return X, st, it.value
+
     def tuning(self):
         """(elements per block, CTAs per SM, refresh weight) of the mixed form's kernels."""
         e, c, r = (ctypes.c_int32() for _ in range(3))

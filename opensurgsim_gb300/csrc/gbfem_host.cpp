@@ -152,6 +152,12 @@ struct gbfem_handle_s
 	// changes (OdeSolverLinearEulerImplicit keeps its first step's system).
 	bool linearReady = false;
 	double linearDt = 0.0;
+	// Compliance (gbfem_apply_compliance): the system matrix of the last step, and its dt.
+	bool systemReady = false;
+	double lastDt = 0.0;
+	DevBuf<double> d_mcgVec, d_mcgPart, d_Re, d_Wn, d_xprev;
+	DevBuf<McgCtl> d_mcgCtl;
+	McgCtl* h_mcgCtl = nullptr;
 	DevBuf<int> d_counters;
 	DevBuf<CgCtl> d_ctl;
 	CgCtl* h_ctl = nullptr;
@@ -225,6 +231,10 @@ struct gbfem_handle_s
 		for (auto* b : {&d_rcol, &d_segChunk, &d_cumW}) b->free();
 		d_slots.free();
 		d_acc.free();
+		for (auto* b : {&d_mcgVec, &d_mcgPart, &d_Re, &d_Wn, &d_xprev}) b->free();
+		d_mcgCtl.free();
+		if (h_mcgCtl) cudaFreeHost(h_mcgCtl);
+		h_mcgCtl = nullptr;
 		if (graphExec) cudaGraphExecDestroy(graphExec);
 		graphExec = nullptr;
 		for (auto& e : graphEv)
@@ -1033,6 +1043,8 @@ gbfem_status step_graph(gbfem_handle h, double dt, int nsteps, uint32_t flags)
 	}
 	h->stats.cg_relative_residual = worst;
 	h->stats.steps += nsteps;
+	h->systemReady = true;
+	h->lastDt = dt;
 	if (acc[4 * (size_t)nseg + 1] != 0.0) return fail(h, GBFEM_CUDA_ERROR, "persistent CG: grid barrier timed out");
 	if (acc[4 * (size_t)nseg] != 0.0)
 	{
@@ -1184,6 +1196,8 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 	GB_CUDA(h, cudaStreamSynchronize(s));
 	GB_CUDA(h, cudaGetLastError());
 	h->stats.steps++;
+	h->systemReady = true;
+	h->lastDt = dt;
 	if (h->h_ctl->nonfinite)
 	{
 		h->active = false;  // FemRepresentation.cpp:285-293
@@ -1341,6 +1355,92 @@ gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, co
 								gbfem_handle* out)
 {
 	return create_impl(meshes, count, params, out);
+}
+
+gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, const double* b, double* x, uint32_t flags,
+									int32_t* iterations)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (ncols < 0 || (ncols > 0 && (!b || !x))) return fail(h, GBFEM_INVALID_ARG, "gbfem_apply_compliance: bad arrays");
+	if (!h->systemReady) return fail(h, GBFEM_INVALID_ARG, "gbfem_apply_compliance: no step has assembled a system yet");
+	const bool warp = (flags & GBFEM_COMPLIANCE_WARPING) != 0;
+	if (warp && h->linear())
+		return fail(h, GBFEM_INVALID_ARG, "compliance warping needs the corotational element");
+	GB_CUDA(h, cudaSetDevice(h->device));
+	const int n = h->n, N = h->N;
+	const Launch L = h->launch();
+	cudaStream_t s = h->stream;
+	const size_t n8 = (size_t)n * kMcgCols;
+	if (!h->d_mcgVec.p)
+	{
+		GB_CUDA(h, h->d_mcgVec.alloc(6 * n8));
+		GB_CUDA(h, h->d_mcgPart.alloc(2 * (size_t)kMcgCols * L.vecGrid));
+		GB_CUDA(h, h->d_mcgCtl.alloc(1));
+		GB_CUDA(h, cudaMemsetAsync(h->d_mcgCtl.p, 0, sizeof(McgCtl), s));
+		GB_CUDA(h, cudaMallocHost(&h->h_mcgCtl, sizeof(McgCtl)));
+	}
+	const DevBody body = h->body();
+	if (warp)
+	{
+		if (!h->d_Re.p)
+		{
+			GB_CUDA(h, h->d_Re.alloc(9 * (size_t)h->E));
+			GB_CUDA(h, h->d_Wn.alloc(9 * (size_t)N));
+			GB_CUDA(h, h->d_xprev.alloc(n));
+		}
+		// The rotations of the last element update: at the positions the last step started from.
+		launch_prev_positions(n, h->d_x.p, h->d_v.p, h->lastDt, h->d_xprev.p, s);
+		launch_element_rotation(body, h->d_xprev.p, h->d_Re.p, s);
+		launch_node_rotation(body, h->d_Re.p, h->d_Wn.p, s);
+	}
+	double *B = h->d_mcgVec.p, *X = B + n8, *R = X + n8, *Z = R + n8, *P = Z + n8, *Q = P + n8;
+	const MatSellT<double> A64{h->nrows, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A.p};
+	const MatSellT<float> A32{h->nrows, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_A32.p};
+	const bool m32 = h->mixed();
+	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * n;
+	std::vector<double> hb(n8);
+	int totalIt = 0;
+	bool allConverged = true;
+	for (int c0 = 0; c0 < ncols; c0 += kMcgCols)
+	{
+		const int k = std::min(kMcgCols, ncols - c0);
+		std::fill(hb.begin(), hb.end(), 0.0);
+		for (int c = 0; c < k; ++c)
+			for (int i = 0; i < n; ++i) hb[(size_t)i * kMcgCols + c] = b[(size_t)(c0 + c) * n + i];
+		GB_CUDA(h, cudaMemcpyAsync(B, hb.data(), sizeof(double) * n8, cudaMemcpyHostToDevice, s));
+		if (warp) launch_apply_node_rotation(N, h->d_Wn.p, B, true, s);
+		launch_mcg_init(n, k, B, h->d_bc.p, m32 ? nullptr : h->d_invdiag.p, m32 ? h->d_invdiag32.p : nullptr, X, R, Z,
+						P, h->d_mcgCtl.p, h->d_mcgPart.p, h->prm.cg_tolerance, maxIter, L);
+		GB_CUDA(h, cudaGetLastError());
+		int chunk = 8;
+		for (long long done = 0;; done += chunk)
+		{
+			for (int j = 0; j < chunk; ++j)
+			{
+				launch_mcg_spmm(m32 ? nullptr : &A64, m32 ? &A32 : nullptr, P, Q, h->d_mcgCtl.p, h->d_mcgPart.p, L);
+				launch_mcg_update(n, m32 ? nullptr : h->d_invdiag.p, m32 ? h->d_invdiag32.p : nullptr, P, Q, X, R, Z,
+								  h->d_mcgCtl.p, h->d_mcgPart.p, L);
+				launch_mcg_pupdate(n, Z, P, h->d_mcgCtl.p, L);
+			}
+			GB_CUDA(h, cudaGetLastError());
+			GB_CUDA(h, cudaMemcpyAsync(h->h_mcgCtl, h->d_mcgCtl.p, sizeof(McgCtl), cudaMemcpyDeviceToHost, s));
+			GB_CUDA(h, cudaStreamSynchronize(s));
+			if (h->h_mcgCtl->allDone) break;
+			if (done > (long long)maxIter + 64) return fail(h, GBFEM_CUDA_ERROR, "compliance CG control block did not finish");
+			chunk = std::min(2 * chunk, 64);
+		}
+		if (warp) launch_apply_node_rotation(N, h->d_Wn.p, X, false, s);
+		GB_CUDA(h, cudaMemcpyAsync(hb.data(), X, sizeof(double) * n8, cudaMemcpyDeviceToHost, s));
+		GB_CUDA(h, cudaStreamSynchronize(s));
+		for (int c = 0; c < k; ++c)
+		{
+			for (int i = 0; i < n; ++i) x[(size_t)(c0 + c) * n + i] = hb[(size_t)i * kMcgCols + c];
+			totalIt += h->h_mcgCtl->iter[c];
+			allConverged = allConverged && h->h_mcgCtl->converged[c];
+		}
+	}
+	if (iterations) *iterations = totalIt;
+	return allConverged ? GBFEM_OK : fail(h, GBFEM_CG_MAXITER, "a compliance column did not converge");
 }
 
 gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm, int32_t* refresh_weight)

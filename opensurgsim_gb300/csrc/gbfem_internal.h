@@ -48,6 +48,18 @@ struct CgCtl
 	int nonfinite, pad1;
 };
 
+// Multi-right-hand-side CG (compliance columns): kMcgCols columns solved together, each with its
+// own scalars and convergence test; vectors interleave the columns per dof ([i * kMcgCols + c]).
+constexpr int kMcgCols = 8;
+struct McgCtl
+{
+	double bb[kMcgCols], rz[kMcgCols], pq[kMcgCols], alpha[kMcgCols], beta[kMcgCols], rr[kMcgCols];
+	double threshold[kMcgCols];
+	int iter[kMcgCols], done[kMcgCols], converged[kMcgCols];
+	int allDone, maxIter;
+	unsigned int ticket[4];
+};
+
 struct Launch
 {
 	int vecGrid = 0;   // blocks of 256 threads for the dof-wise kernels
@@ -113,6 +125,25 @@ void launch_state_update(int n, const double* dv, double* dvPrev, const double* 
 						 double dt, int trackNewton, CgCtl* ctl, double* part, const Launch& L);
 void launch_validity(int n, const double* x, const double* v, CgCtl* ctl, double* part, const Launch& L);
 void launch_scatter_values(int count, const int* idx, const double* vals, double* dst, cudaStream_t s);
+// Compliance (multi-right-hand-side CG on the stored system, compliance warping).
+void launch_mcg_init(int n, int ncols, const double* B, const uint8_t* bc, const double* invd64, const float* invd32,
+					 double* X, double* R, double* Z, double* P, McgCtl* ctl, double* part, double tol, int maxIter,
+					 const Launch& L);
+void launch_mcg_spmm(const MatSellT<double>* A64, const MatSellT<float>* A32, const double* P, double* Q,
+					 McgCtl* ctl, double* part, const Launch& L);
+void launch_mcg_update(int n, const double* invd64, const float* invd32, const double* P, const double* Q, double* X,
+					   double* R, double* Z, McgCtl* ctl, double* part, const Launch& L);
+void launch_mcg_pupdate(int n, const double* Z, double* P, const McgCtl* ctl, const Launch& L);
+// Per-element rotation of the polar decomposition at positions x (9 per element, row-major).
+void launch_element_rotation(const DevBody& b, const double* x, double* Re, cudaStream_t s);
+// Per-node warping rotation: the running slerp average of the node's element rotations in element
+// order (Fem3DCorotationalTetrahedronRepresentation.cpp:112-140).
+void launch_node_rotation(const DevBody& b, const double* Re, double* Wn, cudaStream_t s);
+// out = x - dt v (the positions a step started from, after x = x_t + dt v).
+void launch_prev_positions(int n, const double* x, const double* v, double dt, double* out, cudaStream_t s);
+// X (n x kMcgCols, interleaved) <- blockdiag(W) X, or its transpose.
+void launch_apply_node_rotation(int N, const double* Wn, double* X, bool transpose, cudaStream_t s);
+
 // Differentiation form (gbfem_adjoint.cu).
 void launch_element_adjoint(const DevBody& b, const double* x, const double* v, const double* mu, const double* dv,
 							double dt, double alpha, double beta, double* gx, double* gv, double* gLogE, double* gNu,

@@ -506,6 +506,340 @@ __global__ void k_scatter_values(int count, const int* __restrict__ idx, const d
 	if (i < count) dst[idx[i]] = vals[i];
 }
 
+// ------------------------------------------------------------------------------------------
+// Multi-right-hand-side CG: the compliance columns (DeformableRepresentation::applyCompliance,
+// DeformableRepresentation.cpp:175-191) solved together on the stored system. Each column follows
+// Eigen's conjugate_gradient (Jacobi preconditioner, x0 = 0, stop at |r|^2 < tol^2 |b|^2 or maxIter)
+// with its own scalars; one SpMM reads the matrix once per iteration for all columns.
+// ------------------------------------------------------------------------------------------
+constexpr int C8 = kMcgCols;
+
+template <typename TD>
+__global__ void k_mcg_init(int n, int ncols, const double* __restrict__ B, const uint8_t* __restrict__ bc,
+						   const TD* __restrict__ invd, double* __restrict__ X, double* __restrict__ R,
+						   double* __restrict__ Z, double* __restrict__ P, McgCtl* ctl, double* part, double tol,
+						   int maxIter)
+{
+	double v[2 * C8];
+#pragma unroll
+	for (int k = 0; k < 2 * C8; ++k) v[k] = 0.0;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const double id = double(invd[i]);
+#pragma unroll
+		for (int c = 0; c < C8; ++c)
+		{
+			const size_t o = (size_t)i * C8 + c;
+			const double b = (bc[i] || c >= ncols) ? 0.0 : B[o];
+			const double z = id * b;
+			R[o] = b;
+			X[o] = 0.0;
+			Z[o] = z;
+			P[o] = z;
+			v[c] += b * b;
+			v[C8 + c] += b * z;
+		}
+	}
+	double tot[2 * C8];
+	if (grid_reduce<OpSum, 2 * C8>(v, part, &ctl->ticket[0], tot) && threadIdx.x == 0)
+	{
+		int all = 1;
+		for (int c = 0; c < C8; ++c)
+		{
+			ctl->bb[c] = tot[c];
+			ctl->rz[c] = tot[C8 + c];
+			ctl->rr[c] = tot[c];
+			ctl->threshold[c] = fmax(tol * tol * tot[c], DBL_MIN);
+			ctl->iter[c] = 0;
+			ctl->converged[c] = 1;
+			ctl->done[c] = (c >= ncols || tot[c] == 0.0 || tot[c] < ctl->threshold[c] || !isfinite(tot[c])) ? 1 : 0;
+			if (!isfinite(tot[c])) ctl->converged[c] = 0;
+			ctl->alpha[c] = ctl->beta[c] = 0.0;
+			all &= ctl->done[c];
+		}
+		ctl->maxIter = maxIter;
+		ctl->allDone = all;
+	}
+}
+
+template <typename T>
+__global__ void k_mcg_spmm(MatSellT<T> A, const double* __restrict__ P, double* __restrict__ Q, McgCtl* ctl,
+						   double* part)
+{
+	double v[C8];
+#pragma unroll
+	for (int c = 0; c < C8; ++c) v[c] = 0.0;
+	for (int rs = blockIdx.x * blockDim.x + threadIdx.x; rs < A.rows; rs += gridDim.x * blockDim.x)
+	{
+		const int I = A.perm[rs];
+		if (I < 0) continue;
+		const int ch = rs >> 5, lane = rs & 31;
+		double acc[3][C8];
+#pragma unroll
+		for (int m = 0; m < 3; ++m)
+#pragma unroll
+			for (int c = 0; c < C8; ++c) acc[m][c] = 0.0;
+		const int k0 = A.off[ch], k1 = A.off[ch + 1];
+		for (int k = k0; k < k1; ++k)
+		{
+			const int J = A.col[k * 32 + lane];
+			const T* vb = A.val + (size_t)k * 288 + lane;
+			double a[9];
+#pragma unroll
+			for (int m = 0; m < 9; ++m) a[m] = double(vb[32 * m]);
+			const double* pj = P + (size_t)J * 3 * C8;
+#pragma unroll
+			for (int c = 0; c < C8; ++c)
+			{
+				const double p0 = pj[c], p1 = pj[C8 + c], p2 = pj[2 * C8 + c];
+				acc[0][c] += a[0] * p0 + a[1] * p1 + a[2] * p2;
+				acc[1][c] += a[3] * p0 + a[4] * p1 + a[5] * p2;
+				acc[2][c] += a[6] * p0 + a[7] * p1 + a[8] * p2;
+			}
+		}
+#pragma unroll
+		for (int m = 0; m < 3; ++m)
+#pragma unroll
+			for (int c = 0; c < C8; ++c)
+			{
+				const size_t o = (size_t)(3 * I + m) * C8 + c;
+				Q[o] = acc[m][c];
+				v[c] += P[o] * acc[m][c];
+			}
+	}
+	double tot[C8];
+	if (grid_reduce<OpSum, C8>(v, part, &ctl->ticket[1], tot) && threadIdx.x == 0)
+		for (int c = 0; c < C8; ++c)
+		{
+			ctl->pq[c] = tot[c];
+			ctl->alpha[c] = ctl->done[c] ? 0.0 : ctl->rz[c] / tot[c];
+		}
+}
+
+template <typename TD>
+__global__ void k_mcg_update(int n, const TD* __restrict__ invd, const double* __restrict__ P,
+							 const double* __restrict__ Q, double* __restrict__ X, double* __restrict__ R,
+							 double* __restrict__ Z, McgCtl* ctl, double* part)
+{
+	double al[C8];
+#pragma unroll
+	for (int c = 0; c < C8; ++c) al[c] = ctl->alpha[c];
+	double v[2 * C8];
+#pragma unroll
+	for (int k = 0; k < 2 * C8; ++k) v[k] = 0.0;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const double id = double(invd[i]);
+#pragma unroll
+		for (int c = 0; c < C8; ++c)
+		{
+			const size_t o = (size_t)i * C8 + c;
+			X[o] += al[c] * P[o];
+			const double r = R[o] - al[c] * Q[o];
+			R[o] = r;
+			const double z = id * r;
+			Z[o] = z;
+			v[c] += r * r;
+			v[C8 + c] += r * z;
+		}
+	}
+	double tot[2 * C8];
+	if (grid_reduce<OpSum, 2 * C8>(v, part, &ctl->ticket[2], tot) && threadIdx.x == 0)
+	{
+		int all = 1;
+		for (int c = 0; c < C8; ++c)
+		{
+			if (!ctl->done[c])
+			{
+				ctl->rr[c] = tot[c];
+				ctl->iter[c] += 1;
+				if (tot[c] < ctl->threshold[c])
+					ctl->done[c] = 1;
+				else if (!isfinite(tot[c]) || ctl->iter[c] >= ctl->maxIter)
+				{
+					ctl->done[c] = 1;
+					ctl->converged[c] = 0;
+				}
+				else
+				{
+					ctl->beta[c] = tot[C8 + c] / ctl->rz[c];
+					ctl->rz[c] = tot[C8 + c];
+				}
+			}
+			all &= ctl->done[c];
+		}
+		ctl->allDone = all;
+	}
+}
+
+__global__ void k_mcg_pupdate(int n, const double* __restrict__ Z, double* __restrict__ P, const McgCtl* ctl)
+{
+	double be[C8];
+	int dn[C8];
+#pragma unroll
+	for (int c = 0; c < C8; ++c)
+	{
+		be[c] = ctl->beta[c];
+		dn[c] = ctl->done[c];
+	}
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+#pragma unroll
+		for (int c = 0; c < C8; ++c)
+		{
+			const size_t o = (size_t)i * C8 + c;
+			if (!dn[c]) P[o] = Z[o] + be[c] * P[o];
+		}
+}
+
+// Rotation of every element at positions x (the polar factor of the corotational update).
+__global__ void k_element_rotation(DevBody b, const double* __restrict__ x, double* __restrict__ Re)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= b.E) return;
+	const int E = b.E;
+	const int4 t4 = b.tets[e];
+	const int nd[4] = {t4.x, t4.y, t4.z, t4.w};
+	double F[9];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			double s = 0.0;
+#pragma unroll
+			for (int a = 1; a < 4; ++a) s += (x[3 * nd[a] + i] - x[3 * nd[0] + i]) * b.rest[(3 * a + j) * E + e];
+			F[3 * i + j] = s;
+		}
+	double R[9];
+	if (!elem::polar_newton(F, R)) elem::polar_svd(F, R);
+#pragma unroll
+	for (int k = 0; k < 9; ++k) Re[(size_t)e * 9 + k] = R[k];
+}
+
+// Unit quaternion (w, x, y, z) of a rotation matrix (row-major), by the largest of the four
+// diagonal combinations (numerically stable for every rotation).
+__device__ void quat_from_matrix(const double* R, double* q)
+{
+	const double t = R[0] + R[4] + R[8];
+	if (t > 0.0)
+	{
+		const double s = 2.0 * sqrt(1.0 + t);
+		q[0] = 0.25 * s;
+		q[1] = (R[7] - R[5]) / s;
+		q[2] = (R[2] - R[6]) / s;
+		q[3] = (R[3] - R[1]) / s;
+	}
+	else if (R[0] > R[4] && R[0] > R[8])
+	{
+		const double s = 2.0 * sqrt(1.0 + R[0] - R[4] - R[8]);
+		q[0] = (R[7] - R[5]) / s;
+		q[1] = 0.25 * s;
+		q[2] = (R[1] + R[3]) / s;
+		q[3] = (R[2] + R[6]) / s;
+	}
+	else if (R[4] > R[8])
+	{
+		const double s = 2.0 * sqrt(1.0 + R[4] - R[0] - R[8]);
+		q[0] = (R[2] - R[6]) / s;
+		q[1] = (R[1] + R[3]) / s;
+		q[2] = 0.25 * s;
+		q[3] = (R[5] + R[7]) / s;
+	}
+	else
+	{
+		const double s = 2.0 * sqrt(1.0 + R[8] - R[0] - R[4]);
+		q[0] = (R[3] - R[1]) / s;
+		q[1] = (R[2] + R[6]) / s;
+		q[2] = (R[5] + R[7]) / s;
+		q[3] = 0.25 * s;
+	}
+}
+
+__device__ void matrix_from_quat(const double* q, double* R)
+{
+	const double w = q[0], x = q[1], y = q[2], z = q[3];
+	R[0] = 1 - 2 * (y * y + z * z);
+	R[1] = 2 * (x * y - w * z);
+	R[2] = 2 * (x * z + w * y);
+	R[3] = 2 * (x * y + w * z);
+	R[4] = 1 - 2 * (x * x + z * z);
+	R[5] = 2 * (y * z - w * x);
+	R[6] = 2 * (x * z - w * y);
+	R[7] = 2 * (y * z + w * x);
+	R[8] = 1 - 2 * (x * x + y * y);
+}
+
+// Spherical linear interpolation from a to b at t along the shorter arc (linear weights when the
+// quaternions are within one rounding unit of each other).
+__device__ void quat_slerp(const double* a, const double* b, double t, double* out)
+{
+	const double d = a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+	const double ad = fabs(d);
+	double s0, s1;
+	if (ad >= 1.0 - DBL_EPSILON)
+	{
+		s0 = 1.0 - t;
+		s1 = t;
+	}
+	else
+	{
+		const double th = acos(ad), st = sin(th);
+		s0 = sin((1.0 - t) * th) / st;
+		s1 = sin(t * th) / st;
+	}
+	if (d < 0.0) s1 = -s1;
+#pragma unroll
+	for (int k = 0; k < 4; ++k) out[k] = s0 * a[k] + s1 * b[k];
+}
+
+__global__ void k_node_rotation(DevBody b, const double* __restrict__ Re, double* __restrict__ Wn)
+{
+	const int I = blockIdx.x * blockDim.x + threadIdx.x;
+	if (I >= b.N) return;
+	const int k0 = b.iptr[I], k1 = b.iptr[I + 1];
+	double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+	if (k1 > k0)
+	{
+		double q[4];
+		quat_from_matrix(Re + (size_t)(b.iidx[k0] >> 2) * 9, q);
+		for (int k = k0 + 1; k < k1; ++k)
+		{
+			double qe[4], qn[4];
+			quat_from_matrix(Re + (size_t)(b.iidx[k] >> 2) * 9, qe);
+			const double i = double(k - k0 + 1);  // the element's 1-based position at this node
+			quat_slerp(q, qe, 1.0 - 1.0 / i, qn);
+#pragma unroll
+			for (int m = 0; m < 4; ++m) q[m] = qn[m];
+		}
+		matrix_from_quat(q, R);
+	}
+#pragma unroll
+	for (int m = 0; m < 9; ++m) Wn[(size_t)I * 9 + m] = R[m];
+}
+
+__global__ void k_apply_node_rotation(int N, const double* __restrict__ Wn, double* __restrict__ X, int transpose)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= N * C8) return;
+	const int I = t / C8, c = t % C8;
+	const double* W = Wn + (size_t)I * 9;
+	const size_t o = (size_t)3 * I * C8 + c;
+	const double x0 = X[o], x1 = X[o + C8], x2 = X[o + 2 * C8];
+	for (int i = 0; i < 3; ++i)
+	{
+		const double r = transpose ? (W[i] * x0 + W[3 + i] * x1 + W[6 + i] * x2)
+								   : (W[3 * i] * x0 + W[3 * i + 1] * x1 + W[3 * i + 2] * x2);
+		X[o + i * C8] = r;
+	}
+}
+
+__global__ void k_prev_positions(int n, const double* __restrict__ x, const double* __restrict__ v, double dt,
+								 double* __restrict__ out)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) out[i] = x[i] - dt * v[i];
+}
+
 inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
@@ -638,6 +972,65 @@ void launch_scatter_values(int count, const int* idx, const double* vals, double
 {
 	if (count <= 0) return;
 	k_scatter_values<<<blocks(count, 256), 256, 0, s>>>(count, idx, vals, dst);
+}
+
+void launch_mcg_init(int n, int ncols, const double* B, const uint8_t* bc, const double* invd64, const float* invd32,
+					 double* X, double* R, double* Z, double* P, McgCtl* ctl, double* part, double tol, int maxIter,
+					 const Launch& L)
+{
+	if (invd64)
+		k_mcg_init<double><<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, ncols, B, bc, invd64, X, R, Z, P, ctl, part, tol,
+																	 maxIter);
+	else
+		k_mcg_init<float><<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, ncols, B, bc, invd32, X, R, Z, P, ctl, part, tol,
+																	maxIter);
+}
+
+void launch_mcg_spmm(const MatSellT<double>* A64, const MatSellT<float>* A32, const double* P, double* Q,
+					 McgCtl* ctl, double* part, const Launch& L)
+{
+	if (A64)
+		k_mcg_spmm<double><<<L.vecGrid, kVecThreads, 0, L.stream>>>(*A64, P, Q, ctl, part);
+	else
+		k_mcg_spmm<float><<<L.vecGrid, kVecThreads, 0, L.stream>>>(*A32, P, Q, ctl, part);
+}
+
+void launch_mcg_update(int n, const double* invd64, const float* invd32, const double* P, const double* Q, double* X,
+					   double* R, double* Z, McgCtl* ctl, double* part, const Launch& L)
+{
+	if (invd64)
+		k_mcg_update<double><<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, invd64, P, Q, X, R, Z, ctl, part);
+	else
+		k_mcg_update<float><<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, invd32, P, Q, X, R, Z, ctl, part);
+}
+
+void launch_mcg_pupdate(int n, const double* Z, double* P, const McgCtl* ctl, const Launch& L)
+{
+	k_mcg_pupdate<<<L.vecGrid, kVecThreads, 0, L.stream>>>(n, Z, P, ctl);
+}
+
+void launch_element_rotation(const DevBody& b, const double* x, double* Re, cudaStream_t s)
+{
+	if (b.E == 0) return;
+	k_element_rotation<<<blocks(b.E, 128), 128, 0, s>>>(b, x, Re);
+}
+
+void launch_node_rotation(const DevBody& b, const double* Re, double* Wn, cudaStream_t s)
+{
+	if (b.N == 0) return;
+	k_node_rotation<<<blocks(b.N, 128), 128, 0, s>>>(b, Re, Wn);
+}
+
+void launch_apply_node_rotation(int N, const double* Wn, double* X, bool transpose, cudaStream_t s)
+{
+	if (N == 0) return;
+	k_apply_node_rotation<<<blocks((long long)N * C8, 256), 256, 0, s>>>(N, Wn, X, transpose ? 1 : 0);
+}
+
+void launch_prev_positions(int n, const double* x, const double* v, double dt, double* out, cudaStream_t s)
+{
+	if (n == 0) return;
+	k_prev_positions<<<blocks(n, 256), 256, 0, s>>>(n, x, v, dt, out);
 }
 
 }  // namespace gbfem

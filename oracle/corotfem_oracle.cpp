@@ -968,6 +968,82 @@ struct MassPointEq : Equation
 // =============================================================================================
 // C interface for the Python test harness (ctypes) and the CPU baseline.
 // =============================================================================================
+// ---------------------------------------------------------------------------------------------
+// Compliance warping rotations (Fem3DCorotationalTetrahedronRepresentation.cpp:112-140): per node,
+// the running slerp average of the rotations of the elements holding it, in element order, with the
+// i-th rotation (1-based) weighted in by slerp(current, R_i, 1 - 1/i). Quaternions from matrices by the
+// largest diagonal combination; slerp along the shorter arc (linear weights when nearly equal).
+void quatFromMatrix(const double R[3][3], double q[4])
+{
+	const double t = R[0][0] + R[1][1] + R[2][2];
+	if (t > 0.0)
+	{
+		const double s = 2.0 * std::sqrt(1.0 + t);
+		q[0] = 0.25 * s;
+		q[1] = (R[2][1] - R[1][2]) / s;
+		q[2] = (R[0][2] - R[2][0]) / s;
+		q[3] = (R[1][0] - R[0][1]) / s;
+	}
+	else if (R[0][0] > R[1][1] && R[0][0] > R[2][2])
+	{
+		const double s = 2.0 * std::sqrt(1.0 + R[0][0] - R[1][1] - R[2][2]);
+		q[0] = (R[2][1] - R[1][2]) / s;
+		q[1] = 0.25 * s;
+		q[2] = (R[0][1] + R[1][0]) / s;
+		q[3] = (R[0][2] + R[2][0]) / s;
+	}
+	else if (R[1][1] > R[2][2])
+	{
+		const double s = 2.0 * std::sqrt(1.0 + R[1][1] - R[0][0] - R[2][2]);
+		q[0] = (R[0][2] - R[2][0]) / s;
+		q[1] = (R[0][1] + R[1][0]) / s;
+		q[2] = 0.25 * s;
+		q[3] = (R[1][2] + R[2][1]) / s;
+	}
+	else
+	{
+		const double s = 2.0 * std::sqrt(1.0 + R[2][2] - R[0][0] - R[1][1]);
+		q[0] = (R[1][0] - R[0][1]) / s;
+		q[1] = (R[0][2] + R[2][0]) / s;
+		q[2] = (R[1][2] + R[2][1]) / s;
+		q[3] = 0.25 * s;
+	}
+}
+
+void matrixFromQuat(const double q[4], double R[3][3])
+{
+	const double w = q[0], x = q[1], y = q[2], z = q[3];
+	R[0][0] = 1 - 2 * (y * y + z * z);
+	R[0][1] = 2 * (x * y - w * z);
+	R[0][2] = 2 * (x * z + w * y);
+	R[1][0] = 2 * (x * y + w * z);
+	R[1][1] = 1 - 2 * (x * x + z * z);
+	R[1][2] = 2 * (y * z - w * x);
+	R[2][0] = 2 * (x * z - w * y);
+	R[2][1] = 2 * (y * z + w * x);
+	R[2][2] = 1 - 2 * (x * x + y * y);
+}
+
+void quatSlerp(const double a[4], const double b[4], double t, double out[4])
+{
+	const double d = a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+	const double ad = std::fabs(d);
+	double s0, s1;
+	if (ad >= 1.0 - DBL_EPSILON)
+	{
+		s0 = 1.0 - t;
+		s1 = t;
+	}
+	else
+	{
+		const double th = std::acos(ad), st = std::sin(th);
+		s0 = std::sin((1.0 - t) * th) / st;
+		s1 = std::sin(t * th) / st;
+	}
+	if (d < 0.0) s1 = -s1;
+	for (int k = 0; k < 4; ++k) out[k] = s0 * a[k] + s1 * b[k];
+}
+
 extern "C" {
 
 struct orc_params
@@ -1172,6 +1248,83 @@ void orc_polar(const double* F9, double* R9, double* S9)
 }
 
 // LinearSparseSolveAndInverseCG::solve on a caller CSC matrix.
+// DeformableRepresentation::applyCompliance (DeformableRepresentation.cpp:175-191): for each column of
+// b (column-major n x ncols), zero the BC rows, solve with the last step's system matrix, zero the BC
+// rows of the solution; with warping, FemRepresentation::applyCompliance (FemRepresentation.cpp:329-340):
+// W (that applied to W^T b), W the per-node rotations of the last element update. Returns ORC_CG_MAXITER
+// if a column's solve did not converge.
+int32_t orc_apply_compliance(void* h, int32_t ncols, const double* b, double* x, int32_t warping, int32_t* iterations)
+{
+	auto* m = static_cast<FemModel*>(h);
+	const int n = m->pat.n, N = n / 3;
+	if (ncols < 0 || (ncols > 0 && (!b || !x)) || m->solver.S.empty()) return ORC_INVALID_ARG;
+	vector<double> W;
+	if (warping)
+	{
+		W.assign(9 * (size_t)N, 0.0);
+		vector<vector<int>> inc(N);
+		for (size_t e = 0; e < m->tets.size(); ++e)
+			for (int a = 0; a < 4; ++a) inc[m->tets[e].n[a]].push_back((int)e);
+		for (int I = 0; I < N; ++I)
+		{
+			double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+			if (!inc[I].empty())
+			{
+				double q[4];
+				quatFromMatrix(m->tets[inc[I][0]].R, q);
+				for (size_t i = 2; i <= inc[I].size(); ++i)
+				{
+					double qe[4], qn[4];
+					quatFromMatrix(m->tets[inc[I][i - 1]].R, qe);
+					quatSlerp(q, qe, 1.0 - 1.0 / (double)i, qn);
+					std::copy(qn, qn + 4, q);
+				}
+				matrixFromQuat(q, R);
+			}
+			for (int i = 0; i < 3; ++i)
+				for (int j = 0; j < 3; ++j) W[9 * (size_t)I + 3 * i + j] = R[i][j];
+		}
+	}
+	int32_t st = ORC_OK;
+	int32_t its = 0;
+	vector<double> col(n), sol(n);
+	for (int c = 0; c < ncols; ++c)
+	{
+		const double* bc = b + (size_t)c * n;
+		for (int I = 0; I < N; ++I)
+			for (int i = 0; i < 3; ++i)
+			{
+				if (!warping)
+					col[3 * I + i] = bc[3 * I + i];
+				else
+				{
+					const double* w = &W[9 * (size_t)I];
+					col[3 * I + i] = w[i] * bc[3 * I] + w[3 + i] * bc[3 * I + 1] + w[6 + i] * bc[3 * I + 2];
+				}
+			}
+		for (int d : m->bcDofs) col[d] = 0.0;
+		CgResult cr = cgSolve(m->pat, m->solver.S.data(), col.data(), sol.data(), m->solver.prm.cgTol,
+							  m->solver.prm.cgMaxIter);
+		its += cr.iterations;
+		if (!cr.converged) st = ORC_CG_MAXITER;
+		for (int d : m->bcDofs) sol[d] = 0.0;
+		double* xc = x + (size_t)c * n;
+		for (int I = 0; I < N; ++I)
+			for (int i = 0; i < 3; ++i)
+			{
+				if (!warping)
+					xc[3 * I + i] = sol[3 * I + i];
+				else
+				{
+					const double* w = &W[9 * (size_t)I + 3 * i];
+					xc[3 * I + i] = w[0] * sol[3 * I] + w[1] * sol[3 * I + 1] + w[2] * sol[3 * I + 2];
+				}
+			}
+	}
+	if (iterations) *iterations = its;
+	return st;
+}
+
 int32_t orc_cg_solve(int32_t n, const int32_t* colptr, const int32_t* rowidx, const double* vals, const double* b,
 					 double* x, double tol, int32_t maxIter, int32_t* iterations, double* error)
 {

@@ -83,6 +83,8 @@ def lib():
         L.orc_tet_compute.argtypes = [D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, D, D,
                                       D, D, I32]
         L.orc_polar.argtypes = [D, D, D]
+        L.orc_apply_compliance.restype = ctypes.c_int32
+        L.orc_apply_compliance.argtypes = [ctypes.c_void_p, ctypes.c_int32, D, D, ctypes.c_int32, I32]
         L.orc_cg_solve.restype = ctypes.c_int32
         L.orc_cg_solve.argtypes = [ctypes.c_int32, I32, I32, D, D, D, ctypes.c_double, ctypes.c_int32, I32, D]
         L.orc_masspoint_step.argtypes = [ctypes.c_double, ctypes.c_double, D, D, D, D]
@@ -193,6 +195,17 @@ class OracleModel:
                np.empty(self.nnz)]
         lib().orc_get_system(self._h, *[_d(a) for a in out])
         return dict(zip(["S", "rhs", "f", "M", "D", "K"], out))
+
+    def apply_compliance(self, B, warping=False):
+        """DeformableRepresentation::applyCompliance on the columns of B (n x k) with the last step's
+        system; with warping, FemRepresentation's compliance warping. Returns (X, status, iterations)."""
+        B = np.asfortranarray(np.asarray(B, dtype=np.float64).reshape(self.n, -1))
+        X = np.zeros_like(B, order="F")
+        it = ctypes.c_int32(0)
+        st = lib().orc_apply_compliance(self._h, B.shape[1], B.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        X.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1 if warping else 0,
+                                        ctypes.byref(it))
+        return X, st, it.value
 
     def mass_per_node(self):
         m = np.empty(self.num_nodes)

@@ -173,3 +173,48 @@ def test_linear_tetrahedron_force_and_constant_stiffness():
     assert np.array_equal(Ks[0], Ks[1])
     # A rigid rotation is not force-free for the linear element (it is for the corotational one).
     assert np.abs(sys_["f"] - g).max() > 1e-3
+
+
+def _dense(colptr, rowidx, vals, n):
+    A = np.zeros((n, n))
+    for c in range(n):
+        for k in range(colptr[c], colptr[c + 1]):
+            A[rowidx[k], c] = vals[k]
+    return A
+
+
+def test_apply_compliance_solves_the_last_system_with_bc_rows_zeroed():
+    """DeformableRepresentation::applyCompliance (DeformableRepresentation.cpp:175-191)."""
+    s = mesh.scene_cube(2, 2, 2)
+    m = O.OracleModel(s.mesh, rayleigh_mass=0.01, rayleigh_stiffness=0.001, cg_tolerance=1e-14)
+    m.step(1e-3)
+    colptr, rowidx = m.pattern()
+    S = _dense(colptr, rowidx, m.system()["S"], m.n)
+    S = np.tril(S) + np.tril(S, -1).T      # the CG reads the lower triangle
+    B = np.random.default_rng(1).normal(size=(m.n, 3))
+    X, st, it = m.apply_compliance(B)
+    assert st == 0 and it > 0
+    bc = s.mesh.bc_dofs
+    Bz = B.copy()
+    Bz[bc] = 0
+    ref = np.linalg.solve(S, Bz)
+    ref[bc] = 0
+    assert np.linalg.norm(X - ref) <= 1e-9 * np.linalg.norm(ref)
+
+
+def test_compliance_warping_uses_the_node_rotations():
+    """FemRepresentation::applyCompliance with warping: for a rigidly rotated body every element (and so
+    every node) has the body's rotation R, and x = (I (x) R) S^-1 (I (x) R^T) b."""
+    s = mesh.scene_cube(2, 2, 2)
+    m = O.OracleModel(s.mesh, gravity_enabled=False, cg_tolerance=1e-14)
+    c, sn = np.cos(0.6), np.sin(0.6)
+    R = np.array([[c, -sn, 0.0], [sn, c, 0.0], [0.0, 0.0, 1.0]]) @ np.array([[1.0, 0, 0], [0, c, -sn], [0, sn, c]])
+    x = (R @ s.mesh.nodes.T).T.ravel()
+    m.set_state(x, np.zeros_like(x))
+    m.step(1e-3)
+    B = np.random.default_rng(2).normal(size=(m.n, 2))
+    Xw, st, _ = m.apply_compliance(B, warping=True)
+    assert st == 0
+    W = np.kron(np.eye(m.n // 3), R)
+    X0, _, _ = m.apply_compliance(W.T @ B)
+    assert np.linalg.norm(Xw - W @ X0) <= 1e-10 * np.linalg.norm(Xw)
