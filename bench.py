@@ -659,6 +659,111 @@ def run_adjoint(args, local):
 
 
 # ------------------------------------------------------------------------------------------------
+# Batched differentiation workload (--config adjoint-batch): 64 meshes, node counts log-uniform in
+# [2000, 100000], per-element log E, 30 steps, FP32 bulk with FP64 refreshes in one batch handle; the
+# gradient of every mesh is compared with the FP64 adjoint of that mesh alone.
+
+ADJB = dict(count=64, lo=2000, hi=100000, seed=11, steps=30, checkpoint=10, markers=16)
+
+
+def run_adjoint_batch(args, local):
+    import numpy as np
+    import torch
+
+    from opensurgsim_gb300 import _lib, build
+    from opensurgsim_gb300.autograd import rollout
+    from opensurgsim_gb300.body import Body
+    from opensurgsim_gb300 import mesh as M
+
+    build.build()
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    scenes = M.scenes_batch(count=ADJB["count"], lo=ADJB["lo"], hi=ADJB["hi"], seed=ADJB["seed"])
+    meshes = [s.mesh for s in scenes]
+    rng = np.random.default_rng(ADJB["seed"])
+    theta = [np.log(m.young) + rng.normal(0, 0.3, m.num_tets) for m in meshes]
+    theta_true = [np.log(m.young) + rng.normal(0, 0.3, m.num_tets) for m in meshes]
+    v0 = []
+    markers = []
+    for m in meshes:
+        v = rng.normal(0, 0.01, 3 * m.num_nodes)
+        v[m.bc_dofs] = 0.0
+        v0.append(v)
+        bc_nodes = set((m.bc_dofs // 3).tolist())
+        free = np.array([i for i in range(m.num_nodes) if i not in bc_nodes])
+        markers.append(np.sort(rng.choice(free, min(ADJB["markers"], free.size), replace=False)))
+    steps, ck = ADJB["steps"], ADJB["checkpoint"]
+    tets = sum(m.num_tets for m in meshes)
+    log(f"adjoint batch: {len(meshes)} meshes, {tets} tets, {sum(m.num_nodes for m in meshes)} nodes")
+
+    def t64(a):
+        return torch.tensor(a, dtype=torch.float64, device=dev)
+
+    # Batch handle (mixed precision): concatenated parameters and states.
+    batch = Body(meshes, precision=_lib.PRECISION_MIXED, device=local, **BATCH_PARAMS)
+    no = batch.node_offsets
+    mk = np.concatenate([np.stack([3 * (no[k] + mm), 3 * (no[k] + mm) + 1, 3 * (no[k] + mm) + 2], 1).ravel()
+                         for k, mm in enumerate(markers)])
+    mk_t = torch.tensor(mk, dtype=torch.long, device=dev)
+    x0 = t64(np.concatenate([m.nodes.ravel() for m in meshes]))
+    v0b = t64(np.concatenate(v0))
+    with torch.no_grad():
+        xT, _ = rollout(batch, t64(np.concatenate(theta_true)), x0, v0b, 1e-3, steps, ck)
+        target = xT[mk_t].clone()
+    th_b = t64(np.concatenate(theta))
+
+    def fwd_bwd():
+        th = th_b.clone().requires_grad_(True)
+        xT_, _ = rollout(batch, th, x0, v0b, 1e-3, steps, ck)
+        L = ((xT_[mk_t] - target) ** 2).sum()
+        L.backward()
+        return th.grad.detach().cpu().numpy()
+
+    with torch.no_grad():  # warm-up (allocations, first launches)
+        rollout(batch, th_b, x0, v0b, 1e-3, 2, ck)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    g_batch = fwd_bwd()
+    torch.cuda.synchronize(dev)
+    sec = time.perf_counter() - t0
+    log(f"batched mixed forward+backward: {sec:.2f} s")
+    batch.close()
+    # FP64 reference adjoint, one mesh at a time.
+    to = np.concatenate([[0], np.cumsum([m.num_tets for m in meshes])])
+    errs = []
+    t0 = time.perf_counter()
+    for k, m in enumerate(meshes):
+        b = Body(m, precision=_lib.PRECISION_FP64, device=local, **BATCH_PARAMS)
+        mkk = torch.tensor(np.stack([3 * markers[k], 3 * markers[k] + 1, 3 * markers[k] + 2], 1).ravel(),
+                           dtype=torch.long, device=dev)
+        th = t64(theta[k]).requires_grad_(True)
+        xk, _ = rollout(b, th, t64(m.nodes.ravel()), t64(v0[k]), 1e-3, steps, ck)
+        L = ((xk[mkk] - target[3 * sum(len(mm) for mm in markers[:k]):3 * sum(len(mm) for mm in markers[:k + 1])])
+             ** 2).sum()
+        L.backward()
+        g64 = th.grad.detach().cpu().numpy()
+        gb = g_batch[to[k]:to[k + 1]]
+        errs.append(float(np.linalg.norm(gb - g64) / max(np.linalg.norm(g64), 1e-300)))
+        b.close()
+    sec64 = time.perf_counter() - t0
+    log(f"FP64 reference adjoint (mesh by mesh): {sec64:.2f} s; gradient error max {max(errs):.2e}")
+    return {
+        "metric": "tet-element-steps/s (forward + backward, batched adjoint, 30 steps)",
+        "value": tets * steps / sec, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": 1e3 * sec / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (seeded cube-grid meshes, seeded parameters)",
+        "config": {"workload": (f"adjoint batch: {len(meshes)} meshes, nodes log-U[2000,100000] (seed {ADJB['seed']}), "
+                                f"{tets} tets, per-element log E = ln E_mesh + N(0, 0.3), {ADJB['markers']} markers "
+                                f"per mesh, {steps} steps, checkpoints every {ck}, mixed precision batch handle"),
+                   "tets": tets},
+        "grad_rel_err_vs_fp64_adjoint": {"max": max(errs), "median": float(np.median(errs)),
+                                         "definition": "per mesh ||g_batch - g_fp64|| / ||g_fp64||"},
+        "fp64_reference_adjoint": {"value": tets * steps / sec64, "how": "FP64 handle per mesh, one after another"},
+        "timing": "host clock around one device-synchronised forward+backward after a short warm-up",
+    }
+
+
+# ------------------------------------------------------------------------------------------------
 # CPU side: the oracle (FP64 C++ restatement of the reference step), the only CPU implementation
 # of the path that runs here (the reference needs Eigen and Boost).
 
@@ -766,7 +871,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube", "adjoint"])
+    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube", "adjoint", "adjoint-batch"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="bar and cube only; the batch is always mixed precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -779,9 +884,10 @@ def main():
         if rank == 0:
             print(json.dumps(line), flush=True)
         return
-    if args.config == "adjoint":
+    if args.config in ("adjoint", "adjoint-batch"):
         if rank == 0:
-            print(json.dumps(run_adjoint(args, local)), flush=True)
+            fn = run_adjoint if args.config == "adjoint" else run_adjoint_batch
+            print(json.dumps(fn(args, local)), flush=True)
         return
     dist = Dist(world)
     if args.config == "batch":

@@ -199,10 +199,11 @@ GBFEM_API gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* 
  * grad_poisson (either may be NULL). One Newton iteration (the reference default). All pointers are
  * device arrays of n (state) or num_tets (gradients) doubles. Rebuilds the step's system at (x, v)
  * and solves it transposed with the handle's CG (the FP64 or the mixed solver); the element
- * derivatives are FP64. Does not change the handle's state. Returns GBFEM_CG_MAXITER if the
- * transposed solve did not converge (the outputs are still written). Corotational elements only. With GBFEM_STEP_TIME_PHASES in
- * flags the call adds its device times to the stats: ms_element (system rebuild), ms_solve
- * (transposed solve), ms_update (element derivatives and the node gather). */
+ * derivatives run in the handle's element precision (FP64, or FP32 for the mixed form). Does not
+ * change the handle's state. Returns GBFEM_CG_MAXITER if the transposed solve did not converge
+ * (the outputs are still written). Corotational elements only. With GBFEM_STEP_TIME_PHASES in flags
+ * the call adds its device times to the stats: ms_element (system rebuild), ms_solve (transposed
+ * solve), ms_update (element derivatives and the node gather). */
 GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,
 										  const double* lx, const double* lv, double* lx_out, double* lv_out,
 										  double* grad_log_young, double* grad_poisson, uint32_t flags);

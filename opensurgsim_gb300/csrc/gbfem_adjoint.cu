@@ -10,7 +10,8 @@
 // where psi(x, v, theta) = mu . rhs - mu . S dv (mu and dv held fixed; BC entries of both are zero,
 // which removes the BC rows and columns the forward replaces by constants). psi is a sum of
 // element terms psi_e, so the per-element kernels below produce d psi_e / d(x_e, v_e, E_e, nu_e):
-//   - x: forward-mode dual numbers through the same element code (9 seeded passes), which
+//   - x: forward-mode dual numbers through the same element code (9 seeded passes; FP64 for the
+//     FP64 form, FP32 for the mixed form, whose forward element math is FP32 too), which
 //     differentiates the rotation, the corotated tangent (its dR/dx terms) and the force exactly;
 //   - v: psi is linear in v, d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e;
 //   - E, nu: psi_e is linear in (lambda V, mu V), so two evaluations with unit moduli give both.
@@ -26,6 +27,7 @@ constexpr int kAdjThreads = 64;
 // One thread per element, its eleven passes in turn (splitting them over threads was measured
 // slower: every pass needs the same large per-thread state, so more threads only add local-memory
 // traffic). gx[e*12 + 3..11], gv[e*12 + 0..11]; gLogE[e], gNu[e] accumulate.
+template <typename S>
 __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, const double* __restrict__ x,
 																 const double* __restrict__ v,
 																 const double* __restrict__ mu,
@@ -61,8 +63,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 	const bool moduli = gLogE || gNu;
 	double pl = 0.0, pm = 0.0;
 	for (int item = 0; item < (moduli ? adj::kAdjItems : adj::kAdjItems - 1); ++item)
-		adj::adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
-						  gv + (size_t)e * 12, &pl, &pm);
+		adj::adjoint_item<S>(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
+							 gv + (size_t)e * 12, &pl, &pm);
 	if (!moduli) return;
 	// lambda V = V E nu / ((1 + nu)(1 - 2 nu)), mu V = V E / (2 (1 + nu)): d/d log E scales both by
 	// one; nu = lambda / (2 (lambda + mu)).
@@ -144,11 +146,15 @@ inline int blocks_of(long long n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_element_adjoint(const DevBody& b, const double* x, const double* v, const double* mu, const double* dv,
 							double dt, double alpha, double beta, double* gx, double* gv, double* gLogE, double* gNu,
-							cudaStream_t s)
+							cudaStream_t s, bool fp32)
 {
 	if (b.E == 0) return;
-	k_element_adjoint<<<blocks_of(b.E, kAdjThreads), kAdjThreads, 0, s>>>(b, x, v, mu, dv, dt, alpha, beta, gx, gv,
-																		  gLogE, gNu);
+	if (fp32)
+		k_element_adjoint<float><<<blocks_of(b.E, kAdjThreads), kAdjThreads, 0, s>>>(b, x, v, mu, dv, dt, alpha, beta,
+																					 gx, gv, gLogE, gNu);
+	else
+		k_element_adjoint<double><<<blocks_of(b.E, kAdjThreads), kAdjThreads, 0, s>>>(b, x, v, mu, dv, dt, alpha, beta,
+																					  gx, gv, gLogE, gNu);
 }
 
 void launch_adjoint_gather(const DevBody& b, const double* gx, const double* gv, const double* lx, const double* lv,

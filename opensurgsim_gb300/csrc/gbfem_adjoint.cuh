@@ -86,33 +86,39 @@ constexpr int kAdjItems = 11;
 // One item of one element: X, R0, V positions / rest positions / velocities of its nodes, MU and DV
 // the adjoint and the step's velocity increment at its dofs (zero on BC dofs). Writes gx[3 + item]
 // (items 0..8), gv[0..11] (item 9) or *pLam, *pMu (item 10).
+// S is the arithmetic of the passes: double (FP64 form) or float (mixed form, FP32 element math
+// with the corotated strain formed as in its forward step).
+template <typename S = double>
 __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const double (&X)[4][3],
 											 const double (&R0)[4][3], const double (&V)[4][3], const double (&MU)[12],
 											 const double (&DV)[12], const double (&g)[4][3], double lamV, double muV,
 											 double cm, double dt, double alpha, double beta, double* gx, double* gv,
 											 double* pLam, double* pMu)
 {
+	using D = ad::DualT<S>;
 	const double c2 = dt + beta;
 	if (item < 9)
 	{
-		Dual gD[4][3];
+		D gD[4][3];
 		for (int a = 0; a < 4; ++a)
-			for (int k = 0; k < 3; ++k) gD[a][k] = Dual(g[a][k]);
+			for (int k = 0; k < 3; ++k) gD[a][k] = D(g[a][k]);
 		const int s = 3 + item;
-		elem::ElemInT<Dual> in;
+		elem::ElemInT<D> in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3);
-		Dual ks[kSlots * 9], rhs[12];
-		elem::compute<Dual, false, elem::ElemInT<Dual>>(in, gD, Dual(lamV), Dual(muV), Dual(cm), ks, 1, rhs, 1,
-														 nullptr, nullptr);
-		gx[s] = element_psi(nd, ks, rhs, MU, DV, c2).d;
+		D ks[kSlots * 9], rhs[12];
+		elem::compute<D, false, elem::ElemInT<D>>(in, gD, D(lamV), D(muV), D(cm), ks, 1, rhs, 1, nullptr, nullptr);
+		gx[s] = double(element_psi(nd, ks, rhs, MU, DV, c2).d);
 	}
 	else if (item == 9)
 	{
 		// d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (K_e: the full element tangent).
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
-		double ks[kSlots * 9], rhs[12], kfull[144], fdbg[12];
-		elem::compute<double, true>(in, g, lamV, muV, cm, ks, 1, rhs, 1, kfull, fdbg);
+		S gS[4][3], ks[kSlots * 9], rhs[12];
+		double kfull[144], fdbg[12];
+		for (int a = 0; a < 4; ++a)
+			for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
+		elem::compute<S, true>(in, gS, S(lamV), S(muV), S(cm), ks, 1, rhs, 1, kfull, fdbg);
 		double sm[3] = {0, 0, 0};
 		for (int a = 0; a < 4; ++a)
 			for (int k = 0; k < 3; ++k) sm[k] += MU[3 * a + k];
@@ -128,11 +134,13 @@ __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const
 		// psi_e's elastic part is linear in (lambda V, mu V): evaluate it with unit moduli.
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
-		double ks[kSlots * 9], rhs[12];
-		elem::compute<double, false>(in, g, 1.0, 0.0, 0.0, ks, 1, rhs, 1, nullptr, nullptr);
-		*pLam = element_psi(nd, ks, rhs, MU, DV, c2);
-		elem::compute<double, false>(in, g, 0.0, 1.0, 0.0, ks, 1, rhs, 1, nullptr, nullptr);
-		*pMu = element_psi(nd, ks, rhs, MU, DV, c2);
+		S gS[4][3], ks[kSlots * 9], rhs[12];
+		for (int a = 0; a < 4; ++a)
+			for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
+		elem::compute<S, false>(in, gS, S(1), S(0), S(0), ks, 1, rhs, 1, nullptr, nullptr);
+		*pLam = double(element_psi(nd, ks, rhs, MU, DV, c2));
+		elem::compute<S, false>(in, gS, S(0), S(1), S(0), ks, 1, rhs, 1, nullptr, nullptr);
+		*pMu = double(element_psi(nd, ks, rhs, MU, DV, c2));
 	}
 }
 

@@ -75,6 +75,12 @@ struct Eps<Dual>
 	static constexpr double eps = DBL_EPSILON;
 	static constexpr double newtonTol2 = 1e-26;
 };
+template <>
+struct Eps<DualF>
+{
+	static constexpr double eps = FLT_EPSILON;
+	static constexpr double newtonTol2 = 1e-11;
+};
 
 // Polar factor by Newton's iteration X <- (g X + X^-T / g) / 2 (Higham), Frobenius scaling on the
 // first iterations. Valid for det F > 0, where the orthogonal polar factor is the rotation that

@@ -1534,7 +1534,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	}
 	tm.mark(2);
 	launch_element_adjoint(body, x, v, h->d_mu.p, dv, dt, alpha, beta, h->d_gx.p, h->d_gv.p, grad_log_young,
-						   grad_poisson, s);
+						   grad_poisson, s, h->mixed());
 	launch_adjoint_gather(body, h->d_gx.p, h->d_gv.p, lx, lv, dt, lx_out, lv_out, s);
 	tm.mark(3);
 	GB_CUDA(h, cudaGetLastError());

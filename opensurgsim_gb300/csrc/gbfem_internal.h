@@ -147,7 +147,7 @@ void launch_apply_node_rotation(int N, const double* Wn, double* X, bool transpo
 // Differentiation form (gbfem_adjoint.cu).
 void launch_element_adjoint(const DevBody& b, const double* x, const double* v, const double* mu, const double* dv,
 							double dt, double alpha, double beta, double* gx, double* gv, double* gLogE, double* gNu,
-							cudaStream_t s);
+							cudaStream_t s, bool fp32 = false);
 void launch_adjoint_gather(const DevBody& b, const double* gx, const double* gv, const double* lx, const double* lv,
 						   double dt, double* lxOut, double* lvOut, cudaStream_t s);
 void launch_adjoint_rhs(int n, const uint8_t* bc, const double* lx, const double* lv, double dt, double* g,
