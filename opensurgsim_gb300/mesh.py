@@ -80,6 +80,60 @@ def cube_grid(a: int, b: int, c: int, h: float = 0.01, jitter: float = 0.1, seed
     return nodes, tets.reshape(-1, 4).astype(np.int32)
 
 
+# Corner order of one hexahedron (Fem3DElementCube node ids) as DivisibleCubeRepresentation.cpp:134-146
+# builds it: grid offsets (di, dj, dk) = 000, 100, 110, 010, 001, 101, 111, 011 -- one face cycled,
+# then the opposite face cycled the same way, which gives a positive volume.
+HEX_CORNERS = ((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1))
+
+
+def hex_grid(a: int, b: int, c: int, h: float = 0.01, jitter: float = 0.0, seed: int = 0) -> tuple:
+    """Nodes (N,3) and hexahedra (E,8) of an a x b x c grid of cubes of edge h (one Fem3DElementCube
+    per cube, corners in HEX_CORNERS order). Interior nodes are jittered as in ``cube_grid``."""
+    nodes, _ = cube_grid(a, b, c, h=h, jitter=jitter, seed=seed) if jitter > 0 else (None, None)
+    if nodes is None:
+        ii, jj, kk = np.meshgrid(np.arange(a + 1), np.arange(b + 1), np.arange(c + 1), indexing="ij")
+        nodes = np.stack([ii.ravel(), jj.ravel(), kk.ravel()], axis=1).astype(np.float64) * h
+    ci, cj, ck = np.meshgrid(np.arange(a), np.arange(b), np.arange(c), indexing="ij")
+    ci, cj, ck = ci.ravel(), cj.ravel(), ck.ravel()
+    hexes = np.empty((ci.size, 8), dtype=np.int64)
+    for q, (dx, dy, dz) in enumerate(HEX_CORNERS):
+        hexes[:, q] = node_id(ci + dx, cj + dy, ck + dz, b, c)
+    return nodes, hexes.astype(np.int32)
+
+
+def scene_hex_cube(a=10, b=10, c=10, h=0.01, seed=0, jitter=0.0, young=1e5, poisson=0.45, density=1000.0,
+                   **kw) -> Scene:
+    """Hexahedral cube-grid scene with uniform material and the z = 0 face fixed."""
+    nodes, hexes = hex_grid(a, b, c, h=h, jitter=jitter, seed=seed)
+    E = hexes.shape[0]
+    mesh = TetMesh(nodes, hexes, np.full(E, young), np.full(E, poisson), np.full(E, density),
+                   face_dofs(a, b, c, 2, 0), (a, b, c), h)
+    return Scene(mesh=mesh, name=f"hex{a}x{b}x{c}", **kw)
+
+
+def scene_divisible_cube(nodes_per_axis: int, **kw) -> Scene:
+    """OpenSurgSim's performance-test cube (DivisibleCubeRepresentation.cpp:30-157 with
+    Fem3DPerformanceTest.cpp:187-205): nodes_per_axis^3 nodes spanning [-n, n]^3 (n = nodes per axis),
+    one hexahedron per grid cell, rho = 980, nu = 0.499, E = 15.3e3, nodes 0, 1 and 2 fixed. Gravity and
+    damping keep the representation defaults (gravity (0, -9.81, 0), no Rayleigh damping)."""
+    n = int(nodes_per_axis)
+    if n < 2:
+        raise ValueError("a divisible cube needs at least 2 nodes per axis")
+    cells = n - 1
+    nodes, hexes = hex_grid(cells, cells, cells, h=2.0 * n / cells)
+    nodes -= float(n)
+    E = hexes.shape[0]
+    mesh = TetMesh(nodes, hexes, np.full(E, 15.3e3), np.full(E, 0.499), np.full(E, 980.0),
+                   np.arange(9, dtype=np.int32), (cells, cells, cells), 2.0 * n / cells)
+    kw.setdefault("rayleigh_mass", 0.0)
+    kw.setdefault("rayleigh_stiffness", 0.0)
+    kw.setdefault("gravity", (0.0, -9.81, 0.0))
+    kw.setdefault("cg_tolerance", 1e-3)
+    kw.setdefault("cg_max_iterations", max(1, int(0.1 * 3 * n ** 3)))
+    kw.setdefault("steps", 10)
+    return Scene(mesh=mesh, name=f"divisiblecube{n}", **kw)
+
+
 def signed_volumes(nodes: np.ndarray, tets: np.ndarray) -> np.ndarray:
     p = nodes[tets]
     ab, ac, ad = p[:, 1] - p[:, 0], p[:, 2] - p[:, 0], p[:, 3] - p[:, 0]

@@ -538,6 +538,163 @@ int tetInitialize(Tet& t, const double* X)
 }
 
 // ---------------------------------------------------------------------------------------------
+// Element: Fem3DElementCube (trilinear hexahedron, 2x2x2 Gauss-Legendre quadrature). A linear
+// element: K and M are computed once at the rest state, f = -K (x - x0) (:129-141).
+// ---------------------------------------------------------------------------------------------
+struct Hex
+{
+	int n[8];
+	double E, nu, rho;
+	double x0[24];
+	double K0[24][24], M0[24][24];
+	double f[24];
+	double volume = 0.0;
+};
+
+// Shape-function signs of the 8 corners (Fem3DElementCube.cpp:72-74).
+const double kHexSignEps[8] = {-1.0, +1.0, +1.0, -1.0, -1.0, +1.0, +1.0, -1.0};
+const double kHexSignEta[8] = {-1.0, -1.0, +1.0, +1.0, -1.0, -1.0, +1.0, +1.0};
+const double kHexSignMu[8] = {-1.0, -1.0, -1.0, -1.0, +1.0, +1.0, +1.0, +1.0};
+
+// gaussQuadrature2Points (GaussLegendreQuadrature.cpp:30-34): +1/sqrt(3) then -1/sqrt(3), weight 1.
+double gaussPoint2(int i) { return (i == 0 ? 1.0 : -1.0) / std::sqrt(3.0); }
+
+// shapeFunction and its derivatives (Fem3DElementCube.cpp:368-398).
+double hexN(int i, double e, double h, double m)
+{
+	return 1.0 / 8.0 * (1 + e * kHexSignEps[i]) * (1 + h * kHexSignEta[i]) * (1 + m * kHexSignMu[i]);
+}
+double hexdNde(int i, double, double h, double m)
+{
+	return 1.0 / 8.0 * kHexSignEps[i] * (1 + h * kHexSignEta[i]) * (1 + m * kHexSignMu[i]);
+}
+double hexdNdh(int i, double e, double, double m)
+{
+	return 1.0 / 8.0 * (1 + e * kHexSignEps[i]) * kHexSignEta[i] * (1 + m * kHexSignMu[i]);
+}
+double hexdNdm(int i, double e, double h, double)
+{
+	return 1.0 / 8.0 * (1 + e * kHexSignEps[i]) * (1 + h * kHexSignEta[i]) * kHexSignMu[i];
+}
+
+// evaluateJ (Fem3DElementCube.cpp:169-211): J(r, axis) = sum_i p_i[axis] dN_i/d(eps, eta, mu)_r.
+// Returns false when J is not invertible (|det J| <= 1e-12, the SURGSIM_ASSERT of :202-207).
+bool hexJacobian(const double* p /*24*/, double e, double h, double m, double Jinv[3][3], double* detJ)
+{
+	double J[3][3] = {};
+	for (int i = 0; i < 8; ++i)
+		for (int axis = 0; axis < 3; ++axis)
+		{
+			J[0][axis] += p[3 * i + axis] * hexdNde(i, e, h, m);
+			J[1][axis] += p[3 * i + axis] * hexdNdh(i, e, h, m);
+			J[2][axis] += p[3 * i + axis] * hexdNdm(i, e, h, m);
+		}
+	*detJ = det33(J);
+	return inverse33(J, Jinv);
+}
+
+// getVolume (Fem3DElementCube.cpp:321-366): sum of w_i w_j w_k det J over the 8 Gauss points.
+// Returns ORC_DEGENERATE when a Jacobian is singular or the volume is not above 1e-12 (:357).
+int hexVolume(const double* p, double* vol)
+{
+	double v = 0.0;
+	for (int i = 0; i < 2; ++i)
+		for (int j = 0; j < 2; ++j)
+			for (int k = 0; k < 2; ++k)
+			{
+				double Jinv[3][3], detJ;
+				if (!hexJacobian(p, gaussPoint2(i), gaussPoint2(j), gaussPoint2(k), Jinv, &detJ)) return ORC_DEGENERATE;
+				v += 1.0 * 1.0 * 1.0 * detJ;
+			}
+	*vol = v;
+	return v > 1e-12 ? ORC_OK : ORC_DEGENERATE;
+}
+
+// Fem3DElementCube::initialize (Fem3DElementCube.cpp:65-95): material checks, rest positions, rest
+// volume, then computeMass (:97-127, addMassMatrixAtPoint :290-319) and computeStiffness (:143-167,
+// evaluateStrainDisplacement :213-251, buildConstitutiveMaterialMatrix :253-265,
+// addStrainStressStiffnessAtPoint :267-288).
+int hexInitialize(Hex& t, const double* X)
+{
+	if (!(t.rho > 0.0) || !(t.nu > 0.0 && t.nu < 0.5) || !(t.E > 0.0)) return ORC_INVALID_ARG;
+	for (int a = 0; a < 8; ++a)
+		for (int k = 0; k < 3; ++k) t.x0[3 * a + k] = X[3 * (size_t)t.n[a] + k];
+	int st = hexVolume(t.x0, &t.volume);
+	if (st != ORC_OK) return st;
+	const double lambda = t.E * t.nu / ((1.0 + t.nu) * (1.0 - 2.0 * t.nu));
+	const double mu = t.E / (2.0 * (1 + t.nu));
+	double C[6][6] = {};
+	C[0][0] = C[1][1] = C[2][2] = 2.0 * mu + lambda;
+	C[0][1] = C[0][2] = C[1][0] = C[1][2] = C[2][0] = C[2][1] = lambda;
+	C[3][3] = C[4][4] = C[5][5] = mu;
+	std::memset(t.M0, 0, sizeof(t.M0));
+	std::memset(t.K0, 0, sizeof(t.K0));
+	for (int gi = 0; gi < 2; ++gi)
+		for (int gj = 0; gj < 2; ++gj)
+			for (int gk = 0; gk < 2; ++gk)
+			{
+				const double e = gaussPoint2(gi), h = gaussPoint2(gj), m = gaussPoint2(gk);
+				double Jinv[3][3], detJ;
+				if (!hexJacobian(t.x0, e, h, m, Jinv, &detJ)) return ORC_DEGENERATE;
+				const double w = 1.0 * 1.0 * 1.0 * detJ;
+				// M += w rho phi^T phi, phi = (N_i I3) side by side.
+				double N[8];
+				for (int i = 0; i < 8; ++i) N[i] = hexN(i, e, h, m);
+				for (int a = 0; a < 8; ++a)
+					for (int b = 0; b < 8; ++b)
+						for (int k = 0; k < 3; ++k) t.M0[3 * a + k][3 * b + k] += (w * t.rho) * (N[a] * N[b]);
+				// B (6x24): dN_i/d(x,y,z) = J^-1 dN_i/d(eps,eta,mu), Voigt rows xx yy zz xy yz zx.
+				double B[6][24] = {};
+				for (int i = 0; i < 8; ++i)
+				{
+					const double dl[3] = {hexdNde(i, e, h, m), hexdNdh(i, e, h, m), hexdNdm(i, e, h, m)};
+					double g[3];
+					for (int r = 0; r < 3; ++r) g[r] = Jinv[r][0] * dl[0] + Jinv[r][1] * dl[1] + Jinv[r][2] * dl[2];
+					B[0][3 * i] = g[0];
+					B[1][3 * i + 1] = g[1];
+					B[2][3 * i + 2] = g[2];
+					B[3][3 * i] = g[1];
+					B[3][3 * i + 1] = g[0];
+					B[4][3 * i + 1] = g[2];
+					B[4][3 * i + 2] = g[1];
+					B[5][3 * i] = g[2];
+					B[5][3 * i + 2] = g[0];
+				}
+				// K += (w B^T) C B, evaluated left to right.
+				double BtC[24][6];
+				for (int r = 0; r < 24; ++r)
+					for (int c = 0; c < 6; ++c)
+					{
+						double s = 0;
+						for (int l = 0; l < 6; ++l) s += (w * B[l][r]) * C[l][c];
+						BtC[r][c] = s;
+					}
+				for (int r = 0; r < 24; ++r)
+					for (int c = 0; c < 24; ++c)
+					{
+						double s = 0;
+						for (int l = 0; l < 6; ++l) s += BtC[r][l] * B[l][c];
+						t.K0[r][c] += s;
+					}
+			}
+	return ORC_OK;
+}
+
+// doUpdateFMDK (Fem3DElementCube.cpp:129-141): f = -K (x - x0); M and K stay the rest matrices.
+void hexUpdateF(Hex& t, const double* X)
+{
+	double u[24];
+	for (int a = 0; a < 8; ++a)
+		for (int k = 0; k < 3; ++k) u[3 * a + k] = X[3 * (size_t)t.n[a] + k] - t.x0[3 * a + k];
+	for (int r = 0; r < 24; ++r)
+	{
+		double s = 0;
+		for (int c = 0; c < 24; ++c) s += t.K0[r][c] * u[c];
+		t.f[r] = -s;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
 // CSC matrix helpers (Eigen::SparseMatrix<double, ColMajor, int> semantics).
 // ---------------------------------------------------------------------------------------------
 struct Pattern
@@ -773,15 +930,17 @@ struct ImplicitEuler
 };
 
 // ---------------------------------------------------------------------------------------------
-// FemRepresentation / Fem3DRepresentation with corotational tetrahedra.
+// FemRepresentation / Fem3DRepresentation with corotational or linear tetrahedra, or hexahedra.
 // ---------------------------------------------------------------------------------------------
 struct FemModel : Equation
 {
 	int numNodes = 0;
 	vector<double> xrest;
+	bool hex = false;     // Fem3DElementCube elements in `hexes` instead of tetrahedra in `tets`
 	vector<Tet> tets;
+	vector<Hex> hexes;
 	vector<double> massPerNode;
-	vector<int> scatter;  // E*144: CSC slot of element entry (3a+i, 3b+j)
+	vector<int> scatter;  // per element (3 npe)^2: CSC slot of element entry (3a+i, 3b+j)
 	double alpha = 0, beta = 0;          // Rayleigh mass / stiffness coefficients
 	double gravity[3] = {0.0, -9.81, 0.0};  // Representation.cpp:36
 	bool gravityEnabled = true;
@@ -791,17 +950,29 @@ struct FemModel : Equation
 	ImplicitEuler solver;
 	int singularGCount = 0, invalidRotationCount = 0, orientationWarnings = 0;
 
+	int nodesPerElement() const { return hex ? 8 : 4; }
+	size_t numElements() const { return hex ? hexes.size() : tets.size(); }
+	const int* elementNodes(size_t e) const { return hex ? hexes[e].n : tets[e].n; }
+
 	// FemRepresentation::doInitialize (FemRepresentation.cpp:85-132) on the rest state.
 	int initialize()
 	{
 		const int n = 3 * numNodes;
+		const int npe = nodesPerElement(), Dm = 3 * npe;
+		const size_t E = numElements();
+		for (size_t e = 0; e < E; ++e)
+			for (int a = 0; a < npe; ++a)
+				if (elementNodes(e)[a] < 0 || elementNodes(e)[a] >= numNodes) return ORC_INVALID_ARG;
 		for (auto& t : tets)
 		{
-			for (int a = 0; a < 4; ++a)
-				if (t.n[a] < 0 || t.n[a] >= numNodes) return ORC_INVALID_ARG;
 			int st = tetInitialize(t, xrest.data());
 			if (st != ORC_OK) return st;
 			orientationWarnings += t.orientationWarning;
+		}
+		for (auto& t : hexes)
+		{
+			int st = hexInitialize(t, xrest.data());
+			if (st != ORC_OK) return st;
 		}
 		// massPerNode += getMass / numNodes (:108-117), getMass = volume * rho (FemElement.cpp:105-108).
 		massPerNode.assign(numNodes, 0.0);
@@ -810,11 +981,19 @@ struct FemModel : Equation
 			double mass = tetVolume(&xrest[3 * t.n[0]], &xrest[3 * t.n[1]], &xrest[3 * t.n[2]], &xrest[3 * t.n[3]]) * t.rho;
 			for (int a = 0; a < 4; ++a) massPerNode[t.n[a]] += mass / 4;
 		}
+		for (auto& t : hexes)
+		{
+			double mass = t.volume * t.rho;
+			for (int a = 0; a < 8; ++a) massPerNode[t.n[a]] += mass / 8;
+		}
 		// Sparsity: union of the 3x3 node blocks of every element, rows sorted per column (:121-132).
 		vector<vector<int>> adj(numNodes);
-		for (auto& t : tets)
-			for (int a = 0; a < 4; ++a)
-				for (int b = 0; b < 4; ++b) adj[t.n[b]].push_back(t.n[a]);
+		for (size_t e = 0; e < E; ++e)
+		{
+			const int* nd = elementNodes(e);
+			for (int a = 0; a < npe; ++a)
+				for (int b = 0; b < npe; ++b) adj[nd[b]].push_back(nd[a]);
+		}
 		for (auto& l : adj)
 		{
 			std::sort(l.begin(), l.end());
@@ -835,21 +1014,21 @@ struct FemModel : Equation
 			}
 		// Scatter map: SparseMatrix.h blockWithSearch (:178-242) resolved once per element entry. The
 		// first row of block (n_a, n_b) in column 3 n_b + j sits at 3 * (position of n_a in adj[n_b]).
-		scatter.resize(tets.size() * 144);
-		for (size_t e = 0; e < tets.size(); ++e)
+		scatter.resize(E * Dm * Dm);
+		for (size_t e = 0; e < E; ++e)
 		{
-			const Tet& t = tets[e];
-			for (int b = 0; b < 4; ++b)
+			const int* nd = elementNodes(e);
+			for (int b = 0; b < npe; ++b)
 			{
-				const vector<int>& col = adj[t.n[b]];
-				for (int a = 0; a < 4; ++a)
+				const vector<int>& col = adj[nd[b]];
+				for (int a = 0; a < npe; ++a)
 				{
-					int pos = (int)(std::lower_bound(col.begin(), col.end(), t.n[a]) - col.begin());
+					int pos = (int)(std::lower_bound(col.begin(), col.end(), nd[a]) - col.begin());
 					for (int j = 0; j < 3; ++j)
 					{
-						int64_t first = pat.colptr[3 * t.n[b] + j] + 3 * pos;
+						int64_t first = pat.colptr[3 * nd[b] + j] + 3 * pos;
 						for (int i = 0; i < 3; ++i)
-							scatter[e * 144 + (3 * a + i) * 12 + 3 * b + j] = (int)(first + i);
+							scatter[e * Dm * Dm + (3 * a + i) * Dm + 3 * b + j] = (int)(first + i);
 					}
 				}
 			}
@@ -873,21 +1052,26 @@ struct FemModel : Equation
 			singularGCount += t.singularG - sg;
 			invalidRotationCount += t.invalidRotation - ir;
 		}
+		for (auto& t : hexes) hexUpdateF(t, X);
 		const int n = pat.n;
 		std::fill(f.begin(), f.end(), 0.0);
 		std::fill(M.begin(), M.end(), 0.0);
 		std::fill(D.begin(), D.end(), 0.0);
 		std::fill(K.begin(), K.end(), 0.0);
-		for (size_t e = 0; e < tets.size(); ++e)  // FemElement::addFMDK (FemElement.cpp:157-166)
+		const int npe = nodesPerElement(), Dm = 3 * npe;
+		for (size_t e = 0; e < numElements(); ++e)  // FemElement::addFMDK (FemElement.cpp:157-166)
 		{
-			const Tet& t = tets[e];
-			for (int a = 0; a < 4; ++a)
-				for (int i = 0; i < 3; ++i) f[3 * t.n[a] + i] += t.f[3 * a + i];
-			const int* s = &scatter[e * 144];
-			for (int r = 0; r < 12; ++r)
-				for (int c = 0; c < 12; ++c) M[s[r * 12 + c]] += t.M[r][c];
-			for (int r = 0; r < 12; ++r)
-				for (int c = 0; c < 12; ++c) K[s[r * 12 + c]] += t.K[r][c];
+			const int* nd = elementNodes(e);
+			const double* fe = hex ? hexes[e].f : tets[e].f;
+			const double* Me = hex ? &hexes[e].M0[0][0] : &tets[e].M[0][0];
+			const double* Ke = hex ? &hexes[e].K0[0][0] : &tets[e].K[0][0];
+			for (int a = 0; a < npe; ++a)
+				for (int i = 0; i < 3; ++i) f[3 * nd[a] + i] += fe[3 * a + i];
+			const int* s = &scatter[e * Dm * Dm];
+			for (int r = 0; r < Dm; ++r)
+				for (int c = 0; c < Dm; ++c) M[s[r * Dm + c]] += Me[r * Dm + c];
+			for (int r = 0; r < Dm; ++r)
+				for (int c = 0; c < Dm; ++c) K[s[r * Dm + c]] += Ke[r * Dm + c];
 		}
 		const int64_t nnz = pat.nnz();
 		if (alpha != 0.0)
@@ -1056,7 +1240,7 @@ struct orc_params
 	double newton_epsilon;
 	double cg_tolerance;
 	int32_t cg_max_iterations;  // <= 0: Eigen default 2n
-	int32_t element_type;       // 0: corotational tetrahedron, 1: linear tetrahedron
+	int32_t element_type;       // 0: corotational tetrahedron, 1: linear tetrahedron, 2: hexahedron
 };
 
 struct orc_stats
@@ -1081,16 +1265,36 @@ void* orc_create(int32_t numNodes, const double* x, int32_t numTets, const int32
 		*status = ORC_INVALID_ARG;
 		return nullptr;
 	}
+	if (prm->element_type < 0 || prm->element_type > 2)
+	{
+		*status = ORC_INVALID_ARG;
+		return nullptr;
+	}
 	m->numNodes = numNodes;
 	m->xrest.assign(x, x + 3 * (size_t)numNodes);
-	m->tets.resize(numTets);
-	for (int e = 0; e < numTets; ++e)
+	m->hex = prm->element_type == 2;
+	if (m->hex)
 	{
-		for (int a = 0; a < 4; ++a) m->tets[e].n[a] = tets[4 * e + a];
-		m->tets[e].E = E[e];
-		m->tets[e].nu = nu[e];
-		m->tets[e].rho = rho[e];
-		m->tets[e].linear = prm->element_type == 1;
+		m->hexes.resize(numTets);
+		for (int e = 0; e < numTets; ++e)
+		{
+			for (int a = 0; a < 8; ++a) m->hexes[e].n[a] = tets[8 * (size_t)e + a];
+			m->hexes[e].E = E[e];
+			m->hexes[e].nu = nu[e];
+			m->hexes[e].rho = rho[e];
+		}
+	}
+	else
+	{
+		m->tets.resize(numTets);
+		for (int e = 0; e < numTets; ++e)
+		{
+			for (int a = 0; a < 4; ++a) m->tets[e].n[a] = tets[4 * e + a];
+			m->tets[e].E = E[e];
+			m->tets[e].nu = nu[e];
+			m->tets[e].rho = rho[e];
+			m->tets[e].linear = prm->element_type == 1;
+		}
 	}
 	std::vector<char> seen(3 * (size_t)numNodes, 0);
 	for (int i = 0; i < numBc; ++i)
@@ -1205,6 +1409,7 @@ void orc_get_mass_per_node(void* h, double* out)
 void orc_get_element(void* h, int32_t e, double* R9, double* K144, double* M144, double* f12)
 {
 	auto* m = static_cast<FemModel*>(h);
+	if (e < 0 || (size_t)e >= m->tets.size()) return;  // tetrahedra only
 	const Tet& t = m->tets[e];
 	if (R9) std::memcpy(R9, t.R, sizeof(t.R));
 	if (K144) std::memcpy(K144, t.K, sizeof(t.K));
@@ -1238,6 +1443,38 @@ int32_t orc_tet_compute(const double* x0, const double* x, double E, double nu, 
 	return ORC_OK;
 }
 
+// Single hexahedron for the element unit tests: rest positions x0 (24), current x (24). Outputs the
+// rest volume, K (576), M (576) and f = -K (x - x0) (24); ORC_DEGENERATE as Fem3DElementCube asserts.
+int32_t orc_hex_compute(const double* x0, const double* x, double E, double nu, double rho, double* vol, double* K,
+						double* M, double* f)
+{
+	Hex t;
+	for (int a = 0; a < 8; ++a) t.n[a] = a;
+	t.E = E;
+	t.nu = nu;
+	t.rho = rho;
+	int st = hexInitialize(t, x0);
+	if (st != ORC_OK) return st;
+	if (vol) *vol = t.volume;
+	if (K) std::memcpy(K, t.K0, sizeof(t.K0));
+	if (M) std::memcpy(M, t.M0, sizeof(t.M0));
+	if (x && f)
+	{
+		hexUpdateF(t, x);
+		std::memcpy(f, t.f, sizeof(t.f));
+	}
+	return ORC_OK;
+}
+
+// Shape function i and its three natural derivatives at (eps, eta, mu).
+void orc_hex_shape(int32_t i, double e, double h, double m, double* out4)
+{
+	out4[0] = hexN(i, e, h, m);
+	out4[1] = hexdNde(i, e, h, m);
+	out4[2] = hexdNdh(i, e, h, m);
+	out4[3] = hexdNdm(i, e, h, m);
+}
+
 void orc_polar(const double* F9, double* R9, double* S9)
 {
 	double F[3][3], R[3][3], S[3][3];
@@ -1258,6 +1495,7 @@ int32_t orc_apply_compliance(void* h, int32_t ncols, const double* b, double* x,
 	auto* m = static_cast<FemModel*>(h);
 	const int n = m->pat.n, N = n / 3;
 	if (ncols < 0 || (ncols > 0 && (!b || !x)) || m->solver.S.empty()) return ORC_INVALID_ARG;
+	if (warping && m->hex) return ORC_INVALID_ARG;  // warping rotations are the corotational tetrahedra's
 	vector<double> W;
 	if (warping)
 	{

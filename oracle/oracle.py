@@ -83,6 +83,9 @@ def lib():
         L.orc_tet_compute.argtypes = [D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, D, D,
                                       D, D, I32]
         L.orc_polar.argtypes = [D, D, D]
+        L.orc_hex_compute.restype = ctypes.c_int32
+        L.orc_hex_compute.argtypes = [D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D]
+        L.orc_hex_shape.argtypes = [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, D]
         L.orc_apply_compliance.restype = ctypes.c_int32
         L.orc_apply_compliance.argtypes = [ctypes.c_void_p, ctypes.c_int32, D, D, ctypes.c_int32, I32]
         L.orc_cg_solve.restype = ctypes.c_int32
@@ -112,7 +115,8 @@ class OracleError(RuntimeError):
 class OracleModel:
     """An OpenSurgSim-style Fem3DRepresentation (corotational or linear tets, implicit Euler, CG) on
     the CPU. element_type 1 selects Fem3DElementTetrahedron; its linear implicit Euler
-    (OdeSolverLinearEulerImplicit) takes the same steps, the system matrix being constant."""
+    (OdeSolverLinearEulerImplicit) takes the same steps, the system matrix being constant.
+    element_type 2 selects Fem3DElementCube: ``mesh.tets`` then holds 8 node ids per element."""
 
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5, cg_tolerance=1e-10,
@@ -234,6 +238,28 @@ def tet_compute(x0, x, E, nu, rho):
                vol=float(out["vol"][0]), R=out["R"].reshape(3, 3), K=out["K"].reshape(12, 12),
                M=out["M"].reshape(12, 12), f=out["f"], orientation_warning=bool(ow.value))
     return res
+
+
+def hex_compute(x0, x, E, nu, rho):
+    """One Fem3DElementCube: rest volume, K (24x24), M (24x24) and f = -K (x - x0). Raises
+    OracleError(2) where the reference's initialize asserts (singular Jacobian, volume <= 1e-12)."""
+    x0 = np.ascontiguousarray(x0, dtype=np.float64).ravel()
+    x = np.ascontiguousarray(x if x is not None else x0, dtype=np.float64).ravel()
+    vol = np.zeros(1)
+    K = np.zeros((24, 24))
+    M = np.zeros((24, 24))
+    f = np.zeros(24)
+    st = lib().orc_hex_compute(_d(x0), _d(x), E, nu, rho, _d(vol), _d(K), _d(M), _d(f))
+    if st != 0:
+        raise OracleError(st, "hexahedron initialize failed")
+    return dict(volume=float(vol[0]), K=K, M=M, f=f)
+
+
+def hex_shape(i, eps, eta, mu):
+    """(N_i, dN_i/deps, dN_i/deta, dN_i/dmu) of Fem3DElementCube at a natural coordinate."""
+    out = np.zeros(4)
+    lib().orc_hex_shape(i, eps, eta, mu, _d(out))
+    return out
 
 
 def polar(F):
