@@ -10,11 +10,12 @@ FemRepresentation::update(dt) of every mesh. The measured form is the batched mi
 same meshes are also stepped through the plain FP64 GPU path one mesh at a time, and the line
 carries that path's throughput, the speed-up over it and the mixed-vs-FP64 displacement error.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config batch|bar|cube]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config batch|bar|cube|hex]
                     [--precision fp64|mixed] [--impl reference]
 
 --config bar is the 40x40x160 compression bar (h 4 mm, 1.28M tets), --config cube the 10x10x10 cube
-(5,000 tets); both take --precision. Inputs are synthetic (seeded). One JSON line on rank 0. Under
+(5,000 tets), --config hex the reference's own performance-test model (DivisibleCubeRepresentation,
+Fem3DElementCube hexahedra) at 64 nodes per axis (250,047 hexahedra); all three take --precision. Inputs are synthetic (seeded). One JSON line on rank 0. Under
 torchrun the batch's meshes shard over the ranks by greedy bin-packing (one GPU each, no data-path
 collective; strong scaling: the job value is all meshes' tet-steps over the slowest rank's time); the
 single-mesh workloads run one replica per rank (weak scaling).
@@ -37,6 +38,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "tet-element-steps/s, mixed+batched vs plain FP64 GPU path at <=1e-6 rel disp err"
 UNIT = "tet-element-steps/s"
+HEX_METRIC = "hex-element-steps/s (Fem3DElementCube, the reference's DivisibleCube performance-test model)"
+HEX_UNIT = "hex-element-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 CG_CAP = 10000
@@ -373,9 +376,17 @@ def run_batch(args, rank, world, local, dist):
 # ------------------------------------------------------------------------------------------------
 # Single-mesh workloads (bar, cube)
 
+HEX_NODES_PER_AXIS = 64  # --config hex: 63^3 = 250,047 hexahedra, 262,144 nodes
+
+
 def build_scene(config):
     from opensurgsim_gb300 import mesh
 
+    if config == "hex":
+        # The reference's own performance-test model (DivisibleCubeRepresentation + Fem3DPerformanceTest:
+        # rho 980, nu 0.499, E 15.3e3, nodes 0-2 fixed, CG tolerance 1e-3, maxIter 0.1 n, dt 1e-3, 10
+        # frames), scaled from its 2..8 nodes per axis to 64.
+        return mesh.scene_divisible_cube(HEX_NODES_PER_AXIS)
     # The explicit CG iteration cap only bounds the run if a solve ever stagnates; at the
     # benchmark's states CG converges in a few hundred iterations, far below it.
     if config == "bar":
@@ -445,6 +456,7 @@ def run_single(args, rank, world, local, dist):
     log(f"timed region: {args.steps} steps in {ms:.1f} ms")
     ms_max = dist.reduce(ms, "max")
     total_units = dist.reduce(m.num_tets * args.steps, "sum")
+    metric, unit = (HEX_METRIC, HEX_UNIT) if args.config == "hex" else (METRIC, UNIT)
     value = total_units / (ms_max / 1e3)
 
     # End to end through the public API with host buffers: prescribed velocities copied in from
@@ -466,6 +478,14 @@ def run_single(args, rank, world, local, dist):
     torch.cuda.synchronize(local)
     e2e_s = dist.reduce(time.perf_counter() - t0, "max")
     e2e_value = total_units / e2e_s
+    workload = {
+        "bar": ("bar40x40x160 (h 4 mm) 20% compression ramp: 1,280,000 tets, 270,641 nodes, "
+                "nnz 30,865,689, E log-U[1e4,1e6], nu U[0.40,0.49], gravity, dt 1e-3, CG tol 1e-10"),
+        "cube": "cube10x10x10: 5,000 tets, E 1e5, nu 0.45",
+        "hex": (f"divisiblecube{HEX_NODES_PER_AXIS} (Fem3DElementCube): {m.num_tets:,} hexahedra, {m.num_nodes:,} "
+                "nodes, rho 980, nu 0.499, E 15.3e3, nodes 0-2 fixed, gravity (0,-9.81,0), no damping, dt 1e-3, "
+                "CG tol 1e-3, maxIter 0.1 n"),
+    }[args.config]
     h2d = (scene.driven_dofs.size * (4 + 8)) if driven else 0
     d2h = 2 * body.n * 8
     peak, peak_kind = load_peak()
@@ -487,9 +507,9 @@ def run_single(args, rank, world, local, dist):
         model = "CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*n) + refreshes x (nnz*4 + nnz/9*4 + 4(N+1) + 3*8*n) + 16n"
     achieved = per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else None
     line = {
-        "metric": METRIC,
+        "metric": metric,
         "value": value,
-        "unit": UNIT,
+        "unit": unit,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -500,12 +520,10 @@ def run_single(args, rank, world, local, dist):
         "dtype": "f64" if prec == _lib.PRECISION_FP64 else "f32+f64",
         "data": "synthetic (seeded cube-grid meshes)",
         "config": {
-            "workload": ("bar40x40x160 (h 4 mm) 20% compression ramp: 1,280,000 tets, 270,641 nodes, "
-                         "nnz 30,865,689, E log-U[1e4,1e6], nu U[0.40,0.49], gravity, dt 1e-3, CG tol 1e-10"
-                         if args.config == "bar" else "cube10x10x10: 5,000 tets, E 1e5, nu 0.45"),
-            "tets": m.num_tets, "nodes": m.num_nodes, "dofs": body.n, "nnz": body.nnz,
+            "workload": workload,
+            "elements": m.num_tets, "nodes": m.num_nodes, "dofs": body.n, "nnz": body.nnz,
             "precision": args.precision, "scenario_steps": [args.warmup, args.warmup + args.steps],
-            "l2": "working set larger than L2 (no flush needed)" if args.config == "bar" else
+            "l2": "working set larger than L2 (no flush needed)" if args.config in ("bar", "hex") else
                   "working set L2-resident (small case)",
             "parallelism": f"replicas x{world}",
         },
@@ -513,7 +531,7 @@ def run_single(args, rank, world, local, dist):
         "cg_iterations_per_step": cg_per_step,
         "step_status": sorted(set(int(s) for s in statuses)),
         "clocks": clocks,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {
             "kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": load_traffic(key),
@@ -854,14 +872,15 @@ def run_reference(args, rank, world):
                   "restatement, -O3, 1 thread (a representation is single-threaded)")
         cores, workload = 1, args.config
         ms = 1e3 * sum(times) / len(times)
+    metric, unit = (HEX_METRIC, HEX_UNIT) if args.config == "hex" else (METRIC, UNIT)
     return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(times),
+        "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": len(times),
         "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cube-grid meshes)",
         "config": {"workload": workload, "precision": "fp64"},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
@@ -871,7 +890,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube", "adjoint", "adjoint-batch"])
+    ap.add_argument("--config", default="batch", choices=["batch", "bar", "cube", "hex", "adjoint", "adjoint-batch"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="bar and cube only; the batch is always mixed precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -918,7 +937,7 @@ def main():
                                f"{threads} host threads; oracle FP64 C++ restatement, -O3")}
             else:
                 v, t = cpu_single_steps(scene, 1)
-                line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                line["cpu_baseline"] = {"value": v, "unit": line["unit"], "cores": 1, "kind": "port",
                                         "sample": f"1 step of the same scene on the host ({t:.1f} s), oracle FP64 "
                                                   "C++ restatement, -O3, 1 thread"}
             log(f"cpu baseline: {v / 1e3:.1f} k tet-steps/s")

@@ -63,8 +63,8 @@ typedef struct gbfem_mesh_desc
 {
 	int32_t num_nodes;
 	const double* rest_positions;   /* [3 * num_nodes], node-major x,y,z */
-	int32_t num_tets;
-	const int32_t* tets;            /* [4 * num_tets] node ids */
+	int32_t num_tets;               /* elements (tetrahedra, or hexahedra for GBFEM_ELEMENT_HEXAHEDRON) */
+	const int32_t* tets;            /* [4 * num_tets] node ids; [8 * num_tets] for hexahedra */
 	const double* young_modulus;    /* [num_tets] */
 	const double* poisson_ratio;    /* [num_tets] */
 	const double* mass_density;     /* [num_tets] */
@@ -85,7 +85,7 @@ typedef struct gbfem_params
 	int32_t precision;              /* gbfem_precision */
 	int32_t device;                 /* CUDA device ordinal */
 	int32_t autotune;               /* mixed form: tune block sizes and the solve schedule on the first step */
-	int32_t element_type;           /* GBFEM_ELEMENT_COROTATIONAL_TET (default) or GBFEM_ELEMENT_LINEAR_TET */
+	int32_t element_type;           /* GBFEM_ELEMENT_COROTATIONAL_TET (default), _LINEAR_TET or _HEXAHEDRON */
 	int32_t reserved[5];
 } gbfem_params;
 
@@ -116,9 +116,19 @@ typedef struct gbfem_stats
  *                    (OdeSolverLinearEulerImplicit.cpp:43-64): the first step assembles and solves the
  *                    full system; later steps (same dt and materials) update only the right-hand side
  *                    and solve with the stored system matrix. The dense compliance matrix the reference
- *                    forms on the first step is not formed (every solve is a CG solve). */
+ *                    forms on the first step is not formed (every solve is a CG solve).
+ *  HEXAHEDRON:       Fem3DElementCube (Fem3DElementCube.cpp:65-141): 8 nodes per element in the order
+ *                    of its shape-function signs (eps, eta, mu) = (-,-,-) (+,-,-) (+,+,-) (-,+,-)
+ *                    (-,-,+) (+,-,+) (+,+,+) (-,+,+); K and M by 2x2x2 Gauss-Legendre quadrature at the
+ *                    rest state, f = -K (x - x0). A linear element: K and M are computed and assembled
+ *                    once on the device, S = (1/dt + alpha) M + (dt + beta) K is formed again only when dt
+ *                    or a material changes, and each step forms its right-hand side in one pass over the
+ *                    stored K and M. gbfem_create fails with GBFEM_DEGENERATE_ELEMENT where the
+ *                    reference's initialize asserts (a Jacobian with |det| <= 1e-12 at a Gauss point, or a
+ *                    rest volume <= 1e-12). */
 #define GBFEM_ELEMENT_COROTATIONAL_TET 0
 #define GBFEM_ELEMENT_LINEAR_TET 1
+#define GBFEM_ELEMENT_HEXAHEDRON 2
 
 /* Flags for gbfem_step. */
 #define GBFEM_STEP_TIME_PHASES 1u   /* record per-phase device times (adds events) */
@@ -229,8 +239,9 @@ GBFEM_API gbfem_status gbfem_get_sizes(gbfem_handle h, int64_t* num_dofs, int64_
 /* Global pattern in CSC (Eigen ColMajor, int StorageIndex): colptr[n+1], rowidx[nnz], rows sorted.
  * The pattern is structurally symmetric, so these are also the CSR arrays. */
 GBFEM_API gbfem_status gbfem_get_pattern(gbfem_handle h, int32_t* colptr, int32_t* rowidx);
-/* Element-to-nonzero map: map[e*144 + (3a+i)*12 + 3b+j] = CSC slot of global entry
- * (3*tet[e][a]+i, 3*tet[e][b]+j) -- the slots FemElement::assembleMatrixBlocksNoInitialize writes. */
+/* Element-to-nonzero map: map[e*D*D + (3a+i)*D + 3b+j] = CSC slot of global entry
+ * (3*tet[e][a]+i, 3*tet[e][b]+j) -- the slots FemElement::assembleMatrixBlocksNoInitialize writes;
+ * D = 12 for tetrahedra, 24 for hexahedra. */
 GBFEM_API gbfem_status gbfem_get_scatter(gbfem_handle h, int32_t* map);
 /* System of the last solve (requires GBFEM_STEP_KEEP_SYSTEM on that step): S values in CSC order
  * with boundary conditions applied (full, not mirrored), rhs[n], and the force vector f[n]. */

@@ -27,6 +27,7 @@ PRECISION_MIXED = 1
 
 ELEMENT_COROTATIONAL_TET = 0
 ELEMENT_LINEAR_TET = 1
+ELEMENT_HEXAHEDRON = 2
 
 STEP_TIME_PHASES = 1
 STEP_KEEP_SYSTEM = 2

@@ -22,8 +22,10 @@ class Body:
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5,
                  cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0,
                  autotune=False, element_type=_lib.ELEMENT_COROTATIONAL_TET):
-        """`mesh` is one TetMesh, or a list of them for a batch (mixed precision only)."""
+        """`mesh` is one TetMesh, or a list of them for a batch (mixed precision only). With
+        element_type ELEMENT_HEXAHEDRON, ``mesh.tets`` holds 8 node ids per element."""
         L = _lib.load()
+        self.nodes_per_element = 8 if element_type == _lib.ELEMENT_HEXAHEDRON else 4
         meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
         self._keep = []
         descs = (_lib.MeshDesc * len(meshes))()
@@ -37,7 +39,7 @@ class Body:
             d = descs[k]
             d.num_nodes = arrs[0].size // 3
             d.rest_positions = dptr(arrs[0])
-            d.num_tets = arrs[1].size // 4
+            d.num_tets = arrs[1].size // self.nodes_per_element
             d.tets = iptr(arrs[1])
             d.young_modulus = dptr(arrs[2])
             d.poisson_ratio = dptr(arrs[3])
@@ -114,7 +116,8 @@ class Body:
     @classmethod
     def from_scene(cls, scene, **over):
         kw = dict(rayleigh_mass=scene.rayleigh_mass, rayleigh_stiffness=scene.rayleigh_stiffness,
-                  gravity=scene.gravity, cg_tolerance=scene.cg_tolerance, cg_max_iterations=scene.cg_max_iterations)
+                  gravity=scene.gravity, cg_tolerance=scene.cg_tolerance, cg_max_iterations=scene.cg_max_iterations,
+                  element_type=scene.element_type)
         kw.update(over)
         return cls(scene.mesh, **kw)
 
@@ -189,7 +192,7 @@ class Body:
         return colptr, rowidx
 
     def scatter(self):
-        m = np.empty(self.num_tets * 144, dtype=np.int32)
+        m = np.empty(self.num_tets * (3 * self.nodes_per_element) ** 2, dtype=np.int32)
         self._check(_lib.load().gbfem_get_scatter(self._h, iptr(m)))
         return m
 

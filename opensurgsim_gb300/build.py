@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbfem.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gbfem_kernels.cu", "gbfem_host.cpp", "gbfem_noalloc.cu", "gbfem_pcg.cu", "gbfem_adjoint.cu"]
+SOURCES = ["gbfem_kernels.cu", "gbfem_host.cpp", "gbfem_noalloc.cu", "gbfem_pcg.cu", "gbfem_adjoint.cu", "gbfem_hex.cu"]
 
 
 def nvcc() -> str:

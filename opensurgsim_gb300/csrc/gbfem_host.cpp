@@ -86,6 +86,35 @@ bool inverse44(const double a[4][4], double inv[4][4])
 	return true;
 }
 
+// Rest checks of Fem3DElementCube::initialize: the Jacobian at each of the 8 Gauss points must be
+// invertible (|det J| > 1e-12, Fem3DElementCube.cpp:202-207) and the rest volume, the sum of the
+// determinants (weights 1, :321-366), above 1e-12 (:357). Returns 0, 1 (singular J) or 2 (volume).
+int hex_rest_check(const double* X, const int32_t* nd, double* volume)
+{
+	static const double sE[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sH[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+						sM[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+	const double q = 1.0 / std::sqrt(3.0);
+	double v = 0.0;
+	for (int gp = 0; gp < 8; ++gp)
+	{
+		const double e = (gp & 4) ? -q : q, h = (gp & 2) ? -q : q, m = (gp & 1) ? -q : q;
+		double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+		for (int i = 0; i < 8; ++i)
+		{
+			const double d[3] = {0.125 * sE[i] * (1 + h * sH[i]) * (1 + m * sM[i]),
+								 0.125 * (1 + e * sE[i]) * sH[i] * (1 + m * sM[i]),
+								 0.125 * (1 + e * sE[i]) * (1 + h * sH[i]) * sM[i]};
+			for (int r = 0; r < 3; ++r)
+				for (int c = 0; c < 3; ++c) J[r][c] += X[3 * (size_t)nd[i] + c] * d[r];
+		}
+		const double det = det33(J);
+		if (!(std::fabs(det) > 1e-12)) return 1;
+		v += det;
+	}
+	*volume = v;
+	return v > 1e-12 ? 0 : 2;
+}
+
 }  // namespace
 
 struct gbfem_handle_s
@@ -102,7 +131,7 @@ struct gbfem_handle_s
 	gbfem_stats stats{};
 
 	// host structure
-	std::vector<int32_t> tets;
+	std::vector<int32_t> tets;     // element node ids, npe() per element
 	std::vector<int> adjPtr, adj;  // node adjacency incl. self (sorted) = BSR structure
 	std::vector<double> cmass;     // per element rho V / 20 (consistent mass coefficient)
 	std::vector<uint8_t> bcMask;
@@ -148,6 +177,16 @@ struct gbfem_handle_s
 	int nrows = 0, nchunks = 0;
 	bool mixed() const { return prm.precision == GBFEM_PRECISION_MIXED; }
 	bool linear() const { return prm.element_type == GBFEM_ELEMENT_LINEAR_TET; }
+	bool hex() const { return prm.element_type == GBFEM_ELEMENT_HEXAHEDRON; }
+	bool corotational() const { return prm.element_type == GBFEM_ELEMENT_COROTATIONAL_TET; }
+	int npe() const { return hex() ? 8 : 4; }
+	// Constant system (linear elements): S is formed once per dt and materials.
+	bool constantSystem() const { return !corotational(); }
+	bool systemCurrent(double dt) const { return constantSystem() && linearReady && linearDt == dt; }
+	// Hexahedra: element node ids, materials, and the assembled K / scalar block masses (SELL layout).
+	DevBuf<int> d_enodes;
+	DevBuf<double> d_young, d_poisson, d_rho, d_K, d_Ms;
+	int graphKernels = 0;  // kernels one launch of the captured step graph runs
 	// Linear elements: the system matrix assembled for linearDt stays valid until dt or a material
 	// changes (OdeSolverLinearEulerImplicit keeps its first step's system).
 	bool linearReady = false;
@@ -244,10 +283,11 @@ struct gbfem_handle_s
 		for (auto* b : {&d_mu, &d_adjG, &d_gx, &d_gv}) b->free();
 		DevBuf<double>* bd[] = {&d_rest, &d_xrest, &d_lmass, &d_nmass, &d_x, &d_v, &d_xt, &d_vt, &d_kslots,
 								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
-								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f};
+								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f, &d_young, &d_poisson, &d_rho,
+								&d_K, &d_Ms};
 		for (auto* b : bd) b->free();
 		DevBuf<int>* bi[] = {&d_perm, &d_off, &d_sellcol, &d_cptr, &d_cidx, &d_iptr, &d_iidx, &d_counters, &d_idx,
-							 &d_sptr, &d_sidx, &d_srow, &d_scol};
+							 &d_sptr, &d_sidx, &d_srow, &d_scol, &d_enodes};
 		for (auto* b : bi) b->free();
 		d_bc.free();
 		d_ctl.free();
@@ -319,6 +359,31 @@ gbfem_status configure_pcg(gbfem_handle h, int cps)
 	return GBFEM_OK;
 }
 
+// Hexahedra: element integrals from the current materials, assembled into K and the scalar block
+// masses (also the per-lower-block masses S is formed from). Any stored system is then stale.
+gbfem_status rebuild_hex_operators(gbfem_handle h)
+{
+	cudaStream_t s = h->stream;
+	struct Scratch
+	{
+		DevBuf<double> slots, smass;
+		~Scratch()
+		{
+			slots.free();
+			smass.free();
+		}
+	} t;
+	GB_CUDA(h, t.slots.alloc((size_t)h->E * kHexSlots * 9));
+	GB_CUDA(h, t.smass.alloc((size_t)h->E * kHexSlots));
+	launch_hex_element(h->E, h->d_enodes.p, h->d_xrest.p, h->d_young.p, h->d_poisson.p, h->d_rho.p, t.slots.p,
+					   t.smass.p, s);
+	launch_assemble_k(h->body(), t.slots.p, t.smass.p, h->d_K.p, h->d_Ms.p, h->d_lmass.p, s);
+	GB_CUDA(h, cudaGetLastError());
+	GB_CUDA(h, cudaStreamSynchronize(s));  // before the scratch is released
+	h->linearReady = false;
+	return GBFEM_OK;
+}
+
 // Everything the step needs from the mesh, computed on the host once.
 gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 {
@@ -326,14 +391,21 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	h->N = N;
 	h->E = E;
 	h->n = 3 * N;
-	h->tets.assign(m->tets, m->tets + 4 * (size_t)E);
+	const int npe = h->npe();
+	h->tets.assign(m->tets, m->tets + npe * (size_t)E);
 	const double* X = m->rest_positions;
 
 	// Rest precompute (Fem3DElementTetrahedron.cpp:92-216; Fem3DElementCorotationalTetrahedron.cpp:57-72).
-	std::vector<double> rest((size_t)kRestFields * E);
-	h->cmass.resize(E);
+	std::vector<double> rest(h->hex() ? 0 : (size_t)kRestFields * E);
+	h->cmass.resize(h->hex() ? 0 : E);
 	std::vector<double> elemMass(E);
-	for (int e = 0; e < E; ++e)
+	for (int e = 0; e < E && h->hex(); ++e)
+	{
+		double vol = 0.0;
+		hex_rest_check(X, &h->tets[8 * (size_t)e], &vol);  // validated before
+		elemMass[e] = vol * m->mass_density[e];            // FemElement::getMass
+	}
+	for (int e = 0; e < E && !h->hex(); ++e)
 	{
 		const int* nd = &h->tets[4 * (size_t)e];
 		for (int a = 0; a < 4; ++a)
@@ -368,14 +440,15 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	// Node adjacency (the union of element node blocks, FemRepresentation.cpp:121-132).
 	std::vector<int> cnt(N + 1, 0);
 	for (int e = 0; e < E; ++e)
-		for (int a = 0; a < 4; ++a) cnt[h->tets[4 * (size_t)e + a] + 1] += 4;
+		for (int a = 0; a < npe; ++a) cnt[h->tets[npe * (size_t)e + a] + 1] += npe;
 	for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
 	std::vector<int> raw(cnt[N]);
 	{
 		std::vector<int> fill(cnt.begin(), cnt.end() - 1);
 		for (int e = 0; e < E; ++e)
-			for (int a = 0; a < 4; ++a)
-				for (int b = 0; b < 4; ++b) raw[fill[h->tets[4 * (size_t)e + a]]++] = h->tets[4 * (size_t)e + b];
+			for (int a = 0; a < npe; ++a)
+				for (int b = 0; b < npe; ++b)
+					raw[fill[h->tets[npe * (size_t)e + a]]++] = h->tets[npe * (size_t)e + b];
 	}
 	h->adjPtr.assign(N + 1, 0);
 	h->adj.clear();
@@ -462,63 +535,72 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 			lblk.push_back(make_int4(I, J, sellBase[k], I == J ? -1 : sellBase[h->blockPos(J, I)]));
 		}
 	h->nl = (int)lblk.size();
-	// Element slot -> lower block contributions, element order inside each block.
-	std::vector<int> slotLower((size_t)E * kSlots);
+	// Element slot -> lower block contributions, element order inside each block. Slots: the npe
+	// diagonal blocks, then the node pairs a < b in lexicographic order.
+	const int spe = h->hex() ? kHexSlots : kSlots;
+	std::vector<int> pa, pb;
+	for (int a = 0; a < npe; ++a)
+	{
+		pa.push_back(a);
+		pb.push_back(a);
+	}
+	for (int a = 0; a < npe; ++a)
+		for (int b = a + 1; b < npe; ++b)
+		{
+			pa.push_back(a);
+			pb.push_back(b);
+		}
+	std::vector<int> slotLower((size_t)E * spe);
 	std::vector<int> cptr(h->nl + 1, 0);
-	static const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
 	for (int e = 0; e < E; ++e)
 	{
-		const int* nd = &h->tets[4 * (size_t)e];
-		for (int s = 0; s < kSlots; ++s)
+		const int* nd = &h->tets[npe * (size_t)e];
+		for (int s = 0; s < spe; ++s)
 		{
-			int I, J;
-			if (s < 4)
-				I = J = nd[s];
-			else
-			{
-				I = std::max(nd[pa[s - 4]], nd[pb[s - 4]]);
-				J = std::min(nd[pa[s - 4]], nd[pb[s - 4]]);
-			}
+			const int I = std::max(nd[pa[s]], nd[pb[s]]), J = std::min(nd[pa[s]], nd[pb[s]]);
 			int L = lowerOfPos[h->blockPos(I, J)];
-			slotLower[(size_t)e * kSlots + s] = L;
+			slotLower[(size_t)e * spe + s] = L;
 			cptr[L + 1]++;
 		}
 	}
 	for (int L = 0; L < h->nl; ++L) cptr[L + 1] += cptr[L];
-	std::vector<int> cidx((size_t)E * kSlots);
-	std::vector<double> lmass(h->nl, 0.0);
+	std::vector<int> cidx((size_t)E * spe);
+	std::vector<double> lmass(h->nl, 0.0);  // hexahedra: summed on the device from the element integrals
 	{
 		std::vector<int> fill(cptr.begin(), cptr.end() - 1);
 		for (int e = 0; e < E; ++e)
-			for (int s = 0; s < kSlots; ++s)
+			for (int s = 0; s < spe; ++s)
 			{
-				int L = slotLower[(size_t)e * kSlots + s];
-				cidx[fill[L]++] = e * kSlots + s;
-				lmass[L] += h->cmass[e] * (s < 4 ? 2.0 : 1.0);
+				int L = slotLower[(size_t)e * spe + s];
+				cidx[fill[L]++] = e * spe + s;
+				if (!h->hex()) lmass[L] += h->cmass[e] * (s < 4 ? 2.0 : 1.0);
 			}
 	}
-	// Node incidences and lumped node masses (FemRepresentation.cpp:102-117).
-	std::vector<int> iptr(N + 1, 0), iidx(4 * (size_t)E);
+	// Node incidences and lumped node masses getMass / numNodes (FemRepresentation.cpp:102-117).
+	std::vector<int> iptr(N + 1, 0), iidx(npe * (size_t)E);
 	for (int e = 0; e < E; ++e)
-		for (int a = 0; a < 4; ++a) iptr[h->tets[4 * (size_t)e + a] + 1]++;
+		for (int a = 0; a < npe; ++a) iptr[h->tets[npe * (size_t)e + a] + 1]++;
 	for (int i = 0; i < N; ++i) iptr[i + 1] += iptr[i];
 	std::vector<double> nmass(N, 0.0);
 	{
 		std::vector<int> fill(iptr.begin(), iptr.end() - 1);
 		for (int e = 0; e < E; ++e)
-			for (int a = 0; a < 4; ++a)
+			for (int a = 0; a < npe; ++a)
 			{
-				int I = h->tets[4 * (size_t)e + a];
-				iidx[fill[I]++] = 4 * e + a;
-				nmass[I] += elemMass[e] / 4;
+				int I = h->tets[npe * (size_t)e + a];
+				iidx[fill[I]++] = npe * e + a;
+				nmass[I] += elemMass[e] / npe;
 			}
 	}
 	h->bcMask.assign(h->n, 0);
 	for (int i = 0; i < m->num_bc_dofs; ++i) h->bcMask[m->bc_dofs[i]] = 1;
 
 	cudaStream_t s = h->stream;
-	GB_CUDA(h, h->d_tets.upload(reinterpret_cast<const int4*>(h->tets.data()), E, s));
-	GB_CUDA(h, h->d_rest.upload(rest.data(), rest.size(), s));
+	if (!h->hex())
+	{
+		GB_CUDA(h, h->d_tets.upload(reinterpret_cast<const int4*>(h->tets.data()), E, s));
+		GB_CUDA(h, h->d_rest.upload(rest.data(), rest.size(), s));
+	}
 	GB_CUDA(h, h->d_xrest.upload(X, h->n, s));
 	GB_CUDA(h, h->d_perm.upload(perm.data(), perm.size(), s));
 	GB_CUDA(h, h->d_off.upload(off.data(), off.size(), s));
@@ -532,30 +614,54 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	GB_CUDA(h, h->d_cptr.upload(cptr.data(), cptr.size(), s));
 	GB_CUDA(h, h->d_cidx.upload(cidx.data(), cidx.size(), s));
 	GB_CUDA(h, h->d_lmass.upload(lmass.data(), lmass.size(), s));
-	GB_CUDA(h, h->d_iptr.upload(iptr.data(), iptr.size(), s));
-	GB_CUDA(h, h->d_iidx.upload(iidx.data(), iidx.size(), s));
+	if (!h->hex())
+	{
+		GB_CUDA(h, h->d_iptr.upload(iptr.data(), iptr.size(), s));
+		GB_CUDA(h, h->d_iidx.upload(iidx.data(), iidx.size(), s));
+	}
 	GB_CUDA(h, h->d_nmass.upload(nmass.data(), nmass.size(), s));
 	GB_CUDA(h, h->d_bc.upload(h->bcMask.data(), h->bcMask.size(), s));
 	GB_CUDA(h, h->d_x.upload(X, h->n, s));
 	GB_CUDA(h, h->d_v.alloc(h->n));
 	GB_CUDA(h, cudaMemsetAsync(h->d_v.p, 0, sizeof(double) * h->n, s));
 	const size_t nv = h->n;
+	if (h->hex())
+	{
+		// Element integrals once, assembled into K and the scalar block masses; the per-element
+		// slots are released afterwards.
+		GB_CUDA(h, h->d_enodes.upload(h->tets.data(), h->tets.size(), s));
+		GB_CUDA(h, h->d_young.upload(m->young_modulus, E, s));
+		GB_CUDA(h, h->d_poisson.upload(m->poisson_ratio, E, s));
+		GB_CUDA(h, h->d_rho.upload(m->mass_density, E, s));
+		GB_CUDA(h, h->d_K.alloc((size_t)sellSlots * 9));
+		GB_CUDA(h, cudaMemsetAsync(h->d_K.p, 0, sizeof(double) * sellSlots * 9, s));  // padding blocks stay 0
+		GB_CUDA(h, h->d_Ms.alloc((size_t)sellSlots));
+		GB_CUDA(h, cudaMemsetAsync(h->d_Ms.p, 0, sizeof(double) * sellSlots, s));
+		gbfem_status st = rebuild_hex_operators(h);
+		if (st != GBFEM_OK) return st;
+	}
 	if (!h->mixed())
 	{
-		GB_CUDA(h, h->d_kslots.alloc((size_t)E * kSlots * 9));
-		GB_CUDA(h, h->d_rhsE.alloc((size_t)E * 12));
+		if (!h->hex())
+		{
+			GB_CUDA(h, h->d_kslots.alloc((size_t)E * kSlots * 9));
+			GB_CUDA(h, h->d_rhsE.alloc((size_t)E * 12));
+		}
 		GB_CUDA(h, h->d_A.alloc((size_t)sellSlots * 9));
 		GB_CUDA(h, cudaMemsetAsync(h->d_A.p, 0, sizeof(double) * sellSlots * 9, s));  // padding blocks stay 0
 		for (DevBuf<double>* b : {&h->d_invdiag, &h->d_r, &h->d_p, &h->d_q}) GB_CUDA(h, b->alloc(nv));
 	}
 	else
 	{
-		// FP32 copy of the FP64 rest precompute (K0 and volume stay FP64-derived).
-		std::vector<float> rest32(rest.begin(), rest.end());
-		GB_CUDA(h, h->d_rest32.upload(rest32.data(), rest32.size(), s));
-		GB_CUDA(h, cudaStreamSynchronize(s));
-		GB_CUDA(h, h->d_kslots32.alloc((size_t)E * kSlots * 9));
-		GB_CUDA(h, h->d_rhsE32.alloc((size_t)E * 12));
+		if (!h->hex())
+		{
+			// FP32 copy of the FP64 rest precompute (K0 and volume stay FP64-derived).
+			std::vector<float> rest32(rest.begin(), rest.end());
+			GB_CUDA(h, h->d_rest32.upload(rest32.data(), rest32.size(), s));
+			GB_CUDA(h, cudaStreamSynchronize(s));
+			GB_CUDA(h, h->d_kslots32.alloc((size_t)E * kSlots * 9));
+			GB_CUDA(h, h->d_rhsE32.alloc((size_t)E * 12));
+		}
 		GB_CUDA(h, h->d_A32.alloc((size_t)sellSlots * 9));
 		GB_CUDA(h, cudaMemsetAsync(h->d_A32.p, 0, sizeof(float) * sellSlots * 9, s));
 		GB_CUDA(h, h->d_invdiag32.alloc(nv));
@@ -862,6 +968,15 @@ gbfem_status check_pcg_error(gbfem_handle h)
 	return GBFEM_OK;
 }
 
+// Hexahedra: the step's right-hand side from the stored K and block masses (x_t, v_t: the state the
+// step started from; the current iterate is the handle's v).
+void enqueue_hex_rhs(gbfem_handle h, double dt, const double* xt, const double* vt, cudaStream_t s)
+{
+	const MatSell3 K{h->nrows, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_K.p};
+	launch_hex_rhs(K, h->d_Ms.p, h->body(), xt, h->d_v.p, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
+				   h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, s);
+}
+
 // Autotuner of the mixed form, run on the first step's own system: times the element kernel at 32
 // and 64 elements per block, then the persistent solve for 2, 3 and 4 CTAs per SM and refresh
 // weights 4, 6 and 8, and keeps the fastest of each. The element kernel's results do not depend on
@@ -883,8 +998,8 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 		return e;
 	};
 	float bestE = 1e30f;
-	int eBest = 64;
-	for (int rep = 0; rep < 2; ++rep)
+	int eBest = h->elemsPerBlock;
+	for (int rep = 0; rep < 2 && !h->hex(); ++rep)
 		for (int ept : {32, 64})
 		{
 			GB_CUDA(h, cudaEventRecord(e0, s));
@@ -900,10 +1015,18 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 			}
 		}
 	h->elemsPerBlock = eBest;
-	launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
-					   h->d_counters.p, s, eBest, h->linear());
-	launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
-	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+	if (h->hex())
+	{
+		launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+		enqueue_hex_rhs(h, dt, xt, vt, s);
+	}
+	else
+	{
+		launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
+						   h->d_counters.p, s, eBest, h->linear());
+		launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+		launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+	}
 	GB_CUDA(h, cudaGetLastError());
 	float bestS = 1e30f;
 	int cBest = h->ctasPerSM, rBest = h->refreshWeight;
@@ -952,12 +1075,23 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	const int nseg = (int)h->segNode.size() - 1;
 	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * h->n;
 	const double c1 = 1.0 / dt + h->prm.rayleigh_mass, c2 = dt + h->prm.rayleigh_stiffness;
-	const bool reuse = h->linear() && h->linearReady && h->linearDt == dt;
-	launch_element_f32(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
-					   h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s,
-					   h->elemsPerBlock, h->linear());
-	if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
-	launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+	const bool reuse = h->systemCurrent(dt);
+	int kernels = 0;
+	if (h->hex())
+	{
+		if (!reuse) launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+		enqueue_hex_rhs(h, dt, h->d_x.p, h->d_v.p, s);
+		kernels = reuse ? 1 : 2;
+	}
+	else
+	{
+		launch_element_f32(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
+						   h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p,
+						   h->d_counters.p, s, h->elemsPerBlock, h->linear());
+		if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+		launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+		kernels = reuse ? 2 : 3;
+	}
 	gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timed ? h->graphEv[0] : nullptr,
 									timed ? h->graphEv[1] : nullptr, /*capturing=*/true);
 	if (st != GBFEM_OK) return st;
@@ -965,6 +1099,7 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	launch_validity(h->n, h->d_x.p, h->d_v.p, h->d_ctl.p, h->d_part.p, L);
 	launch_step_accumulate(h->d_seg.p, nseg, &h->d_ctl.p->nonfinite, &h->d_pcgGlobal.p->err, h->d_acc.p, s);
 	GB_CUDA(h, cudaGetLastError());
+	h->graphKernels = kernels + 4;  // + solve, state update, validity, accumulate
 	return GBFEM_OK;
 }
 
@@ -1014,7 +1149,7 @@ gbfem_status step_graph(gbfem_handle h, double dt, int nsteps, uint32_t flags)
 	for (int i = 0; i < nsteps; ++i)
 	{
 		GB_CUDA(h, cudaGraphLaunch(h->graphExec, s));
-		h->launches += 7;  // element, assembly, rhs, solve, state update, validity, accumulate
+		h->launches += h->graphKernels;
 		if (timed)
 		{
 			GB_CUDA(h, cudaStreamSynchronize(s));
@@ -1059,6 +1194,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 	const bool keep = (flags & GBFEM_STEP_KEEP_SYSTEM) != 0;
 	if (keep && h->mixed())
 		return fail(h, GBFEM_INVALID_ARG, "GBFEM_STEP_KEEP_SYSTEM is available in the FP64 form only");
+	if (keep && h->hex()) return fail(h, GBFEM_INVALID_ARG, "GBFEM_STEP_KEEP_SYSTEM is available for tetrahedra only");
 	if (keep)
 	{
 		gbfem_status st = ensure_system_maps(h);
@@ -1100,22 +1236,31 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 				gbfem_status tst = tune_mixed(h, xt, vt, dt, c1, c2, maxIter);
 				if (tst != GBFEM_OK) return tst;
 			}
-			const bool reuse = h->linear() && h->linearReady && h->linearDt == dt;
-			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
-							   reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock,
-							   h->linear());
-			tm.mark(1);
-			if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
-			if (h->linear() && !reuse)
+			const bool reuse = h->systemCurrent(dt);
+			if (h->hex())
+			{
+				enqueue_hex_rhs(h, dt, xt, vt, s);
+				tm.mark(1);
+				if (!reuse) launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+			}
+			else
+			{
+				launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
+								   h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p,
+								   h->d_counters.p, s, h->elemsPerBlock, h->linear());
+				tm.mark(1);
+				if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+				launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+			}
+			if (h->constantSystem() && !reuse)
 			{
 				h->linearReady = true;
 				h->linearDt = dt;
 				h->tuneVersion++;  // a captured step graph must be rebuilt (right-hand side only from now on)
 			}
-			launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 			tm.mark(2);
 			GB_CUDA(h, cudaGetLastError());
-			h->launches += reuse ? 2 : 3;
+			h->launches += (h->hex() ? 1 : 2) + (reuse ? 0 : 1);
 			gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
@@ -1138,19 +1283,28 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 		}
 		else
 		{
-			const bool reuse = h->linear() && h->linearReady && h->linearDt == dt && !keep;
-			launch_element_fp64(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
-								h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots.p, h->d_rhsE.p,
-								keep ? h->d_kfull.p : nullptr, keep ? h->d_fE.p : nullptr, h->d_counters.p, s,
-								h->linear());
-			tm.mark(1);
-			if (!reuse) launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
-			if (h->linear() && !reuse)
+			const bool reuse = h->systemCurrent(dt) && !keep;
+			if (h->hex())
+			{
+				enqueue_hex_rhs(h, dt, xt, vt, s);
+				tm.mark(1);
+				if (!reuse) launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			}
+			else
+			{
+				launch_element_fp64(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
+									h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots.p, h->d_rhsE.p,
+									keep ? h->d_kfull.p : nullptr, keep ? h->d_fE.p : nullptr, h->d_counters.p, s,
+									h->linear());
+				tm.mark(1);
+				if (!reuse) launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+				launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+			}
+			if (h->constantSystem() && !reuse)
 			{
 				h->linearReady = true;
 				h->linearDt = dt;
 			}
-			launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 			if (keep)
 			{
 				launch_assemble_full_csc((int)h->nnz, h->d_sptr.p, h->d_sidx.p, h->d_srow.p, h->d_scol.p,
@@ -1159,7 +1313,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 			}
 			tm.mark(2);
 			GB_CUDA(h, cudaGetLastError());
-			h->launches += keep ? 5 : (reuse ? 2 : 3);
+			h->launches += keep ? 5 : (h->hex() ? 1 : 2) + (reuse ? 0 : 1);
 			gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
@@ -1234,7 +1388,7 @@ gbfem_status gbfem_params_default(gbfem_params* out)
 namespace {
 
 // Checks one mesh description (Fem3DRepresentation / FemElement / OdeState input checks).
-gbfem_status validate_mesh(const gbfem_mesh_desc* m, int index)
+gbfem_status validate_mesh(const gbfem_mesh_desc* m, int index, int elementType)
 {
 	const std::string where = index >= 0 ? "mesh " + std::to_string(index) + ": " : std::string();
 	if (!m) return fail(nullptr, GBFEM_INVALID_ARG, where + "mesh is NULL");
@@ -1242,15 +1396,33 @@ gbfem_status validate_mesh(const gbfem_mesh_desc* m, int index)
 		!m->poisson_ratio || !m->mass_density || (m->num_bc_dofs > 0 && !m->bc_dofs) || m->num_bc_dofs < 0)
 		return fail(nullptr, GBFEM_INVALID_ARG, where + "empty mesh or missing arrays");
 	if (m->num_nodes > INT32_MAX / 3) return fail(nullptr, GBFEM_INVALID_ARG, where + "too many nodes");
-	for (int64_t i = 0; i < 4LL * m->num_tets; ++i)
+	const int npe = elementType == GBFEM_ELEMENT_HEXAHEDRON ? 8 : 4;
+	for (int64_t i = 0; i < (int64_t)npe * m->num_tets; ++i)
 		if (m->tets[i] < 0 || m->tets[i] >= m->num_nodes)
 			return fail(nullptr, GBFEM_INVALID_ARG, where + "Invalid nodeId " + std::to_string(m->tets[i]));
+	if (elementType == GBFEM_ELEMENT_HEXAHEDRON)
+		for (int32_t e = 0; e < m->num_tets; ++e)
+		{
+			const int32_t* nd = m->tets + 8 * (size_t)e;
+			for (int a = 0; a < 8; ++a)
+				for (int b = a + 1; b < 8; ++b)
+					if (nd[a] == nd[b])
+						return fail(nullptr, GBFEM_INVALID_ARG, where + "hexahedron " + std::to_string(e) + " repeats a node");
+			double vol = 0.0;
+			const int chk = hex_rest_check(m->rest_positions, nd, &vol);
+			if (chk == 1)
+				return fail(nullptr, GBFEM_DEGENERATE_ELEMENT,
+							where + "hexahedron " + std::to_string(e) + ": non invertible Jacobian at a Gauss point");
+			if (chk == 2)
+				return fail(nullptr, GBFEM_DEGENERATE_ELEMENT,
+							where + "hexahedron " + std::to_string(e) + " ill-defined, its volume is " + std::to_string(vol));
+		}
 	for (int32_t e = 0; e < m->num_tets; ++e)
 	{
 		// FemElement::initialize material checks (FemElement.cpp:33-43).
 		const double rho = m->mass_density[e], nu = m->poisson_ratio[e], Ey = m->young_modulus[e];
 		if (!(rho > 0.0) || !(nu > 0.0 && nu < 0.5) || !(Ey > 0.0))
-			return fail(nullptr, GBFEM_INVALID_ARG, where + "invalid material on tet " + std::to_string(e));
+			return fail(nullptr, GBFEM_INVALID_ARG, where + "invalid material on element " + std::to_string(e));
 	}
 	for (int32_t i = 0; i < m->num_bc_dofs; ++i)
 		if (m->bc_dofs[i] < 0 || m->bc_dofs[i] >= 3 * m->num_nodes)
@@ -1264,14 +1436,16 @@ gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbf
 	if (!out) return fail(nullptr, GBFEM_INVALID_ARG, "out is NULL");
 	*out = nullptr;
 	if (!meshes || !prm || count <= 0) return fail(nullptr, GBFEM_INVALID_ARG, "mesh or params is NULL");
+	if (!(prm->newton_max_iterations >= 1) || !(prm->newton_epsilon >= 0.0) || !(prm->cg_tolerance >= 0.0) ||
+		prm->precision < 0 || prm->precision > 1 || prm->element_type < 0 || prm->element_type > 2)
+		return fail(nullptr, GBFEM_INVALID_ARG, "invalid solver parameters");
 	for (int32_t k = 0; k < count; ++k)
 	{
-		gbfem_status st = validate_mesh(&meshes[k], count > 1 ? k : -1);
+		gbfem_status st = validate_mesh(&meshes[k], count > 1 ? k : -1, prm->element_type);
 		if (st != GBFEM_OK) return st;
 	}
-	if (!(prm->newton_max_iterations >= 1) || !(prm->newton_epsilon >= 0.0) || !(prm->cg_tolerance >= 0.0) ||
-		prm->precision < 0 || prm->precision > 1 || prm->element_type < 0 || prm->element_type > 1)
-		return fail(nullptr, GBFEM_INVALID_ARG, "invalid solver parameters");
+	const int npe = prm->element_type == GBFEM_ELEMENT_HEXAHEDRON ? 8 : 4;
+	const int slotsPerElement = prm->element_type == GBFEM_ELEMENT_HEXAHEDRON ? kHexSlots : kSlots;
 	if (count > 1 && prm->precision != GBFEM_PRECISION_MIXED)
 		return fail(nullptr, GBFEM_INVALID_ARG, "a batch of meshes is stepped in the mixed-precision form");
 	// Concatenate the meshes (node ids, boundary-condition dofs shifted by the node offsets).
@@ -1282,14 +1456,14 @@ gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbf
 		E += meshes[k].num_tets;
 		B += meshes[k].num_bc_dofs;
 	}
-	if (N > INT32_MAX / 3 || E > INT32_MAX / kSlots) return fail(nullptr, GBFEM_INVALID_ARG, "batch too large");
+	if (N > INT32_MAX / 3 || E > INT32_MAX / slotsPerElement) return fail(nullptr, GBFEM_INVALID_ARG, "batch too large");
 	std::vector<double> X, Ey, Nu, Rho;
 	std::vector<int32_t> T, Bc;
 	std::vector<int> segNode{0}, segTet{0};
 	if (count > 1)
 	{
 		X.reserve(3 * N);
-		T.reserve(4 * E);
+		T.reserve(npe * E);
 		Ey.reserve(E);
 		Nu.reserve(E);
 		Rho.reserve(E);
@@ -1302,7 +1476,7 @@ gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbf
 		if (count > 1)
 		{
 			X.insert(X.end(), m.rest_positions, m.rest_positions + 3 * (size_t)m.num_nodes);
-			for (int64_t i = 0; i < 4LL * m.num_tets; ++i) T.push_back(m.tets[i] + n0);
+			for (int64_t i = 0; i < (int64_t)npe * m.num_tets; ++i) T.push_back(m.tets[i] + n0);
 			Ey.insert(Ey.end(), m.young_modulus, m.young_modulus + m.num_tets);
 			Nu.insert(Nu.end(), m.poisson_ratio, m.poisson_ratio + m.num_tets);
 			Rho.insert(Rho.end(), m.mass_density, m.mass_density + m.num_tets);
@@ -1364,7 +1538,7 @@ gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, const double*
 	if (ncols < 0 || (ncols > 0 && (!b || !x))) return fail(h, GBFEM_INVALID_ARG, "gbfem_apply_compliance: bad arrays");
 	if (!h->systemReady) return fail(h, GBFEM_INVALID_ARG, "gbfem_apply_compliance: no step has assembled a system yet");
 	const bool warp = (flags & GBFEM_COMPLIANCE_WARPING) != 0;
-	if (warp && h->linear())
+	if (warp && !h->corotational())
 		return fail(h, GBFEM_INVALID_ARG, "compliance warping needs the corotational element");
 	GB_CUDA(h, cudaSetDevice(h->device));
 	const int n = h->n, N = h->N;
@@ -1472,6 +1646,16 @@ gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t c
 gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, const double* poisson)
 {
 	if (!h || !young) return GBFEM_INVALID_ARG;
+	GB_CUDA(h, cudaSetDevice(h->device));
+	if (h->hex())
+	{
+		// Stream-ordered copies of the caller's device arrays, then K and M again.
+		GB_CUDA(h, cudaMemcpyAsync(h->d_young.p, young, sizeof(double) * h->E, cudaMemcpyDeviceToDevice, h->stream));
+		if (poisson)
+			GB_CUDA(h, cudaMemcpyAsync(h->d_poisson.p, poisson, sizeof(double) * h->E, cudaMemcpyDeviceToDevice,
+									   h->stream));
+		return rebuild_hex_operators(h);
+	}
 	launch_set_materials(h->E, young, poisson, h->d_rest.p, h->mixed() ? h->d_rest32.p : nullptr, h->stream);
 	h->linearReady = false;  // the stored linear system no longer matches
 	GB_CUDA(h, cudaGetLastError());
@@ -1486,7 +1670,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	if (!h) return GBFEM_INVALID_ARG;
 	if (!x || !v || !dv || !lx || !lv || !lx_out || !lv_out || !(dt > 0.0))
 		return fail(h, GBFEM_INVALID_ARG, "gbfem_adjoint_step: null array or dt <= 0");
-	if (h->linear()) return fail(h, GBFEM_INVALID_ARG, "gbfem_adjoint_step: corotational elements only");
+	if (!h->corotational()) return fail(h, GBFEM_INVALID_ARG, "gbfem_adjoint_step: corotational elements only");
 	cudaStream_t s = h->stream;
 	const DevBody body = h->body();
 	const int n = h->n;
@@ -1608,7 +1792,7 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), h->stream));
 	gbfem_status result = GBFEM_OK;
 	int sidx = 0;
-	const bool needPlainStep = (h->prm.autotune && !h->tuned) || (h->linear() && !(h->linearReady && h->linearDt == dt));
+	const bool needPlainStep = (h->prm.autotune && !h->tuned) || (h->constantSystem() && !h->systemCurrent(dt));
 	if ((flags & GBFEM_STEP_GRAPH) && needPlainStep && nsteps > 0)
 	{
 		result = step_once(h, dt, flags & ~GBFEM_STEP_GRAPH);  // the first step tunes, outside any graph
@@ -1758,15 +1942,17 @@ gbfem_status gbfem_get_pattern(gbfem_handle h, int32_t* colptr, int32_t* rowidx)
 gbfem_status gbfem_get_scatter(gbfem_handle h, int32_t* map)
 {
 	if (!h || !map) return GBFEM_INVALID_ARG;
+	const int npe = h->npe(), D = 3 * npe;
 	for (int e = 0; e < h->E; ++e)
 	{
-		const int* nd = &h->tets[4 * (size_t)e];
-		for (int a = 0; a < 4; ++a)
-			for (int b = 0; b < 4; ++b)
+		const int* nd = &h->tets[npe * (size_t)e];
+		for (int a = 0; a < npe; ++a)
+			for (int b = 0; b < npe; ++b)
 				for (int j = 0; j < 3; ++j)
 				{
 					int64_t first = h->cscSlot(3 * nd[a], 3 * nd[b] + j);
-					for (int i = 0; i < 3; ++i) map[(size_t)e * 144 + (3 * a + i) * 12 + 3 * b + j] = (int32_t)(first + i);
+					for (int i = 0; i < 3; ++i)
+						map[(size_t)e * D * D + (3 * a + i) * D + 3 * b + j] = (int32_t)(first + i);
 				}
 	}
 	return GBFEM_OK;

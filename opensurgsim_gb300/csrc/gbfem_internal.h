@@ -155,6 +155,22 @@ void launch_adjoint_rhs(int n, const uint8_t* bc, const double* lx, const double
 void launch_set_materials(int E, const double* young, const double* poisson, double* rest, float* rest32,
 						  cudaStream_t s);
 
+// Hexahedra (gbfem_hex.cu). Element integrals once (36 lower-triangle node blocks and their scalar
+// masses per element, slot order: 8 diagonal blocks, then the node pairs a < b lexicographically),
+// the assembled K and scalar block masses in the SELL layout, S from them, the per-step right-hand side.
+constexpr int kHexSlots = 36;
+void launch_hex_element(int E, const int* nodes, const double* xrest, const double* young, const double* poisson,
+						const double* rho, double* slots, double* smass, cudaStream_t s);
+void launch_assemble_k(const DevBody& b, const double* slots, const double* smass, double* K, double* Ms,
+					   double* lmass, cudaStream_t s);
+void launch_system_from_k(const DevBody& b, const double* K, double c1, double c2, double* A, double* invdiag,
+						  cudaStream_t s);
+void launch_system_from_k(const DevBody& b, const double* K, double c1, double c2, float* A, float* invdiag,
+						  cudaStream_t s);
+void launch_hex_rhs(const MatSell3& K, const double* Ms, const DevBody& b, const double* xt, const double* vn,
+					const double* vt, double dt, double alpha, double beta, const double* gravity, int gravityOn,
+					double* rhs, cudaStream_t s);
+
 // Partial-sum buffer size needed by the reductions for a given vecGrid.
 constexpr int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }
 

@@ -108,7 +108,7 @@ def scene_hex_cube(a=10, b=10, c=10, h=0.01, seed=0, jitter=0.0, young=1e5, pois
     E = hexes.shape[0]
     mesh = TetMesh(nodes, hexes, np.full(E, young), np.full(E, poisson), np.full(E, density),
                    face_dofs(a, b, c, 2, 0), (a, b, c), h)
-    return Scene(mesh=mesh, name=f"hex{a}x{b}x{c}", **kw)
+    return Scene(mesh=mesh, name=f"hex{a}x{b}x{c}", element_type=2, **kw)
 
 
 def scene_divisible_cube(nodes_per_axis: int, **kw) -> Scene:
@@ -131,7 +131,7 @@ def scene_divisible_cube(nodes_per_axis: int, **kw) -> Scene:
     kw.setdefault("cg_tolerance", 1e-3)
     kw.setdefault("cg_max_iterations", max(1, int(0.1 * 3 * n ** 3)))
     kw.setdefault("steps", 10)
-    return Scene(mesh=mesh, name=f"divisiblecube{n}", **kw)
+    return Scene(mesh=mesh, name=f"divisiblecube{n}", element_type=2, **kw)
 
 
 def signed_volumes(nodes: np.ndarray, tets: np.ndarray) -> np.ndarray:
@@ -165,6 +165,7 @@ class Scene:
     driven_velocity: float = 0.0            # z velocity of the driven dofs during the ramp
     ramp_steps: int = 0
     name: str = ""
+    element_type: int = 0                   # 0 corotational tetrahedra, 1 linear tetrahedra, 2 hexahedra
 
     def driven_values(self, step: int) -> np.ndarray:
         """Prescribed velocities (per driven dof) before `step`: the z component carries the ramp."""

@@ -141,6 +141,7 @@ class OracleModel:
         st = ctypes.c_int32(0)
         self.num_nodes = mesh.nodes.shape[0]
         self.num_tets = mesh.tets.shape[0]
+        self._npe = 8 if element_type == 2 else 4
         self.n = 3 * self.num_nodes
         self._h = L.orc_create(self.num_nodes, _d(self._nodes), self.num_tets, _i(self._tets), _d(self._E),
                                _d(self._nu), _d(self._rho), self._bc.size, _i(self._bc), ctypes.byref(p),
@@ -154,7 +155,7 @@ class OracleModel:
     def from_scene(cls, scene, **over):
         kw = dict(rayleigh_mass=scene.rayleigh_mass, rayleigh_stiffness=scene.rayleigh_stiffness,
                   gravity=scene.gravity, cg_tolerance=scene.cg_tolerance,
-                  cg_max_iterations=scene.cg_max_iterations)
+                  cg_max_iterations=scene.cg_max_iterations, element_type=scene.element_type)
         kw.update(over)
         return cls(scene.mesh, **kw)
 
@@ -189,7 +190,7 @@ class OracleModel:
         return colptr, rowidx
 
     def scatter(self):
-        m = np.empty(self.num_tets * 144, dtype=np.int32)
+        m = np.empty(self.num_tets * (3 * self._npe) ** 2, dtype=np.int32)
         lib().orc_get_scatter(self._h, _i(m))
         return m
 

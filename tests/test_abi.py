@@ -51,15 +51,57 @@ def test_params_default(lib):
     assert p.cg_tolerance == np.finfo(float).eps and p.cg_max_iterations == 0  # Eigen defaults
 
 
-def _desc(m):
+def _desc(m, npe=4):
     from opensurgsim_gb300 import _lib
 
     keep = [np.ascontiguousarray(m.nodes, np.float64).ravel(), np.ascontiguousarray(m.tets, np.int32).ravel(),
             np.ascontiguousarray(m.young, np.float64), np.ascontiguousarray(m.poisson, np.float64),
             np.ascontiguousarray(m.density, np.float64), np.ascontiguousarray(m.bc_dofs, np.int32)]
-    d = _lib.MeshDesc(keep[0].size // 3, _lib.dptr(keep[0]), keep[1].size // 4, _lib.iptr(keep[1]), _lib.dptr(keep[2]),
-                      _lib.dptr(keep[3]), _lib.dptr(keep[4]), keep[5].size, _lib.iptr(keep[5]))
+    d = _lib.MeshDesc(keep[0].size // 3, _lib.dptr(keep[0]), keep[1].size // npe, _lib.iptr(keep[1]),
+                      _lib.dptr(keep[2]), _lib.dptr(keep[3]), _lib.dptr(keep[4]), keep[5].size,
+                      _lib.iptr(keep[5]) if keep[5].size else None)
     return d, keep
+
+
+def _create_hex(lib, m):
+    from opensurgsim_gb300 import _lib
+
+    d, keep = _desc(m, npe=8)
+    p = _lib.Params()
+    lib.gbfem_params_default(ctypes.byref(p))
+    p.element_type = _lib.ELEMENT_HEXAHEDRON
+    h = ctypes.c_void_p()
+    st = lib.gbfem_create(ctypes.byref(d), ctypes.byref(p), ctypes.byref(h))
+    if h.value:
+        lib.gbfem_destroy(h)
+    return st
+
+
+def test_hexahedron_orderings_checked_on_the_host(lib):
+    """Fem3DElementCubeTests.cpp NodeOrderingTest / VolumeTest cases through gbfem_create: the
+    orderings the reference's initialize rejects fail with DEGENERATE_ELEMENT before any device
+    work; the accepted ones pass the host checks (and then need a GPU)."""
+    from opensurgsim_gb300 import _lib, mesh
+    from test_oracle_hex import NODE_IDS, POINTS, hex_orderings
+
+    for ids, bad in hex_orderings():
+        m = mesh.TetMesh(POINTS.copy(), np.array([ids], np.int32), np.array([1e6]), np.array([0.45]),
+                         np.array([1000.0]), np.zeros(0, np.int32))
+        st = _create_hex(lib, m)
+        if bad:
+            assert st == _lib.GBFEM_DEGENERATE_ELEMENT, ids
+        else:
+            assert st in (_lib.GBFEM_OK, _lib.GBFEM_CUDA_ERROR), ids
+    flat = POINTS.copy()
+    flat[4:] = flat[:4]
+    m = mesh.TetMesh(flat, np.array([NODE_IDS], np.int32), np.array([1e6]), np.array([0.45]), np.array([1000.0]),
+                     np.zeros(0, np.int32))
+    assert _create_hex(lib, m) == _lib.GBFEM_DEGENERATE_ELEMENT
+    rep = list(NODE_IDS)
+    rep[5] = rep[0]
+    m.nodes = POINTS.copy()
+    m.tets = np.array([rep], np.int32)
+    assert _create_hex(lib, m) == _lib.GBFEM_INVALID_ARG
 
 
 @pytest.mark.parametrize("bad", ["node", "material", "bc", "nu", "repeat", "empty"])
