@@ -6,8 +6,8 @@
 // resident in HBM in the SELL-32 layout of the system matrix and
 //   * forms S = (1/dt + alpha) M + (dt + beta) K with the boundary conditions once per dt
 //     (k_system_from_k), and
-//   * forms each step's right-hand side in one pass over K and M (k_hex_rhs), reading the state
-//     vectors through L2:
+//   * forms each step's right-hand side in one pass over K and M (k_hex_rhs, after k_hex_uw has
+//     formed the two per-node vectors it needs), reading them through L2:
 //       rhs = f(x_n, v_n) + K (x_n - x_t - dt v_n) - M (v_n - v_t) / dt
 //           = -K (x_t - x0 + (dt + beta) v_n) - M (alpha v_n + (v_n - v_t) / dt) + g m_lumped
 //     (OdeSolverEulerImplicit.cpp:124-161 with FemRepresentation::computeFMDK, :479-545; x_n cancels).
@@ -216,13 +216,34 @@ __global__ void k_system_from_k(DevBody b, const double* __restrict__ K, double 
 	}
 }
 
-// One thread per SELL row (a warp is one chunk of 32 rows: every K value, mass and column load is
-// coalesced); the state vectors are gathered per block column.
+// Per node: u = (x_t - x0) + (dt + beta) v_n and w = alpha v_n + (v_n - v_t) / dt, one 48-byte
+// record (u, w) per node, so the matrix pass below gathers one record per block column and spends
+// only its 12 FMAs per block on FP64 arithmetic (FP64 issues at 1/64 of the FP32 rate here).
+__global__ void k_hex_uw(int N, const double* __restrict__ xrest, const double* __restrict__ xt,
+						 const double* __restrict__ vn, const double* __restrict__ vt, double alpha, double c2,
+						 double inv_dt, double2* __restrict__ uw)
+{
+	const int I = blockIdx.x * blockDim.x + threadIdx.x;
+	if (I >= N) return;
+	double u[3], w[3];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		const double v = vn[3 * I + i];
+		u[i] = (xt[3 * I + i] - xrest[3 * I + i]) + c2 * v;
+		w[i] = alpha * v + (v - vt[3 * I + i]) * inv_dt;
+	}
+	uw[3 * (size_t)I] = make_double2(u[0], u[1]);
+	uw[3 * (size_t)I + 1] = make_double2(u[2], w[0]);
+	uw[3 * (size_t)I + 2] = make_double2(w[1], w[2]);
+}
+
+// rhs = -(K u + M w) + g m_lumped with the boundary rows zeroed. One thread per SELL row (a warp is
+// one chunk of 32 rows: every K value, mass and column load is coalesced).
 __global__ void __launch_bounds__(256)
-	k_hex_rhs(MatSell3 K, const double* __restrict__ Ms, const double* __restrict__ xrest,
-			  const double* __restrict__ nmass, const uint8_t* __restrict__ bc, const double* __restrict__ xt,
-			  const double* __restrict__ vn, const double* __restrict__ vt, double alpha, double c2, double inv_dt,
-			  double g0, double g1, double g2, int gravityOn, double* __restrict__ rhs)
+	k_hex_rhs(MatSell3 K, const double* __restrict__ Ms, const double2* __restrict__ uw,
+			  const double* __restrict__ nmass, const uint8_t* __restrict__ bc, double g0, double g1, double g2,
+			  int gravityOn, double* __restrict__ rhs)
 {
 	const int rs = blockIdx.x * blockDim.x + threadIdx.x;
 	if (rs >= K.rows) return;
@@ -235,17 +256,10 @@ __global__ void __launch_bounds__(256)
 		const int J = K.col[k * 32 + lane];
 		const double* kb = K.val + (size_t)k * 288 + lane;
 		const double m = Ms[k * 32 + lane];
-		double u[3], w[3];
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
-		{
-			const double v = vn[3 * J + i];
-			u[i] = (xt[3 * J + i] - xrest[3 * J + i]) + c2 * v;
-			w[i] = alpha * v + (v - vt[3 * J + i]) * inv_dt;
-		}
-		a0 += kb[0] * u[0] + kb[32] * u[1] + kb[64] * u[2] + m * w[0];
-		a1 += kb[96] * u[0] + kb[128] * u[1] + kb[160] * u[2] + m * w[1];
-		a2 += kb[192] * u[0] + kb[224] * u[1] + kb[256] * u[2] + m * w[2];
+		const double2 r0 = uw[3 * (size_t)J], r1 = uw[3 * (size_t)J + 1], r2 = uw[3 * (size_t)J + 2];
+		a0 += kb[0] * r0.x + kb[32] * r0.y + kb[64] * r1.x + m * r1.y;
+		a1 += kb[96] * r0.x + kb[128] * r0.y + kb[160] * r1.x + m * r2.x;
+		a2 += kb[192] * r0.x + kb[224] * r0.y + kb[256] * r1.x + m * r2.y;
 	}
 	double r0 = -a0, r1 = -a1, r2 = -a2;
 	if (gravityOn)  // FemRepresentation::addGravityForce (:641-662), lumped rho V / 8 per node
@@ -293,11 +307,13 @@ void launch_system_from_k(const DevBody& b, const double* K, double c1, double c
 
 void launch_hex_rhs(const MatSell3& K, const double* Ms, const DevBody& b, const double* xt, const double* vn,
 					const double* vt, double dt, double alpha, double beta, const double* gravity, int gravityOn,
-					double* rhs, cudaStream_t s)
+					double* uw, double* rhs, cudaStream_t s)
 {
 	if (K.rows == 0) return;
-	k_hex_rhs<<<blocks_for(K.rows, 256), 256, 0, s>>>(K, Ms, b.xrest, b.nmass, b.bc, xt, vn, vt, alpha, dt + beta,
-													  1.0 / dt, gravity[0], gravity[1], gravity[2], gravityOn, rhs);
+	double2* uw2 = reinterpret_cast<double2*>(uw);  // 6 doubles per node, 16-byte aligned allocation
+	k_hex_uw<<<blocks_for(b.N, 256), 256, 0, s>>>(b.N, b.xrest, xt, vn, vt, alpha, dt + beta, 1.0 / dt, uw2);
+	k_hex_rhs<<<blocks_for(K.rows, 256), 256, 0, s>>>(K, Ms, uw2, b.nmass, b.bc, gravity[0], gravity[1], gravity[2],
+													  gravityOn, rhs);
 }
 
 }  // namespace gbfem

@@ -167,9 +167,10 @@ void launch_system_from_k(const DevBody& b, const double* K, double c1, double c
 						  cudaStream_t s);
 void launch_system_from_k(const DevBody& b, const double* K, double c1, double c2, float* A, float* invdiag,
 						  cudaStream_t s);
+// uw: scratch of 6 doubles per node (16-byte aligned); two launches.
 void launch_hex_rhs(const MatSell3& K, const double* Ms, const DevBody& b, const double* xt, const double* vn,
 					const double* vt, double dt, double alpha, double beta, const double* gravity, int gravityOn,
-					double* rhs, cudaStream_t s);
+					double* uw, double* rhs, cudaStream_t s);
 
 // Partial-sum buffer size needed by the reductions for a given vecGrid.
 constexpr int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }

@@ -210,17 +210,21 @@ __device__ __forceinline__ int2 seg_ctas(const PcgArgs& a, const SetView& V, con
 	return make_int2(cta_of(V.Wp[s], V.tot, G), cta_of(wl, V.tot, G));
 }
 
-// Calls f(slot, s, c) for this warp's share of the CTA's positions: slot = t - lo, s the
-// segment and c the chunk of position t.
+// Calls f(slot, s, c) for the CTA's positions [lo, hi): slot = t - lo, s the segment and c the
+// chunk of position t. Warps take the next position from a shared counter (zeroed before the
+// phase), so a warp that drew short chunks takes more of them; the results do not depend on
+// which warp ran a position (partials are kept per slot and summed in slot order).
 template <typename F>
-__device__ __forceinline__ void for_chunks(const SetView& V, const int* sc, int nseg, F f)
+__device__ __forceinline__ void for_chunks(const SetView& V, const int* sc, int nseg, int* next, F f)
 {
-	int t = V.lo + (threadIdx.x >> 5);
-	if (t >= V.hi) return;
-	int s = seg_of(V.Cp, nseg, t);
-	for (; t < V.hi; t += kWarps)
+	const int lane = threadIdx.x & 31;
+	for (;;)
 	{
-		while (V.Cp[s + 1] <= t) ++s;
+		int k = 0;
+		if (lane == 0) k = atomicAdd(next, 1);
+		const int t = V.lo + __shfl_sync(kFull, k, 0);
+		if (t >= V.hi) return;
+		const int s = seg_of(V.Cp, nseg, t);
 		f(t - V.lo, s, sc[s] + (t - V.Cp[s]));
 	}
 }
@@ -380,6 +384,8 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	int* Wp = Cp + (nseg + 1);                         // active set: weight prefix
 	__shared__ int shRange[4];
 	__shared__ int shFinished;
+	__shared__ int shNext;  // next position of the current phase (for_chunks)
+	if (threadIdx.x == 0) shNext = 0;
 	for (int i = threadIdx.x; i <= nseg; i += blockDim.x) sc[i] = a.segChunk[i];
 	__syncthreads();
 
@@ -498,13 +504,16 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		if (force || nf > 0 || (phase1 && (shRefresh > 0 || weighted))) weighted = rebuild(phase1);
 	};
 	auto barrier = [&]() {
+		// Every warp has left the phase's for_chunks (reduce_segments began with __syncthreads);
+		// grid_barrier's __syncthreads orders this reset before the next phase's first draw.
+		if (threadIdx.x == 0) shNext = 0;
 		const bool ok = grid_barrier(a.g, ph);
 		++ph;
 		return ok;
 	};
 
 	// ---- I1: gather b, invdiag into row space; x = 0; p = 0; |b|^2 per segment.
-	for_chunks(all, sc, nseg, [&](int slot, int, int c) {
+	for_chunks(all, sc, nseg, &shNext, [&](int slot, int, int c) {
 		const int rs = 32 * c + lane;
 		const int I = a.perm[rs];
 		double bb = 0.0;
@@ -542,7 +551,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 
 	// ---- I2: r = b / s (FP32), z = invdiag r, rz, |r|^2.
 	phase_start(false, true);
-	for_chunks(actC, sc, nseg, [&](int slot, int s, int c) {
+	for_chunks(actC, sc, nseg, &shNext, [&](int slot, int s, int c) {
 		const int rs = 32 * c + lane;
 		const double inv = 1.0 / ldd(&a.seg[s].s);
 		float rz = 0.f, rr = 0.f, z[3];
@@ -578,7 +587,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		// q = A p_new; pq. mode 1: r64 = b - A (x64 + x_delta) in FP64.
 		phase_start(true, false);
 		if (finished >= nseg) break;
-		for_chunks(actW, sc, nseg, [&](int slot, int s, int c) {
+		for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
 			double part, betaD;
 			int mode;
@@ -635,7 +644,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		// ---- Phase 2. mode 0: x_delta += alpha s p, r -= alpha q, z = invdiag r; |r|^2, r.z; decide
 		// on a refresh. mode 2: fold x, r = r64 / s, z = invdiag r, p *= ratio; |r|^2, r.z.
 		phase_start(false, false);
-		for_chunks(actC, sc, nseg, [&](int slot, int s, int c) {
+		for_chunks(actC, sc, nseg, &shNext, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
 			float s0 = 0.f, s1 = 0.f, z[3];
 			double betaD;
@@ -730,7 +739,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	}
 
 	// ---- Out: x (dof space) = x64 + x_delta.
-	for_chunks(all, sc, nseg, [&](int, int, int c) {
+	for_chunks(all, sc, nseg, &shNext, [&](int, int, int c) {
 		const int rs = 32 * c + lane;
 		const int I = a.perm[rs];
 		if (I < 0) return;

@@ -4,7 +4,8 @@ Reads the element layout that ``Fem3DPlyReaderDelegate`` / ``FemPlyReaderDelegat
 (``Physics/Fem3DPlyReaderDelegate.cpp:30-100``, ``Physics/FemPlyReaderDelegate.cpp:31-191``) consume:
 
 - ``vertex`` with ``x y z``;
-- ``3d_element`` with a ``vertex_indices`` list (4 ids for tetrahedra), optionally carrying its own
+- ``3d_element`` with a ``vertex_indices`` list (4 ids per tetrahedron or 8 per hexahedron, the
+  counts Fem3DPlyReaderDelegate.cpp:76 accepts; one count per file), optionally carrying its own
   ``mass_density``, ``poisson_ratio`` and ``young_modulus``;
 - ``material`` (one row: ``mass_density poisson_ratio young_modulus``) applied to every element that
   carries none;
@@ -106,7 +107,8 @@ def _read_elements(f, fmt, elements):
 
 
 def load_fem3d(path) -> TetMesh:
-    """Read a tetrahedral FEM-3D PLY file (the format Fem3DRepresentation::loadFem reads)."""
+    """Read a FEM-3D PLY file (the format Fem3DRepresentation::loadFem reads). ``tets`` of the result
+    has 4 columns for tetrahedra, 8 for hexahedra (Fem3DElementCube node order)."""
     with open(path, "rb") as f:
         fmt, elements = _parse_header(f)
         data = _read_elements(f, fmt, elements)
@@ -118,8 +120,11 @@ def mesh_from_ply_data(data) -> TetMesh:
         raise PlyError("missing vertex or 3d_element")
     nodes = np.array([[r["x"], r["y"], r["z"]] for r in data["vertex"]], dtype=np.float64)
     els = data["3d_element"]
-    if any(len(r["vertex_indices"]) != 4 for r in els):
-        raise PlyError("only 4-node (tetrahedral) 3d_elements are supported")
+    counts = {len(r["vertex_indices"]) for r in els}
+    if not counts <= {4, 8}:
+        raise PlyError("3d_element vertex counts must be 4 (tetrahedra) or 8 (hexahedra)")
+    if len(counts) > 1:
+        raise PlyError("a mesh holds one element type: 4- and 8-node 3d_elements are mixed")
     tets = np.array([r["vertex_indices"] for r in els], dtype=np.int64)
     if tets.min() < 0 or tets.max() >= nodes.shape[0]:
         raise PlyError("element refers to a missing vertex")

@@ -75,7 +75,7 @@ def _write_ascii(path, m, material_per_element=False):
         f.write("3 0 1 2\n")
         for e, t in enumerate(m.tets):
             extra = " %.17g %.17g %.17g" % (m.density[e], m.poisson[e], m.young[e]) if material_per_element else ""
-            f.write("4 %d %d %d %d%s\n" % (*t, extra))
+            f.write("%d %s%s\n" % (len(t), " ".join(str(int(i)) for i in t), extra))
         if not material_per_element:
             f.write("%.17g %.17g %.17g\n" % (m.density[0], m.poisson[0], m.young[0]))
         for n in m.bc_dofs[::3] // 3:
@@ -112,6 +112,19 @@ def test_ply_roundtrip(tmp_path, kind):
     assert np.allclose(r.nodes, m.nodes, rtol=0, atol=0)
     assert np.array_equal(r.tets, m.tets) and np.array_equal(r.bc_dofs, m.bc_dofs)
     assert np.allclose(r.young, m.young) and np.allclose(r.poisson, m.poisson) and np.allclose(r.density, m.density)
+
+
+def test_ply_hexahedra(tmp_path):
+    from oracle import oracle as O
+
+    m = mesh.scene_divisible_cube(3).mesh
+    path = tmp_path / "hex.ply"
+    _write_ascii(path, m)
+    r = ply.load_fem3d(path)
+    assert r.tets.shape == (8, 8) and np.array_equal(r.tets, m.tets)
+    assert np.array_equal(r.bc_dofs, m.bc_dofs) and np.allclose(r.young, 15.3e3)
+    o = O.OracleModel(r, element_type=2)
+    assert o.mass_per_node().sum() == pytest.approx(980.0 * 6.0 ** 3)
 
 
 def test_ply_rejects_bad_files(tmp_path):
