@@ -95,7 +95,7 @@ typedef struct gbfem_stats
 	int32_t steps;                  /* steps applied */
 	int32_t cg_iterations;          /* summed over steps and Newton iterations (Eigen's count) */
 	int32_t cg_max_iterations_hit;  /* number of solves that stopped at maxIterations */
-	int32_t refinement_sweeps;      /* mixed precision: FP64 residual evaluations */
+	int32_t refinement_sweeps;      /* mixed precision: true-residual evaluations (refreshes) */
 	double cg_relative_residual;    /* of the last solve: sqrt(|r|^2/|b|^2) */
 	double ms_element, ms_assemble, ms_solve, ms_update;  /* device time per phase (if timed) */
 	int32_t singular_g;             /* element updates that hit the singular-G early return */
@@ -187,7 +187,7 @@ GBFEM_API gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, con
 
 /* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
  * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
- * CTAs per SM and refresh weights 4, 6, 8 on its own system, and keeps the fastest. The solve's
+ * CTAs per SM and refresh weights 1 to 4 on its own system, and keeps the fastest. The solve's
  * partition sets the rounding of its sums, so a run that must repeat another bit for bit reads the
  * choice with gbfem_get_tuning and pins it with gbfem_set_tuning (which also disables autotune). */
 GBFEM_API gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm,
@@ -229,7 +229,7 @@ GBFEM_API gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* 
  * each mesh's system matrix (count entries) in the batch. Any pointer may be NULL. */
 GBFEM_API gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets,
 										int32_t* tet_offsets, int64_t* nnz_per_mesh);
-/* Per mesh, over the last gbfem_step call: CG iterations, FP64 residual refreshes, converged (all
+/* Per mesh, over the last gbfem_step call: CG iterations, true-residual refreshes, converged (all
  * steps), worst relative residual. Arrays of `count` entries (any may be NULL). */
 GBFEM_API gbfem_status gbfem_batch_segment_stats(gbfem_handle h, int32_t* iterations, int32_t* refreshes,
 												 int32_t* converged, double* relative_residual);

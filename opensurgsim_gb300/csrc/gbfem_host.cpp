@@ -904,7 +904,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	a.x = x;
 	a.brs = h->d_brs.p;
 	a.r64 = h->d_r64.p;
-	a.x64 = h->d_x64.p;
+	a.xhl = reinterpret_cast<float2*>(h->d_x64.p);  // 8 bytes per dof: one float pair
 	a.xd = h->d_xd.p;
 	a.invd = h->d_invd.p;
 	a.r = h->d_r32.p;
@@ -984,7 +984,7 @@ void enqueue_hex_rhs(gbfem_handle h, double dt, const double* xt, const double* 
 
 // Autotuner of the mixed form, run on the first step's own system: times the element kernel at 32
 // and 64 elements per block, then the persistent solve for 2, 3 and 4 CTAs per SM and refresh
-// weights 4, 6 and 8, and keeps the fastest of each. The element kernel's results do not depend on
+// weights 1 to 4, and keeps the fastest of each. The element kernel's results do not depend on
 // its block size; the solve's partition does change its rounding (not its convergence test), so a
 // run that must reproduce another bit for bit pins the choice with gbfem_set_tuning.
 gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, double dt, double c1, double c2,
@@ -1042,7 +1042,7 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 			(void)cudaGetLastError();  // an infeasible candidate is skipped; clear any error it left
 			continue;
 		}
-		for (int rw : {4, 6, 8})
+		for (int rw : {1, 2, 3, 4})
 		{
 			h->refreshWeight = rw;
 			gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, e0, e1);

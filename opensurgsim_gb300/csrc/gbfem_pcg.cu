@@ -1,15 +1,16 @@
 // gbfem_pcg.cu -- persistent mixed-precision CG over a batch of independent systems (segments).
 //
 // One cooperative launch runs a whole solve for every segment (mesh) of a batch: FP32 CG
-// iterations on the FP32 SELL-32 matrix with per-segment scalars, the solution accumulated in
-// FP64 (FP32 deltas folded at each refresh), and per-segment "reliable updates": when a
-// segment's FP32 residual has dropped by `drop` since its last refresh (or looks converged), its
-// true FP64 residual b - A x is recomputed and convergence is decided on it, at the same
+// iterations on the FP32 SELL-32 matrix with per-segment scalars, the solution accumulated as a
+// float pair hi + lo (~48 bits; FP32 deltas folded at each refresh), and per-segment "reliable
+// updates": when a segment's FP32 residual has dropped by `drop` since its last refresh (or looks
+// converged), its true residual b - A x is recomputed in double-float arithmetic (FP64 products
+// would run at 1/64 of the FP32 rate) and convergence is decided on it, at the same
 // |r|^2 < tol^2 |b|^2 rule as the FP64 form (Eigen's ConjugateGradient).
 //
 // Work is cut into chunks of 32 matrix rows (one node row per lane); segments own contiguous
 // chunk ranges. Every iteration has two phases separated by grid barriers: phase 1 is the SpMV
-// (or, for a segment due for a refresh, the FP64 residual), phase 2 the row-local update (or the
+// (or, for a segment due for a refresh, the true residual), phase 2 the row-local update (or the
 // rescale after a refresh). Each phase walks only the chunks of the segments still iterating
 // (the active set), split over the CTAs by exact integer arithmetic on cumulative weights: the
 // SpMV phase balances block columns, the row-local phase chunk counts. Every CTA recomputes
@@ -302,7 +303,9 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 }
 
 // q[row] (3 floats) = sum over the chunk's SELL slots of A_block * p(J), with p(J) = z(J) + beta p_old(J)
-// formed on the fly from the packed records; four slots' loads are issued before any is used.
+// formed on the fly from the packed records; four slots' loads are issued before any is used. The
+// matrix (values, columns) is read once per pass with the streaming hint (evict first), so L2 keeps
+// the gathered z/p records, which rows a mesh layer apart reuse.
 __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __restrict__ zp, int c, int lane,
 											float beta, float& a0, float& a1, float& a2)
 {
@@ -312,7 +315,7 @@ __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __re
 	{
 		int J[4];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) J[u] = __ldg(&a.col[(k + u) * 32 + lane]);
+		for (int u = 0; u < 4; ++u) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
 		float4 zj[4], pj[4];
 #pragma unroll
 		for (int u = 0; u < 4; ++u)
@@ -325,45 +328,87 @@ __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __re
 		{
 			const float* vb = a.val + (size_t)(k + u) * 288 + lane;
 			const float p0 = zj[u].x + beta * pj[u].x, p1 = zj[u].y + beta * pj[u].y, p2 = zj[u].z + beta * pj[u].z;
-			a0 += __ldg(vb) * p0 + __ldg(vb + 32) * p1 + __ldg(vb + 64) * p2;
-			a1 += __ldg(vb + 96) * p0 + __ldg(vb + 128) * p1 + __ldg(vb + 160) * p2;
-			a2 += __ldg(vb + 192) * p0 + __ldg(vb + 224) * p1 + __ldg(vb + 256) * p2;
+			a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
+			a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
+			a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
 		}
 	}
 	for (; k < k1; ++k)
 	{
-		const int J = __ldg(&a.col[k * 32 + lane]);
+		const int J = __ldcs(&a.col[k * 32 + lane]);
 		const float* vb = a.val + (size_t)k * 288 + lane;
 		const float4 zj = zp[2 * J], pj = zp[2 * J + 1];
 		const float p0 = zj.x + beta * pj.x, p1 = zj.y + beta * pj.y, p2 = zj.z + beta * pj.z;
-		a0 += __ldg(vb) * p0 + __ldg(vb + 32) * p1 + __ldg(vb + 64) * p2;
-		a1 += __ldg(vb + 96) * p0 + __ldg(vb + 128) * p1 + __ldg(vb + 160) * p2;
-		a2 += __ldg(vb + 192) * p0 + __ldg(vb + 224) * p1 + __ldg(vb + 256) * p2;
+		a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
+		a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
+		a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
 	}
 }
 
-// FP64 residual rows of chunk c: r64 = b - A (x64 + x_delta); returns the lane's |r|^2 share.
+// Error-free transformations in FP32 (Knuth's TwoSum; the product's rounding error by FMA):
+// a + b = s + e and a * b = p + e exactly. The _rn intrinsics keep the compiler from contracting or
+// reassociating them.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+	s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// True residual rows of chunk c: r64 = b - A (x_hl + x_delta); returns the lane's |r|^2 share.
+// A x is accumulated in double-float arithmetic: per column the solution t + u = (hi + x_delta) + lo
+// with t the rounded sum, every product a t split exactly into p + e by FMA, p added to the row's
+// high word by TwoSum and the low parts (TwoSum error, product error, a u) into its low word, the
+// pair renormalised once a block. Only b - (hi + lo) runs in FP64, once per row. On random rows of up
+// to 81 terms with strong cancellation the error stays within 1.4e-14 of sum |a x| (FP64
+// accumulation of the same rows: ~1e-14), at about 140 FP32 operations a block against 9 FP64 FMAs,
+// which run at 1/64 of the FP32 rate here.
 __device__ __forceinline__ double residual_row(const PcgArgs& a, int c, int rs, int lane)
 {
-	double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+	float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
 	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
 	for (int k = k0; k < k1; ++k)
 	{
-		const int J = __ldg(&a.col[k * 32 + lane]);
+		const int J = __ldcs(&a.col[k * 32 + lane]);
 		const float* vp = a.val + (size_t)k * 288 + lane;
-		const double x0 = a.x64[3 * J] + double(a.xd[3 * J]);
-		const double x1 = a.x64[3 * J + 1] + double(a.xd[3 * J + 1]);
-		const double x2 = a.x64[3 * J + 2] + double(a.xd[3 * J + 2]);
-		a0 += double(__ldg(vp)) * x0 + double(__ldg(vp + 32)) * x1 + double(__ldg(vp + 64)) * x2;
-		a1 += double(__ldg(vp + 96)) * x0 + double(__ldg(vp + 128)) * x1 + double(__ldg(vp + 160)) * x2;
-		a2 += double(__ldg(vp + 192)) * x0 + double(__ldg(vp + 224)) * x1 + double(__ldg(vp + 256)) * x2;
+		float t[3], u[3];
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			const float2 x = a.xhl[3 * J + j];
+			float e;
+			two_sum(x.x, a.xd[3 * J + j], t[j], e);
+			u[j] = __fadd_rn(e, x.y);
+		}
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				const float v = __ldcs(vp + 32 * (3 * i + j));
+				const float p = __fmul_rn(v, t[j]);
+				const float pe = __fmaf_rn(v, t[j], -p);
+				float hs, he;
+				two_sum(sh[i], p, hs, he);
+				sh[i] = hs;
+				sl[i] = __fadd_rn(sl[i], __fadd_rn(he, __fmaf_rn(v, u[j], pe)));
+			}
+		// Renormalise each row's pair once a block, so the low word stays below half an ulp of the
+		// high word and its own rounding stays at 2^-48 of the partial sum.
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+			float hs, hl;
+			two_sum(sh[i], sl[i], hs, hl);
+			sh[i] = hs;
+			sl[i] = hl;
+		}
 	}
-	const double aa[3] = {a0, a1, a2};
 	double rr = 0.0;
 #pragma unroll
 	for (int i = 0; i < 3; ++i)
 	{
-		const double ri = a.brs[3 * rs + i] - aa[i];
+		const double ri = a.brs[3 * rs + i] - (double(sh[i]) + double(sl[i]));
 		a.r64[3 * rs + i] = ri;
 		rr += ri * ri;
 	}
@@ -412,7 +457,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	actW.Wp = Wp;
 	actC.Wp = nullptr;
 	// Rebuild the active-set prefixes and this CTA's ranges (segments stamped before phase ph are
-	// out). In phase 1 a segment switched to its FP64 residual in the phase before weighs
+	// out). In phase 1 a segment switched to its true residual in the phase before weighs
 	// refreshWeight times its block columns. Returns whether any segment was so weighted.
 	__shared__ int shWeighted;
 	auto rebuild = [&](bool phase1) {
@@ -524,7 +569,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			a.brs[3 * rs + k] = bi;
 			a.r64[3 * rs + k] = bi;
 			a.invd[3 * rs + k] = (I >= 0) ? a.invdiag[3 * I + k] : 0.f;
-			a.x64[3 * rs + k] = 0.0;
+			a.xhl[3 * rs + k] = make_float2(0.f, 0.f);
 			a.xd[3 * rs + k] = 0.f;
 			bb += bi * bi;
 		}
@@ -584,7 +629,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	for (int it = 0; it < maxLoop; ++it)
 	{
 		// ---- Phase 1. mode 0: p_new = z + beta p_old (own rows, and on the fly for gathered rows);
-		// q = A p_new; pq. mode 1: r64 = b - A (x64 + x_delta) in FP64.
+		// q = A p_new; pq. mode 1: r64 = b - A (x_hl + x_delta), accumulated in double-float.
 		phase_start(true, false);
 		if (finished >= nseg) break;
 		for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
@@ -600,9 +645,9 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				const float4 zi = zpOld[2 * rs], pi = zpOld[2 * rs + 1];
 				const float4 pn = make_float4(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z, 0.f);
 				zpNew[2 * rs + 1] = pn;
-				a.q[3 * rs] = a0;
-				a.q[3 * rs + 1] = a1;
-				a.q[3 * rs + 2] = a2;
+				__stcs(&a.q[3 * rs], a0);
+				__stcs(&a.q[3 * rs + 1], a1);
+				__stcs(&a.q[3 * rs + 2], a2);
 				part = warp_sum(pn.x * a0 + pn.y * a1 + pn.z * a2);
 			}
 			else
@@ -661,11 +706,12 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 #pragma unroll
 				for (int i = 0; i < 3; ++i)
 				{
+					// Row-local vectors, touched once a phase: streaming hint (L2 keeps the z/p records).
 					const int d = 3 * rs + i;
-					a.xd[d] += as * pv[i];
-					const float ri = a.r[d] - alpha * a.q[d];
-					a.r[d] = ri;
-					z[i] = a.invd[d] * ri;
+					__stcs(&a.xd[d], __ldcs(&a.xd[d]) + as * pv[i]);
+					const float ri = __ldcs(&a.r[d]) - alpha * __ldcs(&a.q[d]);
+					__stcs(&a.r[d], ri);
+					z[i] = __ldcs(&a.invd[d]) * ri;
 					s0 += ri * ri;
 					s1 += ri * z[i];
 				}
@@ -678,11 +724,16 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				for (int i = 0; i < 3; ++i)
 				{
 					const int d = 3 * rs + i;
-					a.x64[d] += double(a.xd[d]);
-					a.xd[d] = 0.f;
-					const float ri = float(a.r64[d] * inv);
-					a.r[d] = ri;
-					z[i] = a.invd[d] * ri;
+					// Fold x_delta into the float pair: TwoSum, then renormalise.
+					const float2 xo = a.xhl[d];
+					float hs, he, h2, l2;
+					two_sum(xo.x, __ldcs(&a.xd[d]), hs, he);
+					two_sum(hs, __fadd_rn(he, xo.y), h2, l2);
+					a.xhl[d] = make_float2(h2, l2);
+					__stcs(&a.xd[d], 0.f);
+					const float ri = float(__ldcs(&a.r64[d]) * inv);
+					__stcs(&a.r[d], ri);
+					z[i] = __ldcs(&a.invd[d]) * ri;
 					s0 += ri * ri;
 					s1 += ri * z[i];
 				}
@@ -719,7 +770,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			}
 			else if (S.s * S.s * tot[0] < S.threshold || tot[0] < a.drop * S.rrLast || S.iter + 1 >= a.maxIter)
 			{
-				S.mode = 1;  // FP64 residual before the next direction
+				S.mode = 1;  // true residual before the next direction
 				S.refreshAt = ph;
 				S.rzPend = S.rz;
 				atomicAdd(&a.g->refreshIn[ph & 1], 1);
@@ -738,13 +789,17 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		zpNew = t;
 	}
 
-	// ---- Out: x (dof space) = x64 + x_delta.
+	// ---- Out: x (dof space) = x_hl + x_delta.
 	for_chunks(all, sc, nseg, &shNext, [&](int, int, int c) {
 		const int rs = 32 * c + lane;
 		const int I = a.perm[rs];
 		if (I < 0) return;
 #pragma unroll
-		for (int k = 0; k < 3; ++k) a.x[3 * I + k] = a.x64[3 * rs + k] + double(a.xd[3 * rs + k]);
+		for (int k = 0; k < 3; ++k)
+		{
+			const float2 xv = a.xhl[3 * rs + k];
+			a.x[3 * I + k] = (double(xv.x) + double(xv.y)) + double(a.xd[3 * rs + k]);
+		}
 	});
 }
 

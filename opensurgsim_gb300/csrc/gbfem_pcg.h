@@ -37,12 +37,13 @@ struct PcgGlobal
 	int finishedSegs;    // total, for diagnostics
 	int err;
 	int finishedIn[2];   // segments finished in a phase, by phase parity
-	int refreshIn[2];    // segments switched to an FP64 residual in a phase, by phase parity
+	int refreshIn[2];    // segments switched to a true-residual refresh in a phase, by phase parity
 };
 
-// Weight of a chunk of a segment doing its FP64 residual (phase 1), relative to an FP32 SpMV chunk:
-// a tuning choice (PcgArgs::refreshWeight), at most kRefreshWeightMax.
-constexpr int kRefreshWeightDefault = 6;
+// Weight of a chunk of a segment doing its true residual (phase 1, double-float), relative to an
+// FP32 SpMV chunk: a tuning choice (PcgArgs::refreshWeight), at most kRefreshWeightMax. Measured
+// best at 2 on the 256-mesh batch (with an FP64 residual it was 6).
+constexpr int kRefreshWeightDefault = 2;
 constexpr int kRefreshWeightMax = 8;
 
 struct PcgArgs
@@ -65,7 +66,7 @@ struct PcgArgs
 	// row-space work vectors
 	double* brs;
 	double* r64;
-	double* x64;
+	float2* xhl;           // FP64 part of the solution as an unevaluated float pair hi + lo, 3 per row
 	float* xd;
 	float* invd;
 	float* r;
