@@ -298,6 +298,56 @@ __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __
 	in.betaDbg = beta;
 }
 
+// Inputs of the FP32 element kernel. Positions relative to node 0 stay FP64 (the Gram differences
+// of the strain are formed from them); the right-hand-side inputs are FP32, formed from the FP64
+// differences x_n - x_t and v_n - v_t (0 in the first Newton iteration), so the gather spends four
+// FP64 subtractions a dof and no FP64 division (FP64 issues at 1/64 of the FP32 rate here).
+struct ElemInF
+{
+	int nd[4];
+	double p[4][3];   // x_n,a - x_n,0
+	double q[4][3];   // x0_a - x0_0
+	float uK[4][3];   // (x_n - x_t) - (beta + dt) v_n
+	float uM[4][3];   // -alpha v_n - (v_n - v_t) / dt
+	float vv[4][3];   // v_n (debug force only; unused by the FP32 kernel)
+	double alphaDbg, betaDbg;
+};
+
+__device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double* __restrict__ xn,
+										   const double* __restrict__ vn, const double* __restrict__ xt,
+										   const double* __restrict__ vt, float c2, float alpha, float inv_dt,
+										   ElemInF& in)
+{
+	const int4 t4 = b.tets[e];
+	in.nd[0] = t4.x;
+	in.nd[1] = t4.y;
+	in.nd[2] = t4.z;
+	in.nd[3] = t4.w;
+	double x0[3], r0[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+	{
+		x0[k] = xn[3 * in.nd[0] + k];
+		r0[k] = b.xrest[3 * in.nd[0] + k];
+	}
+#pragma unroll
+	for (int a = 0; a < 4; ++a)
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			const int d = 3 * in.nd[a] + k;
+			const double xa = xn[d], va = vn[d];
+			in.p[a][k] = xa - x0[k];
+			in.q[a][k] = b.xrest[d] - r0[k];
+			const float vf = float(va);
+			in.uK[a][k] = __fmaf_rn(-c2, vf, float(xa - xt[d]));
+			in.uM[a][k] = -alpha * vf - float(va - vt[d]) * inv_dt;
+			in.vv[a][k] = vf;
+		}
+	in.alphaDbg = 0.0;
+	in.betaDbg = 0.0;
+}
+
 // Rotation, tangent blocks and right-hand-side share of one element.
 //   ks[k * ksStride], k = slot*9 + entry: the element's lower-triangle blocks (kSlots of them);
 //   rhs[j * rhsStride], j = 3a+i: f_e + K_e uK + M0 uM (the element's share of the

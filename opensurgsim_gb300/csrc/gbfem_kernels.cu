@@ -67,15 +67,15 @@ __global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __r
 	const int E = b.E;
 	if (e < E)
 	{
-		elem::ElemIn in;
-		elem::gather(b, e, xn, vn, xt, vt, dt, alpha, beta, in);
+		elem::ElemInF in;
+		elem::gather_f32(b, e, xn, vn, xt, vt, float(dt + beta), float(alpha), float(1.0 / dt), in);
 		float g[4][3];
 #pragma unroll
 		for (int a = 0; a < 4; ++a)
 #pragma unroll
 			for (int k = 0; k < 3; ++k) g[a][k] = b.rest32[(3 * a + k) * E + e];
 		const float lamV = b.rest32[13 * E + e], muV = b.rest32[14 * E + e], cm = b.rest32[15 * E + e];
-		const int fl = elem::compute<float, false, elem::ElemIn, kLinear>(
+		const int fl = elem::compute<float, false, elem::ElemInF, kLinear>(
 			in, g, lamV, muV, cm, kslots ? &sks[0][threadIdx.x] : nullptr, kT + 1, &srhs[0][threadIdx.x], kT + 1,
 			nullptr, nullptr);
 		if (fl & 1) atomicAdd(&counters[1], 1);
