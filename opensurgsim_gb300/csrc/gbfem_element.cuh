@@ -300,8 +300,9 @@ __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __
 
 // Inputs of the FP32 element kernel. Positions relative to node 0 stay FP64 (the Gram differences
 // of the strain are formed from them); the right-hand-side inputs are FP32, formed from the FP64
-// differences x_n - x_t and v_n - v_t (0 in the first Newton iteration), so the gather spends four
-// FP64 subtractions a dof and no FP64 division (FP64 issues at 1/64 of the FP32 rate here).
+// differences x_n - x_t and v_n - v_t, which are not even read in the first Newton iteration (the
+// state is the step's start state, both differences are 0). No FP64 division (FP64 issues at 1/64
+// of the FP32 rate here).
 struct ElemInF
 {
 	int nd[4];
@@ -318,6 +319,7 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 										   const double* __restrict__ vt, float c2, float alpha, float inv_dt,
 										   ElemInF& in)
 {
+	const bool startState = (xt == xn) && (vt == vn);  // uniform over the grid
 	const int4 t4 = b.tets[e];
 	in.nd[0] = t4.x;
 	in.nd[1] = t4.y;
@@ -340,8 +342,16 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 			in.p[a][k] = xa - x0[k];
 			in.q[a][k] = b.xrest[d] - r0[k];
 			const float vf = float(va);
-			in.uK[a][k] = __fmaf_rn(-c2, vf, float(xa - xt[d]));
-			in.uM[a][k] = -alpha * vf - float(va - vt[d]) * inv_dt;
+			if (startState)
+			{
+				in.uK[a][k] = -c2 * vf;
+				in.uM[a][k] = -alpha * vf;
+			}
+			else
+			{
+				in.uK[a][k] = __fmaf_rn(-c2, vf, float(xa - xt[d]));
+				in.uM[a][k] = -alpha * vf - float(va - vt[d]) * inv_dt;
+			}
 			in.vv[a][k] = vf;
 		}
 	in.alphaDbg = 0.0;
