@@ -427,11 +427,19 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	int* sc = reinterpret_cast<int*>(dsm + 2 * M);     // segChunk copy (chunk prefix of all segments)
 	int* Cp = sc + (nseg + 1);                         // active set: chunk prefix
 	int* Wp = Cp + (nseg + 1);                         // active set: weight prefix
+	int* segW = Wp + (nseg + 1);                       // per-segment SpMV weight (block columns + 2 per chunk)
 	__shared__ int shRange[4];
 	__shared__ int shFinished;
 	__shared__ int shNext;  // next position of the current phase (for_chunks)
+	// Scalars of the segments in this CTA's range for the current phase (cache_segments).
+	constexpr int kSegCache = 32;
+	__shared__ double cBeta[kSegCache], cAlpha[kSegCache], cS[kSegCache], cRatio[kSegCache];
+	__shared__ int cMode[kSegCache];
+	__shared__ int cFirst, cCount;
 	if (threadIdx.x == 0) shNext = 0;
 	for (int i = threadIdx.x; i <= nseg; i += blockDim.x) sc[i] = a.segChunk[i];
+	__syncthreads();
+	for (int s = threadIdx.x; s < nseg; s += blockDim.x) segW[s] = __ldg(&a.cumW[sc[s + 1]]) - __ldg(&a.cumW[sc[s]]);
 	__syncthreads();
 
 	// zp records: float4 pair per row, .x/.y/.z used: [2*rs] = z = invdiag * r, [2*rs + 1] = p.
@@ -461,28 +469,36 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	// refreshWeight times its block columns. Returns whether any segment was so weighted.
 	__shared__ int shWeighted;
 	auto rebuild = [&](bool phase1) {
+		// Stage every segment's chunk count and weight in Cp[s + 1] / Wp[s + 1] with one round of
+		// loads by all threads, then scan them in place in warp 0.
+		if (threadIdx.x == 0) shWeighted = 0;
+		__syncthreads();
+		for (int s = threadIdx.x; s < nseg; s += blockDim.x)
+		{
+			int c = 0, w = 0;
+			const int d = ldi(&a.seg[s].done);
+			if (d == 0 || d > ph)
+			{
+				c = sc[s + 1] - sc[s];
+				w = segW[s];
+				if (phase1 && ldi(&a.seg[s].refreshAt) == ph - 1)
+				{
+					w *= a.refreshWeight;
+					atomicExch(&shWeighted, 1);
+				}
+			}
+			Cp[s + 1] = c;
+			Wp[s + 1] = w;
+		}
+		__syncthreads();
 		if (warp == 0)
 		{
-			int carryC = 0, carryW = 0, weighted = 0;
+			int carryC = 0, carryW = 0;
 			if (lane == 0) Cp[0] = Wp[0] = 0;
 			for (int base = 0; base < nseg; base += 32)
 			{
 				const int s = base + lane;
-				int c = 0, w = 0;
-				if (s < nseg)
-				{
-					const int d = ldi(&a.seg[s].done);
-					if (d == 0 || d > ph)
-					{
-						c = sc[s + 1] - sc[s];
-						w = __ldg(&a.cumW[sc[s + 1]]) - __ldg(&a.cumW[sc[s]]);
-						if (phase1 && ldi(&a.seg[s].refreshAt) == ph - 1)
-						{
-							w *= a.refreshWeight;
-							weighted = 1;
-						}
-					}
-				}
+				int c = (s < nseg) ? Cp[s + 1] : 0, w = (s < nseg) ? Wp[s + 1] : 0;
 #pragma unroll
 				for (int o = 1; o < 32; o <<= 1)
 				{
@@ -501,7 +517,6 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				carryC += __shfl_sync(kFull, c, 31);
 				carryW += __shfl_sync(kFull, w, 31);
 			}
-			weighted = __any_sync(kFull, weighted);
 			__syncwarp();
 			const int lo = weighted_start(a, Cp, Wp, sc, nseg, B, G);
 			const int hi = weighted_start(a, Cp, Wp, sc, nseg, B + 1, G);
@@ -512,7 +527,6 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				shRange[1] = hi;
 				shRange[2] = (int)((n * B + G - 1) / G);
 				shRange[3] = (int)((n * (B + 1) + G - 1) / G);
-				shWeighted = weighted;
 			}
 		}
 		__syncthreads();
@@ -547,6 +561,56 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		const int nf = shFinished;
 		finished += nf;
 		if (force || nf > 0 || (phase1 && (shRefresh > 0 || weighted))) weighted = rebuild(phase1);
+	};
+	// Scalars of the segments overlapping this CTA's range of view V, loaded once per phase by all
+	// threads (the chunk loops then read shared memory instead of two dependent L2 loads a chunk).
+	// They were written before the phase's grid barrier and do not change while the segment's chunks
+	// are processed (a segment's reduction completes only after all of its chunks).
+	auto cache_segments = [&](const SetView& V) {
+		if (threadIdx.x == 0)
+		{
+			int s0 = 0, cnt = 0;
+			if (V.lo < V.hi)
+			{
+				s0 = seg_of(V.Cp, nseg, V.lo);
+				cnt = min(seg_of(V.Cp, nseg, V.hi - 1) - s0 + 1, kSegCache);
+			}
+			cFirst = s0;
+			cCount = cnt;
+		}
+		__syncthreads();
+		for (int i = threadIdx.x; i < cCount; i += blockDim.x)
+		{
+			const SegCtl* S = &a.seg[cFirst + i];
+			double beta;
+			int mode;
+			load_beta_mode(S, beta, mode);
+			const double2 as2 = ldv2(&S->alpha);
+			cBeta[i] = beta;
+			cMode[i] = mode;
+			cAlpha[i] = as2.x;
+			cS[i] = as2.y;
+			cRatio[i] = ldd(&S->ratio);
+		}
+		__syncthreads();
+	};
+	// {beta, mode, alpha, s, ratio} of segment s: from the phase's cache, else from global memory.
+	auto seg_scalars = [&](int s, double& beta, int& mode, double& alpha, double& sv, double& ratio) {
+		const int ci = s - cFirst;
+		if (ci >= 0 && ci < cCount)
+		{
+			beta = cBeta[ci];
+			mode = cMode[ci];
+			alpha = cAlpha[ci];
+			sv = cS[ci];
+			ratio = cRatio[ci];
+			return;
+		}
+		load_beta_mode(&a.seg[s], beta, mode);
+		const double2 as2 = ldv2(&a.seg[s].alpha);
+		alpha = as2.x;
+		sv = as2.y;
+		ratio = ldd(&a.seg[s].ratio);
 	};
 	auto barrier = [&]() {
 		// Every warp has left the phase's for_chunks (reduce_segments began with __syncthreads);
@@ -632,11 +696,12 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		// q = A p_new; pq. mode 1: r64 = b - A (x_hl + x_delta), accumulated in double-float.
 		phase_start(true, false);
 		if (finished >= nseg) break;
+		cache_segments(actW);
 		for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
-			double part, betaD;
+			double part, betaD, alphaU, sU, ratioU;
 			int mode;
-			load_beta_mode(&a.seg[s], betaD, mode);
+			seg_scalars(s, betaD, mode, alphaU, sU, ratioU);
 			if (mode == 0)
 			{
 				const float beta = float(betaD);
@@ -689,18 +754,17 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		// ---- Phase 2. mode 0: x_delta += alpha s p, r -= alpha q, z = invdiag r; |r|^2, r.z; decide
 		// on a refresh. mode 2: fold x, r = r64 / s, z = invdiag r, p *= ratio; |r|^2, r.z.
 		phase_start(false, false);
+		cache_segments(actC);
 		for_chunks(actC, sc, nseg, &shNext, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
 			float s0 = 0.f, s1 = 0.f, z[3];
-			double betaD;
+			double betaD, alphaD, sD, ratioD;
 			int mode;
-			load_beta_mode(&a.seg[s], betaD, mode);
-			const double2 as2 = ldv2(&a.seg[s].alpha);  // {alpha, s}
+			seg_scalars(s, betaD, mode, alphaD, sD, ratioD);
 			if (mode == 0)
 			{
-				const double alphaD = as2.x;
 				const float alpha = float(alphaD);
-				const float as = float(alphaD * as2.y);
+				const float as = float(alphaD * sD);
 				const float4 pn = zpNew[2 * rs + 1];
 				const float pv[3] = {pn.x, pn.y, pn.z};
 #pragma unroll
@@ -718,8 +782,8 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			}
 			else
 			{
-				const double inv = 1.0 / as2.y;
-				const float ratio = float(ldd(&a.seg[s].ratio));
+				const double inv = 1.0 / sD;
+				const float ratio = float(ratioD);
 #pragma unroll
 				for (int i = 0; i < 3; ++i)
 				{

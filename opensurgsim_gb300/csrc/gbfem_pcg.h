@@ -77,10 +77,11 @@ struct PcgArgs
 	PcgGlobal* g;
 };
 
-// Dynamic shared memory of one CTA: the active-set prefix arrays and the chunk partials.
+// Dynamic shared memory of one CTA: the chunk partials, the segment chunk prefix, the active-set
+// prefix arrays and the per-segment base weights.
 inline size_t pcg_smem_bytes(int nsegs, int maxChunksPerCta)
 {
-	return 2 * sizeof(double) * (size_t)maxChunksPerCta + 3 * sizeof(int) * (size_t)(nsegs + 1);
+	return 2 * sizeof(double) * (size_t)maxChunksPerCta + 4 * sizeof(int) * (size_t)(nsegs + 1);
 }
 
 __global__ void k_pcg_persistent(PcgArgs a);
