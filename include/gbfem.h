@@ -185,6 +185,18 @@ GBFEM_API gbfem_status gbfem_reactivate(gbfem_handle h);
 GBFEM_API gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, const double* b, double* x, uint32_t flags,
 											  int32_t* iterations);
 
+/* Fem3DRepresentation::addExternalGeneralizedForce (Fem3DRepresentation.cpp:133-197) with a
+ * Fem3DLocalization: a force `force` (3) at the point of element `element` with natural (barycentric)
+ * coordinates coord[4] (coord[8] for hexahedra), and an optional 3x3 stiffness and damping (row-major;
+ * NULL for none). Element node a receives coord[a] * force and node pair (a, b) coord[a] coord[b] *
+ * stiffness / damping. Calls accumulate; the next gbfem_step applies them to its first step
+ * (FemRepresentation::computeFMDK, FemRepresentation.cpp:527-544: f += F, K += K_ext, D += D_ext, in
+ * every Newton iteration of that step) and then clears them (DeformableRepresentation::afterUpdate,
+ * DeformableRepresentation.cpp:242-252). Element ids of a batch handle run over the concatenated
+ * meshes. The adjoint step does not see them. */
+GBFEM_API gbfem_status gbfem_add_external_force(gbfem_handle h, int32_t element, const double* coord, const double* force,
+												const double* stiffness, const double* damping);
+
 /* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
  * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
  * CTAs per SM and refresh weights 1 to 4 on its own system, and keeps the fastest. The solve's

@@ -91,6 +91,17 @@ class Body:
         _lib.load().gbfem_batch_segment_stats(self._h, iptr(it), iptr(rf), iptr(cv), dptr(res))
         return dict(iterations=it, refreshes=rf, converged=cv, relative_residual=res)
 
+    def add_external_force(self, element, coord, force, stiffness=None, damping=None):
+        """Fem3DRepresentation::addExternalGeneralizedForce for the next step: a force (3) at the point
+        of `element` with natural coordinates `coord`, optional 3x3 stiffness and damping."""
+        c = np.ascontiguousarray(coord, dtype=np.float64)
+        F = np.ascontiguousarray(force, dtype=np.float64)
+        K = np.ascontiguousarray(stiffness, dtype=np.float64).ravel() if stiffness is not None else None
+        Dm = np.ascontiguousarray(damping, dtype=np.float64).ravel() if damping is not None else None
+        self._check(_lib.load().gbfem_add_external_force(self._h, int(element), dptr(c), dptr(F),
+                                                         dptr(K) if K is not None else None,
+                                                         dptr(Dm) if Dm is not None else None))
+
     def apply_compliance(self, B, warping=False):
         """Solve the last step's system for the columns of B (n x k): applyCompliance semantics (BC rows
         zeroed in and out), optionally with compliance warping. Returns (X, status, iterations)."""

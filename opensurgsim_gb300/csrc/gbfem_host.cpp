@@ -2,6 +2,8 @@
 // and element-to-nonzero maps, step orchestration on the handle's CUDA stream.
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -187,6 +189,14 @@ struct gbfem_handle_s
 	DevBuf<int> d_enodes;
 	DevBuf<double> d_young, d_poisson, d_rho, d_K, d_Ms, d_uw;
 	int graphKernels = 0;  // kernels one launch of the captured step graph runs
+	// External generalized forces for the next step (gbfem_add_external_force): node forces, and
+	// K (9) and D (9) per node pair keyed I * N + J; the lower-block map to place them in S.
+	bool extPending = false, extActive = false;
+	std::vector<double> extF;
+	std::map<int64_t, std::array<double, 18>> extBlocks;
+	std::vector<int> lowerOfPosHost;
+	std::vector<int4> lblkHost;
+	DevBuf<unsigned char> d_ext;
 	// Linear elements: the system matrix assembled for linearDt stays valid until dt or a material
 	// changes (OdeSolverLinearEulerImplicit keeps its first step's system).
 	bool linearReady = false;
@@ -289,6 +299,7 @@ struct gbfem_handle_s
 		DevBuf<int>* bi[] = {&d_perm, &d_off, &d_sellcol, &d_cptr, &d_cidx, &d_iptr, &d_iidx, &d_counters, &d_idx,
 							 &d_sptr, &d_sidx, &d_srow, &d_scol, &d_enodes};
 		for (auto* b : bi) b->free();
+		d_ext.free();
 		d_bc.free();
 		d_ctl.free();
 		if (stream) cudaStreamDestroy(stream);
@@ -535,6 +546,8 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 			lblk.push_back(make_int4(I, J, sellBase[k], I == J ? -1 : sellBase[h->blockPos(J, I)]));
 		}
 	h->nl = (int)lblk.size();
+	h->lowerOfPosHost = lowerOfPos;
+	h->lblkHost = lblk;
 	// Element slot -> lower block contributions, element order inside each block. Slots: the npe
 	// diagonal blocks, then the node pairs a < b in lexicographic order.
 	const int spe = h->hex() ? kHexSlots : kSlots;
@@ -1194,12 +1207,94 @@ gbfem_status step_graph(gbfem_handle h, double dt, int nsteps, uint32_t flags)
 	return GBFEM_OK;
 }
 
+// Applies the pending external generalized forces after the step's assembly (FemRepresentation::
+// computeFMDK, FemRepresentation.cpp:527-544: f += F_ext, K += K_ext, D += D_ext): S gains D + dt K on
+// the lower blocks the CG reads, the right-hand side F + K (x_n - x_t - dt v_n), both skipping
+// boundary-condition rows and columns. Two launches.
+gbfem_status apply_external(gbfem_handle h, double dt, const double* xt, cudaStream_t s)
+{
+	const int N = h->N;
+	std::vector<ExtBlock> blocks;
+	std::vector<ExtRow> rows;
+	std::vector<ExtCol> cols;
+	std::vector<char> rowSeen(N, 0);
+	auto row_of = [&](int I) -> ExtRow& {
+		if (rows.empty() || rows.back().I != I)
+		{
+			ExtRow r{};
+			r.I = I;
+			r.k0 = r.k1 = (int)cols.size();
+			for (int i = 0; i < 3; ++i) r.F[i] = h->extF[3 * (size_t)I + i];
+			rows.push_back(r);
+			rowSeen[I] = 1;
+		}
+		return rows.back();
+	};
+	for (const auto& kv : h->extBlocks)  // keys in (I, J) order
+	{
+		const int I = (int)(kv.first / N), J = (int)(kv.first % N);
+		const auto& v = kv.second;
+		ExtRow& r = row_of(I);
+		ExtCol c{};
+		c.J = J;
+		for (int k = 0; k < 9; ++k) c.K[k] = v[k];
+		cols.push_back(c);
+		r.k1 = (int)cols.size();
+		if (I >= J)
+		{
+			const int pos = h->blockPos(I, J);
+			const int L = pos >= 0 ? h->lowerOfPosHost[pos] : -1;
+			if (L < 0) return fail(h, GBFEM_CUDA_ERROR, "internal error: external block outside the pattern");
+			ExtBlock b{};
+			b.z = h->lblkHost[L].z;
+			b.w = h->lblkHost[L].w;
+			b.I = I;
+			b.J = J;
+			for (int k = 0; k < 9; ++k) b.v[k] = v[9 + k] + dt * v[k];
+			blocks.push_back(b);
+		}
+	}
+	for (int I = 0; I < N; ++I)  // nodes with a force and no external block
+		if (!rowSeen[I] && (h->extF[3 * (size_t)I] != 0.0 || h->extF[3 * (size_t)I + 1] != 0.0 ||
+							h->extF[3 * (size_t)I + 2] != 0.0))
+		{
+			ExtRow r{};
+			r.I = I;
+			r.k0 = r.k1 = 0;
+			for (int i = 0; i < 3; ++i) r.F[i] = h->extF[3 * (size_t)I + i];
+			rows.push_back(r);
+		}
+	const size_t bB = sizeof(ExtBlock) * blocks.size(), bR = sizeof(ExtRow) * rows.size(), bC = sizeof(ExtCol) * cols.size();
+	const size_t total = bB + bR + bC;
+	if (total == 0) return GBFEM_OK;
+	if (h->d_ext.n < total) GB_CUDA(h, h->d_ext.alloc(total));
+	std::vector<unsigned char> pack(total);
+	std::memcpy(pack.data(), blocks.data(), bB);
+	std::memcpy(pack.data() + bB, rows.data(), bR);
+	std::memcpy(pack.data() + bB + bR, cols.data(), bC);
+	GB_CUDA(h, cudaMemcpyAsync(h->d_ext.p, pack.data(), total, cudaMemcpyHostToDevice, s));
+	const ExtBlock* dB = reinterpret_cast<const ExtBlock*>(h->d_ext.p);
+	const ExtRow* dR = reinterpret_cast<const ExtRow*>(h->d_ext.p + bB);
+	const ExtCol* dC = reinterpret_cast<const ExtCol*>(h->d_ext.p + bB + bR);
+	if (h->mixed())
+		launch_ext_system((int)blocks.size(), dB, h->d_bc.p, h->d_A32.p, h->d_invdiag32.p, s);
+	else
+		launch_ext_system((int)blocks.size(), dB, h->d_bc.p, h->d_A.p, h->d_invdiag.p, s);
+	launch_ext_rhs((int)rows.size(), dR, dC, h->d_bc.p, h->d_x.p, xt, h->d_v.p, dt, h->d_rhs.p, s);
+	GB_CUDA(h, cudaGetLastError());
+	GB_CUDA(h, cudaStreamSynchronize(s));  // the host pack is released on return
+	h->launches += 2;
+	return GBFEM_OK;
+}
+
 gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 {
 	const bool keep = (flags & GBFEM_STEP_KEEP_SYSTEM) != 0;
 	if (keep && h->mixed())
 		return fail(h, GBFEM_INVALID_ARG, "GBFEM_STEP_KEEP_SYSTEM is available in the FP64 form only");
 	if (keep && h->hex()) return fail(h, GBFEM_INVALID_ARG, "GBFEM_STEP_KEEP_SYSTEM is available for tetrahedra only");
+	if (keep && h->extActive)
+		return fail(h, GBFEM_INVALID_ARG, "GBFEM_STEP_KEEP_SYSTEM does not export external forces");
 	if (keep)
 	{
 		gbfem_status st = ensure_system_maps(h);
@@ -1263,9 +1358,14 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 				h->linearDt = dt;
 				h->tuneVersion++;  // a captured step graph must be rebuilt (right-hand side only from now on)
 			}
-			tm.mark(2);
 			GB_CUDA(h, cudaGetLastError());
 			h->launches += 2 + (reuse ? 0 : 1);
+			if (h->extActive)
+			{
+				gbfem_status est = apply_external(h, dt, xt, s);
+				if (est != GBFEM_OK) return est;
+			}
+			tm.mark(2);
 			gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
@@ -1316,9 +1416,14 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 										 h->d_kfull.p, h->d_smass.p, h->d_bc.p, c1, c2, h->d_S.p, s);
 				launch_rhs_gather(body, h->d_fE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_f.p, 0, s);
 			}
-			tm.mark(2);
 			GB_CUDA(h, cudaGetLastError());
 			h->launches += keep ? 5 : 2 + (reuse ? 0 : 1);
+			if (h->extActive)
+			{
+				gbfem_status est = apply_external(h, dt, xt, s);
+				if (est != GBFEM_OK) return est;
+			}
+			tm.mark(2);
 			gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
@@ -1668,6 +1773,38 @@ gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, con
 	return GBFEM_OK;
 }
 
+gbfem_status gbfem_add_external_force(gbfem_handle h, int32_t element, const double* coord, const double* force,
+									   const double* stiffness, const double* damping)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (element < 0 || element >= h->E || !coord || !force)
+		return fail(h, GBFEM_INVALID_ARG, "gbfem_add_external_force: bad element or null coord/force");
+	const int npe = h->npe(), N = h->N;
+	const int32_t* nd = &h->tets[npe * (size_t)element];
+	if (!h->extPending)
+	{
+		h->extF.assign(h->n, 0.0);
+		h->extBlocks.clear();
+	}
+	for (int a = 0; a < npe; ++a)
+		for (int i = 0; i < 3; ++i) h->extF[3 * (size_t)nd[a] + i] += force[i] * coord[a];
+	if (stiffness || damping)
+		for (int a = 0; a < npe; ++a)
+			for (int b = 0; b < npe; ++b)
+			{
+				auto it = h->extBlocks.find((int64_t)nd[a] * N + nd[b]);
+				if (it == h->extBlocks.end()) it = h->extBlocks.emplace((int64_t)nd[a] * N + nd[b], std::array<double, 18>{}).first;
+				const double w = coord[a] * coord[b];
+				for (int k = 0; k < 9; ++k)
+				{
+					if (stiffness) it->second[k] += w * stiffness[k];
+					if (damping) it->second[9 + k] += w * damping[k];
+				}
+			}
+	h->extPending = true;
+	return GBFEM_OK;
+}
+
 gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* dv,
 								const double* lx, const double* lv, double* lx_out, double* lv_out,
 								double* grad_log_young, double* grad_poisson, uint32_t flags)
@@ -1797,11 +1934,31 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), h->stream));
 	gbfem_status result = GBFEM_OK;
 	int sidx = 0;
-	const bool needPlainStep = (h->prm.autotune && !h->tuned) || (h->constantSystem() && !h->systemCurrent(dt));
+	// Pending external forces apply to the first step of this call only (the reference clears them
+	// after each update, DeformableRepresentation::afterUpdate).
+	h->extActive = h->extPending && nsteps > 0;
+	const bool needPlainStep = (h->prm.autotune && !h->tuned) || (h->constantSystem() && !h->systemCurrent(dt)) ||
+							   h->extActive;
+	auto end_external = [&]() {
+		if (!h->extActive) return;
+		h->extActive = false;
+		h->extPending = false;
+		h->extBlocks.clear();
+		std::fill(h->extF.begin(), h->extF.end(), 0.0);
+		if (h->constantSystem()) h->linearReady = false;  // the stored system holds this step's K_ext, D_ext
+	};
 	if ((flags & GBFEM_STEP_GRAPH) && needPlainStep && nsteps > 0)
 	{
 		result = step_once(h, dt, flags & ~GBFEM_STEP_GRAPH);  // the first step tunes, outside any graph
+		end_external();
 		sidx = 1;
+		const bool fatal = result == GBFEM_NONFINITE || result == GBFEM_CUDA_ERROR || result == GBFEM_OUT_OF_MEMORY ||
+						   result == GBFEM_INVALID_ARG;
+		if (!fatal && sidx < nsteps && h->constantSystem() && !h->systemCurrent(dt))
+		{
+			result = step_once(h, dt, flags & ~GBFEM_STEP_GRAPH);  // rebuild the stored system without K_ext
+			sidx = 2;
+		}
 	}
 	if ((flags & GBFEM_STEP_GRAPH) && sidx < nsteps &&
 		!(result == GBFEM_NONFINITE || result == GBFEM_CUDA_ERROR || result == GBFEM_OUT_OF_MEMORY))
@@ -1813,6 +1970,7 @@ gbfem_status gbfem_step(gbfem_handle h, double dt, int32_t nsteps, uint32_t flag
 	for (; sidx < nsteps; ++sidx)
 	{
 		gbfem_status st = step_once(h, dt, flags);
+		end_external();
 		if (st == GBFEM_NONFINITE || st == GBFEM_CUDA_ERROR || st == GBFEM_OUT_OF_MEMORY || st == GBFEM_INVALID_ARG)
 		{
 			result = st;

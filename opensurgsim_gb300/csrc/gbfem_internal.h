@@ -172,6 +172,29 @@ void launch_hex_rhs(const MatSell3& K, const double* Ms, const DevBody& b, const
 					const double* vt, double dt, double alpha, double beta, const double* gravity, int gravityOn,
 					double* uw, double* rhs, cudaStream_t s);
 
+// External generalized forces of one step (Fem3DRepresentation::addExternalGeneralizedForce):
+// updates of lower system blocks (I >= J; z/w the SELL bases of (I,J) and (J,I), w < 0 on the
+// diagonal) with D + dt K, and right-hand-side rows with F + sum_J K_IJ (x_n - x_t - dt v_n)_J.
+struct ExtBlock
+{
+	int z, w, I, J;
+	double v[9];
+};
+struct ExtRow
+{
+	int I, k0, k1, pad;
+	double F[3];
+};
+struct ExtCol
+{
+	int J, pad;
+	double K[9];
+};
+void launch_ext_system(int count, const ExtBlock* blocks, const uint8_t* bc, double* A, double* invdiag, cudaStream_t s);
+void launch_ext_system(int count, const ExtBlock* blocks, const uint8_t* bc, float* A, float* invdiag, cudaStream_t s);
+void launch_ext_rhs(int count, const ExtRow* rows, const ExtCol* cols, const uint8_t* bc, const double* xn,
+					const double* xt, const double* vn, double dt, double* rhs, cudaStream_t s);
+
 // Partial-sum buffer size needed by the reductions for a given vecGrid.
 constexpr int partial_slots(int vecGrid) { return 4 * (vecGrid + 1024); }
 

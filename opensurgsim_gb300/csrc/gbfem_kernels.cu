@@ -1033,4 +1033,86 @@ void launch_prev_positions(int n, const double* x, const double* v, double dt, d
 	k_prev_positions<<<blocks(n, 256), 256, 0, s>>>(n, x, v, dt, out);
 }
 
+
+namespace {
+
+// One thread per external block: adds D + dt K into the system the CG reads (lower block and its
+// mirror; the diagonal block through its lower triangle), leaving boundary rows and columns as the
+// boundary conditions set them, and refreshes the Jacobi diagonal of a diagonal block.
+template <typename T>
+__global__ void k_ext_system(int count, const ExtBlock* __restrict__ blocks, const uint8_t* __restrict__ bc,
+							 T* __restrict__ A, T* __restrict__ invdiag)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= count) return;
+	const ExtBlock& e = blocks[t];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			const int r = 3 * e.I + i, c = 3 * e.J + j;
+			if (bc[r] | bc[c]) continue;
+			if (e.I == e.J)
+				A[(size_t)e.z + 32 * (3 * i + j)] += T(i >= j ? e.v[3 * i + j] : e.v[3 * j + i]);
+			else
+			{
+				A[(size_t)e.z + 32 * (3 * i + j)] += T(e.v[3 * i + j]);
+				A[(size_t)e.w + 32 * (3 * j + i)] += T(e.v[3 * i + j]);
+			}
+		}
+	if (e.I == e.J)
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+			if (bc[3 * e.I + i]) continue;
+			const T d = A[(size_t)e.z + 32 * (4 * i)];
+			invdiag[3 * e.I + i] = (d != T(0)) ? T(1) / d : T(1);
+		}
+}
+
+__global__ void k_ext_rhs(int count, const ExtRow* __restrict__ rows, const ExtCol* __restrict__ cols,
+						  const uint8_t* __restrict__ bc, const double* __restrict__ xn, const double* __restrict__ xt,
+						  const double* __restrict__ vn, double dt, double* __restrict__ rhs)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= count) return;
+	const ExtRow& r = rows[t];
+	double acc[3] = {r.F[0], r.F[1], r.F[2]};
+	for (int k = r.k0; k < r.k1; ++k)
+	{
+		const ExtCol& c = cols[k];
+		double u[3];
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			const int d = 3 * c.J + j;
+			u[j] = (xn[d] - xt[d]) - dt * vn[d];
+		}
+#pragma unroll
+		for (int i = 0; i < 3; ++i) acc[i] += c.K[3 * i] * u[0] + c.K[3 * i + 1] * u[1] + c.K[3 * i + 2] * u[2];
+	}
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+		if (!bc[3 * r.I + i]) rhs[3 * r.I + i] += acc[i];
+}
+
+}  // namespace
+
+void launch_ext_system(int count, const ExtBlock* ext, const uint8_t* bc, double* A, double* invdiag, cudaStream_t s)
+{
+	if (count > 0) k_ext_system<double><<<blocks(count, 128), 128, 0, s>>>(count, ext, bc, A, invdiag);
+}
+
+void launch_ext_system(int count, const ExtBlock* ext, const uint8_t* bc, float* A, float* invdiag, cudaStream_t s)
+{
+	if (count > 0) k_ext_system<float><<<blocks(count, 128), 128, 0, s>>>(count, ext, bc, A, invdiag);
+}
+
+void launch_ext_rhs(int count, const ExtRow* rows, const ExtCol* cols, const uint8_t* bc, const double* xn,
+					const double* xt, const double* vn, double dt, double* rhs, cudaStream_t s)
+{
+	if (count > 0) k_ext_rhs<<<blocks(count, 128), 128, 0, s>>>(count, rows, cols, bc, xn, xt, vn, dt, rhs);
+}
+
 }  // namespace gbfem

@@ -949,8 +949,42 @@ struct FemModel : Equation
 	bool active = true;
 	ImplicitEuler solver;
 	int singularGCount = 0, invalidRotationCount = 0, orientationWarnings = 0;
+	// External generalized force, stiffness and damping of the coming update
+	// (DeformableRepresentation m_externalGeneralized*), on the pattern; cleared after each step.
+	bool hasExternal = false;
+	vector<double> fExt, kExt, dExt;
 
 	int nodesPerElement() const { return hex ? 8 : 4; }
+
+	// Fem3DRepresentation::addExternalGeneralizedForce (Fem3DRepresentation.cpp:133-197) with a
+	// Fem3DLocalization at element e, natural coordinates coord[npe]: f_ext[node_a] += coord_a F,
+	// K_ext / D_ext block (a, b) += coord_a coord_b K / D (K or D may be null).
+	int addExternalForce(int e, const double* coord, const double* F, const double* Kx, const double* Dx)
+	{
+		if (e < 0 || (size_t)e >= numElements() || !coord || !F) return ORC_INVALID_ARG;
+		const int npe = nodesPerElement(), Dm = 3 * npe;
+		if (!hasExternal)
+		{
+			fExt.assign(pat.n, 0.0);
+			kExt.assign(pat.nnz(), 0.0);
+			dExt.assign(pat.nnz(), 0.0);
+		}
+		const int* nd = elementNodes(e);
+		for (int a = 0; a < npe; ++a)
+			for (int i = 0; i < 3; ++i) fExt[3 * nd[a] + i] += F[i] * coord[a];
+		const int* sm = &scatter[(size_t)e * Dm * Dm];
+		for (int a = 0; a < npe; ++a)
+			for (int b = 0; b < npe; ++b)
+				for (int i = 0; i < 3; ++i)
+					for (int j = 0; j < 3; ++j)
+					{
+						const int k = sm[(3 * a + i) * Dm + 3 * b + j];
+						if (Kx) kExt[k] += coord[a] * coord[b] * Kx[3 * i + j];
+						if (Dx) dExt[k] += coord[a] * coord[b] * Dx[3 * i + j];
+					}
+		hasExternal = true;
+		return ORC_OK;
+	}
 	size_t numElements() const { return hex ? hexes.size() : tets.size(); }
 	const int* elementNodes(size_t e) const { return hex ? hexes[e].n : tets[e].n; }
 
@@ -1093,6 +1127,15 @@ struct FemModel : Equation
 			spmv(pat, K.data(), V, tmp.data());
 			for (int i = 0; i < n; ++i) f[i] -= 1.0 * beta * tmp[i];
 		}
+		if (hasExternal)  // external generalized force, stiffness, damping (:527-544)
+		{
+			for (int i = 0; i < n; ++i) f[i] += fExt[i];
+			for (int64_t k = 0; k < pat.nnz(); ++k)
+			{
+				K[k] += kExt[k];
+				D[k] += dExt[k];
+			}
+		}
 	}
 
 	// FemRepresentation::update (:232-294) without the compliance matrix.
@@ -1105,6 +1148,7 @@ struct FemModel : Equation
 		solver.solve(*this, dt, x.data(), v.data(), xNew.data(), vNew.data());
 		x.swap(xNew);
 		v.swap(vNew);
+		hasExternal = false;  // DeformableRepresentation::afterUpdate (DeformableRepresentation.cpp:242-252)
 		// OdeState::isValid (OdeState.cpp:268-278): finite sums of positions and velocities.
 		double sx = 0, sv = 0;
 		for (int i = 0; i < n; ++i)
@@ -1441,6 +1485,13 @@ int32_t orc_tet_compute(const double* x0, const double* x, double E, double nu, 
 	if (M) std::memcpy(M, t.M, sizeof(t.M));
 	if (f) std::memcpy(f, t.f, sizeof(t.f));
 	return ORC_OK;
+}
+
+// Fem3DRepresentation::addExternalGeneralizedForce for the next step (see FemModel::addExternalForce).
+int32_t orc_add_external_force(void* h, int32_t element, const double* coord, const double* force,
+							   const double* stiffness, const double* damping)
+{
+	return static_cast<FemModel*>(h)->addExternalForce(element, coord, force, stiffness, damping);
 }
 
 // Single hexahedron for the element unit tests: rest positions x0 (24), current x (24). Outputs the

@@ -86,6 +86,8 @@ def lib():
         L.orc_hex_compute.restype = ctypes.c_int32
         L.orc_hex_compute.argtypes = [D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D]
         L.orc_hex_shape.argtypes = [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, D]
+        L.orc_add_external_force.restype = ctypes.c_int32
+        L.orc_add_external_force.argtypes = [P, ctypes.c_int32, D, D, D, D]
         L.orc_apply_compliance.restype = ctypes.c_int32
         L.orc_apply_compliance.argtypes = [ctypes.c_void_p, ctypes.c_int32, D, D, ctypes.c_int32, I32]
         L.orc_cg_solve.restype = ctypes.c_int32
@@ -200,6 +202,18 @@ class OracleModel:
                np.empty(self.nnz)]
         lib().orc_get_system(self._h, *[_d(a) for a in out])
         return dict(zip(["S", "rhs", "f", "M", "D", "K"], out))
+
+    def add_external_force(self, element, coord, force, stiffness=None, damping=None):
+        """Fem3DRepresentation::addExternalGeneralizedForce at element `element` (natural coordinates
+        `coord`) for the next step: force (3), optional 3x3 stiffness and damping."""
+        c = np.ascontiguousarray(coord, dtype=np.float64)
+        F = np.ascontiguousarray(force, dtype=np.float64)
+        K = np.ascontiguousarray(stiffness, dtype=np.float64).ravel() if stiffness is not None else None
+        Dm = np.ascontiguousarray(damping, dtype=np.float64).ravel() if damping is not None else None
+        st = lib().orc_add_external_force(self._h, int(element), _d(c), _d(F), _d(K) if K is not None else None,
+                                          _d(Dm) if Dm is not None else None)
+        if st != 0:
+            raise OracleError(st, "add_external_force")
 
     def apply_compliance(self, B, warping=False):
         """DeformableRepresentation::applyCompliance on the columns of B (n x k) with the last step's

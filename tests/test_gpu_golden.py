@@ -1,4 +1,5 @@
-"""GPU parity on OpenSurgSim's own test meshes (Tetrahedron.ply, wound_deformable.ply) against the
+"""GPU parity on OpenSurgSim's own test meshes (Tetrahedron.ply, wound_deformable.ply, singleTet.ply,
+sharedTet.ply, tripleTet.ply) and the one-cube scene of RenderTestFem3DCorotational.cpp against the
 committed FP64 oracle vectors (tests/golden, made by tests/golden/make_fixtures.py)."""
 
 import json
@@ -22,7 +23,8 @@ def load(name):
     return m, g
 
 
-@pytest.mark.parametrize("name", ["tetrahedron", "wound_deformable"])
+@pytest.mark.parametrize("name", ["tetrahedron", "wound_deformable", "single_tet", "shared_tet", "triple_tet",
+                                  "render_cube5"])
 @pytest.mark.parametrize("precision,tol", [(_lib.PRECISION_FP64, 1e-9), (_lib.PRECISION_MIXED, 1e-6)])
 def test_reference_mesh_steps_match_oracle(gpu_lib, name, precision, tol):
     m, g = load(name)

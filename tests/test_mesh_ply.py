@@ -139,18 +139,21 @@ def test_ply_rejects_bad_files(tmp_path):
         ply.load_fem3d(tmp_path / "x.ply")
 
 
-@pytest.mark.parametrize("name,counts", [("tetrahedron", (26, 44, 4)), ("wound_deformable", (391, 1476, 79))])
+@pytest.mark.parametrize("name,counts", [("tetrahedron", (26, 44, 4)), ("wound_deformable", (391, 1476, 79)),
+                                         ("single_tet", (4, 1, 1)), ("shared_tet", (7, 2, 1)), ("triple_tet", (10, 3, 1)),
+                                         ("render_cube5", (8, 5, 2))])
 def test_golden_meshes_from_the_reference(name, counts):
     d = json.load(open(os.path.join(GOLDEN, f"{name}_mesh.json")))
     assert (len(d["nodes"]), len(d["tets"]), len(d["bc_dofs"]) // 3) == counts
 
 
-def test_golden_oracle_vectors_reproduce():
+@pytest.mark.parametrize("name", ["tetrahedron", "single_tet", "shared_tet", "triple_tet", "render_cube5"])
+def test_golden_oracle_vectors_reproduce(name):
     """The committed oracle vectors are what the oracle computes now (pins the oracle itself)."""
     from oracle import oracle as O
 
-    d = json.load(open(os.path.join(GOLDEN, "tetrahedron_mesh.json")))
-    g = json.load(open(os.path.join(GOLDEN, "tetrahedron_oracle.json")))
+    d = json.load(open(os.path.join(GOLDEN, f"{name}_mesh.json")))
+    g = json.load(open(os.path.join(GOLDEN, f"{name}_oracle.json")))
     m = mesh.TetMesh(np.array(d["nodes"]), np.array(d["tets"], np.int32), np.array(d["young"]),
                      np.array(d["poisson"]), np.array(d["density"]), np.array(d["bc_dofs"], np.int32))
     st = g["step"]

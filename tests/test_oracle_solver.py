@@ -218,3 +218,59 @@ def test_compliance_warping_uses_the_node_rotations():
     W = np.kron(np.eye(m.n // 3), R)
     X0, _, _ = m.apply_compliance(W.T @ B)
     assert np.linalg.norm(Xw - W @ X0) <= 1e-10 * np.linalg.norm(Xw)
+
+
+@pytest.mark.parametrize("gravity,damping", [(False, False), (False, True), (True, False), (True, True)])
+def test_fmdk_gravity_damping_and_external_force(gravity, damping):
+    """FemRepresentationTests.cpp:236-410 restated on a real mesh, with an external generalized force
+    (Fem3DRepresentation.cpp:133-197, applied by FemRepresentation.cpp:527-544):
+    f = sum f_e [+ m_node g] [- alpha M v - beta K v] + F_ext, D = [alpha M + beta K] + D_ext,
+    K = sum K_e + K_ext, M = sum M_e."""
+    import scipy.sparse as sp
+
+    s = mesh.scene_cube(2, 2, 2, seed=3)
+    a, b = (0.02, 0.003) if damping else (0.0, 0.0)
+    g = np.array([0.0, -9.81, 0.0])
+    base = O.OracleModel(s.mesh, gravity_enabled=False, cg_tolerance=1e-14)
+    m = O.OracleModel(s.mesh, rayleigh_mass=a, rayleigh_stiffness=b, gravity=tuple(g), gravity_enabled=gravity,
+                      cg_tolerance=1e-14)
+    rng = np.random.default_rng(11)
+    x = s.mesh.nodes.ravel() + rng.normal(0, 1e-4, 3 * s.mesh.num_nodes)
+    v = rng.normal(0, 0.05, x.size)
+    for mod in (base, m):
+        mod.set_state(x, v)
+    e = 7
+    coord = np.array([0.1, 0.2, 0.3, 0.4])
+    F = np.array([1.5, -2.0, 0.5])
+    Kx = rng.normal(size=(3, 3))
+    Dx = rng.normal(size=(3, 3))
+    m.add_external_force(e, coord, F, Kx, Dx)
+    assert base.step(1e-3) == 0 and m.step(1e-3) == 0
+    colptr, rowidx = m.pattern()
+    n = m.n
+    sb, sm = base.system(), m.system()
+    mat = lambda vals: sp.csc_matrix((vals, rowidx, colptr), shape=(n, n))
+    # External blocks on the pattern, from the scatter map of element e.
+    kext = np.zeros(m.nnz)
+    dext = np.zeros(m.nnz)
+    fext = np.zeros(n)
+    nd = s.mesh.tets[e]
+    slots = m.scatter().reshape(-1, 12, 12)[e]
+    for aa in range(4):
+        fext[3 * nd[aa]:3 * nd[aa] + 3] += coord[aa] * F
+        for bb in range(4):
+            kext[slots[3 * aa:3 * aa + 3, 3 * bb:3 * bb + 3].ravel()] += coord[aa] * coord[bb] * Kx.ravel()
+            dext[slots[3 * aa:3 * aa + 3, 3 * bb:3 * bb + 3].ravel()] += coord[aa] * coord[bb] * Dx.ravel()
+    assert np.allclose(sm["M"], sb["M"], rtol=0, atol=0)
+    assert np.allclose(sm["K"], sb["K"] + kext, rtol=1e-14, atol=1e-12 * np.abs(sb["K"]).max())
+    assert np.allclose(sm["D"], a * sb["M"] + b * sb["K"] + dext, rtol=1e-14, atol=1e-12 * np.abs(sb["K"]).max())
+    want = sb["f"] + fext - a * (mat(sb["M"]) @ v) - b * (mat(sb["K"]) @ v)
+    if gravity:
+        want += np.repeat(m.mass_per_node(), 3) * np.tile(g, s.mesh.num_nodes)
+    assert np.allclose(sm["f"], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+    # Cleared after the step (DeformableRepresentation::afterUpdate): the next step has no external load.
+    m2 = O.OracleModel(s.mesh, rayleigh_mass=a, rayleigh_stiffness=b, gravity=tuple(g), gravity_enabled=gravity,
+                       cg_tolerance=1e-14)
+    m2.set_state(*m.state())
+    assert m.step(1e-3) == 0 and m2.step(1e-3) == 0
+    assert np.array_equal(m.state()[0], m2.state()[0])
