@@ -123,12 +123,13 @@ private:
 
 namespace Physics {
 
-// Tetrahedral mesh in the form Fem3D carries it (vertices, 4-node elements with their material,
+// Volume mesh in the form Fem3D carries it (vertices, 4- or 8-node elements with their material,
 // boundary-condition vertices), cf. Physics/Fem3DRepresentation.cpp:70-126.
 struct Fem3D
 {
 	std::vector<double> vertices;          // 3 * N
-	std::vector<int32_t> tetrahedra;       // 4 * E
+	std::vector<int32_t> tetrahedra;       // 4 * E (tetrahedral element types)
+	std::vector<int32_t> cubes;            // 8 * E (SurgSim::Physics::Fem3DElementCube)
 	std::vector<double> youngModulus, poissonRatio, massDensity;  // E each
 	std::vector<int32_t> boundaryConditions;  // vertex ids; all 3 dofs of each are fixed
 };
@@ -144,10 +145,17 @@ public:
 		if (m_handle) throw Framework::AssertionFailure("The Fem cannot be set after initialization");
 		m_mesh = mesh;
 	}
+	// The element factory names of the three provided element types.
 	void setFemElementType(const std::string& type)
 	{
-		if (type != "SurgSim::Physics::Fem3DElementCorotationalTetrahedron")
-			throw Framework::AssertionFailure("only SurgSim::Physics::Fem3DElementCorotationalTetrahedron is provided");
+		if (type == "SurgSim::Physics::Fem3DElementCorotationalTetrahedron")
+			m_params.element_type = GBFEM_ELEMENT_COROTATIONAL_TET;
+		else if (type == "SurgSim::Physics::Fem3DElementTetrahedron")
+			m_params.element_type = GBFEM_ELEMENT_LINEAR_TET;
+		else if (type == "SurgSim::Physics::Fem3DElementCube")
+			m_params.element_type = GBFEM_ELEMENT_HEXAHEDRON;
+		else
+			throw Framework::AssertionFailure("unsupported element type " + type);
 		m_elementType = type;
 	}
 	const std::string& getFemElementType() const { return m_elementType; }
@@ -187,8 +195,9 @@ public:
 		gbfem_mesh_desc d{};
 		d.num_nodes = (int32_t)(m_mesh.vertices.size() / 3);
 		d.rest_positions = m_mesh.vertices.data();
-		d.num_tets = (int32_t)(m_mesh.tetrahedra.size() / 4);
-		d.tets = m_mesh.tetrahedra.data();
+		const bool cube = m_params.element_type == GBFEM_ELEMENT_HEXAHEDRON;
+		d.num_tets = cube ? (int32_t)(m_mesh.cubes.size() / 8) : (int32_t)(m_mesh.tetrahedra.size() / 4);
+		d.tets = cube ? m_mesh.cubes.data() : m_mesh.tetrahedra.data();
 		d.young_modulus = m_mesh.youngModulus.data();
 		d.poisson_ratio = m_mesh.poissonRatio.data();
 		d.mass_density = m_mesh.massDensity.data();
@@ -215,6 +224,17 @@ public:
 			return;
 		}
 		if (st != GBFEM_CG_MAXITER) detail::check(st, m_handle.get(), "Fem3DRepresentation::update");
+	}
+	// Fem3DRepresentation::addExternalGeneralizedForce with a Fem3DLocalization (element, natural
+	// coordinates): applied to the next update, then cleared. K and D are row-major 3x3 or null.
+	void addExternalGeneralizedForce(int32_t element, const std::vector<double>& coordinate, const double force[3],
+									 const double* K = nullptr, const double* D = nullptr)
+	{
+		if (!m_handle) throw Framework::AssertionFailure("addExternalGeneralizedForce before initialize");
+		const size_t npe = m_params.element_type == GBFEM_ELEMENT_HEXAHEDRON ? 8 : 4;
+		if (coordinate.size() != npe) throw Framework::AssertionFailure("coordinate has the wrong size");
+		detail::check(gbfem_add_external_force(m_handle.get(), element, coordinate.data(), force, K, D), m_handle.get(),
+					  "addExternalGeneralizedForce");
 	}
 	bool isActive() const { return m_active; }
 	void setLocalActive(bool active)

@@ -166,8 +166,13 @@ def test_cpp_facade_compiles_and_links(lib, tmp_path):
     src.write_text('#include "surgsim_compat/surgsim_gb300.h"\n'
                    "int main() { surgsim_gb300::Physics::Fem3DRepresentation r(\"t\");\n"
                    "r.setFemElementType(\"SurgSim::Physics::Fem3DElementCorotationalTetrahedron\");\n"
+                   "r.setFemElementType(\"SurgSim::Physics::Fem3DElementTetrahedron\");\n"
+                   "r.setFemElementType(\"SurgSim::Physics::Fem3DElementCube\");\n"
                    "surgsim_gb300::Math::LinearSparseSolveAndInverseCG cg; cg.setTolerance(1e-10);\n"
-                   "try { r.setFemElementType(\"SurgSim::Physics::Fem3DElementCube\"); return 1; }\n"
+                   "try { r.setFemElementType(\"SurgSim::Physics::Fem1DElementBeam\"); return 1; }\n"
+                   "catch (const surgsim_gb300::Framework::AssertionFailure&) {}\n"
+                   "const double f[3] = {1, 0, 0};\n"
+                   "try { r.addExternalGeneralizedForce(0, std::vector<double>(8, 0.125), f); return 2; }\n"
                    "catch (const surgsim_gb300::Framework::AssertionFailure&) {} return 0; }\n")
     exe = tmp_path / "f"
     subprocess.run([gxx, "-std=c++17", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"), str(src),
