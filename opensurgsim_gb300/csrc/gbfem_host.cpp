@@ -181,6 +181,13 @@ struct gbfem_handle_s
 	bool linear() const { return prm.element_type == GBFEM_ELEMENT_LINEAR_TET; }
 	bool hex() const { return prm.element_type == GBFEM_ELEMENT_HEXAHEDRON; }
 	bool corotational() const { return prm.element_type == GBFEM_ELEMENT_COROTATIONAL_TET; }
+	// CG iteration cap of a step: the caller's, else Eigen's default 2n. The mixed form's default adds
+	// 64: FP32 CG loses conjugacy on very small systems and was measured needing up to ~2.5 n iterations
+	// there (18-27 free dofs at tolerance 1e-12), where FP64 needs at most n; at scale the counts match.
+	int stepMaxIter() const
+	{
+		return prm.cg_max_iterations > 0 ? prm.cg_max_iterations : (mixed() ? 2 * n + 64 : 2 * n);
+	}
 	int npe() const { return hex() ? 8 : 4; }
 	// Constant system (linear elements): S is formed once per dt and materials.
 	bool constantSystem() const { return !corotational(); }
@@ -1091,7 +1098,7 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	cudaStream_t s = h->stream;
 	const Launch L = h->launch();
 	const int nseg = (int)h->segNode.size() - 1;
-	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * h->n;
+	const int maxIter = h->stepMaxIter();
 	const double c1 = 1.0 / dt + h->prm.rayleigh_mass, c2 = dt + h->prm.rayleigh_stiffness;
 	const bool reuse = h->systemCurrent(dt);
 	int kernels = 0;
@@ -1304,7 +1311,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 	cudaStream_t s = h->stream;
 	const DevBody body = h->body();
 	const int newtonMax = std::max(1, (int)h->prm.newton_max_iterations);
-	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * h->n;
+	const int maxIter = h->stepMaxIter();
 	const double c1 = 1.0 / dt + h->prm.rayleigh_mass;
 	const double c2 = dt + h->prm.rayleigh_stiffness;
 	double* xt = h->d_x.p;
@@ -1825,7 +1832,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	}
 	const double alpha = h->prm.rayleigh_mass, beta = h->prm.rayleigh_stiffness;
 	const double c1 = 1.0 / dt + alpha, c2 = dt + beta;
-	const int maxIter = h->prm.cg_max_iterations > 0 ? h->prm.cg_max_iterations : 2 * n;
+	const int maxIter = h->stepMaxIter();
 	PhaseTimer tm;
 	tm.init((flags & GBFEM_STEP_TIME_PHASES) != 0, s);
 	tm.mark(0);
