@@ -307,13 +307,22 @@ struct ElemInF
 {
 	int nd[4];
 	double p[4][3];   // x_n,a - x_n,0
-	double q[4][3];   // x0_a - x0_0
+	double q[4][3];   // x0_a - x0_0 (linear tetrahedra)
+	// Corotational: the element's precomputed rest edges (FP32, [3(a-1)+k][E]) and rest Gram
+	// ([(a,c)][E], FP64), read where they are used.
+	const float* qf32;
+	const double* qg;
+	int E, e;
 	float uK[4][3];   // (x_n - x_t) - (beta + dt) v_n
 	float uM[4][3];   // -alpha v_n - (v_n - v_t) / dt
 	float vv[4][3];   // v_n (debug force only; unused by the FP32 kernel)
 	double alphaDbg, betaDbg;
 };
 
+// kLinear: q in FP64 from the rest positions (u = x - x0 is formed from it); corotational: the
+// per-element rest edges (FP32) and rest Gram (FP64) precomputed at creation, so the rest positions
+// are not gathered.
+template <bool kLinear>
 __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double* __restrict__ xn,
 										   const double* __restrict__ vn, const double* __restrict__ xt,
 										   const double* __restrict__ vt, float c2, float alpha, float inv_dt,
@@ -325,12 +334,16 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 	in.nd[1] = t4.y;
 	in.nd[2] = t4.z;
 	in.nd[3] = t4.w;
+	in.qf32 = b.qf32;
+	in.qg = b.qg;
+	in.E = b.E;
+	in.e = e;
 	double x0[3], r0[3];
 #pragma unroll
 	for (int k = 0; k < 3; ++k)
 	{
 		x0[k] = xn[3 * in.nd[0] + k];
-		r0[k] = b.xrest[3 * in.nd[0] + k];
+		if constexpr (kLinear) r0[k] = b.xrest[3 * in.nd[0] + k];
 	}
 #pragma unroll
 	for (int a = 0; a < 4; ++a)
@@ -340,7 +353,7 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 			const int d = 3 * in.nd[a] + k;
 			const double xa = xn[d], va = vn[d];
 			in.p[a][k] = xa - x0[k];
-			in.q[a][k] = b.xrest[d] - r0[k];
+			if constexpr (kLinear) in.q[a][k] = b.xrest[d] - r0[k];
 			const float vf = float(va);
 			if (startState)
 			{
@@ -356,6 +369,33 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 		}
 	in.alphaDbg = 0.0;
 	in.betaDbg = 0.0;
+}
+
+// Rest Gram entry q_a . q_c (a <= c, both in 1..3) and rest edge components for the FP32 strain:
+// precomputed in the mixed kernel's input, formed from the rest positions otherwise.
+__host__ __device__ __forceinline__ int gram_index(int a, int c)
+{
+	return (a == 1) ? (c - 1) : (a == 2 ? 1 + c : 5);  // (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)
+}
+template <typename In>
+__host__ __device__ __forceinline__ double rest_gram(const In& in, int a, int c)
+{
+	const auto* qa = in.q[a];
+	const auto* qc = in.q[c];
+	return double(qa[0]) * double(qc[0]) + double(qa[1]) * double(qc[1]) + double(qa[2]) * double(qc[2]);
+}
+__host__ __device__ __forceinline__ double rest_gram(const ElemInF& in, int a, int c)
+{
+	return in.qg[(size_t)gram_index(a, c) * in.E + in.e];
+}
+template <typename In>
+__host__ __device__ __forceinline__ float rest_edge(const In& in, int a, int k)
+{
+	return float(in.q[a][k]);
+}
+__host__ __device__ __forceinline__ float rest_edge(const ElemInF& in, int a, int k)
+{
+	return a == 0 ? 0.f : in.qf32[(size_t)(3 * (a - 1) + k) * in.E + in.e];
 }
 
 // Rotation, tangent blocks and right-hand-side share of one element.
@@ -484,9 +524,7 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			{
 				const double* pa = in.p[a + 1];
 				const double* pc = in.p[c + 1];
-				const double* qa = in.q[a + 1];
-				const double* qc = in.q[c + 1];
-				Dl[a][c] = Dl[c][a] = (pa[0] * pc[0] + pa[1] * pc[1] + pa[2] * pc[2]) - (qa[0] * qc[0] + qa[1] * qc[1] + qa[2] * qc[2]);
+				Dl[a][c] = Dl[c][a] = (pa[0] * pc[0] + pa[1] * pc[1] + pa[2] * pc[2]) - rest_gram(in, a + 1, c + 1);
 			}
 		T CD[3][3], CmI[9];  // CD = Dl G^T (rows a), CmI = G Dl G^T with G = [g_1 g_2 g_3]
 #pragma unroll
@@ -516,7 +554,7 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 #pragma unroll
 			for (int i = 0; i < 3; ++i)
 			{
-				w[a][i] = Em[3 * i] * T(in.q[a][0]) + Em[3 * i + 1] * T(in.q[a][1]) + Em[3 * i + 2] * T(in.q[a][2]);
+				w[a][i] = Em[3 * i] * rest_edge(in, a, 0) + Em[3 * i + 1] * rest_edge(in, a, 1) + Em[3 * i + 2] * rest_edge(in, a, 2);
 				ut[a][i] = R[i] * T(in.uK[a][0]) + R[3 + i] * T(in.uK[a][1]) + R[6 + i] * T(in.uK[a][2]) - w[a][i];
 			}
 	}

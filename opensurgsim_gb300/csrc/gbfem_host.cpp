@@ -195,6 +195,9 @@ struct gbfem_handle_s
 	// Hexahedra: element node ids, materials, and the assembled K / scalar block masses (SELL layout).
 	DevBuf<int> d_enodes;
 	DevBuf<double> d_young, d_poisson, d_rho, d_K, d_Ms, d_uw;
+	// Mixed form, corotational: per-element rest edges (FP32) and rest Gram (FP64).
+	DevBuf<float> d_qf32;
+	DevBuf<double> d_qg;
 	int graphKernels = 0;  // kernels one launch of the captured step graph runs
 	// External generalized forces for the next step (gbfem_add_external_force): node forces, and
 	// K (9) and D (9) per node pair keyed I * N + J; the lower-block map to place them in S.
@@ -245,6 +248,8 @@ struct gbfem_handle_s
 		b.iidx = d_iidx.p;
 		b.nmass = d_nmass.p;
 		b.bc = d_bc.p;
+		b.qf32 = d_qf32.p;
+		b.qg = d_qg.p;
 		return b;
 	}
 
@@ -307,6 +312,8 @@ struct gbfem_handle_s
 							 &d_sptr, &d_sidx, &d_srow, &d_scol, &d_enodes};
 		for (auto* b : bi) b->free();
 		d_ext.free();
+		d_qf32.free();
+		d_qg.free();
 		d_bc.free();
 		d_ctl.free();
 		if (stream) cudaStreamDestroy(stream);
@@ -674,6 +681,29 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	}
 	else
 	{
+		if (h->corotational())
+		{
+			// Rest edges q_a = x0_a - x0_0 (FP32) and their Gram q_a . q_c (FP64) per element, so the FP32
+			// element kernel neither gathers rest positions nor recomputes these constants each step.
+			std::vector<float> qf((size_t)9 * E);
+			std::vector<double> qg((size_t)6 * E);
+			for (int e = 0; e < E; ++e)
+			{
+				const int32_t* nd = &h->tets[4 * (size_t)e];
+				double q[4][3];
+				for (int a = 0; a < 4; ++a)
+					for (int k = 0; k < 3; ++k) q[a][k] = X[3 * (size_t)nd[a] + k] - X[3 * (size_t)nd[0] + k];
+				for (int a = 1; a < 4; ++a)
+					for (int k = 0; k < 3; ++k) qf[(size_t)(3 * (a - 1) + k) * E + e] = float(q[a][k]);
+				int pi = 0;
+				for (int a = 1; a < 4; ++a)
+					for (int c = a; c < 4; ++c)
+						qg[(size_t)(pi++) * E + e] = q[a][0] * q[c][0] + q[a][1] * q[c][1] + q[a][2] * q[c][2];
+			}
+			GB_CUDA(h, h->d_qf32.upload(qf.data(), qf.size(), s));
+			GB_CUDA(h, h->d_qg.upload(qg.data(), qg.size(), s));
+			GB_CUDA(h, cudaStreamSynchronize(s));
+		}
 		if (!h->hex())
 		{
 			// FP32 copy of the FP64 rest precompute (K0 and volume stay FP64-derived).

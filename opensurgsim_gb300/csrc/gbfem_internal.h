@@ -35,6 +35,10 @@ struct DevBody
 	const int* iidx = nullptr;      // 4E: e*4 + a, element order
 	const double* nmass = nullptr;  // N lumped node mass (gravity)
 	const uint8_t* bc = nullptr;    // n boundary-condition mask
+	// Mixed form, corotational: per-element rest edges q_a = x0_a - x0_0 (a = 1..3, FP32, [3(a-1)+k][E])
+	// and rest Gram q_a . q_c ([6][E], FP64).
+	const float* qf32 = nullptr;
+	const double* qg = nullptr;
 };
 
 // Device control block of one FP64 CG solve; all scalars live on the device.

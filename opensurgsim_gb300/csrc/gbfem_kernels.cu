@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __r
 	if (e < E)
 	{
 		elem::ElemInF in;
-		elem::gather_f32(b, e, xn, vn, xt, vt, float(dt + beta), float(alpha), float(1.0 / dt), in);
+		elem::gather_f32<kLinear>(b, e, xn, vn, xt, vt, float(dt + beta), float(alpha), float(1.0 / dt), in);
 		float g[4][3];
 #pragma unroll
 		for (int a = 0; a < 4; ++a)
