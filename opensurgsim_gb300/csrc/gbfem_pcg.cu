@@ -231,13 +231,13 @@ __device__ __forceinline__ void for_chunks(const SetView& V, const int* sc, int 
 }
 
 // Reduce this CTA's chunk partials per segment (sp[k * M + slot]) and complete segments across
-// CTAs; fin(s, totals) runs once per segment in lane 0 of warp 0 of the completing CTA.
+// CTAs; fin(s, totals) runs once per segment in lane 0 of one warp of the completing CTA. The
+// segments of the CTA's range are independent: warp w takes the range's segments w, w + 8, ...
 template <int NV, typename Fin>
 __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* sc, const double* sp, Fin fin)
 {
 	__syncthreads();
-	if ((threadIdx.x >> 5) != 0) return;
-	const int lane = threadIdx.x & 31;
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	const int nseg = a.nsegs, G = gridDim.x, B = blockIdx.x, M = a.maxChunksPerCta;
 	auto arrive = [&](int s, int2 fl, const double* v) {
 		const int which = (B > fl.x) ? 0 : 1;  // 0: first slot (CTAs after bf), 1: last slot (bf)
@@ -267,7 +267,7 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 	};
 	if (V.lo < V.hi)
 	{
-		for (int s = seg_of(V.Cp, nseg, V.lo); s < nseg && V.Cp[s] < V.hi; ++s)
+		for (int s = seg_of(V.Cp, nseg, V.lo) + wid; s < nseg && V.Cp[s] < V.hi; s += kWarps)
 		{
 			if (V.Cp[s + 1] == V.Cp[s]) continue;
 			const int t0 = max(V.lo, V.Cp[s]), t1 = min(V.hi, V.Cp[s + 1]);
@@ -288,7 +288,7 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 				arrive(s, fl, v);
 		}
 	}
-	else if (V.lo < V.n)
+	else if (V.lo < V.n && wid == 0)
 	{
 		// An empty range strictly inside a segment still counts among that segment's CTAs.
 		const int s = seg_of(V.Cp, nseg, V.lo);
