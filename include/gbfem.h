@@ -263,6 +263,22 @@ GBFEM_API gbfem_status gbfem_get_system(gbfem_handle h, double* S_csc, double* r
 /* Human-readable message of the last failure on h (or of the last failed create when h is NULL). */
 GBFEM_API gbfem_status gbfem_last_error(gbfem_handle h, char* buf, size_t len);
 
+/* Self-test of the bounded wait of the batched solve's grid barrier. No counterpart in the
+ * reference (its solve runs on one CPU thread and never waits on another). The mixed-precision
+ * solve is one cooperative launch whose blocks wait for one another at a grid barrier every
+ * phase; each wait gives up after a wall-time limit (1 s in the solve), records an error, and the
+ * step returns GBFEM_CUDA_ERROR instead of hanging. This runs that same barrier code on the current
+ * device, without a handle, in one cooperative block per SM, for `phases` barriers.
+ *   stall == 0: a plain run; GBFEM_OK once every block passed every barrier.
+ *   stall != 0: the barrier's arrival counter starts past its last arrival, so no block is ever
+ *     released (a flag that nothing sets): every wait must run out after timeout_ns, and the call
+ *     returns GBFEM_CUDA_ERROR, the status a solve whose barrier timed out reports. The CUDA
+ *     context stays usable.
+ * timeout_ns in [1000, 2e9]; phases in [1, 1e6]. *phases_passed (may be NULL) = fewest barriers a
+ * block passed; *max_wait_ns (may be NULL) = longest time a block spent in the kernel. */
+GBFEM_API gbfem_status gbfem_barrier_selftest(int32_t phases, int32_t stall, int64_t timeout_ns,
+											  int32_t* phases_passed, int64_t* max_wait_ns);
+
 /* ---- LinearSparseSolveAndInverseCG on a caller matrix (LinearSparseSolveAndInverse.cpp:99-129).
  * Jacobi-preconditioned CG reading only the lower triangle (row >= col) of the CSC matrix, zero
  * initial guess, stop when |r|^2 < max(tol^2 |b|^2, DBL_MIN) or after max_iterations

@@ -43,7 +43,7 @@ EXPORTED = [
     "gbfem_cg_create", "gbfem_cg_set_tolerance", "gbfem_cg_set_max_iterations", "gbfem_cg_solve",
     "gbfem_cg_destroy", "gbfem_cg_solve_noalloc", "gbfem_batch_create", "gbfem_batch_info",
     "gbfem_batch_segment_stats", "gbfem_set_materials_device", "gbfem_adjoint_step", "gbfem_get_tuning",
-    "gbfem_set_tuning", "gbfem_apply_compliance", "gbfem_add_external_force",
+    "gbfem_set_tuning", "gbfem_apply_compliance", "gbfem_add_external_force", "gbfem_barrier_selftest",
 ]
 
 
@@ -150,6 +150,8 @@ def load():
         "gbfem_set_tuning": (S, [H, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
         "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9 + [ctypes.c_uint32]),
         "gbfem_add_external_force": (S, [H, ctypes.c_int32, D, D, D, D]),
+        "gbfem_barrier_selftest": (S, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+                                       ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)]),
         "gbfem_cg_solve_noalloc": (S, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),

@@ -966,6 +966,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	a.maxChunksPerCta = h->maxChunksPerCta;
 	a.refreshWeight = h->refreshWeight;
 	a.pad = 0;
+	a.barrierTimeoutNs = kBarrierTimeoutNs;
 	a.seg = h->d_seg.p;
 	a.g = h->d_pcgGlobal.p;
 	const unsigned evFlags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -2175,6 +2176,90 @@ gbfem_status gbfem_last_error(gbfem_handle h, char* buf, size_t len)
 	if (!buf || len == 0) return GBFEM_INVALID_ARG;
 	const std::string& s = h ? h->err : g_lastCreateError;
 	std::snprintf(buf, len, "%s", s.c_str());
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_barrier_selftest(int32_t phases, int32_t stall, int64_t timeout_ns, int32_t* phases_passed,
+									int64_t* max_wait_ns)
+{
+	if (phases < 1 || phases > 1000000 || timeout_ns < 1000 || timeout_ns > 2000000000LL)
+	{
+		set_global_error("gbfem_barrier_selftest: phases must be in [1, 1e6] and timeout_ns in [1000, 2e9]");
+		return GBFEM_INVALID_ARG;
+	}
+	auto cuda_fail = [](const char* what, cudaError_t e) {
+		set_global_error(std::string("gbfem_barrier_selftest: ") + what + ": " + cudaGetErrorString(e));
+		return GBFEM_CUDA_ERROR;
+	};
+	int dev = 0, sms = 0, coop = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+	if (e != cudaSuccess) return cuda_fail("device query", e);
+	if (!coop || sms < 2)
+	{
+		set_global_error("gbfem_barrier_selftest: the device has no cooperative launch or fewer than 2 SMs");
+		return GBFEM_CUDA_ERROR;
+	}
+	const int G = sms;  // one 32-thread block per SM: co-resident, as the cooperative launch checks
+	DevBuf<PcgGlobal> g;
+	DevBuf<long long> out;
+	auto release = [&]() {
+		g.free();
+		out.free();
+	};
+	e = g.alloc(1);
+	if (e == cudaSuccess) e = out.alloc(2 * (size_t)G);
+	if (e != cudaSuccess)
+	{
+		release();
+		return cuda_fail("cudaMalloc", e);
+	}
+	cudaStream_t st = nullptr;
+	e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+	if (e != cudaSuccess)
+	{
+		release();
+		return cuda_fail("cudaStreamCreate", e);
+	}
+	e = cudaMemsetAsync(g.p, 0, sizeof(PcgGlobal), st);
+	if (e == cudaSuccess) e = cudaMemsetAsync(out.p, 0, sizeof(long long) * 2 * G, st);
+	if (e == cudaSuccess)
+	{
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(G);
+		cfg.blockDim = dim3(32);
+		cfg.stream = st;
+		cudaLaunchAttribute attr[1];
+		attr[0].id = cudaLaunchAttributeCooperative;
+		attr[0].val.cooperative = 1;
+		cfg.attrs = attr;
+		cfg.numAttrs = 1;
+		e = cudaLaunchKernelEx(&cfg, k_barrier_selftest, g.p, (int)phases, (int)(stall != 0), (long long)timeout_ns,
+							   out.p);
+	}
+	std::vector<long long> hout(2 * (size_t)G, 0);
+	PcgGlobal hg = {};
+	if (e == cudaSuccess) e = cudaMemcpyAsync(hout.data(), out.p, sizeof(long long) * 2 * G, cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(&hg, g.p, sizeof(PcgGlobal), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	cudaStreamDestroy(st);
+	release();
+	if (e != cudaSuccess) return cuda_fail("launch", e);
+	long long minPassed = phases, maxWait = 0;
+	for (int b = 0; b < G; ++b)
+	{
+		minPassed = std::min(minPassed, hout[2 * b]);
+		maxWait = std::max(maxWait, hout[2 * b + 1]);
+	}
+	if (phases_passed) *phases_passed = (int32_t)minPassed;
+	if (max_wait_ns) *max_wait_ns = maxWait;
+	if (hg.err || minPassed < phases)
+	{
+		set_global_error("gbfem_barrier_selftest: a grid-barrier wait ran out after " + std::to_string(timeout_ns) +
+						 " ns; fewest barriers passed by a block: " + std::to_string(minPassed));
+		return GBFEM_CUDA_ERROR;
+	}
 	return GBFEM_OK;
 }
 

@@ -30,7 +30,9 @@ namespace gbfem {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr long long kSpinLimit = 50000000LL;  // ~seconds; the barrier never waits that long when co-resident
+// Backstop on the polls of one barrier wait (each poll is an L2 round trip plus a short sleep);
+// the wall-time limit (PcgArgs::barrierTimeoutNs) ends a wait first.
+constexpr long long kSpinLimit = 50000000LL;
 constexpr int kWarps = kPcgThreads / 32;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
@@ -68,10 +70,19 @@ __device__ __forceinline__ void load_beta_mode(const SegCtl* S, double& beta, in
 	mode = (int)(unsigned)(__double_as_longlong(v.y) & 0xffffffffLL);
 }
 
+__device__ __forceinline__ unsigned long long global_ns()
+{
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
 // Grid-wide barrier ending phase `ph` (all blocks co-resident: cooperative launch). The last
 // block to arrive clears the event counters that phase ph + 1 will count into.
-// Returns false on timeout.
-__device__ bool grid_barrier(PcgGlobal* g, int ph)
+// A waiting block gives up after `timeoutNs` of wall time (or kSpinLimit polls, whichever comes
+// first), records the error in g->err and returns false. Once g->err is set every block returns
+// false from its next barrier, and a block already waiting stops within 1024 polls.
+__device__ bool grid_barrier(PcgGlobal* g, int ph, long long timeoutNs)
 {
 	__syncthreads();
 	__shared__ int ok;
@@ -90,10 +101,12 @@ __device__ bool grid_barrier(PcgGlobal* g, int ph)
 		}
 		else
 		{
+			const unsigned long long t0 = global_ns();
 			long long spins = 0;
 			while (ld_acquire(&g->barGen) == gen)
 			{
-				if (++spins > kSpinLimit)
+				if (++spins > kSpinLimit || (long long)(global_ns() - t0) > timeoutNs ||
+					((spins & 1023) == 0 && ldi(&g->err)))
 				{
 					atomicExch(&g->err, 1);
 					ok = 0;
@@ -616,7 +629,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		// Every warp has left the phase's for_chunks (reduce_segments began with __syncthreads);
 		// grid_barrier's __syncthreads orders this reset before the next phase's first draw.
 		if (threadIdx.x == 0) shNext = 0;
-		const bool ok = grid_barrier(a.g, ph);
+		const bool ok = grid_barrier(a.g, ph, a.barrierTimeoutNs);
 		++ph;
 		return ok;
 	};
@@ -889,6 +902,28 @@ __global__ void k_step_accumulate(const SegCtl* __restrict__ seg, int nseg, cons
 }
 
 }  // namespace
+
+__global__ void __launch_bounds__(32) k_barrier_selftest(PcgGlobal* g, int phases, int stall, long long timeoutNs,
+														 long long* out)
+{
+	// Block 0 adds gridDim.x before its own first arrival (same thread, same address: in order).
+	// Arrivals before the add come from the other gridDim.x - 1 blocks and return at most
+	// gridDim.x - 2; arrivals after it return at least gridDim.x. None returns gridDim.x - 1, so no
+	// block releases the barrier and every wait runs out.
+	if (stall && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&g->barCount, gridDim.x);
+	const unsigned long long t0 = global_ns();
+	int passed = 0;
+	for (int ph = 0; ph < phases; ++ph)
+	{
+		if (!grid_barrier(g, ph, timeoutNs)) break;
+		++passed;
+	}
+	if (threadIdx.x == 0)
+	{
+		out[2 * blockIdx.x] = passed;
+		out[2 * blockIdx.x + 1] = (long long)(global_ns() - t0);
+	}
+}
 
 void launch_step_accumulate(const SegCtl* seg, int nseg, const int* ctlNonfinite, const int* pcgErr, double* acc,
 							cudaStream_t s)

@@ -46,11 +46,17 @@ struct PcgGlobal
 constexpr int kRefreshWeightDefault = 2;
 constexpr int kRefreshWeightMax = 8;
 
+// Wall-time limit of one grid-barrier wait. A phase of the persistent solve is one pass over at
+// most the whole matrix (tens of ms for the largest system that fits in HBM), so a wait this long
+// means a block is gone; the solve then ends with PcgGlobal::err set.
+constexpr long long kBarrierTimeoutNs = 1000000000LL;
+
 struct PcgArgs
 {
 	int nchunks, nsegs, maxIter, maxChunksPerCta;
 	int refreshWeight, pad;
 	double tol, drop;
+	long long barrierTimeoutNs;  // wall time a block waits at a grid barrier before it reports an error
 	// SELL-32 matrix in row space (column = neighbour row position), FP32 values
 	const int* off;        // nchunks + 1
 	const int* col;
@@ -85,6 +91,12 @@ inline size_t pcg_smem_bytes(int nsegs, int maxChunksPerCta)
 }
 
 __global__ void k_pcg_persistent(PcgArgs a);
+
+// Self-test of the grid barrier on a PcgGlobal of its own (zeroed by the caller): `phases` barriers
+// over a cooperative grid. With `stall` set, the arrival counter starts at gridDim.x, so no block is
+// ever the last to arrive and every wait must run out after timeoutNs; each block records in
+// out[2 * block] the barriers it passed and in out[2 * block + 1] the wall time it spent, in ns.
+__global__ void k_barrier_selftest(PcgGlobal* g, int phases, int stall, long long timeoutNs, long long* out);
 
 // Per-step statistics kept on the device (graph-launched steps): acc[4*s + 0/1/2/3] += iterations,
 // += refreshes, min= converged, max= relative residual of segment s; acc[4*nseg] = 1 once a step's
