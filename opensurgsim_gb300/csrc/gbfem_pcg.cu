@@ -346,15 +346,33 @@ __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __re
 			a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
 		}
 	}
-	for (; k < k1; ++k)
+	// The last 1 to 3 slots in one round as well (the count is the same in every lane), instead of
+	// one dependent column -> record -> value chain each.
+	const int rem = k1 - k;
+	if (rem > 0)
 	{
-		const int J = __ldcs(&a.col[k * 32 + lane]);
-		const float* vb = a.val + (size_t)k * 288 + lane;
-		const float4 zj = zp[2 * J], pj = zp[2 * J + 1];
-		const float p0 = zj.x + beta * pj.x, p1 = zj.y + beta * pj.y, p2 = zj.z + beta * pj.z;
-		a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
-		a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
-		a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
+		int J[3];
+		float4 zj[3], pj[3];
+#pragma unroll
+		for (int u = 0; u < 3; ++u)
+			if (u < rem) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
+#pragma unroll
+		for (int u = 0; u < 3; ++u)
+			if (u < rem)
+			{
+				zj[u] = zp[2 * J[u]];
+				pj[u] = zp[2 * J[u] + 1];
+			}
+#pragma unroll
+		for (int u = 0; u < 3; ++u)
+			if (u < rem)
+			{
+				const float* vb = a.val + (size_t)(k + u) * 288 + lane;
+				const float p0 = zj[u].x + beta * pj[u].x, p1 = zj[u].y + beta * pj[u].y, p2 = zj[u].z + beta * pj[u].z;
+				a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
+				a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
+				a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
+			}
 	}
 }
 
@@ -380,9 +398,13 @@ __device__ __forceinline__ double residual_row(const PcgArgs& a, int c, int rs, 
 {
 	float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
 	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
+	// The next slot's column is loaded one slot ahead, so a slot waits on one gather, not a
+	// column load followed by a gather.
+	int Jn = (k0 < k1) ? __ldcs(&a.col[k0 * 32 + lane]) : 0;
 	for (int k = k0; k < k1; ++k)
 	{
-		const int J = __ldcs(&a.col[k * 32 + lane]);
+		const int J = Jn;
+		if (k + 1 < k1) Jn = __ldcs(&a.col[(k + 1) * 32 + lane]);
 		const float* vp = a.val + (size_t)k * 288 + lane;
 		float t[3], u[3];
 #pragma unroll
@@ -774,21 +796,34 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			double betaD, alphaD, sD, ratioD;
 			int mode;
 			seg_scalars(s, betaD, mode, alphaD, sD, ratioD);
+			// Row-local vectors, touched once a phase: streaming hint (L2 keeps the z/p records). All
+			// of a row's loads are issued before its first store (the compiler cannot move a load
+			// of one array past a store to another), so a chunk waits on one round of latency.
+			const int d0 = 3 * rs;
+			float iv[3];
+#pragma unroll
+			for (int i = 0; i < 3; ++i) iv[i] = __ldcs(&a.invd[d0 + i]);
 			if (mode == 0)
 			{
 				const float alpha = float(alphaD);
 				const float as = float(alphaD * sD);
+				float xv[3], rv[3], qv[3];
+#pragma unroll
+				for (int i = 0; i < 3; ++i)
+				{
+					xv[i] = __ldcs(&a.xd[d0 + i]);
+					rv[i] = __ldcs(&a.r[d0 + i]);
+					qv[i] = __ldcs(&a.q[d0 + i]);
+				}
 				const float4 pn = zpNew[2 * rs + 1];
 				const float pv[3] = {pn.x, pn.y, pn.z};
 #pragma unroll
 				for (int i = 0; i < 3; ++i)
 				{
-					// Row-local vectors, touched once a phase: streaming hint (L2 keeps the z/p records).
-					const int d = 3 * rs + i;
-					__stcs(&a.xd[d], __ldcs(&a.xd[d]) + as * pv[i]);
-					const float ri = __ldcs(&a.r[d]) - alpha * __ldcs(&a.q[d]);
-					__stcs(&a.r[d], ri);
-					z[i] = __ldcs(&a.invd[d]) * ri;
+					const float ri = rv[i] - alpha * qv[i];
+					__stcs(&a.xd[d0 + i], xv[i] + as * pv[i]);
+					__stcs(&a.r[d0 + i], ri);
+					z[i] = iv[i] * ri;
 					s0 += ri * ri;
 					s1 += ri * z[i];
 				}
@@ -797,24 +832,32 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			{
 				const double inv = 1.0 / sD;
 				const float ratio = float(ratioD);
+				float2 xo[3];
+				float xv[3];
+				double rv[3];
 #pragma unroll
 				for (int i = 0; i < 3; ++i)
 				{
-					const int d = 3 * rs + i;
+					xo[i] = a.xhl[d0 + i];
+					xv[i] = __ldcs(&a.xd[d0 + i]);
+					rv[i] = __ldcs(&a.r64[d0 + i]);
+				}
+				const float4 po = zpOld[2 * rs + 1];
+#pragma unroll
+				for (int i = 0; i < 3; ++i)
+				{
 					// Fold x_delta into the float pair: TwoSum, then renormalise.
-					const float2 xo = a.xhl[d];
 					float hs, he, h2, l2;
-					two_sum(xo.x, __ldcs(&a.xd[d]), hs, he);
-					two_sum(hs, __fadd_rn(he, xo.y), h2, l2);
-					a.xhl[d] = make_float2(h2, l2);
-					__stcs(&a.xd[d], 0.f);
-					const float ri = float(__ldcs(&a.r64[d]) * inv);
-					__stcs(&a.r[d], ri);
-					z[i] = __ldcs(&a.invd[d]) * ri;
+					two_sum(xo[i].x, xv[i], hs, he);
+					two_sum(hs, __fadd_rn(he, xo[i].y), h2, l2);
+					a.xhl[d0 + i] = make_float2(h2, l2);
+					__stcs(&a.xd[d0 + i], 0.f);
+					const float ri = float(rv[i] * inv);
+					__stcs(&a.r[d0 + i], ri);
+					z[i] = iv[i] * ri;
 					s0 += ri * ri;
 					s1 += ri * z[i];
 				}
-				const float4 po = zpOld[2 * rs + 1];
 				zpNew[2 * rs + 1] = make_float4(po.x * ratio, po.y * ratio, po.z * ratio, 0.f);
 			}
 			zpNew[2 * rs] = make_float4(z[0], z[1], z[2], 0.f);
