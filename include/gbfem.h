@@ -82,7 +82,8 @@ typedef struct gbfem_params
 	double newton_epsilon;          /* default 1e-5 (infinity norm of the solution variation) */
 	double cg_tolerance;            /* LinearSparseSolveAndInverseCG::setTolerance */
 	int32_t cg_max_iterations;      /* setMaxIterations; <= 0 selects Eigen's default 2n (mixed form: 2n + 64,
-	                                   FP32 CG needs up to ~2.5n iterations on systems of a few tens of dofs) */
+	                                   FP32 CG needs up to ~2.5n iterations on systems of a few tens of dofs;
+	                                   in a batch, n is each mesh's own dof count) */
 	int32_t precision;              /* gbfem_precision */
 	int32_t device;                 /* CUDA device ordinal */
 	int32_t autotune;               /* mixed form: tune block sizes and the solve schedule on the first step */

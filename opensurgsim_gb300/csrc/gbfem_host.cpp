@@ -153,6 +153,8 @@ struct gbfem_handle_s
 	DevBuf<double> d_brs, d_r64, d_x64;
 	DevBuf<int> d_rcol, d_segChunk, d_cumW;  // row-space columns, chunk range per segment, chunk weights
 	DevBuf<double> d_slots;                  // cross-CTA partials of the persistent solve
+	DevBuf<int> d_segMaxIter;                // default CG cap of each segment: 2 n_segment + 64
+	int segMaxIterMax = 0;
 	int maxChunksPerCta = 0;
 	size_t pcgSmem = 0;
 	// Tuning of the mixed form (picked by the autotuner or set by gbfem_set_tuning).
@@ -289,7 +291,7 @@ struct gbfem_handle_s
 							   &d_pA, &d_pB, &d_q32};
 		for (auto* b : bf) b->free();
 		for (auto* b : {&d_brs, &d_r64, &d_x64}) b->free();
-		for (auto* b : {&d_rcol, &d_segChunk, &d_cumW}) b->free();
+		for (auto* b : {&d_rcol, &d_segChunk, &d_cumW, &d_segMaxIter}) b->free();
 		d_slots.free();
 		d_acc.free();
 		for (auto* b : {&d_mcgVec, &d_mcgPart, &d_Re, &d_Wn, &d_xprev}) b->free();
@@ -744,6 +746,16 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		if (cst != GBFEM_OK) return cst;
 		GB_CUDA(h, h->d_cumW.upload(cumW.data(), cumW.size(), s));
 		GB_CUDA(h, h->d_slots.alloc(4 * 4 * (size_t)h->smCount));  // any grid of up to 4 CTAs per SM
+		// Each mesh of a batch has its own default CG cap, as each representation's solver would
+		// (Eigen's 2n for its own n; the FP32 CG needs the extra 64 on systems of a few dozen dofs).
+		std::vector<int> segCap(nseg);
+		h->segMaxIterMax = 0;
+		for (int sg = 0; sg < nseg; ++sg)
+		{
+			segCap[sg] = 2 * 3 * (h->segNode[sg + 1] - h->segNode[sg]) + 64;
+			h->segMaxIterMax = std::max(h->segMaxIterMax, segCap[sg]);
+		}
+		GB_CUDA(h, h->d_segMaxIter.upload(segCap.data(), segCap.size(), s));
 		GB_CUDA(h, h->d_acc.alloc(4 * (size_t)nseg + 2));
 		GB_CUDA(h, cudaStreamSynchronize(s));
 	}
@@ -937,7 +949,10 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	PcgArgs a;
 	a.nchunks = h->nchunks;
 	a.nsegs = nseg;
-	a.maxIter = maxIter;
+	// Without an explicit cg_max_iterations every segment stops at its own default cap.
+	const bool segCaps = h->prm.cg_max_iterations <= 0;
+	a.maxIter = segCaps ? h->segMaxIterMax : maxIter;
+	a.segMaxIter = segCaps ? h->d_segMaxIter.p : nullptr;
 	a.tol = h->prm.cg_tolerance;
 	// Refresh when |r|^2 has dropped 1e5x (the residual norm ~300x) since the last refresh: FP32 CG keeps
 	// several digits of headroom below that, and each refresh is an FP64 pass (9 FP64 FMAs a block).

@@ -647,6 +647,8 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		sv = as2.y;
 		ratio = ldd(&a.seg[s].ratio);
 	};
+	// CG iteration cap of segment s.
+	auto seg_cap = [&](int s) { return a.segMaxIter ? __ldg(&a.segMaxIter[s]) : a.maxIter; };
 	auto barrier = [&]() {
 		// Every warp has left the phase's for_chunks (reduce_segments began with __syncthreads);
 		// grid_barrier's __syncthreads orders this reset before the next phase's first draw.
@@ -769,7 +771,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				S.converged = 1;  // like Eigen, the converging iteration is not counted
 				finish(S);
 			}
-			else if (!isfinite(tot[0]) || S.iter + 1 >= a.maxIter)
+			else if (!isfinite(tot[0]) || S.iter + 1 >= seg_cap(s))
 			{
 				S.converged = 0;
 				S.nonfinite = !isfinite(tot[0]);
@@ -888,7 +890,7 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				S.nonfinite = 1;
 				finish(S);
 			}
-			else if (S.s * S.s * tot[0] < S.threshold || tot[0] < a.drop * S.rrLast || S.iter + 1 >= a.maxIter)
+			else if (S.s * S.s * tot[0] < S.threshold || tot[0] < a.drop * S.rrLast || S.iter + 1 >= seg_cap(s))
 			{
 				S.mode = 1;  // true residual before the next direction
 				S.refreshAt = ph;

@@ -63,6 +63,7 @@ struct PcgArgs
 	const float* val;
 	const int* perm;       // row position -> node id, -1 for padding rows
 	const int* segChunk;   // nsegs + 1: first chunk of each segment (segments own contiguous chunks)
+	const int* segMaxIter; // nsegs: per-segment CG iteration cap, or null: maxIter for every segment
 	const int* cumW;       // nchunks + 1: prefix of (block columns + kPcgChunkWeight) per chunk
 	double* slots;         // 4 * grid cross-CTA partials: [value k][first/last][cta]
 	// in / out (dof space, FP64)
