@@ -100,3 +100,20 @@ def test_timed_graph_steps_report_the_solve_time(gpu_lib):
     st = g.stats()
     assert st["spmv_timed"] == 3 and st["ms_spmv"] > 0.0
     assert np.array_equal(a.state()[0], g.state()[0])
+
+
+def test_default_cg_cap_is_per_mesh(gpu_lib):
+    """With tolerance 0 no mesh converges, so each stops at its own cap 2 n_mesh + 64 (as each
+    representation's own solver would), not at the batch's 2 n + 64."""
+    from opensurgsim_gb300.body import Body
+
+    scenes = [mesh.scene_cube(a, b, c, seed=k, young=float(E)) for k, (a, b, c, E) in enumerate(DIMS)]
+    b = Body([s.mesh for s in scenes], gravity=(0, 0, -9.81), cg_tolerance=0.0, precision=_lib.PRECISION_MIXED)
+    assert b.step(1e-3, 1) == _lib.GBFEM_CG_MAXITER
+    st = b.segment_stats()
+    it, conv = st["iterations"], st["converged"]
+    caps = [2 * 3 * s.mesh.num_nodes + 64 for s in scenes]
+    assert not conv.any()
+    for k, cap in enumerate(caps):
+        assert cap - 2 <= it[k] <= cap, (k, it[k], cap)
+    assert max(caps) < 2 * b.n + 64
