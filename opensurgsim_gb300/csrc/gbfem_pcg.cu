@@ -552,16 +552,18 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 				carryC += __shfl_sync(kFull, c, 31);
 				carryW += __shfl_sync(kFull, w, 31);
 			}
-			__syncwarp();
-			const int lo = weighted_start(a, Cp, Wp, sc, nseg, B, G);
-			const int hi = weighted_start(a, Cp, Wp, sc, nseg, B + 1, G);
+		}
+		__syncthreads();
+		// This CTA's first position (warp 0) and the next CTA's (warp 1) are independent searches,
+		// each a few dependent L2 rounds: run them side by side.
+		if (warp < 2)
+		{
+			const int pos = weighted_start(a, Cp, Wp, sc, nseg, B + warp, G);
 			if (lane == 0)
 			{
 				const long long n = Cp[nseg];
-				shRange[0] = lo;
-				shRange[1] = hi;
-				shRange[2] = (int)((n * B + G - 1) / G);
-				shRange[3] = (int)((n * (B + 1) + G - 1) / G);
+				shRange[warp] = pos;
+				shRange[2 + warp] = (int)((n * (B + warp) + G - 1) / G);
 			}
 		}
 		__syncthreads();
