@@ -792,6 +792,7 @@ def batch_cpu_sample(scenes):
 
 def cpu_batch_steps(scenes, steps):
     """`steps` steps of every sampled mesh, one mesh per task on ceil(0.5 * cores) host threads."""
+    import numpy as np
     from oracle import oracle as O
 
     models = [O.OracleModel.from_scene(s) for s in scenes]
@@ -800,14 +801,25 @@ def cpu_batch_steps(scenes, steps):
     O.step_many(models, 1e-3, steps, threads)
     sec = time.perf_counter() - t0
     tets = sum(s.mesh.num_tets for s in scenes)
-    return tets * steps / sec, sec, threads
+    split = np.sum([m.last_step_times() for m in models], axis=0)
+    return tets * steps / sec, sec, threads, phase_split(split, "CPU seconds of the last step summed over the meshes")
+
+
+def phase_split(t3, how):
+    """The CPU step by part, as the oracle times it."""
+    tot = float(sum(t3))
+    names = ("element_and_assembly", "system_bc_rhs", "pcg")
+    return {"seconds": {k: float(v) for k, v in zip(names, t3)},
+            "share": {k: (float(v) / tot if tot > 0 else 0.0) for k, v in zip(names, t3)}, "how": how}
 
 
 def cpu_single_steps(scene, steps):
+    import numpy as np
     from oracle import oracle as O
 
     model = O.OracleModel.from_scene(scene)
     t_total = 0.0
+    split = np.zeros(3)
     for s in range(steps):
         if scene.driven_dofs is not None:
             x, v = model.state()
@@ -816,7 +828,8 @@ def cpu_single_steps(scene, steps):
         t0 = time.perf_counter()
         model.step(scene.dt)
         t_total += time.perf_counter() - t0
-    return scene.mesh.num_tets * steps / t_total, t_total
+        split += model.last_step_times()
+    return scene.mesh.num_tets * steps / t_total, t_total, phase_split(split, f"seconds over {steps} step(s)")
 
 
 def run_reference(args, rank, world):
@@ -929,17 +942,18 @@ def main():
             log("cpu baseline: oracle on the host")
             if args.config == "batch":
                 sample = batch_cpu_sample(scenes)
-                v, t, threads = cpu_batch_steps(sample, 1)
+                v, t, threads, split = cpu_batch_steps(sample, 1)
                 line["cpu_baseline"] = {
                     "value": v, "unit": UNIT, "cores": threads, "kind": "port",
                     "sample": (f"1 step of every 4th mesh of the batch ({len(sample)} meshes, "
                                f"{sum(s.mesh.num_tets for s in sample)} tets) in {t:.1f} s, one mesh per task on "
-                               f"{threads} host threads; oracle FP64 C++ restatement, -O3")}
+                               f"{threads} host threads; oracle FP64 C++ restatement, -O3"),
+                    "phase_split": split}
             else:
-                v, t = cpu_single_steps(scene, 1)
+                v, t, split = cpu_single_steps(scene, 1)
                 line["cpu_baseline"] = {"value": v, "unit": line["unit"], "cores": 1, "kind": "port",
                                         "sample": f"1 step of the same scene on the host ({t:.1f} s), oracle FP64 "
-                                                  "C++ restatement, -O3, 1 thread"}
+                                                  "C++ restatement, -O3, 1 thread", "phase_split": split}
             log(f"cpu baseline: {v / 1e3:.1f} k tet-steps/s")
         print(json.dumps(line), flush=True)
     dist.close()

@@ -1404,6 +1404,16 @@ int32_t orc_step(void* h, double dt, int32_t nsteps, orc_stats* stats)
 	return st;
 }
 
+// Seconds of the model's last step by part: element updates and assembly of f, M, D, K; the system
+// S, its boundary conditions and the right-hand side; the CG solve.
+void orc_last_step_times(void* h, double* t3)
+{
+	const auto& st = static_cast<FemModel*>(h)->solver.stats;
+	t3[0] = st.tElement;
+	t3[1] = st.tSystem;
+	t3[2] = st.tSolve;
+}
+
 void orc_get_state(void* h, double* x, double* v)
 {
 	auto* m = static_cast<FemModel*>(h);

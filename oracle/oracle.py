@@ -79,6 +79,8 @@ def lib():
         L.orc_get_system.argtypes = [P, D, D, D, D, D, D]
         L.orc_get_mass_per_node.argtypes = [P, D]
         L.orc_get_element.argtypes = [P, ctypes.c_int32, D, D, D, D]
+        L.orc_last_step_times.argtypes = [P, D]
+        L.orc_last_step_times.restype = None
         L.orc_tet_compute.restype = ctypes.c_int32
         L.orc_tet_compute.argtypes = [D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, D, D,
                                       D, D, I32]
@@ -173,6 +175,12 @@ class OracleModel:
     def step(self, dt, nsteps=1):
         st = lib().orc_step(self._h, dt, nsteps, ctypes.byref(self.last_stats))
         return st
+
+    def last_step_times(self):
+        """Seconds of the last step: (element + assembly, system + BC + rhs, CG)."""
+        t = np.zeros(3)
+        lib().orc_last_step_times(self._h, _d(t))
+        return t
 
     def state(self):
         x = np.empty(self.n)
