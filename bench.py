@@ -151,6 +151,16 @@ def load_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+# FP64 arithmetic of the corotational element kernel (k_element_fp64), per tet: 1,717 DFMA, 742 DMUL
+# and 189 DADD executed (ncu counters sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum
+# over one launch on the 10x10x10 cube, 5,000 tets) = 2 * 1717 + 742 + 189 FLOPs. The kernel does
+# the polar decomposition, the corotational tangent and the force in closed form, so this is below
+# the reference's ~6-7k FMAs per tet for the same element update.
+ELEMENT_FP64_FLOPS_PER_TET = 2 * 1717 + 742 + 189
+# GB300 FP64 (non-tensor) peak, NVIDIA's nominal figure; no measured FP64 peak is available.
+FP64_PEAK_TFLOPS = 1.25
+
+
 def load_traffic(kernel_key):
     """Per-launch DRAM bytes of a kernel from the committed ncu summary (profiles/traffic.json)."""
     try:
@@ -478,6 +488,20 @@ def run_single(args, rank, world, local, dist):
     torch.cuda.synchronize(local)
     e2e_s = dist.reduce(time.perf_counter() - t0, "max")
     e2e_value = total_units / e2e_s
+    fp64_alu = None
+    if prec == _lib.PRECISION_FP64 and args.config != "hex":
+        # The element kernel is bound by the FP64 pipe, not HBM: one more (untimed) step with phase
+        # events gives its device time.
+        set_driven(step)
+        body.step(dt, 1, _lib.STEP_TIME_PHASES)
+        step += 1
+        el_ms = body.stats()["ms_element"]
+        if el_ms > 0:
+            tflops = m.num_tets * ELEMENT_FP64_FLOPS_PER_TET / (el_ms / 1e3) / 1e12
+            fp64_alu = {"kernel": "k_element_fp64", "bound": "fp64 pipe", "achieved": tflops,
+                        "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": tflops / FP64_PEAK_TFLOPS,
+                        "flops_per_tet": ELEMENT_FP64_FLOPS_PER_TET, "launch_ms": el_ms,
+                        "peak_source": "nominal (no measured FP64 peak)"}
     workload = {
         "bar": ("bar40x40x160 (h 4 mm) 20% compression ramp: 1,280,000 tets, 270,641 nodes, "
                 "nnz 30,865,689, E log-U[1e4,1e6], nu U[0.40,0.49], gravity, dt 1e-3, CG tol 1e-10"),
@@ -539,6 +563,8 @@ def run_single(args, rank, world, local, dist):
             "peak_source": f"{peak_kind} (hbm_gbs)", "bytes_model": model,
         },
     }
+    if fp64_alu:
+        line["fp64_alu"] = fp64_alu
     body.close()
     return line, scene
 
