@@ -18,8 +18,9 @@
 //
 // Per-segment sums are deterministic: each CTA sums its chunk partials of a segment in chunk
 // order; a segment spread over CTAs bf..bl is completed by the last of them to arrive (ticket
-// counter), which adds the CTAs' partials in CTA order. Grid barriers spin with an iteration
-// limit: on timeout the kernel records an error and returns (the host reports GBFEM_CUDA_ERROR).
+// counter), which adds the CTAs' partials in CTA order. A grid-barrier wait gives up after a
+// wall-time limit (1 s in the solve): the kernel records an error and returns (the host reports
+// GBFEM_CUDA_ERROR).
 
 #include <cfloat>
 #include <cstdint>
