@@ -117,3 +117,29 @@ def test_default_cg_cap_is_per_mesh(gpu_lib):
     for k, cap in enumerate(caps):
         assert cap - 2 <= it[k] <= cap, (k, it[k], cap)
     assert max(caps) < 2 * b.n + 64
+
+
+def test_thousands_of_tiny_meshes_on_one_cta_per_sm(gpu_lib):
+    """5,000 one-chunk meshes on a grid of one CTA per SM: each CTA's range holds more meshes than
+    the solve's per-phase shared-memory scalar cache (those beyond it read their scalars from
+    global memory), and every mesh must still match the oracle."""
+    from oracle import oracle as O
+    from opensurgsim_gb300.body import Body
+
+    kw = dict(rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0, 0, -9.81), cg_tolerance=1e-10)
+    scenes = [mesh.scene_cube(1 + k % 2, 1 + (k // 2) % 2, 1 + (k // 4) % 2, seed=k, young=1e4 * (1 + k % 97))
+              for k in range(5000)]
+    b = Body([s.mesh for s in scenes], precision=_lib.PRECISION_MIXED, **kw)
+    b.set_tuning(64, 1, 2)
+    assert b.step(1e-3, 2) == _lib.GBFEM_OK
+    x, _ = b.state()
+    assert b.segment_stats()["converged"].all()
+    for k in range(0, 5000, 199):
+        s = scenes[k]
+        o = O.OracleModel(s.mesh, **kw)
+        assert o.step(1e-3, 2) == 0
+        ox, _ = o.state()
+        n0, n1 = b.node_offsets[k], b.node_offsets[k + 1]
+        x0 = s.mesh.nodes.ravel()
+        u, uo = x[3 * n0:3 * n1] - x0, ox - x0
+        assert np.linalg.norm(u - uo) <= 1e-6 * np.linalg.norm(uo), k
