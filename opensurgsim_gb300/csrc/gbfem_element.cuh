@@ -27,6 +27,15 @@
 namespace gbfem {
 namespace elem {
 
+// Knuth's TwoSum in FP32: a + b = s + e exactly. The _rn intrinsics keep the compiler from
+// contracting or reassociating it.
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e)
+{
+	s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 template <typename T>
 __host__ __device__ __forceinline__ void cofactor3(const T* X, T* C)
 {
@@ -298,20 +307,23 @@ __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __
 	in.betaDbg = beta;
 }
 
-// Inputs of the FP32 element kernel. Positions relative to node 0 stay FP64 (the Gram differences
-// of the strain are formed from them); the right-hand-side inputs are FP32, formed from the FP64
-// differences x_n - x_t and v_n - v_t, which are not even read in the first Newton iteration (the
-// state is the step's start state, both differences are 0). No FP64 division (FP64 issues at 1/64
-// of the FP32 rate here).
+// Inputs of the FP32 element kernel. FP64 issues at 1/64 of the FP32 rate here, so the corotational
+// kernel runs no FP64 at all: its per-node inputs come from the node pass (k_node_prep) in FP32,
+// positions as unevaluated float pairs hi + lo (~2^-48 relative), and the edges relative to node 0
+// and the Gram differences of the strain are formed in double-float arithmetic. The right-hand-side
+// inputs are FP32 differences x_n - x_t, v_n - v_t (zero, and not read, in the first Newton
+// iteration). The linear tetrahedron keeps FP64 edges p and rest edges q (its strain needs no Gram).
 struct ElemInF
 {
 	int nd[4];
-	double p[4][3];   // x_n,a - x_n,0
+	double p[4][3];   // x_n,a - x_n,0 (linear tetrahedra)
 	double q[4][3];   // x0_a - x0_0 (linear tetrahedra)
+	float ph[4][3];   // corotational: x_n,a - x_n,0 as a float pair ph + pl
+	float pl[4][3];
 	// Corotational: the element's precomputed rest edges (FP32, [3(a-1)+k][E]) and rest Gram
-	// ([(a,c)][E], FP64), read where they are used.
+	// q_a . q_c as float pairs ([(a,c)][E]), read where they are used.
 	const float* qf32;
-	const double* qg;
+	const float2* qg2;
 	int E, e;
 	float uK[4][3];   // (x_n - x_t) - (beta + dt) v_n
 	float uM[4][3];   // -alpha v_n - (v_n - v_t) / dt
@@ -319,9 +331,10 @@ struct ElemInF
 	double alphaDbg, betaDbg;
 };
 
-// kLinear: q in FP64 from the rest positions (u = x - x0 is formed from it); corotational: the
-// per-element rest edges (FP32) and rest Gram (FP64) precomputed at creation, so the rest positions
-// are not gathered.
+// kLinear: p and q in FP64 from the positions and rest positions (u = x - x0 is formed from them).
+// Corotational: FP32 node-pass values only (x as float pairs, v, and the differences to the step's
+// start state); the rest edges (FP32) and rest Gram (float pairs) are precomputed per element, so
+// rest positions are not gathered.
 template <bool kLinear>
 __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double* __restrict__ xn,
 										   const double* __restrict__ vn, const double* __restrict__ xt,
@@ -335,38 +348,84 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 	in.nd[2] = t4.z;
 	in.nd[3] = t4.w;
 	in.qf32 = b.qf32;
-	in.qg = b.qg;
+	in.qg2 = b.qg2;
 	in.E = b.E;
 	in.e = e;
-	double x0[3], r0[3];
-#pragma unroll
-	for (int k = 0; k < 3; ++k)
+	if constexpr (!kLinear)
 	{
-		x0[k] = xn[3 * in.nd[0] + k];
-		if constexpr (kLinear) r0[k] = b.xrest[3 * in.nd[0] + k];
-	}
+		// Node pass outputs: x as (hi, lo), v, and x_n - x_t, v_n - v_t past the first Newton iteration.
+		float xh[4][3], xl[4][3];
 #pragma unroll
-	for (int a = 0; a < 4; ++a)
+		for (int a = 0; a < 4; ++a)
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				const int d = 3 * in.nd[a] + k;
+				const float2 xp = b.nodeX[d];
+				xh[a][k] = xp.x;
+				xl[a][k] = xp.y;
+				const float vf = b.nodeV[d];
+				if (startState)
+				{
+					in.uK[a][k] = -c2 * vf;
+					in.uM[a][k] = -alpha * vf;
+				}
+				else
+				{
+					in.uK[a][k] = __fmaf_rn(-c2, vf, b.nodeDx[d]);
+					in.uM[a][k] = -alpha * vf - b.nodeDv[d] * inv_dt;
+				}
+				in.vv[a][k] = vf;
+			}
+		// Edge a: (xh_a - xh_0) exactly as a TwoSum pair, plus (xl_a - xl_0), renormalised.
 #pragma unroll
 		for (int k = 0; k < 3; ++k)
 		{
-			const int d = 3 * in.nd[a] + k;
-			const double xa = xn[d], va = vn[d];
-			in.p[a][k] = xa - x0[k];
-			if constexpr (kLinear) in.q[a][k] = b.xrest[d] - r0[k];
-			const float vf = float(va);
-			if (startState)
-			{
-				in.uK[a][k] = -c2 * vf;
-				in.uM[a][k] = -alpha * vf;
-			}
-			else
-			{
-				in.uK[a][k] = __fmaf_rn(-c2, vf, float(xa - xt[d]));
-				in.uM[a][k] = -alpha * vf - float(va - vt[d]) * inv_dt;
-			}
-			in.vv[a][k] = vf;
+			in.ph[0][k] = 0.f;
+			in.pl[0][k] = 0.f;
 		}
+#pragma unroll
+		for (int a = 1; a < 4; ++a)
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				float s, es;
+				df_two_sum(xh[a][k], -xh[0][k], s, es);
+				df_two_sum(s, __fadd_rn(es, __fsub_rn(xl[a][k], xl[0][k])), in.ph[a][k], in.pl[a][k]);
+			}
+	}
+	else
+	{
+		double x0[3], r0[3];
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			x0[k] = xn[3 * in.nd[0] + k];
+			r0[k] = b.xrest[3 * in.nd[0] + k];
+		}
+#pragma unroll
+		for (int a = 0; a < 4; ++a)
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				const int d = 3 * in.nd[a] + k;
+				const double xa = xn[d], va = vn[d];
+				in.p[a][k] = xa - x0[k];
+				in.q[a][k] = b.xrest[d] - r0[k];
+				const float vf = float(va);
+				if (startState)
+				{
+					in.uK[a][k] = -c2 * vf;
+					in.uM[a][k] = -alpha * vf;
+				}
+				else
+				{
+					in.uK[a][k] = __fmaf_rn(-c2, vf, float(xa - xt[d]));
+					in.uM[a][k] = -alpha * vf - float(va - vt[d]) * inv_dt;
+				}
+				in.vv[a][k] = vf;
+			}
+	}
 	in.alphaDbg = 0.0;
 	in.betaDbg = 0.0;
 }
@@ -384,9 +443,49 @@ __host__ __device__ __forceinline__ double rest_gram(const In& in, int a, int c)
 	const auto* qc = in.q[c];
 	return double(qa[0]) * double(qc[0]) + double(qa[1]) * double(qc[1]) + double(qa[2]) * double(qc[2]);
 }
-__host__ __device__ __forceinline__ double rest_gram(const ElemInF& in, int a, int c)
+// Gram difference p_a . p_c - q_a . q_c (a, c in 1..3), rounded to FP32 at the end: from FP64 edges,
+// or, for the corotational FP32 kernel, in double-float (each product's rounding error by FMA, the
+// sums by TwoSum, the rest Gram as a float pair), so the cancellation between the two Grams of a
+// rotated, barely strained element keeps the strain to FP32 relative accuracy with no FP64.
+template <typename In>
+__host__ __device__ __forceinline__ float gram_diff(const In& in, int a, int c)
 {
-	return in.qg[(size_t)gram_index(a, c) * in.E + in.e];
+	const double* pa = in.p[a];
+	const double* pc = in.p[c];
+	return float((pa[0] * pc[0] + pa[1] * pc[1] + pa[2] * pc[2]) - rest_gram(in, a, c));
+}
+__device__ __forceinline__ float gram_diff(const ElemInF& in, int a, int c)
+{
+	float sh = 0.f, sl = 0.f;
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+	{
+		const float P = __fmul_rn(in.ph[a][k], in.ph[c][k]);
+		const float e = __fmaf_rn(in.ph[a][k], in.ph[c][k], -P);
+		const float cross = __fmaf_rn(in.ph[a][k], in.pl[c][k], __fmul_rn(in.pl[a][k], in.ph[c][k]));
+		float t, et;
+		df_two_sum(sh, P, t, et);
+		sh = t;
+		sl = __fadd_rn(sl, __fadd_rn(et, __fadd_rn(e, cross)));
+	}
+	const float2 q = in.qg2[(size_t)gram_index(a, c) * in.E + in.e];
+	float d, ed;
+	df_two_sum(sh, -q.x, d, ed);
+	return __fadd_rn(d, __fadd_rn(ed, __fsub_rn(sl, q.y)));
+}
+// Edge a of the element (x_a - x_0), component i, in the kernel's type.
+template <typename T, bool kLinear, typename In>
+__host__ __device__ __forceinline__ T edge(const In& in, int a, int i)
+{
+	return T(in.p[a][i]);
+}
+template <typename T, bool kLinear>
+__host__ __device__ __forceinline__ T edge(const ElemInF& in, int a, int i)
+{
+	if constexpr (kLinear)
+		return T(in.p[a][i]);
+	else
+		return T(in.ph[a][i]) + T(in.pl[a][i]);
 }
 template <typename In>
 __host__ __device__ __forceinline__ float rest_edge(const In& in, int a, int k)
@@ -419,7 +518,8 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 	for (int i = 0; i < 3; ++i)
 #pragma unroll
 		for (int j = 0; j < 3; ++j)
-			F[3 * i + j] = T(in.p[1][i]) * g[1][j] + T(in.p[2][i]) * g[2][j] + T(in.p[3][i]) * g[3][j];
+			F[3 * i + j] = edge<T, kLinear>(in, 1, i) * g[1][j] + edge<T, kLinear>(in, 2, i) * g[2][j] +
+						   edge<T, kLinear>(in, 3, i) * g[3][j];
 	T R[9];
 	if constexpr (kLinear)
 	{
@@ -437,7 +537,9 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			for (int i = 0; i < 3; ++i)
 #pragma unroll
 				for (int j = 0; j < 3; ++j)
-					Fd[3 * i + j] = in.p[1][i] * double(g[1][j]) + in.p[2][i] * double(g[2][j]) + in.p[3][i] * double(g[3][j]);
+					Fd[3 * i + j] = edge<double, kLinear>(in, 1, i) * double(g[1][j]) +
+									edge<double, kLinear>(in, 2, i) * double(g[2][j]) +
+									edge<double, kLinear>(in, 3, i) * double(g[3][j]);
 			polar_svd(Fd, Rd);
 #pragma unroll
 			for (int k = 0; k < 9; ++k) R[k] = T(Rd[k]);
@@ -515,17 +617,13 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 		// An FP32 rotation is orthogonal only to ~1e-7, and its symmetric error would read as a
 		// spurious strain of that size. Since p_a = F q_a and F = R S, R^T p_a - q_a = (S - I) q_a,
 		// with S - I = (C - I)(S + I)^-1 and C - I = sum_ab (p_a.p_b - q_a.q_b) g_a g_b^T: the Gram
-		// differences are formed in FP64, everything after in FP32 with eps32-relative accuracy.
-		double Dl[3][3];
+		// differences are formed without loss to cancellation (gram_diff), everything after in FP32
+		// with eps32-relative accuracy.
+		T Dl[3][3];
 #pragma unroll
 		for (int a = 0; a < 3; ++a)
 #pragma unroll
-			for (int c = a; c < 3; ++c)
-			{
-				const double* pa = in.p[a + 1];
-				const double* pc = in.p[c + 1];
-				Dl[a][c] = Dl[c][a] = (pa[0] * pc[0] + pa[1] * pc[1] + pa[2] * pc[2]) - rest_gram(in, a + 1, c + 1);
-			}
+			for (int c = a; c < 3; ++c) Dl[a][c] = Dl[c][a] = gram_diff(in, a + 1, c + 1);
 		T CD[3][3], CmI[9];  // CD = Dl G^T (rows a), CmI = G Dl G^T with G = [g_1 g_2 g_3]
 #pragma unroll
 		for (int a = 0; a < 3; ++a)

@@ -199,7 +199,10 @@ struct gbfem_handle_s
 	DevBuf<double> d_young, d_poisson, d_rho, d_K, d_Ms, d_uw;
 	// Mixed form, corotational: per-element rest edges (FP32) and rest Gram (FP64).
 	DevBuf<float> d_qf32;
-	DevBuf<double> d_qg;
+	DevBuf<float2> d_qg2;
+	// Node pass outputs of the FP32 corotational element kernel (x as float pairs, v, x - x_t, v - v_t).
+	DevBuf<float2> d_nodeX;
+	DevBuf<float> d_nodeV, d_nodeDx, d_nodeDv;
 	int graphKernels = 0;  // kernels one launch of the captured step graph runs
 	// External generalized forces for the next step (gbfem_add_external_force): node forces, and
 	// K (9) and D (9) per node pair keyed I * N + J; the lower-block map to place them in S.
@@ -251,7 +254,11 @@ struct gbfem_handle_s
 		b.nmass = d_nmass.p;
 		b.bc = d_bc.p;
 		b.qf32 = d_qf32.p;
-		b.qg = d_qg.p;
+		b.qg2 = d_qg2.p;
+		b.nodeX = d_nodeX.p;
+		b.nodeV = d_nodeV.p;
+		b.nodeDx = d_nodeDx.p;
+		b.nodeDv = d_nodeDv.p;
 		return b;
 	}
 
@@ -315,7 +322,9 @@ struct gbfem_handle_s
 		for (auto* b : bi) b->free();
 		d_ext.free();
 		d_qf32.free();
-		d_qg.free();
+		d_qg2.free();
+		d_nodeX.free();
+		for (auto* b : {&d_nodeV, &d_nodeDx, &d_nodeDv}) b->free();
 		d_bc.free();
 		d_ctl.free();
 		if (stream) cudaStreamDestroy(stream);
@@ -685,10 +694,11 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	{
 		if (h->corotational())
 		{
-			// Rest edges q_a = x0_a - x0_0 (FP32) and their Gram q_a . q_c (FP64) per element, so the FP32
-			// element kernel neither gathers rest positions nor recomputes these constants each step.
+			// Rest edges q_a = x0_a - x0_0 (FP32) and their Gram q_a . q_c (an unevaluated float pair:
+			// hi = the FP64 Gram rounded, lo = the rest rounded) per element, so the FP32 element kernel
+			// neither gathers rest positions nor recomputes these constants each step.
 			std::vector<float> qf((size_t)9 * E);
-			std::vector<double> qg((size_t)6 * E);
+			std::vector<float2> qg((size_t)6 * E);
 			for (int e = 0; e < E; ++e)
 			{
 				const int32_t* nd = &h->tets[4 * (size_t)e];
@@ -700,10 +710,16 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 				int pi = 0;
 				for (int a = 1; a < 4; ++a)
 					for (int c = a; c < 4; ++c)
-						qg[(size_t)(pi++) * E + e] = q[a][0] * q[c][0] + q[a][1] * q[c][1] + q[a][2] * q[c][2];
+					{
+						const double gq = q[a][0] * q[c][0] + q[a][1] * q[c][1] + q[a][2] * q[c][2];
+						const float hi = float(gq);
+						qg[(size_t)(pi++) * E + e] = make_float2(hi, float(gq - double(hi)));
+					}
 			}
 			GB_CUDA(h, h->d_qf32.upload(qf.data(), qf.size(), s));
-			GB_CUDA(h, h->d_qg.upload(qg.data(), qg.size(), s));
+			GB_CUDA(h, h->d_qg2.upload(qg.data(), qg.size(), s));
+			GB_CUDA(h, h->d_nodeX.alloc(nv));
+			for (DevBuf<float>* b : {&h->d_nodeV, &h->d_nodeDx, &h->d_nodeDv}) GB_CUDA(h, b->alloc(nv));
 			GB_CUDA(h, cudaStreamSynchronize(s));
 		}
 		if (!h->hex())
@@ -1156,12 +1172,12 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	}
 	else
 	{
-		launch_element_f32(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
-						   h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p,
-						   h->d_counters.p, s, h->elemsPerBlock, h->linear());
+		const int ek = launch_element_f32(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
+										  h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p,
+										  h->d_rhsE32.p, h->d_counters.p, s, h->elemsPerBlock, h->linear());
 		if (!reuse) launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 		launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
-		kernels = reuse ? 2 : 3;
+		kernels = ek + (reuse ? 1 : 2);
 	}
 	gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timed ? h->graphEv[0] : nullptr,
 									timed ? h->graphEv[1] : nullptr, /*capturing=*/true);
@@ -1390,6 +1406,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 				if (tst != GBFEM_OK) return tst;
 			}
 			const bool reuse = h->systemCurrent(dt);
+			int ek = 1;  // kernels of the element update (hexahedra: the right-hand-side pair counts as one)
 			if (h->hex())
 			{
 				enqueue_hex_rhs(h, dt, xt, vt, s);
@@ -1398,7 +1415,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 			}
 			else
 			{
-				launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
+				ek = launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, h->prm.rayleigh_mass,
 								   h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots32.p, h->d_rhsE32.p,
 								   h->d_counters.p, s, h->elemsPerBlock, h->linear());
 				tm.mark(1);
@@ -1412,7 +1429,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 				h->tuneVersion++;  // a captured step graph must be rebuilt (right-hand side only from now on)
 			}
 			GB_CUDA(h, cudaGetLastError());
-			h->launches += 2 + (reuse ? 0 : 1);
+			h->launches += ek + 1 + (reuse ? 0 : 1);
 			if (h->extActive)
 			{
 				gbfem_status est = apply_external(h, dt, xt, s);
@@ -1883,9 +1900,10 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	tm.init((flags & GBFEM_STEP_TIME_PHASES) != 0, s);
 	tm.mark(0);
 	// The step's system at (x, v), as the first Newton iteration of step_once builds it.
+	int ek = 1;
 	if (h->mixed())
 	{
-		launch_element_f32(body, x, v, x, v, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s);
+		ek = launch_element_f32(body, x, v, x, v, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s);
 		launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 	}
 	else
@@ -1896,7 +1914,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	}
 	launch_adjoint_rhs(n, h->d_bc.p, lx, lv, dt, h->d_adjG.p, s);
 	GB_CUDA(h, cudaGetLastError());
-	h->launches += 3;
+	h->launches += ek + 2;
 	tm.mark(1);
 	bool converged = true;
 	if (h->mixed())

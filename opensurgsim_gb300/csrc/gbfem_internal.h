@@ -36,9 +36,15 @@ struct DevBody
 	const double* nmass = nullptr;  // N lumped node mass (gravity)
 	const uint8_t* bc = nullptr;    // n boundary-condition mask
 	// Mixed form, corotational: per-element rest edges q_a = x0_a - x0_0 (a = 1..3, FP32, [3(a-1)+k][E])
-	// and rest Gram q_a . q_c ([6][E], FP64).
+	// and rest Gram q_a . q_c as unevaluated float pairs hi + lo ([6][E]); per-dof inputs of the FP32
+	// element kernel that its node pass writes each time it runs: x as a float pair, v, and (past the
+	// first Newton iteration) x_n - x_t and v_n - v_t.
 	const float* qf32 = nullptr;
-	const double* qg = nullptr;
+	const float2* qg2 = nullptr;
+	float2* nodeX = nullptr;
+	float* nodeV = nullptr;
+	float* nodeDx = nullptr;
+	float* nodeDv = nullptr;
 };
 
 // Device control block of one FP64 CG solve; all scalars live on the device.
@@ -98,10 +104,11 @@ struct MatCsr
 void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
 						 double dt, double alpha, double beta, double* kslots, double* rhsE, double* kfull,
 						 double* fE, int* counters, cudaStream_t s, bool linear = false);
-// elemsPerBlock: 32 or 64 (a tuning choice; results do not depend on it).
-void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
-						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
-						cudaStream_t s, int elemsPerBlock = 64, bool linear = false);
+// elemsPerBlock: 32 or 64 (a tuning choice; results do not depend on it). Corotational elements
+// first run the node pass (FP32 node inputs). Returns the number of kernels launched.
+int launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
+					   double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
+					   cudaStream_t s, int elemsPerBlock = 64, bool linear = false);
 void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,
 					 cudaStream_t s);
 void launch_assemble(const DevBody& b, const float* kslots, double c1, double c2, float* A, float* invdiag,

@@ -48,6 +48,28 @@ __global__ void __launch_bounds__(kElemThreads) k_element_fp64(DevBody b, const 
 	if (fl & 2) atomicAdd(&counters[0], 1);
 }
 
+// Node pass of the FP32 corotational element kernel: its per-dof inputs formed once per node rather
+// than once per incident element (~24 elements a node), in the only FP64 arithmetic of the FP32
+// element update: x as an unevaluated float pair (hi = x rounded, lo = x - hi rounded), v, and,
+// past the first Newton iteration, x_n - x_t and v_n - v_t.
+__global__ void k_node_prep(int n, const double* __restrict__ xn, const double* __restrict__ vn,
+							const double* __restrict__ xt, const double* __restrict__ vt, bool start,
+							float2* __restrict__ X, float* __restrict__ V, float* __restrict__ Dx,
+							float* __restrict__ Dv)
+{
+	const int d = blockIdx.x * blockDim.x + threadIdx.x;
+	if (d >= n) return;
+	const double x = xn[d], v = vn[d];
+	const float hi = float(x);
+	X[d] = make_float2(hi, float(x - double(hi)));
+	V[d] = float(v);
+	if (!start)
+	{
+		Dx[d] = float(x - xt[d]);
+		Dv[d] = float(v - vt[d]);
+	}
+}
+
 // FP32 element kernel of the mixed form, kT elements per block (a tuning choice). Results are
 // staged in shared memory and written out with coalesced stores (element-major, the layout the
 // assembly gathers).
@@ -870,11 +892,18 @@ void launch_element_fp64(const DevBody& b, const double* xn, const double* vn, c
 																  nullptr, nullptr, counters);
 }
 
-void launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
-						double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
-						cudaStream_t s, int elemsPerBlock, bool linear)
+int launch_element_f32(const DevBody& b, const double* xn, const double* vn, const double* xt, const double* vt,
+					   double dt, double alpha, double beta, float* kslots, float* rhsE, int* counters,
+					   cudaStream_t s, int elemsPerBlock, bool linear)
 {
-	if (b.E == 0) return;
+	if (b.E == 0) return 0;
+	int kernels = 1;
+	if (!linear)
+	{
+		k_node_prep<<<blocks(b.n, 256), 256, 0, s>>>(b.n, xn, vn, xt, vt, (xt == xn) && (vt == vn), b.nodeX, b.nodeV,
+													 b.nodeDx, b.nodeDv);
+		kernels = 2;
+	}
 	if (elemsPerBlock == 32)
 	{
 		if (linear)
@@ -890,6 +919,7 @@ void launch_element_f32(const DevBody& b, const double* xn, const double* vn, co
 	else
 		k_element_f32<64, false><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
 																 counters);
+	return kernels;
 }
 
 void launch_assemble(const DevBody& b, const double* kslots, double c1, double c2, double* A, double* invdiag,

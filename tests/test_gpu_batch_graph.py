@@ -33,7 +33,9 @@ def test_graph_steps_equal_regular_steps_bit_for_bit(gpu_lib):
     assert np.array_equal(xa, xg) and np.array_equal(va, vg)
     sg = g.segment_stats()
     assert np.all(sg["converged"] == 1) and np.all(sg["iterations"] > 0)
-    assert g.stats()["kernel_launches"] == 4 * 7
+    # Per graph step: node pass, element update, assembly, right-hand side, solve, state update,
+    # validity check, statistics.
+    assert g.stats()["kernel_launches"] == 4 * 8
 
 
 def test_graph_is_recaptured_when_dt_changes(gpu_lib):
