@@ -274,7 +274,129 @@ __global__ void __launch_bounds__(256)
 	rhs[3 * I + 2] = bc[3 * I + 2] ? 0.0 : r2;
 }
 
+// ---- Mixed form: the same right-hand side without FP64 in the matrix pass (FP64 issues at 1/64 of
+// the FP32 rate here, and the FP64 pass is bound by it). K and the slot masses are stored once as
+// unevaluated float pairs hi + lo (~2^-48 relative), u and w per node likewise; the pass forms each
+// product's rounding error by FMA, adds the terms of a row by TwoSum and renormalises the pair once
+// a block, so the row sums keep ~2^-44 of the terms' magnitude (the rows' cancellation against
+// gravity, added in FP64 at the end, stays exact enough for the mixed solve's refinement).
+
+__device__ __forceinline__ void hex_two_sum(float a, float b, float& s, float& e)
+{
+	s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (sh, sl) += a * b for float pairs a, b (the lo * lo term is below the pair's precision).
+__device__ __forceinline__ void hex_acc(float& sh, float& sl, float2 a, float2 b)
+{
+	const float P = __fmul_rn(a.x, b.x);
+	const float e = __fmaf_rn(a.x, b.x, -P);
+	const float cross = __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x));
+	float t, et;
+	hex_two_sum(sh, P, t, et);
+	sh = t;
+	sl = __fadd_rn(sl, __fadd_rn(et, __fadd_rn(e, cross)));
+}
+
+__global__ void k_split_pairs(size_t n, const double* __restrict__ src, float2* __restrict__ dst)
+{
+	const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const double v = src[i];
+	const float hi = float(v);
+	dst[i] = make_float2(hi, float(v - double(hi)));
+}
+
+// u = x_t - x0 + (dt + beta) v_n and w = alpha v_n + (v_n - v_t) / dt in FP64, stored as float pairs:
+// three float4 per node {u0, u1}, {u2, w0}, {w1, w2}.
+__global__ void k_hex_uw_df(int N, const double* __restrict__ xrest, const double* __restrict__ xt,
+							const double* __restrict__ vn, const double* __restrict__ vt, double alpha, double c2,
+							double inv_dt, float4* __restrict__ uw)
+{
+	const int I = blockIdx.x * blockDim.x + threadIdx.x;
+	if (I >= N) return;
+	float h[6], l[6];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		const double v = vn[3 * I + i];
+		const double u = (xt[3 * I + i] - xrest[3 * I + i]) + c2 * v;
+		const double w = alpha * v + (v - vt[3 * I + i]) * inv_dt;
+		h[i] = float(u);
+		l[i] = float(u - double(h[i]));
+		h[3 + i] = float(w);
+		l[3 + i] = float(w - double(h[3 + i]));
+	}
+	uw[3 * (size_t)I] = make_float4(h[0], l[0], h[1], l[1]);
+	uw[3 * (size_t)I + 1] = make_float4(h[2], l[2], h[3], l[3]);
+	uw[3 * (size_t)I + 2] = make_float4(h[4], l[4], h[5], l[5]);
+}
+
+__global__ void __launch_bounds__(256)
+	k_hex_rhs_df(MatSell3 K, const float2* __restrict__ Kp, const float2* __restrict__ Msp,
+				 const float4* __restrict__ uw, const double* __restrict__ nmass, const uint8_t* __restrict__ bc,
+				 double g0, double g1, double g2, int gravityOn, double* __restrict__ rhs)
+{
+	const int rs = blockIdx.x * blockDim.x + threadIdx.x;
+	if (rs >= K.rows) return;
+	const int I = K.perm[rs];
+	if (I < 0) return;
+	const int c = rs >> 5, lane = rs & 31;
+	float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
+	for (int k = K.off[c]; k < K.off[c + 1]; ++k)
+	{
+		const int J = K.col[k * 32 + lane];
+		const float2* kb = Kp + (size_t)k * 288 + lane;
+		const float2 m = Msp[k * 32 + lane];
+		const float4 r0 = uw[3 * (size_t)J], r1 = uw[3 * (size_t)J + 1], r2 = uw[3 * (size_t)J + 2];
+		const float2 u[3] = {make_float2(r0.x, r0.y), make_float2(r0.z, r0.w), make_float2(r1.x, r1.y)};
+		const float2 w[3] = {make_float2(r1.z, r1.w), make_float2(r2.x, r2.y), make_float2(r2.z, r2.w)};
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+#pragma unroll
+			for (int j = 0; j < 3; ++j) hex_acc(sh[i], sl[i], kb[32 * (3 * i + j)], u[j]);
+			hex_acc(sh[i], sl[i], m, w[i]);
+			float t, e;
+			hex_two_sum(sh[i], sl[i], t, e);
+			sh[i] = t;
+			sl[i] = e;
+		}
+	}
+	double r[3];
+#pragma unroll
+	for (int i = 0; i < 3; ++i) r[i] = -(double(sh[i]) + double(sl[i]));
+	if (gravityOn)  // FemRepresentation::addGravityForce (:641-662), lumped rho V / 8 per node
+	{
+		const double mI = nmass[I];
+		r[0] += g0 * mI;
+		r[1] += g1 * mI;
+		r[2] += g2 * mI;
+	}
+#pragma unroll
+	for (int i = 0; i < 3; ++i) rhs[3 * I + i] = bc[3 * I + i] ? 0.0 : r[i];
+}
+
 }  // namespace
+
+void launch_split_pairs(size_t n, const double* src, float2* dst, cudaStream_t s)
+{
+	if (n == 0) return;
+	k_split_pairs<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, dst);
+}
+
+void launch_hex_rhs_df(const MatSell3& K, const float2* Kp, const float2* Msp, const DevBody& b, const double* xt,
+					   const double* vn, const double* vt, double dt, double alpha, double beta, const double* gravity,
+					   int gravityOn, double* uw, double* rhs, cudaStream_t s)
+{
+	if (K.rows == 0) return;
+	float4* uw4 = reinterpret_cast<float4*>(uw);  // 48 bytes per node, 16-byte aligned allocation
+	k_hex_uw_df<<<blocks_for(b.N, 256), 256, 0, s>>>(b.N, b.xrest, xt, vn, vt, alpha, dt + beta, 1.0 / dt, uw4);
+	k_hex_rhs_df<<<blocks_for(K.rows, 256), 256, 0, s>>>(K, Kp, Msp, uw4, b.nmass, b.bc, gravity[0], gravity[1],
+														 gravity[2], gravityOn, rhs);
+}
 
 void launch_hex_element(int E, const int* nodes, const double* xrest, const double* young, const double* poisson,
 						const double* rho, double* slots, double* smass, cudaStream_t s)

@@ -197,6 +197,7 @@ struct gbfem_handle_s
 	// Hexahedra: element node ids, materials, and the assembled K / scalar block masses (SELL layout).
 	DevBuf<int> d_enodes;
 	DevBuf<double> d_young, d_poisson, d_rho, d_K, d_Ms, d_uw;
+	DevBuf<float2> d_Kp, d_Msp;  // mixed form: K and the slot masses as float pairs (right-hand side)
 	// Mixed form, corotational: per-element rest edges (FP32) and rest Gram (FP64).
 	DevBuf<float> d_qf32;
 	DevBuf<float2> d_qg2;
@@ -317,6 +318,8 @@ struct gbfem_handle_s
 								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f, &d_young, &d_poisson, &d_rho,
 								&d_K, &d_Ms, &d_uw};
 		for (auto* b : bd) b->free();
+		d_Kp.free();
+		d_Msp.free();
 		DevBuf<int>* bi[] = {&d_perm, &d_off, &d_sellcol, &d_cptr, &d_cidx, &d_iptr, &d_iidx, &d_counters, &d_idx,
 							 &d_sptr, &d_sidx, &d_srow, &d_scol, &d_enodes};
 		for (auto* b : bi) b->free();
@@ -414,6 +417,14 @@ gbfem_status rebuild_hex_operators(gbfem_handle h)
 	launch_hex_element(h->E, h->d_enodes.p, h->d_xrest.p, h->d_young.p, h->d_poisson.p, h->d_rho.p, t.slots.p,
 					   t.smass.p, s);
 	launch_assemble_k(h->body(), t.slots.p, t.smass.p, h->d_K.p, h->d_Ms.p, h->d_lmass.p, s);
+	if (h->mixed())
+	{
+		const size_t slots = (size_t)h->sellSlots;
+		if (!h->d_Kp.p) GB_CUDA(h, h->d_Kp.alloc(9 * slots));
+		if (!h->d_Msp.p) GB_CUDA(h, h->d_Msp.alloc(slots));
+		launch_split_pairs(9 * slots, h->d_K.p, h->d_Kp.p, s);
+		launch_split_pairs(slots, h->d_Ms.p, h->d_Msp.p, s);
+	}
 	GB_CUDA(h, cudaGetLastError());
 	GB_CUDA(h, cudaStreamSynchronize(s));  // before the scratch is released
 	h->linearReady = false;
@@ -1060,8 +1071,12 @@ gbfem_status check_pcg_error(gbfem_handle h)
 void enqueue_hex_rhs(gbfem_handle h, double dt, const double* xt, const double* vt, cudaStream_t s)
 {
 	const MatSell3 K{h->nrows, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_K.p};
-	launch_hex_rhs(K, h->d_Ms.p, h->body(), xt, h->d_v.p, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
-				   h->prm.gravity, h->prm.gravity_enabled, h->d_uw.p, h->d_rhs.p, s);
+	if (h->mixed())
+		launch_hex_rhs_df(K, h->d_Kp.p, h->d_Msp.p, h->body(), xt, h->d_v.p, vt, dt, h->prm.rayleigh_mass,
+						  h->prm.rayleigh_stiffness, h->prm.gravity, h->prm.gravity_enabled, h->d_uw.p, h->d_rhs.p, s);
+	else
+		launch_hex_rhs(K, h->d_Ms.p, h->body(), xt, h->d_v.p, vt, dt, h->prm.rayleigh_mass, h->prm.rayleigh_stiffness,
+					   h->prm.gravity, h->prm.gravity_enabled, h->d_uw.p, h->d_rhs.p, s);
 }
 
 // Autotuner of the mixed form, run on the first step's own system: times the element kernel at 32

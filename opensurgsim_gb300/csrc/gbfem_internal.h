@@ -182,6 +182,13 @@ void launch_system_from_k(const DevBody& b, const double* K, double c1, double c
 void launch_hex_rhs(const MatSell3& K, const double* Ms, const DevBody& b, const double* xt, const double* vn,
 					const double* vt, double dt, double alpha, double beta, const double* gravity, int gravityOn,
 					double* uw, double* rhs, cudaStream_t s);
+// Mixed form: the same right-hand side from K and the slot masses stored as float pairs (Kp, Msp,
+// launch_split_pairs), in double-float arithmetic with no FP64 in the matrix pass; same scratch.
+void launch_hex_rhs_df(const MatSell3& K, const float2* Kp, const float2* Msp, const DevBody& b, const double* xt,
+					   const double* vn, const double* vt, double dt, double alpha, double beta, const double* gravity,
+					   int gravityOn, double* uw, double* rhs, cudaStream_t s);
+// dst[i] = {hi, lo}: src[i] as an unevaluated float pair (hi = src rounded, lo = the rest rounded).
+void launch_split_pairs(size_t n, const double* src, float2* dst, cudaStream_t s);
 
 // External generalized forces of one step (Fem3DRepresentation::addExternalGeneralizedForce):
 // updates of lower system blocks (I >= J; z/w the SELL bases of (I,J) and (J,I), w < 0 on the
