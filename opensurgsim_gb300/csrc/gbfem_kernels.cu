@@ -194,13 +194,39 @@ __global__ void k_rhs_gather(DevBody b, const T* __restrict__ rhsE, double g0, d
 	if (I >= b.N) return;
 	double s0 = 0, s1 = 0, s2 = 0;
 	const int k1 = b.iptr[I + 1];
-	for (int k = b.iptr[I]; k < k1; ++k)
+	if constexpr (std::is_same<T, float>::value)
 	{
-		const int c = b.iidx[k];
-		const T* src = rhsE + (size_t)(c >> 2) * 12 + 3 * (c & 3);
-		s0 += double(src[0]);
-		s1 += double(src[1]);
-		s2 += double(src[2]);
+		// FP32 contributions summed exactly enough as float pairs (TwoSum; the errors' own sum keeps
+		// ~2^-48 of the total) and converted to FP64 once: an FP64 add and conversion per contribution
+		// (~140 FP64 instructions a node) would issue at 1/64 of the FP32 rate.
+		float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+		for (int k = b.iptr[I]; k < k1; ++k)
+		{
+			const int c = b.iidx[k];
+			const float* src = rhsE + (size_t)(c >> 2) * 12 + 3 * (c & 3);
+#pragma unroll
+			for (int i = 0; i < 3; ++i)
+			{
+				float t, e;
+				elem::df_two_sum(h[i], src[i], t, e);
+				h[i] = t;
+				l[i] = __fadd_rn(l[i], e);
+			}
+		}
+		s0 = double(h[0]) + double(l[0]);
+		s1 = double(h[1]) + double(l[1]);
+		s2 = double(h[2]) + double(l[2]);
+	}
+	else
+	{
+		for (int k = b.iptr[I]; k < k1; ++k)
+		{
+			const int c = b.iidx[k];
+			const T* src = rhsE + (size_t)(c >> 2) * 12 + 3 * (c & 3);
+			s0 += double(src[0]);
+			s1 += double(src[1]);
+			s2 += double(src[2]);
+		}
 	}
 	if (gravityOn)  // FemRepresentation::addGravityForce (:641-662)
 	{
