@@ -1099,9 +1099,10 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 		if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
 		return e;
 	};
-	float bestE = 1e30f;
-	int eBest = h->elemsPerBlock;
-	for (int rep = 0; rep < 2 && !h->hex(); ++rep)
+	// Element kernel: the candidates alternate; the first round warms up, the best of the next three
+	// counts for each (one timing alone has picked the slower variant).
+	float bestE32 = 1e30f, bestE64 = 1e30f;
+	for (int rep = 0; rep < 4 && !h->hex(); ++rep)
 		for (int ept : {32, 64})
 		{
 			GB_CUDA(h, cudaEventRecord(e0, s));
@@ -1110,13 +1111,10 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 			GB_CUDA(h, cudaGetLastError());
 			GB_CUDA(h, cudaEventRecord(e1, s));
 			GB_CUDA(h, elapsed());
-			if (rep == 1 && t < bestE)
-			{
-				bestE = t;
-				eBest = ept;
-			}
+			float& best = (ept == 32) ? bestE32 : bestE64;
+			if (rep > 0) best = std::min(best, t);
 		}
-	h->elemsPerBlock = eBest;
+	if (!h->hex()) h->elemsPerBlock = (bestE32 < bestE64) ? 32 : 64;
 	if (h->hex())
 	{
 		launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
@@ -1125,7 +1123,7 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 	else
 	{
 		launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
-						   h->d_counters.p, s, eBest, h->linear());
+						   h->d_counters.p, s, h->elemsPerBlock, h->linear());
 		launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 		launch_rhs_gather(body, h->d_rhsE32.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
 	}

@@ -77,10 +77,12 @@ template <int kT, bool kLinear>
 __global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __restrict__ xn,
 															   const double* __restrict__ vn,
 															   const double* __restrict__ xt,
-															   const double* __restrict__ vt, double dt, double alpha,
-															   double beta, float* __restrict__ kslots,
+															   const double* __restrict__ vt, float c2, float alpha,
+															   float inv_dt, float* __restrict__ kslots,
 															   float* __restrict__ rhsE, int* counters)
 {
+	// c2 = dt + beta, alpha and 1/dt arrive in FP32 from the host: formed in each thread they would
+	// cost an FP64 add and an FP64 division per element.
 	constexpr int kV = kSlots * 9;
 	__shared__ float sks[kV][kT + 1];
 	__shared__ float srhs[12][kT + 1];
@@ -90,7 +92,7 @@ __global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __r
 	if (e < E)
 	{
 		elem::ElemInF in;
-		elem::gather_f32<kLinear>(b, e, xn, vn, xt, vt, float(dt + beta), float(alpha), float(1.0 / dt), in);
+		elem::gather_f32<kLinear>(b, e, xn, vn, xt, vt, c2, alpha, inv_dt, in);
 		float g[4][3];
 #pragma unroll
 		for (int a = 0; a < 4; ++a)
@@ -923,6 +925,7 @@ int launch_element_f32(const DevBody& b, const double* xn, const double* vn, con
 					   cudaStream_t s, int elemsPerBlock, bool linear)
 {
 	if (b.E == 0) return 0;
+	const float c2f = float(dt + beta), alphaf = float(alpha), invdtf = float(1.0 / dt);
 	int kernels = 1;
 	if (!linear)
 	{
@@ -933,17 +936,17 @@ int launch_element_f32(const DevBody& b, const double* xn, const double* vn, con
 	if (elemsPerBlock == 32)
 	{
 		if (linear)
-			k_element_f32<32, true><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+			k_element_f32<32, true><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, c2f, alphaf, invdtf, kslots, rhsE,
 																	counters);
 		else
-			k_element_f32<32, false><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+			k_element_f32<32, false><<<blocks(b.E, 32), 32, 0, s>>>(b, xn, vn, xt, vt, c2f, alphaf, invdtf, kslots, rhsE,
 																	 counters);
 	}
 	else if (linear)
-		k_element_f32<64, true><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+		k_element_f32<64, true><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, c2f, alphaf, invdtf, kslots, rhsE,
 																counters);
 	else
-		k_element_f32<64, false><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, dt, alpha, beta, kslots, rhsE,
+		k_element_f32<64, false><<<blocks(b.E, 64), 64, 0, s>>>(b, xn, vn, xt, vt, c2f, alphaf, invdtf, kslots, rhsE,
 																 counters);
 	return kernels;
 }
