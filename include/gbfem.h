@@ -200,9 +200,8 @@ GBFEM_API gbfem_status gbfem_add_external_force(gbfem_handle h, int32_t element,
 												const double* stiffness, const double* damping);
 
 /* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
- * step times the persistent solve at 2, 3, 4 CTAs per SM and refresh weights 1 to 4 on its own
- * system and keeps the fastest; the element kernel runs 64 elements per block (32 only when set
- * here: timed at a first step's rest state 32 can win, at the deformed states after it 64 does). The solve's
+ * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
+ * CTAs per SM and refresh weights 1 to 4 on its own system, and keeps the fastest. The solve's
  * partition sets the rounding of its sums, so a run that must repeat another bit for bit reads the
  * choice with gbfem_get_tuning and pins it with gbfem_set_tuning (which also disables autotune). */
 GBFEM_API gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm,

@@ -1079,10 +1079,11 @@ void enqueue_hex_rhs(gbfem_handle h, double dt, const double* xt, const double* 
 					   h->prm.gravity, h->prm.gravity_enabled, h->d_uw.p, h->d_rhs.p, s);
 }
 
-// Autotuner of the mixed form, run on the first step's own system: times the persistent solve for
-// 2, 3 and 4 CTAs per SM and refresh weights 1 to 4 and keeps the fastest. The solve's partition
-// changes the rounding of its sums (not its convergence test), so a run that must reproduce another
-// bit for bit pins the choice with gbfem_set_tuning.
+// Autotuner of the mixed form, run on the first step's own system: times the element kernel at 32
+// and 64 elements per block, then the persistent solve for 2, 3 and 4 CTAs per SM and refresh
+// weights 1 to 4, and keeps the fastest of each. The element kernel's results do not depend on
+// its block size; the solve's partition does change its rounding (not its convergence test), so a
+// run that must reproduce another bit for bit pins the choice with gbfem_set_tuning.
 gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, double dt, double c1, double c2,
 						int maxIter)
 {
@@ -1098,10 +1099,22 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 		if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
 		return e;
 	};
-	// The element kernel's block size is not tuned here: timed on the first step's state (often the
-	// rest state, where the polar iteration ends at once and the kernel is bound by memory) 32
-	// elements per block wins, while at the deformed states of the steps after it 64 does (2.62 vs
-	// 3.16 ms on the 256-mesh batch). It stays at 64 unless gbfem_set_tuning sets it.
+	// Element kernel: the candidates alternate; the first round warms up, the best of the next three
+	// counts for each.
+	float bestE32 = 1e30f, bestE64 = 1e30f;
+	for (int rep = 0; rep < 4 && !h->hex(); ++rep)
+		for (int ept : {32, 64})
+		{
+			GB_CUDA(h, cudaEventRecord(e0, s));
+			launch_element_f32(body, h->d_x.p, h->d_v.p, xt, vt, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p,
+							   h->d_counters.p, s, ept, h->linear());
+			GB_CUDA(h, cudaGetLastError());
+			GB_CUDA(h, cudaEventRecord(e1, s));
+			GB_CUDA(h, elapsed());
+			float& best = (ept == 32) ? bestE32 : bestE64;
+			if (rep > 0) best = std::min(best, t);
+		}
+	if (!h->hex()) h->elemsPerBlock = (bestE32 < bestE64) ? 32 : 64;
 	if (h->hex())
 	{
 		launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
