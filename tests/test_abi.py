@@ -158,6 +158,14 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
     assert "exceeds" in _lib.last_error(None)
 
 
+def test_barrier_selftest_validates_its_arguments_before_any_device_work(lib):
+    from opensurgsim_gb300 import _lib
+
+    for phases, timeout_ns in ((0, 1_000_000), (1_000_001, 1_000_000), (1, 999), (1, 2_000_000_001)):
+        assert lib.gbfem_barrier_selftest(phases, 1, timeout_ns, None, None) == _lib.GBFEM_INVALID_ARG
+        assert "barrier_selftest" in _lib.last_error(None)
+
+
 def test_cpp_facade_compiles_and_links(lib, tmp_path):
     gxx = shutil.which("g++")
     if not gxx:
