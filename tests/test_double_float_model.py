@@ -92,3 +92,41 @@ def test_double_float_gram_difference_keeps_the_strain_under_large_rigid_motion(
     assert worst_df < 4e-6, worst_df
     # the same quantity in plain FP32 is lost to cancellation at small strains
     assert worst_f32 > 1e-2, worst_f32
+
+
+def hex_acc(sh, sl, a, b):
+    """(sh, sl) += a * b for float pairs, as k_hex_rhs_df accumulates a row (gbfem_hex.cu)."""
+    P = f32(a[0] * b[0])
+    e = f32(np.float64(a[0]) * np.float64(b[0]) - np.float64(P))                 # FMA(a.hi, b.hi, -P)
+    cross = f32(np.float64(a[0]) * np.float64(b[1]) + np.float64(f32(a[1] * b[0])))  # FMA(a.hi, b.lo, a.lo*b.hi)
+    t, et = two_sum(sh, P)
+    return t, f32(sl + f32(et + f32(e + cross)))
+
+
+def test_double_float_row_sums_of_the_hexahedron_right_hand_side():
+    """A row of K u + m w (81 blocks of 3 terms plus a mass term, values of both signs spanning six
+    decades) from float-pair operands, renormalised once a block: within ~2^-44 of the terms'
+    absolute sum, as the FP64 pass is within ~2^-52 * sqrt(terms)."""
+    rng = np.random.default_rng(11)
+    worst = 0.0
+    for trial in range(50):
+        nblk = 81
+        K = rng.normal(size=(nblk, 3)) * 10.0 ** rng.uniform(-3, 3, (nblk, 1))
+        u = rng.normal(size=(nblk, 3)) * 1e-3
+        m = rng.uniform(0, 1e-2, nblk)
+        w = rng.normal(size=nblk) * 1e-2
+        sh, sl = f32(0), f32(0)
+        exact = Fraction(0)
+        absum = 0.0
+        for b in range(nblk):
+            for j in range(3):
+                sh, sl = hex_acc(sh, sl, pair(K[b, j]), pair(u[b, j]))
+                exact += Fraction(float(K[b, j])) * Fraction(float(u[b, j]))
+                absum += abs(K[b, j] * u[b, j])
+            sh, sl = hex_acc(sh, sl, pair(m[b]), pair(w[b]))
+            exact += Fraction(float(m[b])) * Fraction(float(w[b]))
+            absum += abs(m[b] * w[b])
+            sh, sl = two_sum(sh, sl)
+        got = np.float64(sh) + np.float64(sl)
+        worst = max(worst, abs(got - float(exact)) / absum)
+    assert worst < 2.0 ** -44, worst
