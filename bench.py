@@ -884,6 +884,8 @@ def run_reference(args, rank, world):
                   f"step(s), one mesh per task on {threads} host threads; oracle FP64 C++ restatement, -O3")
         cores, workload = threads, "batch256 (every 4th mesh)"
         ms = 1e3 * sum(times) / len(times)
+        split = phase_split([sum(m.last_step_times()[i] for m in models) for i in range(3)],
+                            "CPU seconds of the last step summed over the meshes")
     else:
         scene = build_scene(args.config)
         model = O.OracleModel.from_scene(scene)
@@ -904,9 +906,12 @@ def run_reference(args, rank, world):
         if args.warmup > 0:
             one()
         times = []
+        parts = [0.0, 0.0, 0.0]
         while len(times) < args.steps and sum(times) < budget_s:
             times.append(one())
+            parts = [p + t for p, t in zip(parts, model.last_step_times())]
         value = scene.mesh.num_tets * len(times) / sum(times)
+        split = phase_split(parts, f"seconds over the {len(times)} timed step(s)")
         sample = (f"{len(times)} timed step(s) of the same scene, capped at {budget_s:.0f} s; oracle FP64 C++ "
                   "restatement, -O3, 1 thread (a representation is single-threaded)")
         cores, workload = 1, args.config
@@ -918,7 +923,8 @@ def run_reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cube-grid meshes)",
         "config": {"workload": workload, "precision": "fp64"},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample,
+                         "phase_split": split},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
