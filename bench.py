@@ -174,6 +174,22 @@ def host_threads():
     return max(1, math.ceil(0.5 * (os.cpu_count() or 1)))
 
 
+def host_info():
+    """The host the CPU numbers were taken on: nproc and the lscpu summary lines."""
+    info = {"nproc": os.cpu_count()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        keep = ("Architecture", "Model name", "Socket(s)", "Core(s) per socket", "Thread(s) per core", "CPU(s)",
+                "CPU max MHz")
+        for ln in out.splitlines():
+            k, _, v = ln.partition(":")
+            if k.strip() in keep:
+                info[k.strip()] = v.strip()
+    except Exception as exc:  # lscpu missing: nproc alone
+        info["lscpu"] = f"unavailable ({exc.__class__.__name__})"
+    return info
+
+
 # ------------------------------------------------------------------------------------------------
 # Algorithmic bytes (HBM) of the solve, per CG iteration and per FP64 residual refresh, for one
 # mesh with scalar non-zeros nnz, N nodes and n = 3N dofs; s = bytes per matrix value. Block
@@ -872,7 +888,7 @@ def run_reference(args, rank, world):
         models = [O2.OracleModel.from_scene(s) for s in scenes]
         threads = host_threads()
         tets = sum(s.mesh.num_tets for s in scenes)
-        O2.step_many(models, 1e-3, max(0, min(args.warmup, 1)), threads)
+        O2.step_many(models, 1e-3, max(0, args.warmup), threads)
         times = []
         budget_s = float(os.environ.get("GBFEM_REFERENCE_BUDGET_S", "150"))
         while len(times) < args.steps and sum(times) < budget_s:
@@ -903,7 +919,7 @@ def run_reference(args, rank, world):
             step += 1
             return time.perf_counter() - t0
 
-        if args.warmup > 0:
+        for _ in range(max(0, args.warmup)):
             one()
         times = []
         parts = [0.0, 0.0, 0.0]
@@ -919,12 +935,12 @@ def run_reference(args, rank, world):
     metric, unit = (HEX_METRIC, HEX_UNIT) if args.config == "hex" else (METRIC, UNIT)
     return {
         "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": len(times),
-        "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": max(0, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cube-grid meshes)",
         "config": {"workload": workload, "precision": "fp64"},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample,
-                         "phase_split": split},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "threads": cores, "kind": "port",
+                         "sample": sample, "phase_split": split, "host": host_info()},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -976,14 +992,16 @@ def main():
                 sample = batch_cpu_sample(scenes)
                 v, t, threads, split = cpu_batch_steps(sample, 1)
                 line["cpu_baseline"] = {
-                    "value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                    "value": v, "unit": UNIT, "cores": threads, "threads": threads, "kind": "port",
+                    "host": host_info(),
                     "sample": (f"1 step of every 4th mesh of the batch ({len(sample)} meshes, "
                                f"{sum(s.mesh.num_tets for s in sample)} tets) in {t:.1f} s, one mesh per task on "
                                f"{threads} host threads; oracle FP64 C++ restatement, -O3"),
                     "phase_split": split}
             else:
                 v, t, split = cpu_single_steps(scene, 1)
-                line["cpu_baseline"] = {"value": v, "unit": line["unit"], "cores": 1, "kind": "port",
+                line["cpu_baseline"] = {"value": v, "unit": line["unit"], "cores": 1, "threads": 1, "kind": "port",
+                                        "host": host_info(),
                                         "sample": f"1 step of the same scene on the host ({t:.1f} s), oracle FP64 "
                                                   "C++ restatement, -O3, 1 thread", "phase_split": split}
             log(f"cpu baseline: {v / 1e3:.1f} k tet-steps/s")

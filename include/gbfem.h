@@ -306,9 +306,15 @@ GBFEM_API gbfem_status gbfem_cg_destroy(gbfem_cg cg);
  * The solve is the one gbfem_cg_solve runs (zero initial guess, Jacobi preconditioner, stop when
  * |r|^2 < max(tol^2 |b|^2, DBL_MIN) or after max_iterations, <= 0 meaning 2n).
  * Limits: n <= GBFEM_NOALLOC_MAX_DOFS, else GBFEM_INVALID_ARG (message from gbfem_last_error(NULL)).
- * The first call on a device looks up the scratch area's device address with that device current;
- * make that first call before any stream capture. Every call shares the one scratch area:
- * calls that overlap on the same GPU race and must be serialised by the caller. */
+ * The matrix is checked on the device before the solve reads through it: rowptr[0] != 0, a
+ * decreasing rowptr or a column index outside [0, n) returns GBFEM_INVALID_ARG (the message names
+ * the first bad row); rowptr must hold n + 1 entries and col / values rowptr[n] each.
+ * The first call in a context of a device (the first call on the device, and the first after the
+ * device was reset) looks up the scratch area's device address with that device current; make that
+ * first call before any stream capture. Each call waits for its stream: it reads the solve's
+ * control block back to the host between batches of iterations. Every call shares the one scratch
+ * area, which keeps the last call's contents (each call clears what must start at zero): calls
+ * that overlap on the same GPU race and must be serialised by the caller. */
 #define GBFEM_NOALLOC_MAX_DOFS 262144
 GBFEM_API gbfem_status gbfem_cg_solve_noalloc(int32_t n, const int32_t* rowptr, const int32_t* col,
 											  const double* values, const double* b, double* x, double tolerance,

@@ -5,8 +5,9 @@ from (x0, v0) and take ``nsteps`` steps of ``dt`` with the body's own step (FP64
 keeping the state every ``checkpoint_every`` steps. Backward: for each checkpoint segment, last
 first, re-run the segment's steps to recover its states, then walk them back with
 ``gbfem_adjoint_step`` (the transposed solve and the per-element derivative kernels), which
-accumulates dL/d(log E) and carries (dL/dx, dL/dv) to the segment's start. Gradients flow to
-``log_young``, ``x0`` and ``v0``.
+accumulates dL/d(log E) and dL/d(nu) and carries (dL/dx, dL/dv) to the segment's start. Gradients
+flow to ``log_young``, ``x0``, ``v0`` and, when given, the per-element Poisson ratios ``poisson``
+(Fem3DElementTetrahedron.cpp:204-205: nu enters K0 through lambda and mu).
 
 The reference has no adjoint; the forward steps are the reference's Fem3DRepresentation::update
 semantics (one Newton iteration). All tensors are float64 on the body's device.
@@ -42,10 +43,13 @@ def _check(body, st, allow=(_lib.GBFEM_OK,)):
         raise GbfemError(st, _lib.last_error(body.handle))
 
 
-def set_young(body, log_young: torch.Tensor):
+def set_young(body, log_young: torch.Tensor, poisson: torch.Tensor = None):
+    """Per-element E = exp(log_young) and, if given, nu = poisson (else each element keeps its nu)."""
     young = torch.exp(log_young.detach().to(torch.float64)).contiguous()
+    nu = None if poisson is None else poisson.detach().to(torch.float64).contiguous()
     torch.cuda.synchronize(young.device)
-    _check(body, _lib.load().gbfem_set_materials_device(body.handle, ctypes.c_void_p(young.data_ptr()), None))
+    _check(body, _lib.load().gbfem_set_materials_device(body.handle, ctypes.c_void_p(young.data_ptr()),
+                                                        None if nu is None else ctypes.c_void_p(nu.data_ptr())))
 
 
 def rollout_states(body, x0, v0, dt, nsteps, keep=None):
@@ -67,11 +71,12 @@ def rollout_states(body, x0, v0, dt, nsteps, keep=None):
 
 
 class ImplicitRollout(torch.autograd.Function):
-    """(x_T, v_T) = rollout(log_young, x0, v0); see the module docstring."""
+    """(x_T, v_T) = rollout(log_young, poisson, x0, v0); see the module docstring. ``poisson`` may
+    be None (each element keeps its Poisson ratio and gets no gradient)."""
 
     @staticmethod
-    def forward(ctx, log_young, x0, v0, body, dt, nsteps, checkpoint_every, flags=0):
-        set_young(body, log_young)
+    def forward(ctx, log_young, poisson, x0, v0, body, dt, nsteps, checkpoint_every, flags=0):
+        set_young(body, log_young, poisson)
         k = max(1, int(checkpoint_every))
         checkpoints = []
         xv, vv = state_views(body)
@@ -87,20 +92,24 @@ class ImplicitRollout(torch.autograd.Function):
                 checkpoints.append((xv.clone(), vv.clone()))
         ctx.body, ctx.dt, ctx.nsteps, ctx.k, ctx.flags = body, dt, nsteps, k, int(flags)
         ctx.checkpoints = checkpoints
-        ctx.save_for_backward(log_young)
+        ctx.has_poisson = poisson is not None
+        ctx.save_for_backward(log_young, poisson if poisson is not None else log_young)
         return xv.clone(), vv.clone()
 
     @staticmethod
     def backward(ctx, gx, gv):
-        (log_young,) = ctx.saved_tensors
+        log_young, poisson = ctx.saved_tensors
+        if not ctx.has_poisson:
+            poisson = None
         body, dt, nsteps, k = ctx.body, ctx.dt, ctx.nsteps, ctx.k
         dev = log_young.device
         n = body.n
         lx = (gx if gx is not None else torch.zeros(n, dtype=torch.float64, device=dev)).to(torch.float64).contiguous().clone()
         lv = (gv if gv is not None else torch.zeros(n, dtype=torch.float64, device=dev)).to(torch.float64).contiguous().clone()
         glog = torch.zeros(body.num_tets, dtype=torch.float64, device=dev)
+        gnu = torch.zeros(body.num_tets, dtype=torch.float64, device=dev) if poisson is not None else None
         L = _lib.load()
-        set_young(body, log_young)
+        set_young(body, log_young, poisson)
         starts = list(range(0, nsteps, k))
         for seg in reversed(range(len(starts))):
             t0 = starts[seg]
@@ -114,14 +123,14 @@ class ImplicitRollout(torch.autograd.Function):
                 dv = (states[t + 1][1] - vt).contiguous()
                 torch.cuda.synchronize(dev)
                 st = L.gbfem_adjoint_step(body.handle, float(dt), *[ctypes.c_void_p(a.data_ptr()) for a in
-                                                                     (xt, vt, dv, lx, lv, lx, lv, glog)], None,
-                                          ctx.flags)
+                                                                     (xt, vt, dv, lx, lv, lx, lv, glog)],
+                                          None if gnu is None else ctypes.c_void_p(gnu.data_ptr()), ctx.flags)
                 _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
         torch.cuda.synchronize(dev)
-        return glog, lx, lv, None, None, None, None, None
+        return glog, gnu, lx, lv, None, None, None, None, None
 
 
-def rollout(body, log_young, x0, v0, dt, nsteps, checkpoint_every=10, flags=0):
-    """Differentiable rollout: returns (x_T, v_T) with gradients to log_young, x0 and v0. ``flags``
-    (e.g. STEP_TIME_PHASES) go to every adjoint step."""
-    return ImplicitRollout.apply(log_young, x0, v0, body, dt, nsteps, checkpoint_every, flags)
+def rollout(body, log_young, x0, v0, dt, nsteps, checkpoint_every=10, flags=0, poisson=None):
+    """Differentiable rollout: returns (x_T, v_T) with gradients to log_young, x0, v0 and (when
+    given, float64 per element) poisson. ``flags`` (e.g. STEP_TIME_PHASES) go to every adjoint step."""
+    return ImplicitRollout.apply(log_young, poisson, x0, v0, body, dt, nsteps, checkpoint_every, flags)

@@ -66,15 +66,12 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 		adj::adjoint_item<S>(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
 							 gv + (size_t)e * 12, &pl, &pm);
 	if (!moduli) return;
-	// lambda V = V E nu / ((1 + nu)(1 - 2 nu)), mu V = V E / (2 (1 + nu)): d/d log E scales both by
-	// one; nu = lambda / (2 (lambda + mu)).
+	// lambda V and mu V are both proportional to E: d/d log E scales each by one.
 	if (gLogE) gLogE[e] += lamV * pl + muV * pm;
 	if (gNu)
 	{
-		const double nu = lamV / (2.0 * (lamV + muV));
-		const double EV = 2.0 * muV * (1.0 + nu);
-		const double dl = EV * (1.0 + 2.0 * nu * nu) / ((1.0 + nu) * (1.0 + nu) * (1.0 - 2.0 * nu) * (1.0 - 2.0 * nu));
-		const double dm = -EV / (2.0 * (1.0 + nu) * (1.0 + nu));
+		double dl, dm;
+		adj::poisson_partials(lamV, muV, &dl, &dm);
 		gNu[e] += dl * pl + dm * pm;
 	}
 }

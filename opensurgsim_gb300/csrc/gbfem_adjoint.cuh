@@ -144,6 +144,18 @@ __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const
 	}
 }
 
+// Chain rule from the element's moduli to its Poisson ratio: with lambda V = V E nu / ((1 + nu)
+// (1 - 2 nu)) and mu V = V E / (2 (1 + nu)) (Fem3DElementTetrahedron.cpp:204-205) at fixed E,
+// d(lambda V)/d nu = V E (1 + 2 nu^2) / ((1 + nu)^2 (1 - 2 nu)^2) and d(mu V)/d nu = -V E / (2 (1 + nu)^2);
+// nu = lambda / (2 (lambda + mu)) and V E = 2 mu V (1 + nu) are recovered from the stored moduli.
+__host__ __device__ inline void poisson_partials(double lamV, double muV, double* dLam, double* dMu)
+{
+	const double nu = lamV / (2.0 * (lamV + muV));
+	const double EV = 2.0 * muV * (1.0 + nu);
+	*dLam = EV * (1.0 + 2.0 * nu * nu) / ((1.0 + nu) * (1.0 + nu) * (1.0 - 2.0 * nu) * (1.0 - 2.0 * nu));
+	*dMu = -EV / (2.0 * (1.0 + nu) * (1.0 + nu));
+}
+
 // All items of one element in one call (gx[0..2] completed from translation invariance).
 __host__ __device__ inline void adjoint_element(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
 												const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],

@@ -13,8 +13,10 @@
 //   which multiplies by the rotated stiffness rather than K0),
 // so that K_e = Krot + extra reproduces Fem3DElementCorotationalTetrahedron.cpp:199-286 and
 // f_e = -K_e (x - R x0) = -(R K0 w + T' zeta) reproduces :103-113. All quantities use positions
-// relative to node 0 (the tangent annihilates translations). The corotated strain w is always
-// formed in FP64: in FP32 it would lose |strain|/eps32 of its digits.
+// relative to node 0 (the tangent annihilates translations). The corotated strain w never comes
+// from plain FP32 differences, which would lose |strain|/eps32 of its digits: the FP64 form takes
+// it from FP64 edges, the FP32 form from Gram differences p.p - q.q formed in double-float
+// arithmetic on float-pair positions (gram_diff below).
 #pragma once
 
 #include <cfloat>

@@ -435,7 +435,11 @@ __global__ void __launch_bounds__(256) k_cg_spmv_csr(MatCsr A, const double* __r
 	for (int row = warp; row < A.rows; row += nwarps)
 	{
 		double a = 0;
-		for (int k = A.rowptr[row] + lane; k < A.rowptr[row + 1]; k += 32) a += A.val[k] * p[A.col[k]];
+		for (int k = A.rowptr[row] + lane; k < A.rowptr[row + 1]; k += 32)
+		{
+			const int c = A.col[k];
+			if ((unsigned)c < (unsigned)A.rows) a += A.val[k] * p[c];  // out-of-range columns are skipped
+		}
 		a = warp_reduce<OpSum>(a);
 		if (lane == 0)
 		{

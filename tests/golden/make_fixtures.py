@@ -8,7 +8,7 @@
   the origin (corner id = dx + 2 dy + 4 dz), split into the same 5 corotational tetrahedra as
   ``mesh.cube_grid``'s even cubes, rho 8000, nu 0.45, E 1e6, Rayleigh 1e-2 / 1e-3, nodes 0 and 1 fixed.
 
-Usage: python tests/golden/make_fixtures.py /root/reference
+Usage: python tests/golden/make_fixtures.py <path of the OpenSurgSim source tree>
 """
 
 import json
@@ -66,4 +66,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <path of the OpenSurgSim source tree>")
+    main(sys.argv[1])

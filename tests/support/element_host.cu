@@ -152,3 +152,9 @@ extern "C" int gbfem_host_adjoint_element(const double* x0, const double* x, con
 	gbfem::adj::adjoint_element(ndv, X, R0, Vel, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
 	return 0;
 }
+
+// d(lambda V)/d nu and d(mu V)/d nu as the adjoint kernel forms them from the stored moduli.
+extern "C" void gbfem_host_poisson_partials(double lamV, double muV, double* dLam, double* dMu)
+{
+	gbfem::adj::poisson_partials(lamV, muV, dLam, dMu);
+}

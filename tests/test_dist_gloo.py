@@ -93,3 +93,33 @@ def test_two_ranks_shard_the_batch_without_overlap():
     a, b = set(res[0][1]), set(res[1][1])
     assert not (a & b) and len(a | b) == 32
     assert res[0][2] == res[0][3] == res[1][2]
+
+
+def test_shard_weight_tracks_oracle_cg_iterations():
+    """The shard weight's iteration model against the oracle's CG iteration counts for one step of
+    a spread of batch meshes (stiff and soft, small and larger): within 35% on each, and the
+    weight orders the meshes' measured solve work (nodes x iterations) almost perfectly."""
+    import numpy as np
+
+    from opensurgsim_gb300 import mesh, shard
+    from oracle import oracle as O
+
+    scenes = mesh.scenes_batch(count=256)
+    order = sorted(range(len(scenes)), key=lambda i: scenes[i].mesh.num_nodes)
+    picks = order[:120:10]  # 12 meshes of 500 to ~4,000 nodes, E across the batch's range
+    est, meas, work_est, work = [], [], [], []
+    for i in picks:
+        s = scenes[i]
+        model = O.OracleModel.from_scene(s)
+        assert model.step(1e-3, 1) == 0
+        it = model.last_stats.cg_iterations
+        e = shard.expected_cg_iterations(s.mesh)
+        est.append(e)
+        meas.append(it)
+        work_est.append(shard.mesh_weight(s.mesh))
+        work.append(s.mesh.num_nodes * (it + shard.ELEMENT_ITERS))
+    est, meas = np.array(est), np.array(meas)
+    assert np.max(np.abs(est - meas) / meas) <= 0.35, list(zip(est.round(1), meas))
+    rank = lambda a: np.argsort(np.argsort(a))  # noqa: E731
+    rho = np.corrcoef(rank(np.array(work_est)), rank(np.array(work)))[0, 1]
+    assert rho >= 0.95, rho

@@ -35,6 +35,8 @@ def elem():
     L.gbfem_host_adjoint_element.argtypes = [D, D, D, ctypes.POINTER(ctypes.c_int)] + [ctypes.c_double] * 6 + \
         [D] * 7
     L.gbfem_host_adjoint_element.restype = ctypes.c_int
+    L.gbfem_host_poisson_partials.argtypes = [ctypes.c_double, ctypes.c_double, D, D]
+    L.gbfem_host_poisson_partials.restype = None
 
     def run(fp32, x0, x, v=None, E=1e6, nu=0.45, rho=1000.0, dt=1e-3, alpha=0.0, beta=0.0, nd=(0, 1, 2, 3)):
         def d(a):
@@ -61,7 +63,13 @@ def elem():
         assert r == 0
         return psi.value, gx, gv, pl.value, pm.value
 
+    def poisson_partials(lamV, muV):
+        dl, dm = ctypes.c_double(), ctypes.c_double()
+        L.gbfem_host_poisson_partials(lamV, muV, ctypes.byref(dl), ctypes.byref(dm))
+        return dl.value, dm.value
+
     run.adjoint = adjoint
+    run.poisson_partials = poisson_partials
     return run
 
 
@@ -196,3 +204,22 @@ def test_element_adjoint_velocity_and_modulus_gradients(elem, seed):
     fdE = (elem.adjoint(x0, x, v, mu, dv, E=E * np.exp(hE), nu=nu, nd=nd)[0] -
            elem.adjoint(x0, x, v, mu, dv, E=E * np.exp(-hE), nu=nu, nd=nd)[0]) / (2 * hE)
     assert abs(lamV * pl + muV * pm - fdE) <= 1e-7 * abs(fdE)
+
+
+@pytest.mark.parametrize("seed,nu", [(0, 0.45), (1, 0.30), (3, 0.49)])
+def test_element_adjoint_poisson_gradient_matches_central_differences(elem, seed, nu):
+    """d psi_e / d nu at fixed E: the element's partials in (lambda V, mu V) times the kernel's chain
+    rule (adj::poisson_partials, the code k_element_adjoint runs) against central differences of
+    psi_e in nu (nu enters K0 through lambda and mu, Fem3DElementTetrahedron.cpp:204-205)."""
+    x0, x, v, mu, dv, nd = _adjoint_case(seed)
+    E = 2.5e5
+    _, _, _, pl, pm = elem.adjoint(x0, x, v, mu, dv, E=E, nu=nu, nd=nd)
+    vol = abs(np.linalg.det(np.c_[x0[1:] - x0[0]])) / 6
+    lamV = E * nu / ((1 + nu) * (1 - 2 * nu)) * vol
+    muV = E / (2 * (1 + nu)) * vol
+    dl, dm = elem.poisson_partials(lamV, muV)
+    g = dl * pl + dm * pm
+    h = 1e-6
+    fd = (elem.adjoint(x0, x, v, mu, dv, E=E, nu=nu + h, nd=nd)[0] -
+          elem.adjoint(x0, x, v, mu, dv, E=E, nu=nu - h, nd=nd)[0]) / (2 * h)
+    assert abs(g - fd) <= 1e-6 * abs(fd), (g, fd)
