@@ -88,7 +88,10 @@ typedef struct gbfem_params
 	int32_t device;                 /* CUDA device ordinal */
 	int32_t autotune;               /* mixed form: tune block sizes and the solve schedule on the first step */
 	int32_t element_type;           /* GBFEM_ELEMENT_COROTATIONAL_TET (default), _LINEAR_TET or _HEXAHEDRON */
-	int32_t reserved[5];
+	int32_t mass_lumping;           /* FemRepresentation::setMassLumping (FemRepresentation.cpp:320-323): 1 sums
+	                                   every row of M onto its diagonal (:499-508) for the system matrix, the
+	                                   Rayleigh mass force (:584-586) and the Newton mass term; default 0 */
+	int32_t reserved[4];
 } gbfem_params;
 
 /* Per-call statistics of the last gbfem_step. */

@@ -75,7 +75,8 @@ class Params(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("autotune", ctypes.c_int32),
         ("element_type", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("mass_lumping", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 

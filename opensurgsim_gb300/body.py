@@ -21,9 +21,10 @@ class Body:
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5,
                  cg_tolerance=np.finfo(float).eps, cg_max_iterations=0, precision=_lib.PRECISION_FP64, device=0,
-                 autotune=False, element_type=_lib.ELEMENT_COROTATIONAL_TET):
+                 autotune=False, element_type=_lib.ELEMENT_COROTATIONAL_TET, mass_lumping=False):
         """`mesh` is one TetMesh, or a list of them for a batch (mixed precision only). With
-        element_type ELEMENT_HEXAHEDRON, ``mesh.tets`` holds 8 node ids per element."""
+        element_type ELEMENT_HEXAHEDRON, ``mesh.tets`` holds 8 node ids per element. mass_lumping is
+        FemRepresentation::setMassLumping (every row of M summed onto its diagonal)."""
         L = _lib.load()
         self.nodes_per_element = 8 if element_type == _lib.ELEMENT_HEXAHEDRON else 4
         meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
@@ -60,6 +61,7 @@ class Body:
         p.device = device
         p.autotune = 1 if autotune else 0
         p.element_type = element_type
+        p.mass_lumping = 1 if mass_lumping else 0
         self.params = p
         h = ctypes.c_void_p()
         if len(meshes) == 1 and not isinstance(mesh, (list, tuple)):

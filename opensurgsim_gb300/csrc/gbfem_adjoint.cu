@@ -13,7 +13,8 @@
 //   - x: forward-mode dual numbers through the same element code (9 seeded passes; FP64 for the
 //     FP64 form, FP32 for the mixed form, whose forward element math is FP32 too), which
 //     differentiates the rotation, the corotated tangent (its dR/dx terms) and the force exactly;
-//   - v: psi is linear in v, d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e;
+//   - v: psi is linear in v, d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (M0 lumped with mass
+//     lumping);
 //   - E, nu: psi_e is linear in (lambda V, mu V), so two evaluations with unit moduli give both.
 
 #include "gbfem_adjoint.cuh"
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 	double pl = 0.0, pm = 0.0;
 	for (int item = 0; item < (moduli ? adj::kAdjItems : adj::kAdjItems - 1); ++item)
 		adj::adjoint_item<S>(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
-							 gv + (size_t)e * 12, &pl, &pm);
+							 gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
 	if (!moduli) return;
 	// lambda V and mu V are both proportional to E: d/d log E scales each by one.
 	if (gLogE) gLogE[e] += lamV * pl + muV * pm;

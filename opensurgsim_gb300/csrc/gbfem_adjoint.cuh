@@ -53,8 +53,10 @@ __host__ __device__ T element_psi(const int (&nd)[4], const T* ks, const T* rhs,
 
 template <typename P>
 __host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
-						   const double (&V)[4][3], double dt, double alpha, double beta, int seedNode, int seedAxis)
+						   const double (&V)[4][3], double dt, double alpha, double beta, int seedNode, int seedAxis,
+						   bool lumped = false)
 {
+	in.lumped = lumped ? 1 : 0;
 #pragma unroll
 	for (int a = 0; a < 4; ++a)
 	{
@@ -93,7 +95,7 @@ __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const
 											 const double (&R0)[4][3], const double (&V)[4][3], const double (&MU)[12],
 											 const double (&DV)[12], const double (&g)[4][3], double lamV, double muV,
 											 double cm, double dt, double alpha, double beta, double* gx, double* gv,
-											 double* pLam, double* pMu)
+											 double* pLam, double* pMu, bool lumped = false)
 {
 	using D = ad::DualT<S>;
 	const double c2 = dt + beta;
@@ -104,16 +106,17 @@ __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const
 			for (int k = 0; k < 3; ++k) gD[a][k] = D(g[a][k]);
 		const int s = 3 + item;
 		elem::ElemInT<D> in;
-		fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3);
+		fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3, lumped);
 		D ks[kSlots * 9], rhs[12];
 		elem::compute<D, false, elem::ElemInT<D>>(in, gD, D(lamV), D(muV), D(cm), ks, 1, rhs, 1, nullptr, nullptr);
 		gx[s] = double(element_psi(nd, ks, rhs, MU, DV, c2).d);
 	}
 	else if (item == 9)
 	{
-		// d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (K_e: the full element tangent).
+		// d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (K_e: the full element tangent; M0 lumped to
+		// 5 cm on the diagonal with mass lumping).
 		elem::ElemIn in;
-		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
+		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
 		S gS[4][3], ks[kSlots * 9], rhs[12];
 		double kfull[144], fdbg[12];
 		for (int a = 0; a < 4; ++a)
@@ -126,7 +129,7 @@ __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const
 		{
 			double t = 0.0;
 			for (int r = 0; r < 12; ++r) t += kfull[r * 12 + c] * MU[r];
-			gv[c] = -c2 * t - alpha * cm * (MU[c] + sm[c % 3]);
+			gv[c] = -c2 * t - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
 		}
 	}
 	else
@@ -161,10 +164,10 @@ __host__ __device__ inline void adjoint_element(const int (&nd)[4], const double
 												const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],
 												const double (&g)[4][3], double lamV, double muV, double cm, double dt,
 												double alpha, double beta, double* gx, double* gv, double* pLam,
-												double* pMu)
+												double* pMu, bool lumped = false)
 {
 	for (int item = 0; item < kAdjItems; ++item)
-		adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
+		adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu, lumped);
 	for (int k = 0; k < 3; ++k) gx[k] = -(gx[3 + k] + gx[6 + k] + gx[9 + k]);
 }
 

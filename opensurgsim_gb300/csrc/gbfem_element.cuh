@@ -273,6 +273,7 @@ struct ElemInT
 	P uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
 	P vv[4][3];   // v_n (debug force only)
 	double alphaDbg, betaDbg;  // Rayleigh coefficients (debug force only)
+	int lumped = 0;  // FemRepresentation::setMassLumping: the element's mass rows summed onto the diagonal
 };
 using ElemIn = ElemInT<double>;
 
@@ -307,6 +308,7 @@ __device__ __forceinline__ void gather(const DevBody& b, int e, const double* __
 		}
 	in.alphaDbg = alpha;
 	in.betaDbg = beta;
+	in.lumped = b.lumped;
 }
 
 // Inputs of the FP32 element kernel. FP64 issues at 1/64 of the FP32 rate here, so the corotational
@@ -331,6 +333,7 @@ struct ElemInF
 	float uM[4][3];   // -alpha v_n - (v_n - v_t) / dt
 	float vv[4][3];   // v_n (debug force only; unused by the FP32 kernel)
 	double alphaDbg, betaDbg;
+	int lumped = 0;   // mass lumping (as ElemInT::lumped)
 };
 
 // kLinear: p and q in FP64 from the positions and rest positions (u = x - x0 is formed from them).
@@ -430,6 +433,7 @@ __device__ __forceinline__ void gather_f32(const DevBody& b, int e, const double
 	}
 	in.alphaDbg = 0.0;
 	in.betaDbg = 0.0;
+	in.lumped = b.lumped;
 }
 
 // Rest Gram entry q_a . q_c (a <= c, both in 1..3) and rest edge components for the FP32 strain:
@@ -766,12 +770,13 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			for (int j = 0; j < 3; ++j)
 				Tp[3 * i + j] = extra ? (Tm[3 * i] * Gi[j] + Tm[3 * i + 1] * Gi[3 + j] + Tm[3 * i + 2] * Gi[6 + j]) : T(0);
 
-		// rhs_a = R K0(u~)_a + T'_a zt + cm (uM_a + sum uM)
+		// rhs_a = R K0(u~)_a + T'_a zt + (M0 uM)_a, M0 uM = cm (uM_a + sum uM); with mass lumping
+		// (FemRepresentation.cpp:499-508) each row of M0 is summed onto its diagonal, 5 cm = rho V / 4.
 #pragma unroll
 		for (int i = 0; i < 3; ++i)
 			rhs[(3 * a + i) * rhsStride] = R[3 * i] * Ku[a][0] + R[3 * i + 1] * Ku[a][1] + R[3 * i + 2] * Ku[a][2] +
 										   Tp[3 * i] * zt[0] + Tp[3 * i + 1] * zt[1] + Tp[3 * i + 2] * zt[2] +
-										   cm * (T(in.uM[a][i]) + sumM[i]);
+										   (in.lumped ? cm * T(5) * T(in.uM[a][i]) : cm * (T(in.uM[a][i]) + sumM[i]));
 
 		T kv[3] = {0, 0, 0};
 #pragma unroll
@@ -815,7 +820,8 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			{
 				const T fe = -(R[3 * i] * KW[a][0] + R[3 * i + 1] * KW[a][1] + R[3 * i + 2] * KW[a][2] +
 							   Tp[3 * i] * zeta[0] + Tp[3 * i + 1] * zeta[1] + Tp[3 * i + 2] * zeta[2]);
-				fdbg[3 * a + i] = double(fe) - in.alphaDbg * double(cm * (T(in.vv[a][i]) + sumV[i])) - in.betaDbg * double(kv[i]);
+				const T mv = in.lumped ? cm * T(5) * T(in.vv[a][i]) : cm * (T(in.vv[a][i]) + sumV[i]);
+				fdbg[3 * a + i] = double(fe) - in.alphaDbg * double(mv) - in.betaDbg * double(kv[i]);
 			}
 		}
 	}

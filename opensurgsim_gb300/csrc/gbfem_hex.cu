@@ -166,6 +166,40 @@ __global__ void k_assemble_k(DevBody b, const double* __restrict__ slots, const 
 	}
 }
 
+// Mass lumping (FemRepresentation::computeFMDK, FemRepresentation.cpp:499-508: every row of M summed
+// onto its diagonal, the rest of the row zeroed, the pattern kept). Pass 1, one thread per SELL row:
+// the row's scalar block masses summed (padding slots hold zero) into rowsum[I], every slot of the
+// row zeroed. Pass 2, one thread per lower block: the diagonal block gets the row sum back, and the
+// lower-block masses S is formed from become the row sums on the diagonal and zero elsewhere.
+__global__ void k_hex_lump_rows(MatSell3 K, double* __restrict__ Ms, double* __restrict__ rowsum)
+{
+	const int rs = blockIdx.x * blockDim.x + threadIdx.x;
+	if (rs >= K.rows) return;
+	const int I = K.perm[rs];
+	if (I < 0) return;
+	const int c = rs >> 5, lane = rs & 31;
+	double m = 0.0;
+	for (int k = K.off[c]; k < K.off[c + 1]; ++k) m += Ms[k * 32 + lane];
+	for (int k = K.off[c]; k < K.off[c + 1]; ++k) Ms[k * 32 + lane] = 0.0;
+	rowsum[I] = m;
+}
+
+__global__ void k_hex_lump_lower(DevBody b, const double* __restrict__ rowsum, double* __restrict__ Ms,
+								 double* __restrict__ lmass)
+{
+	const int L = blockIdx.x * blockDim.x + threadIdx.x;
+	if (L >= b.nl) return;
+	const int4 lb = b.lblk[L];
+	if (lb.x != lb.y)
+	{
+		lmass[L] = 0.0;
+		return;
+	}
+	const double m = rowsum[lb.x];
+	lmass[L] = m;
+	Ms[(size_t)(lb.z / 288) * 32 + lb.z % 288] = m;
+}
+
 // S = c1 M + c2 K from the stored K (its lower block) with the boundary conditions, as k_assemble.
 template <typename T>
 __global__ void k_system_from_k(DevBody b, const double* __restrict__ K, double c1, double c2, T* __restrict__ A,
@@ -411,6 +445,14 @@ void launch_assemble_k(const DevBody& b, const double* slots, const double* smas
 {
 	if (b.nl == 0) return;
 	k_assemble_k<<<blocks_for(b.nl, 128), 128, 0, s>>>(b, slots, smass, K, Ms, lmass);
+}
+
+void launch_hex_lump_masses(const DevBody& b, const MatSell3& K, double* Ms, double* lmass, double* rowsum,
+							cudaStream_t s)
+{
+	if (b.nl == 0 || K.rows == 0) return;
+	k_hex_lump_rows<<<blocks_for(K.rows, 256), 256, 0, s>>>(K, Ms, rowsum);
+	k_hex_lump_lower<<<blocks_for(b.nl, 128), 128, 0, s>>>(b, rowsum, Ms, lmass);
 }
 
 void launch_system_from_k(const DevBody& b, const double* K, double c1, double c2, double* A, double* invdiag,

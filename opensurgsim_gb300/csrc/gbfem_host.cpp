@@ -260,6 +260,7 @@ struct gbfem_handle_s
 		b.nodeV = d_nodeV.p;
 		b.nodeDx = d_nodeDx.p;
 		b.nodeDv = d_nodeDv.p;
+		b.lumped = prm.mass_lumping ? 1 : 0;
 		return b;
 	}
 
@@ -405,11 +406,12 @@ gbfem_status rebuild_hex_operators(gbfem_handle h)
 	cudaStream_t s = h->stream;
 	struct Scratch
 	{
-		DevBuf<double> slots, smass;
+		DevBuf<double> slots, smass, rowsum;
 		~Scratch()
 		{
 			slots.free();
 			smass.free();
+			rowsum.free();
 		}
 	} t;
 	GB_CUDA(h, t.slots.alloc((size_t)h->E * kHexSlots * 9));
@@ -417,6 +419,12 @@ gbfem_status rebuild_hex_operators(gbfem_handle h)
 	launch_hex_element(h->E, h->d_enodes.p, h->d_xrest.p, h->d_young.p, h->d_poisson.p, h->d_rho.p, t.slots.p,
 					   t.smass.p, s);
 	launch_assemble_k(h->body(), t.slots.p, t.smass.p, h->d_K.p, h->d_Ms.p, h->d_lmass.p, s);
+	if (h->prm.mass_lumping)
+	{
+		GB_CUDA(h, t.rowsum.alloc((size_t)h->N));
+		const MatSell3 K{h->nrows, h->d_perm.p, h->d_off.p, h->d_sellcol.p, h->d_K.p};
+		launch_hex_lump_masses(h->body(), K, h->d_Ms.p, h->d_lmass.p, t.rowsum.p, s);
+	}
 	if (h->mixed())
 	{
 		const size_t slots = (size_t)h->sellSlots;
@@ -622,7 +630,11 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 			{
 				int L = slotLower[(size_t)e * spe + s];
 				cidx[fill[L]++] = e * spe + s;
-				if (!h->hex()) lmass[L] += h->cmass[e] * (s < 4 ? 2.0 : 1.0);
+				// Consistent mass rho V / 20 ([2 on the diagonal, 1 off] x I3); with mass lumping each row
+				// summed onto the diagonal block: 5 cm = rho V / 4, off-diagonal blocks 0.
+				if (!h->hex())
+					lmass[L] += h->prm.mass_lumping ? (s < 4 ? 5.0 * h->cmass[e] : 0.0)
+													: h->cmass[e] * (s < 4 ? 2.0 : 1.0);
 			}
 	}
 	// Node incidences and lumped node masses getMass / numNodes (FemRepresentation.cpp:102-117).
@@ -828,7 +840,8 @@ gbfem_status ensure_system_maps(gbfem_handle h)
 			int k = slot[(size_t)e * 144 + l];
 			sidx[fill[k]++] = e * 144 + l;
 			int a = l / 36, i = (l / 12) % 3, b = (l % 12) / 3, j = l % 3;
-			if (i == j) smass[k] += h->cmass[e] * (a == b ? 2.0 : 1.0);
+			if (i == j)
+				smass[k] += h->prm.mass_lumping ? (a == b ? 5.0 * h->cmass[e] : 0.0) : h->cmass[e] * (a == b ? 2.0 : 1.0);
 		}
 	for (int J = 0; J < h->N; ++J)
 		for (int j = 0; j < 3; ++j)
@@ -1630,7 +1643,8 @@ gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbf
 	*out = nullptr;
 	if (!meshes || !prm || count <= 0) return fail(nullptr, GBFEM_INVALID_ARG, "mesh or params is NULL");
 	if (!(prm->newton_max_iterations >= 1) || !(prm->newton_epsilon >= 0.0) || !(prm->cg_tolerance >= 0.0) ||
-		prm->precision < 0 || prm->precision > 1 || prm->element_type < 0 || prm->element_type > 2)
+		prm->precision < 0 || prm->precision > 1 || prm->element_type < 0 || prm->element_type > 2 ||
+		prm->mass_lumping < 0 || prm->mass_lumping > 1)
 		return fail(nullptr, GBFEM_INVALID_ARG, "invalid solver parameters");
 	for (int32_t k = 0; k < count; ++k)
 	{

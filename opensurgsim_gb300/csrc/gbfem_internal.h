@@ -45,6 +45,7 @@ struct DevBody
 	float* nodeV = nullptr;
 	float* nodeDx = nullptr;
 	float* nodeDv = nullptr;
+	int lumped = 0;                 // mass lumping (FemRepresentation::setMassLumping)
 };
 
 // Device control block of one FP64 CG solve; all scalars live on the device.
@@ -174,6 +175,10 @@ void launch_hex_element(int E, const int* nodes, const double* xrest, const doub
 						const double* rho, double* slots, double* smass, cudaStream_t s);
 void launch_assemble_k(const DevBody& b, const double* slots, const double* smass, double* K, double* Ms,
 					   double* lmass, cudaStream_t s);
+// Mass lumping of the stored scalar block masses (Ms, both triangles) and the lower-block masses:
+// row sums onto the diagonal, zero elsewhere; rowsum: N doubles of scratch.
+void launch_hex_lump_masses(const DevBody& b, const MatSell3& K, double* Ms, double* lmass, double* rowsum,
+							cudaStream_t s);
 void launch_system_from_k(const DevBody& b, const double* K, double c1, double c2, double* A, double* invdiag,
 						  cudaStream_t s);
 void launch_system_from_k(const DevBody& b, const double* K, double c1, double c2, float* A, float* invdiag,

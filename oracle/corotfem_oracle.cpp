@@ -942,6 +942,7 @@ struct FemModel : Equation
 	vector<double> massPerNode;
 	vector<int> scatter;  // per element (3 npe)^2: CSC slot of element entry (3a+i, 3b+j)
 	double alpha = 0, beta = 0;          // Rayleigh mass / stiffness coefficients
+	bool massLumping = false;            // FemRepresentation::setMassLumping (FemRepresentation.cpp:320-323)
 	double gravity[3] = {0.0, -9.81, 0.0};  // Representation.cpp:36
 	bool gravityEnabled = true;
 	// state (current) and scratch
@@ -1108,6 +1109,16 @@ struct FemModel : Equation
 				for (int c = 0; c < Dm; ++c) K[s[r * Dm + c]] += Ke[r * Dm + c];
 		}
 		const int64_t nnz = pat.nnz();
+		if (massLumping)
+		{
+			// :499-508: for every row, sum = M.row(i).sum() (Eigen walks a column-major row in column
+			// order); zeroRow(i) keeps the pattern; M(i, i) = sum.
+			vector<double> rowSum(n, 0.0);
+			for (int c = 0; c < n; ++c)
+				for (int k = pat.colptr[c]; k < pat.colptr[c + 1]; ++k) rowSum[pat.rowidx[k]] += M[k];
+			for (int c = 0; c < n; ++c)
+				for (int k = pat.colptr[c]; k < pat.colptr[c + 1]; ++k) M[k] = (pat.rowidx[k] == c) ? rowSum[c] : 0.0;
+		}
 		if (alpha != 0.0)
 			for (int64_t k = 0; k < nnz; ++k) D[k] = D[k] + M[k] * alpha;  // :511-514
 		if (beta != 0.0)
@@ -1119,7 +1130,18 @@ struct FemModel : Equation
 		vector<double> tmp(n);
 		if (alpha != 0.0)
 		{
-			spmv(pat, M.data(), V, tmp.data());
+			if (massLumping)  // :584-586: the diagonal of M times v
+			{
+				for (int c = 0; c < n; ++c)
+				{
+					double d = 0.0;
+					for (int k = pat.colptr[c]; k < pat.colptr[c + 1]; ++k)
+						if (pat.rowidx[k] == c) d = M[k];
+					tmp[c] = d * V[c];
+				}
+			}
+			else
+				spmv(pat, M.data(), V, tmp.data());
 			for (int i = 0; i < n; ++i) f[i] -= (1.0 * alpha) * tmp[i];
 		}
 		if (beta != 0.0)
@@ -1285,6 +1307,7 @@ struct orc_params
 	double cg_tolerance;
 	int32_t cg_max_iterations;  // <= 0: Eigen default 2n
 	int32_t element_type;       // 0: corotational tetrahedron, 1: linear tetrahedron, 2: hexahedron
+	int32_t mass_lumping;       // FemRepresentation::setMassLumping
 };
 
 struct orc_stats
@@ -1357,6 +1380,7 @@ void* orc_create(int32_t numNodes, const double* x, int32_t numTets, const int32
 	}
 	m->alpha = prm->rayleigh_mass;
 	m->beta = prm->rayleigh_stiffness;
+	m->massLumping = prm->mass_lumping != 0;
 	for (int k = 0; k < 3; ++k) m->gravity[k] = prm->gravity[k];
 	m->gravityEnabled = prm->gravity_enabled != 0;
 	m->solver.prm.newtonMaxIter = std::max(1, (int)prm->newton_max_iterations);

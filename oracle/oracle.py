@@ -30,7 +30,8 @@ class OrcParams(ctypes.Structure):
         ("newton_epsilon", ctypes.c_double),
         ("cg_tolerance", ctypes.c_double),
         ("cg_max_iterations", ctypes.c_int32),
-        ("element_type", ctypes.c_int32),   # 0 corotational tetrahedron, 1 linear tetrahedron
+        ("element_type", ctypes.c_int32),   # 0 corotational tetrahedron, 1 linear tetrahedron, 2 hexahedron
+        ("mass_lumping", ctypes.c_int32),   # FemRepresentation::setMassLumping
     ]
 
 
@@ -124,7 +125,7 @@ class OracleModel:
 
     def __init__(self, mesh, rayleigh_mass=0.0, rayleigh_stiffness=0.0, gravity=(0.0, -9.81, 0.0),
                  gravity_enabled=True, newton_max_iterations=1, newton_epsilon=1e-5, cg_tolerance=1e-10,
-                 cg_max_iterations=0, element_type=0):
+                 cg_max_iterations=0, element_type=0, mass_lumping=False):
         L = lib()
         self._nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64).ravel()
         self._tets = np.ascontiguousarray(mesh.tets, dtype=np.int32).ravel()
@@ -142,6 +143,7 @@ class OracleModel:
         p.cg_tolerance = cg_tolerance
         p.cg_max_iterations = cg_max_iterations
         p.element_type = element_type
+        p.mass_lumping = 1 if mass_lumping else 0
         st = ctypes.c_int32(0)
         self.num_nodes = mesh.nodes.shape[0]
         self.num_tets = mesh.tets.shape[0]

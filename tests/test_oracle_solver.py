@@ -274,3 +274,45 @@ def test_fmdk_gravity_damping_and_external_force(gravity, damping):
     m2.set_state(*m.state())
     assert m.step(1e-3) == 0 and m2.step(1e-3) == 0
     assert np.array_equal(m.state()[0], m2.state()[0])
+
+
+@pytest.mark.parametrize("element_type", [0, 2])
+def test_mass_lumping(element_type):
+    """FemRepresentationTests.cpp:529-572 (MassLumpingTest: after an update with mass lumping on, M
+    is diagonal), plus what FemRepresentation.cpp:499-508 and :584-586 imply: every row of the
+    lumped M holds the consistent M's row sum on its diagonal (the pattern kept, explicit zeros
+    elsewhere); D = alpha M_lumped + beta K; the Rayleigh mass force is alpha diag(M) v; for
+    tetrahedra the lumped diagonal is the node's rho V / 4 sum (massPerNode)."""
+    import scipy.sparse as sp
+
+    if element_type == 2:
+        s = mesh.scene_hex_cube(2, 3, 2, jitter=0.1, seed=4)
+    else:
+        s = mesh.scene_cube(2, 2, 3, seed=3)
+    a, b = 0.02, 0.003
+    kw = dict(rayleigh_mass=a, rayleigh_stiffness=b, gravity_enabled=False, cg_tolerance=1e-14,
+              element_type=element_type)
+    cons = O.OracleModel(s.mesh, **kw)
+    lump = O.OracleModel(s.mesh, mass_lumping=True, **kw)
+    rng = np.random.default_rng(5)
+    x = s.mesh.nodes.ravel() + rng.normal(0, 1e-4, 3 * s.mesh.num_nodes)
+    v = rng.normal(0, 0.05, x.size)
+    for mod in (cons, lump):
+        mod.set_state(x, v)
+        assert mod.step(1e-3) == 0
+    colptr, rowidx = lump.pattern()
+    n = lump.n
+    sc, sl = cons.system(), lump.system()
+    Mc = sp.csc_matrix((sc["M"], rowidx, colptr), shape=(n, n))
+    Ml = sp.csc_matrix((sl["M"], rowidx, colptr), shape=(n, n))
+    dense = Ml.toarray()
+    assert np.count_nonzero(dense - np.diag(np.diag(dense))) == 0  # isDiagonal()
+    assert np.allclose(np.diag(dense), np.asarray(Mc.sum(axis=1)).ravel(), rtol=1e-14, atol=0)
+    assert Ml.nnz == Mc.nnz  # zeroRow keeps the pattern
+    if element_type == 0:
+        assert np.allclose(np.diag(dense), np.repeat(lump.mass_per_node(), 3), rtol=1e-13)
+    assert np.allclose(sl["K"], sc["K"], rtol=0, atol=0)
+    assert np.allclose(sl["D"], a * sl["M"] + b * sl["K"], rtol=1e-14, atol=1e-14 * np.abs(sl["K"]).max())
+    # f differs from the consistent model only in the Rayleigh mass force.
+    want = sc["f"] + a * (Mc @ v) - a * np.diag(dense) * v
+    assert np.allclose(sl["f"], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
