@@ -202,6 +202,14 @@ GBFEM_API gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, con
 GBFEM_API gbfem_status gbfem_add_external_force(gbfem_handle h, int32_t element, const double* coord, const double* force,
 												const double* stiffness, const double* damping);
 
+/* Solver settings after creation: OdeSolverEulerImplicit::setNewtonRaphsonMaximumIteration /
+ * setNewtonRaphsonEpsilonConvergence (OdeSolverEulerImplicit.cpp:31-53) and
+ * LinearSparseSolveAndInverseCG::setTolerance / setMaxIterations (LinearSparseSolveAndInverse.cpp:99-117),
+ * which the reference allows at any time; they take effect at the next step (a captured step graph
+ * is captured again). newton_max_iterations >= 1; cg_max_iterations <= 0 selects the default cap. */
+GBFEM_API gbfem_status gbfem_set_solver_params(gbfem_handle h, int32_t newton_max_iterations, double newton_epsilon,
+											   double cg_tolerance, int32_t cg_max_iterations);
+
 /* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
  * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
  * CTAs per SM and refresh weights 1 to 4 on its own system, and keeps the fastest. The solve's

@@ -1850,6 +1850,23 @@ gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t c
 	return GBFEM_OK;
 }
 
+gbfem_status gbfem_set_solver_params(gbfem_handle h, int32_t newton_max_iterations, double newton_epsilon,
+									 double cg_tolerance, int32_t cg_max_iterations)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (newton_max_iterations < 1 || !(newton_epsilon >= 0.0) || !(cg_tolerance >= 0.0))
+		return fail(h, GBFEM_INVALID_ARG, "gbfem_set_solver_params: newton_max_iterations >= 1, epsilon and tolerance >= 0");
+	const bool changed = h->prm.newton_max_iterations != newton_max_iterations ||
+						 h->prm.newton_epsilon != newton_epsilon || h->prm.cg_tolerance != cg_tolerance ||
+						 h->prm.cg_max_iterations != cg_max_iterations;
+	h->prm.newton_max_iterations = newton_max_iterations;
+	h->prm.newton_epsilon = newton_epsilon;
+	h->prm.cg_tolerance = cg_tolerance;
+	h->prm.cg_max_iterations = cg_max_iterations;
+	if (changed) h->tuneVersion++;  // a captured step graph holds the old tolerance and cap: capture again
+	return GBFEM_OK;
+}
+
 gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, const double* poisson)
 {
 	if (!h || !young) return GBFEM_INVALID_ARG;

@@ -43,15 +43,19 @@ def _pair(precision, element_type=0, tol=1e-12, lumping=True, **over):
 @pytest.mark.parametrize("element_type", [0, 1, 2])
 @pytest.mark.parametrize("newton", [1, 2])
 def test_lumped_steps_match_oracle(gpu_lib, precision, gate, element_type, newton):
+    """Displacements within the form's gate (FP64 1e-8, mixed 1e-6); velocities within 1e-8 (FP64)
+    and 1e-5 (mixed: each step's velocity increment carries the FP32 tangent's ~1e-7 relative error
+    directly, where the displacement integrates it)."""
     s, b, o = _pair(precision, element_type, newton_max_iterations=newton, newton_epsilon=1e-12)
     rest = s.mesh.nodes.ravel()
+    vgate = gate if precision == _lib.PRECISION_FP64 else 1e-5
     for _ in range(3):
         assert b.step(1e-3, 10) == _lib.GBFEM_OK
         assert o.step(1e-3, 10) == 0
         gx, gv = b.state()
         ox, ov = o.state()
         assert rel(gx - rest, ox - rest) <= gate
-        assert rel(gv, ov) <= gate
+        assert rel(gv, ov) <= vgate
 
 
 def test_lumping_changes_the_step(gpu_lib):
