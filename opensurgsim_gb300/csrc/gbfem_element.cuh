@@ -143,9 +143,10 @@ __host__ __device__ bool polar_newton(const T* F, T* R)
 }
 
 // SVD-based polar factor for any F (one-sided Jacobi, bounded sweeps): proper rotation with the
-// reflection placed on the smallest singular value, R = U diag(1,1,det(U V^T)) V^T.
+// reflection placed on the smallest singular value, R = U diag(1,1,det(U V^T)) V^T. sig (optional)
+// receives the eigenvalues of S = R^T F, the singular values with that sign on the smallest.
 template <typename T>
-__host__ __device__ void polar_svd(const T* F, T* R)
+__host__ __device__ void polar_svd(const T* F, T* R, T* sig = nullptr)
 {
 	T A[9], V[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
 #pragma unroll
@@ -231,6 +232,12 @@ __host__ __device__ void polar_svd(const T* F, T* R)
 	}
 	const T x = (det3(U) * det3(Vs) < T(0)) ? T(-1) : T(1);
 	for (int k = 0; k < 3; ++k) U[3 * k + 2] *= x;
+	if (sig)
+	{
+		sig[0] = sv[o[0]];
+		sig[1] = sv[o[1]];
+		sig[2] = x * sv[o[2]];
+	}
 	for (int i = 0; i < 3; ++i)
 		for (int j = 0; j < 3; ++j)
 			R[3 * i + j] = U[3 * i] * Vs[3 * j] + U[3 * i + 1] * Vs[3 * j + 1] + U[3 * i + 2] * Vs[3 * j + 2];
@@ -512,7 +519,8 @@ __host__ __device__ __forceinline__ float rest_edge(const ElemInF& in, int a, in
 // ks may be null (right-hand side only). kLinear: the linear tetrahedron of
 // Fem3DElementTetrahedron::doUpdateFMDK (Fem3DElementTetrahedron.cpp:77-90): R = I, K_e = K0,
 // f_e = -K0 (x - x0), no rotation terms.
-// Returns a bitmask: 1 = polar fallback to the FP64 SVD, 2 = singular G (extra terms skipped).
+// Returns a bitmask: 1 = polar fallback to the FP64 SVD, 2 = singular G (extra terms skipped);
+// 4 is internal (the FP32 form's FP64 singular-G decision on the SVD path).
 template <typename T, bool kDebug, typename In = ElemIn, bool kLinear = false>
 __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV, T cm, T* ks, int ksStride, T* rhs,
 					   int rhsStride, double* kfull, double* fdbg)
@@ -538,7 +546,7 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 		// always at least FP64.
 		if constexpr (std::is_same<T, float>::value)
 		{
-			double Fd[9], Rd[9];
+			double Fd[9], Rd[9], sg[3];
 #pragma unroll
 			for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -546,9 +554,14 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 					Fd[3 * i + j] = edge<double, kLinear>(in, 1, i) * double(g[1][j]) +
 									edge<double, kLinear>(in, 2, i) * double(g[2][j]) +
 									edge<double, kLinear>(in, 3, i) * double(g[3][j]);
-			polar_svd(Fd, Rd);
+			polar_svd(Fd, Rd, sg);
 #pragma unroll
 			for (int k = 0; k < 9; ++k) R[k] = T(Rd[k]);
+			// The reference's singular-G test is absolute (|det G| <= 1e-12, :210), below what the
+			// FP32 G resolves (its entries carry ~1e-7 of rounding). On this path it is decided in
+			// FP64: det G = det(tr(S) I - S) (det R = 1) = (s2 + s3)(s1 + s3)(s1 + s2) over the
+			// eigenvalues s of S = R^T F.
+			if (!(fabs((sg[1] + sg[2]) * (sg[0] + sg[2]) * (sg[0] + sg[1])) > 1e-12)) flags |= 4;
 		}
 		else
 			polar_svd(F, R);
@@ -587,7 +600,7 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 		const T d = Gm[0] * C[0] + Gm[1] * C[1] + Gm[2] * C[2];
 		// (An FP32 form of this test moved the FP32 element kernel from 168 to 190 registers, one
 		// block per SM fewer; the conversion costs less than that.)
-		extra = fabs(double(d)) > 1e-12;
+		extra = (std::is_same<T, float>::value && (flags & 1)) ? !(flags & 4) : fabs(double(d)) > 1e-12;
 		const T id = T(1) / d;
 #pragma unroll
 		for (int i = 0; i < 3; ++i)

@@ -72,9 +72,10 @@ __global__ void k_node_prep(int n, const double* __restrict__ xn, const double* 
 
 // FP32 element kernel of the mixed form, kT elements per block (a tuning choice). Results are
 // staged in shared memory and written out with coalesced stores (element-major, the layout the
-// assembly gathers).
+// assembly gathers). Launch bounds hold it at 384 threads (6 blocks of 64) per SM: 168 registers,
+// which the FP64 singular-G decision of the rare SVD path would otherwise raise to ~188.
 template <int kT, bool kLinear>
-__global__ void __launch_bounds__(kT) k_element_f32(DevBody b, const double* __restrict__ xn,
+__global__ void __launch_bounds__(kT, 384 / kT) k_element_f32(DevBody b, const double* __restrict__ xn,
 															   const double* __restrict__ vn,
 															   const double* __restrict__ xt,
 															   const double* __restrict__ vt, float c2, float alpha,

@@ -96,7 +96,7 @@ def test_facade_steps_c1_for_100_steps_like_the_oracle(facade_exe, tmp_path):
     assert np.max(np.abs(r["S"] - S)) <= 1e-12 * np.max(np.abs(S))
     n = scene.mesh.num_dofs
     b = np.stack([1.0 + 0.001 * np.arange(n), np.where(np.arange(n) % 3 == 2, -1.0, 0.5)], axis=1)
-    want, _ = o.apply_compliance(b)
+    want, _, _ = o.apply_compliance(b)
     assert rel(r["applied"], want) <= 1e-8
 
 
@@ -111,7 +111,7 @@ def test_facade_compliance_matrix_on_a_small_body(facade_exe, tmp_path):
     o = O.OracleModel.from_scene(scene)
     assert o.step(scene.dt, 6) == 0
     n = scene.mesh.num_dofs
-    want, _ = o.apply_compliance(np.eye(n))
+    want, _, _ = o.apply_compliance(np.eye(n))
     assert rel(r["C"], want) <= 1e-8
     bc = scene.mesh.bc_dofs
     assert np.all(r["C"][bc, :] == 0.0) and np.all(r["C"][:, bc] == 0.0)
