@@ -43,6 +43,7 @@ HEX_UNIT = "hex-element-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 CG_CAP = 10000
+BAR_SCENARIO_STEPS = 200  # --config bar --steps 200: the whole compression scenario, both forms
 BATCH = dict(count=256, lo=500, hi=50000, seed=3)
 BATCH_PARAMS = dict(rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0.0, 0.0, -9.81), cg_tolerance=1e-10)
 COMPARE_STEPS = 4  # steps of the FP64-path comparison (1 untimed + 3 timed) and of the error check
@@ -585,6 +586,157 @@ def run_single(args, rank, world, local, dist):
     return line, scene
 
 
+def run_bar_full(args, rank, world, local, dist):
+    """The 40x40x160 compression bar over its whole scenario (50 ramp steps, then hold; 200 steps),
+    plain FP64 and mixed forms side by side on the same GPU. After every step the mixed form's
+    displacement is compared with the FP64 form's on the device; both forms are timed per step with
+    CUDA events on their own streams. W warm-up steps run first (the mixed form autotunes), then both
+    bodies are put back at rest and the timed run starts at step 0 of the scenario."""
+    import numpy as np
+    import torch
+
+    from opensurgsim_gb300 import _lib, build
+    from opensurgsim_gb300.autograd import state_views
+    from opensurgsim_gb300.body import Body
+
+    build.build()
+    torch.cuda.set_device(local)
+    scene = build_scene("bar")
+    m = scene.mesh
+    log(f"bar full run: {m.num_tets} tets, {m.num_nodes} nodes, {args.steps} steps, both forms")
+    bodies = {"fp64": Body.from_scene(scene, precision=_lib.PRECISION_FP64, device=local),
+              "mixed": Body.from_scene(scene, precision=_lib.PRECISION_MIXED, device=local, autotune=True)}
+    flags = {"fp64": 0, "mixed": _lib.STEP_GRAPH}
+    L = _lib.load()
+    d_dofs = torch.from_numpy(scene.driven_dofs.astype(np.int32)).cuda(local)
+    ramp = torch.from_numpy(scene.driven_values(0)).cuda(local)
+    hold = torch.zeros_like(ramp)
+    rest = torch.from_numpy(m.nodes.ravel().copy()).cuda(local)
+    views = {k: state_views(b) for k, b in bodies.items()}
+    streams = {k: torch.cuda.ExternalStream(b.stream(), device=local) for k, b in bodies.items()}
+
+    def drive(b, step):
+        vals = ramp if step < scene.ramp_steps else hold
+        L.gbfem_set_velocities_device(b.handle, d_dofs.numel(), d_dofs.data_ptr(), vals.data_ptr())
+
+    for k, b in bodies.items():
+        for s in range(args.warmup):
+            drive(b, s)
+            b.step(scene.dt, 1, flags[k])
+    torch.cuda.synchronize(local)
+    for k, b in bodies.items():  # back to rest: the timed run is the scenario from its first step
+        x, v = views[k]
+        x.copy_(rest)
+        v.zero_()
+    torch.cuda.synchronize(local)
+    tuning = bodies["mixed"].tuning()
+    dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    evs = {k: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)] for k in bodies}
+    agg = {k: dict(cg_iterations=0, kernel_launches=0, polar_fallbacks=0, singular_g=0, ms_spmv=0.0,
+                   refinement_sweeps=0) for k in bodies}
+    statuses = {k: set() for k in bodies}
+    errs = []
+    u64n = []
+    for s in range(args.steps):
+        for k, b in bodies.items():
+            drive(b, s)
+            e0, e1 = evs[k][s]
+            e0.record(streams[k])
+            timing = _lib.STEP_TIME_KERNELS if k == "mixed" else 0  # the persistent solve's own events
+            statuses[k].add(int(b.step(scene.dt, 1, flags[k] | timing)))
+            e1.record(streams[k])
+            st = b.stats()
+            for key in agg[k]:
+                agg[k][key] += st[key]
+        # Relative displacement error of the mixed form against the FP64 form, on the device.
+        u64 = views["fp64"][0] - rest
+        d = views["mixed"][0] - views["fp64"][0]
+        n64 = float(torch.linalg.vector_norm(u64))
+        errs.append(float(torch.linalg.vector_norm(d)) / max(n64, 1e-300))
+        u64n.append(n64)
+    torch.cuda.synchronize(local)
+    clocks = sampler.stop()
+    dist.barrier()
+    ms = {k: sum(e0.elapsed_time(e1) for e0, e1 in evs[k]) for k in bodies}
+    units = m.num_tets * args.steps
+    val = {k: dist.reduce(units, "sum") / (dist.reduce(ms[k], "max") / 1e3) for k in bodies}
+    log(f"fp64 {val['fp64'] / 1e6:.1f} M, mixed {val['mixed'] / 1e6:.1f} M tet-steps/s; max err {max(errs):.2e}")
+
+    # End to end (mixed, public API, host buffers) over 10 further hold steps: prescribed velocities
+    # in from pinned host memory, x and v read back every step.
+    bm = bodies["mixed"]
+    h_dofs = scene.driven_dofs.astype(np.int32)
+    h_vals = torch.zeros(h_dofs.size, dtype=torch.float64).pin_memory().numpy()
+    h_x = torch.empty(bm.n, dtype=torch.float64).pin_memory().numpy()
+    h_v = torch.empty(bm.n, dtype=torch.float64).pin_memory().numpy()
+    e2e_steps = 10
+    torch.cuda.synchronize(local)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        bm.set_velocities(h_dofs, h_vals)
+        bm.step(scene.dt, 1, _lib.STEP_GRAPH)
+        L.gbfem_get_state(bm.handle, _lib.dptr(h_x), _lib.dptr(h_v))
+    torch.cuda.synchronize(local)
+    e2e_value = m.num_tets * e2e_steps / (time.perf_counter() - t0)
+
+    peak, peak_kind = load_peak()
+    am = agg["mixed"]
+    solve_ms = am["ms_spmv"] / args.steps
+    per_launch = (am["cg_iterations"] / args.steps * bytes_per_iteration(bm.nnz, bm.num_nodes, 4)
+                  + am["refinement_sweeps"] / args.steps * bytes_per_refresh(bm.nnz, bm.num_nodes, 4) + 16 * bm.n)
+    achieved = per_launch / (solve_ms / 1e3) / 1e9 if solve_ms > 0 else None
+    errs_a = np.array(errs)
+    ramp_end = min(scene.ramp_steps, args.steps)
+    line = {
+        "metric": METRIC, "value": val["mixed"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms["mixed"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded cube-grid mesh)",
+        "config": {
+            "workload": ("bar40x40x160 (h 4 mm) whole scenario: 20% compression ramp over 50 steps, then held; "
+                         f"{args.steps} steps from rest; 1,280,000 tets, 270,641 nodes, E log-U[1e4,1e6], "
+                         "nu U[0.40,0.49], gravity, dt 1e-3, CG tol 1e-10; plain FP64 and mixed forms side by side"),
+            "elements": m.num_tets, "nodes": m.num_nodes, "dofs": bm.n, "nnz": bm.nnz, "precision": "mixed",
+            "tuning": {"elements_per_block": tuning[0], "ctas_per_sm": tuning[1], "refresh_weight": tuning[2]},
+            "l2": "working set larger than L2 (no flush needed)", "parallelism": f"replicas x{world}",
+        },
+        "gpu_launches": int(am["kernel_launches"]),
+        "cg_iterations_per_step": am["cg_iterations"] / args.steps,
+        "step_status": sorted(statuses["mixed"]),
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h_dofs.size * (4 + 8)),
+                "d2h_bytes_per_step": 2 * bm.n * 8,
+                "how": f"{e2e_steps} hold steps after the timed run, host clock"},
+        "roofline": {
+            "kernel": "k_pcg_persistent (mixed)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": load_traffic("pcg_persistent_bar"),
+            "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": solve_ms,
+            "peak_source": f"{peak_kind} (hbm_gbs)",
+            "bytes_model": ("CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*n) + refreshes x "
+                            "(nnz*4 + nnz/9*4 + 4(N+1) + 3*8*n) + 16n"),
+        },
+        "fp64_path": {"value": val["fp64"], "unit": UNIT, "ms_per_step": ms["fp64"] / args.steps,
+                      "cg_iterations_per_step": agg["fp64"]["cg_iterations"] / args.steps,
+                      "step_status": sorted(statuses["fp64"]),
+                      "how": "plain FP64 form, same scenario and steps, device-timed per step"},
+        "speedup_vs_fp64_path": val["mixed"] / val["fp64"],
+        "rel_disp_err_vs_fp64": {
+            "max": float(errs_a.max()), "final": float(errs_a[-1]), "max_ramp": float(errs_a[:ramp_end].max()),
+            "max_hold": float(errs_a[ramp_end:].max()) if args.steps > ramp_end else None,
+            "every_10_steps": [float(e) for e in errs_a[9::10]],
+            "definition": "||u_mixed - u_fp64|| / ||u_fp64||, u = x - x_rest, after every step"},
+        "inversions": {"polar_fallbacks_fp64": agg["fp64"]["polar_fallbacks"],
+                       "polar_fallbacks_mixed": am["polar_fallbacks"],
+                       "singular_g_fp64": agg["fp64"]["singular_g"], "singular_g_mixed": am["singular_g"],
+                       "how": "element updates that took the SVD polar path (det F <= 0), summed over the run"},
+    }
+    for b in bodies.values():
+        b.close()
+    return line, scene
+
+
 # ------------------------------------------------------------------------------------------------
 # Differentiation workload (--config adjoint): identification of per-element log E on a 20x20x40
 # cube grid (80,000 tets) from 64 marker positions after 50 steps.
@@ -972,6 +1124,8 @@ def main():
     dist = Dist(world)
     if args.config == "batch":
         line, scenes = run_batch(args, rank, world, local, dist)
+    elif args.config == "bar" and args.steps >= BAR_SCENARIO_STEPS:
+        line, scene = run_bar_full(args, rank, world, local, dist)
     else:
         line, scene = run_single(args, rank, world, local, dist)
     if rank == 0:

@@ -139,7 +139,7 @@ typedef struct gbfem_stats
 #define GBFEM_STEP_TIME_PHASES 1u   /* record per-phase device times (adds events) */
 #define GBFEM_STEP_KEEP_SYSTEM 2u   /* keep the full S / rhs / f of the last solve for export */
 #define GBFEM_STEP_TIME_KERNELS 4u  /* time every CG matrix-vector launch with CUDA events */
-#define GBFEM_STEP_GRAPH 8u         /* mixed form, one Newton iteration: capture the step into a CUDA graph
+#define GBFEM_STEP_GRAPH 8u         /* mixed form or batch, one Newton iteration: capture the step into a CUDA graph
                                        once and launch it nsteps times with no host round trip between
                                        steps (statistics and the finiteness check are read at the end,
                                        so a non-finite state is reported after the last step) */
@@ -246,8 +246,12 @@ GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const doubl
 /* ---- Batching: many independent meshes (each its own OpenSurgSim representation, stepped like
  * one FreeMotion pass over them, FreeMotion.cpp:55-80) in one body. Node ids, boundary-condition
  * dofs and states are concatenated in mesh order; every mesh keeps its own CG scalars and
- * convergence test, and one persistent launch solves all of them. Requires
- * GBFEM_PRECISION_MIXED. gbfem_step, gbfem_get_state, gbfem_set_velocities ... act on the batch. */
+ * convergence test, and one persistent launch solves all of them: in the mixed form its FP32 CG with
+ * FP64 refreshes; in the FP64 form (GBFEM_PRECISION_FP64) every mesh's Eigen CG in FP64 (the same
+ * iteration and stopping rule as a single FP64 handle, which solves with separate launches per
+ * iteration), after the FP64 element update and assembly. Both take GBFEM_STEP_GRAPH and the
+ * autotuner (CTAs per SM of the solve). gbfem_step, gbfem_get_state, gbfem_set_velocities ... act on
+ * the batch. */
 GBFEM_API gbfem_status gbfem_batch_create(int32_t count, const gbfem_mesh_desc* meshes, const gbfem_params* params,
 										  gbfem_handle* out);
 /* Number of meshes, their node / tet offsets (count + 1 entries each) and the scalar non-zeros of

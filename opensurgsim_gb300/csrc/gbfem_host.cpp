@@ -151,6 +151,7 @@ struct gbfem_handle_s
 	// mixed-precision form
 	DevBuf<float> d_rest32, d_kslots32, d_rhsE32, d_A32, d_invdiag32, d_xd, d_invd, d_r32, d_pA, d_pB, d_q32;
 	DevBuf<double> d_brs, d_r64, d_x64;
+	DevBuf<double> d_invd64, d_q64, d_zA64, d_zB64;  // FP64 batches: row-space vectors of the persistent solve
 	DevBuf<int> d_rcol, d_segChunk, d_cumW;  // row-space columns, chunk range per segment, chunk weights
 	DevBuf<double> d_slots;                  // cross-CTA partials of the persistent solve
 	DevBuf<int> d_segMaxIter;                // default CG cap of each segment: 2 n_segment + 64
@@ -180,6 +181,10 @@ struct gbfem_handle_s
 	std::vector<double> segStats;  // per segment over the last gbfem_step: iterations, refreshes, converged, residual
 	int nrows = 0, nchunks = 0;
 	bool mixed() const { return prm.precision == GBFEM_PRECISION_MIXED; }
+	// A batch of meshes (segments); its solve is the persistent launch in either precision.
+	bool batched() const { return segNode.size() > 2; }
+	// Solved by the persistent launch (k_pcg_persistent): the mixed form, and FP64 batches.
+	bool persistent() const { return mixed() || batched(); }
 	bool linear() const { return prm.element_type == GBFEM_ELEMENT_LINEAR_TET; }
 	bool hex() const { return prm.element_type == GBFEM_ELEMENT_HEXAHEDRON; }
 	bool corotational() const { return prm.element_type == GBFEM_ELEMENT_COROTATIONAL_TET; }
@@ -299,7 +304,7 @@ struct gbfem_handle_s
 		DevBuf<float>* bf[] = {&d_rest32, &d_kslots32, &d_rhsE32, &d_A32, &d_invdiag32, &d_xd, &d_invd, &d_r32,
 							   &d_pA, &d_pB, &d_q32};
 		for (auto* b : bf) b->free();
-		for (auto* b : {&d_brs, &d_r64, &d_x64}) b->free();
+		for (auto* b : {&d_brs, &d_r64, &d_x64, &d_invd64, &d_q64, &d_zA64, &d_zB64}) b->free();
 		for (auto* b : {&d_rcol, &d_segChunk, &d_cumW, &d_segMaxIter}) b->free();
 		d_slots.free();
 		d_acc.free();
@@ -363,14 +368,14 @@ gbfem_status fail(gbfem_handle h, gbfem_status st, const std::string& msg)
 
 // The persistent solve's dynamic shared memory limit is a process-wide attribute of the kernel:
 // only ever raised, so a launch sized for one handle never breaks another's.
-cudaError_t raise_pcg_smem_limit(size_t bytes)
+cudaError_t raise_pcg_smem_limit(size_t bytes, bool f64)
 {
 	static std::mutex mu;
-	static size_t current = 48 * 1024;
+	static size_t current[2] = {48 * 1024, 48 * 1024};
 	std::lock_guard<std::mutex> lock(mu);
-	if (bytes <= current) return cudaSuccess;
-	const cudaError_t e = cudaFuncSetAttribute(k_pcg_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-	if (e == cudaSuccess) current = bytes;
+	if (bytes <= current[f64]) return cudaSuccess;
+	const cudaError_t e = pcg_set_max_dynamic_smem(f64, (int)bytes);
+	if (e == cudaSuccess) current[f64] = bytes;
 	return e;
 }
 
@@ -387,9 +392,10 @@ gbfem_status configure_pcg(gbfem_handle h, int cps)
 	const int M = (int)std::max(mW, mC);
 	const size_t smem = pcg_smem_bytes(nseg, M);
 	if (smem > 160 * 1024) return fail(h, GBFEM_INVALID_ARG, "batch too large for the persistent solve");
-	GB_CUDA(h, raise_pcg_smem_limit(smem));
+	const bool f64 = !h->mixed();
+	GB_CUDA(h, raise_pcg_smem_limit(smem, f64));
 	int perSM = 0;
-	GB_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_pcg_persistent, kPcgThreads, smem));
+	GB_CUDA(h, pcg_occupancy(f64, &perSM, smem));
 	if (perSM < std::min(cps, (G + h->smCount - 1) / h->smCount))
 		return fail(h, GBFEM_INVALID_ARG, "persistent solve: " + std::to_string(cps) + " CTAs per SM do not fit");
 	h->pcgGrid = G;
@@ -666,7 +672,7 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	GB_CUDA(h, h->d_perm.upload(perm.data(), perm.size(), s));
 	GB_CUDA(h, h->d_off.upload(off.data(), off.size(), s));
 	GB_CUDA(h, h->d_sellcol.upload(scol.data(), scol.size(), s));
-	if (h->mixed())
+	if (h->persistent())
 	{
 		GB_CUDA(h, h->d_rcol.upload(rcol.data(), rcol.size(), s));
 		GB_CUDA(h, h->d_segChunk.upload(segChunk.data(), segChunk.size(), s));
@@ -702,6 +708,45 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		gbfem_status st = rebuild_hex_operators(h);
 		if (st != GBFEM_OK) return st;
 	}
+	// The persistent solve's control structures (mixed form, FP64 batches): per-segment CG state, the
+	// chunk weights its partition balances, the grid and the per-segment iteration caps.
+	auto setup_persistent = [&]() -> gbfem_status {
+		GB_CUDA(h, h->d_seg.alloc(nseg));
+		GB_CUDA(h, h->d_pcgGlobal.alloc(1));
+		GB_CUDA(h, cudaMallocHost(&h->h_seg, sizeof(SegCtl) * nseg));
+		// Persistent grid: as many co-resident CTAs as fit, at most 4 per SM. The kernel splits the
+		// chunks of the segments still iterating over the CTAs itself; the host bounds the largest
+		// share (shared-memory partials) from the chunk weights.
+		std::vector<int> cumW(nchunks + 1, 0);
+		int wmin = INT32_MAX;
+		for (int c = 0; c < nchunks; ++c)
+		{
+			const int w = off[c + 1] - off[c] + kPcgChunkWeight;
+			wmin = std::min(wmin, w);
+			if ((int64_t)cumW[c] + w > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "matrix too large for the persistent solve");
+			cumW[c + 1] = cumW[c] + w;
+		}
+		GB_CUDA(h, cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, h->device));
+		h->chunkWeightTotal = cumW[nchunks];
+		h->chunkWeightMin = std::max(1, wmin);
+		gbfem_status cst = GBFEM_INVALID_ARG;
+		for (int cps = 4; cps >= 1 && cst != GBFEM_OK; --cps) cst = configure_pcg(h, cps);
+		if (cst != GBFEM_OK) return cst;
+		GB_CUDA(h, h->d_cumW.upload(cumW.data(), cumW.size(), s));
+		GB_CUDA(h, h->d_slots.alloc(4 * 4 * (size_t)h->smCount));  // any grid of up to 4 CTAs per SM
+		// Each mesh of a batch has its own default CG cap, as each representation's solver would
+		// (Eigen's 2n for its own n; the FP32 CG needs the extra 64 on systems of a few dozen dofs).
+		std::vector<int> segCap(nseg);
+		h->segMaxIterMax = 0;
+		for (int sg = 0; sg < nseg; ++sg)
+		{
+			segCap[sg] = 2 * 3 * (h->segNode[sg + 1] - h->segNode[sg]) + (h->mixed() ? 64 : 0);
+			h->segMaxIterMax = std::max(h->segMaxIterMax, segCap[sg]);
+		}
+		GB_CUDA(h, h->d_segMaxIter.upload(segCap.data(), segCap.size(), s));
+		GB_CUDA(h, h->d_acc.alloc(4 * (size_t)nseg + 2));
+		return GBFEM_OK;
+	};
 	if (!h->mixed())
 	{
 		if (!h->hex())
@@ -712,6 +757,16 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		GB_CUDA(h, h->d_A.alloc((size_t)sellSlots * 9));
 		GB_CUDA(h, cudaMemsetAsync(h->d_A.p, 0, sizeof(double) * sellSlots * 9, s));  // padding blocks stay 0
 		for (DevBuf<double>* b : {&h->d_invdiag, &h->d_r, &h->d_p, &h->d_q}) GB_CUDA(h, b->alloc(nv));
+		if (h->batched())
+		{
+			// FP64 batch: the persistent FP64 CG's row-space vectors; z and p of a row in one 64-byte record.
+			const size_t nr = 3 * (size_t)nrows;
+			for (DevBuf<double>* b : {&h->d_invd64, &h->d_q64, &h->d_r64, &h->d_x64}) GB_CUDA(h, b->alloc(nr));
+			for (DevBuf<double>* b : {&h->d_zA64, &h->d_zB64}) GB_CUDA(h, b->alloc(8 * (size_t)nrows));
+			gbfem_status pst = setup_persistent();
+			if (pst != GBFEM_OK) return pst;
+			GB_CUDA(h, cudaStreamSynchronize(s));
+		}
 	}
 	else
 	{
@@ -762,40 +817,8 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		// z and p of each row packed in one 32-byte record (one sector per neighbour gather)
 		for (DevBuf<float>* b : {&h->d_pA, &h->d_pB}) GB_CUDA(h, b->alloc(8 * (size_t)nrows));
 		for (DevBuf<double>* b : {&h->d_brs, &h->d_r64, &h->d_x64}) GB_CUDA(h, b->alloc(nr));
-		GB_CUDA(h, h->d_seg.alloc(nseg));
-		GB_CUDA(h, h->d_pcgGlobal.alloc(1));
-		GB_CUDA(h, cudaMallocHost(&h->h_seg, sizeof(SegCtl) * nseg));
-		// Persistent grid: as many co-resident CTAs as fit, at most 4 per SM. The kernel splits the
-		// chunks of the segments still iterating over the CTAs itself; the host bounds the largest
-		// share (shared-memory partials) from the chunk weights.
-		std::vector<int> cumW(nchunks + 1, 0);
-		int wmin = INT32_MAX;
-		for (int c = 0; c < nchunks; ++c)
-		{
-			const int w = off[c + 1] - off[c] + kPcgChunkWeight;
-			wmin = std::min(wmin, w);
-			if ((int64_t)cumW[c] + w > INT32_MAX) return fail(h, GBFEM_INVALID_ARG, "matrix too large for the persistent solve");
-			cumW[c + 1] = cumW[c] + w;
-		}
-		GB_CUDA(h, cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, h->device));
-		h->chunkWeightTotal = cumW[nchunks];
-		h->chunkWeightMin = std::max(1, wmin);
-		gbfem_status cst = GBFEM_INVALID_ARG;
-		for (int cps = 4; cps >= 1 && cst != GBFEM_OK; --cps) cst = configure_pcg(h, cps);
-		if (cst != GBFEM_OK) return cst;
-		GB_CUDA(h, h->d_cumW.upload(cumW.data(), cumW.size(), s));
-		GB_CUDA(h, h->d_slots.alloc(4 * 4 * (size_t)h->smCount));  // any grid of up to 4 CTAs per SM
-		// Each mesh of a batch has its own default CG cap, as each representation's solver would
-		// (Eigen's 2n for its own n; the FP32 CG needs the extra 64 on systems of a few dozen dofs).
-		std::vector<int> segCap(nseg);
-		h->segMaxIterMax = 0;
-		for (int sg = 0; sg < nseg; ++sg)
-		{
-			segCap[sg] = 2 * 3 * (h->segNode[sg + 1] - h->segNode[sg]) + 64;
-			h->segMaxIterMax = std::max(h->segMaxIterMax, segCap[sg]);
-		}
-		GB_CUDA(h, h->d_segMaxIter.upload(segCap.data(), segCap.size(), s));
-		GB_CUDA(h, h->d_acc.alloc(4 * (size_t)nseg + 2));
+		gbfem_status pst = setup_persistent();
+		if (pst != GBFEM_OK) return pst;
 		GB_CUDA(h, cudaStreamSynchronize(s));
 	}
 	for (DevBuf<double>* b : {&h->d_rhs, &h->d_dv}) GB_CUDA(h, b->alloc(nv));
@@ -1024,6 +1047,13 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	a.barrierTimeoutNs = kBarrierTimeoutNs;
 	a.seg = h->d_seg.p;
 	a.g = h->d_pcgGlobal.p;
+	a.val64 = h->d_A.p;  // FP64 batches (k_pcg_persistent<true>)
+	a.invdiag64 = h->d_invdiag.p;
+	a.invd64 = h->d_invd64.p;
+	a.x64 = h->d_x64.p;
+	a.q64 = h->d_q64.p;
+	a.zA64 = h->d_zA64.p;
+	a.zB64 = h->d_zB64.p;
 	const unsigned evFlags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
 	if (ev0) GB_CUDA(h, cudaEventRecordWithFlags(ev0, st, evFlags));
 	cudaLaunchConfig_t cfg = {};
@@ -1036,7 +1066,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	attr[0].val.cooperative = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	GB_CUDA(h, cudaLaunchKernelEx(&cfg, k_pcg_persistent, a));
+	GB_CUDA(h, pcg_launch(!h->mixed(), cfg, a));
 	if (ev1) GB_CUDA(h, cudaEventRecordWithFlags(ev1, st, evFlags));
 	h->launches += 1;
 	return GBFEM_OK;
@@ -1115,7 +1145,10 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 	// Element kernel: the candidates alternate; the first round warms up, the best of the next three
 	// counts for each.
 	float bestE32 = 1e30f, bestE64 = 1e30f;
-	for (int rep = 0; rep < 4 && !h->hex(); ++rep)
+	// FP64 batches are tuned after their step's FP64 assembly (the system is in place): only the
+	// solve's CTAs per SM.
+	const bool f64 = !h->mixed();
+	for (int rep = 0; rep < 4 && !h->hex() && !f64; ++rep)
 		for (int ept : {32, 64})
 		{
 			GB_CUDA(h, cudaEventRecord(e0, s));
@@ -1127,8 +1160,10 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 			float& best = (ept == 32) ? bestE32 : bestE64;
 			if (rep > 0) best = std::min(best, t);
 		}
-	if (!h->hex()) h->elemsPerBlock = (bestE32 < bestE64) ? 32 : 64;
-	if (h->hex())
+	if (!h->hex() && !f64) h->elemsPerBlock = (bestE32 < bestE64) ? 32 : 64;
+	if (f64)
+		;  // the step's FP64 system and right-hand side are already assembled
+	else if (h->hex())
 	{
 		launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 		enqueue_hex_rhs(h, dt, xt, vt, s);
@@ -1152,6 +1187,7 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 		}
 		for (int rw : {1, 2, 3, 4})
 		{
+			if (f64 && rw != kRefreshWeightDefault) continue;  // the FP64 solve has no refreshes
 			h->refreshWeight = rw;
 			gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, e0, e1);
 			if (st != GBFEM_OK) return st;
@@ -1174,7 +1210,7 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 	h->tuned = true;
 	h->tuneVersion++;
 	h->err.clear();
-	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));  // count the real step only
+	if (!f64) GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));  // count the real step only
 	return GBFEM_OK;
 }
 
@@ -1190,7 +1226,26 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 	const double c1 = 1.0 / dt + h->prm.rayleigh_mass, c2 = dt + h->prm.rayleigh_stiffness;
 	const bool reuse = h->systemCurrent(dt);
 	int kernels = 0;
-	if (h->hex())
+	if (!h->mixed())
+	{
+		// FP64 batch: the FP64 element update and assembly, then the persistent FP64 solve.
+		if (h->hex())
+		{
+			if (!reuse) launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			enqueue_hex_rhs(h, dt, h->d_x.p, h->d_v.p, s);
+			kernels = reuse ? 2 : 3;
+		}
+		else
+		{
+			launch_element_fp64(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
+								h->prm.rayleigh_stiffness, reuse ? nullptr : h->d_kslots.p, h->d_rhsE.p, nullptr, nullptr,
+								h->d_counters.p, s, h->linear());
+			if (!reuse) launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+			kernels = 1 + (reuse ? 1 : 2);
+		}
+	}
+	else if (h->hex())
 	{
 		if (!reuse) launch_system_from_k(body, h->d_K.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
 		enqueue_hex_rhs(h, dt, h->d_x.p, h->d_v.p, s);
@@ -1221,9 +1276,9 @@ gbfem_status enqueue_step_mixed(gbfem_handle h, double dt, bool timed)
 // finiteness check are accumulated on the device and read once at the end.
 gbfem_status step_graph(gbfem_handle h, double dt, int nsteps, uint32_t flags)
 {
-	if (!h->mixed() || h->prm.newton_max_iterations > 1 || (flags & GBFEM_STEP_KEEP_SYSTEM))
+	if (!h->persistent() || h->prm.newton_max_iterations > 1 || (flags & GBFEM_STEP_KEEP_SYSTEM))
 		return fail(h, GBFEM_INVALID_ARG,
-					"GBFEM_STEP_GRAPH needs the mixed form, one Newton iteration and no GBFEM_STEP_KEEP_SYSTEM");
+					"GBFEM_STEP_GRAPH needs the mixed form or a batch, one Newton iteration and no GBFEM_STEP_KEEP_SYSTEM");
 	cudaStream_t s = h->stream;
 	const int nseg = (int)h->segNode.size() - 1;
 	const bool timed = (flags & GBFEM_STEP_TIME_KERNELS) != 0;
@@ -1382,6 +1437,27 @@ gbfem_status apply_external(gbfem_handle h, double dt, const double* xt, cudaStr
 	return GBFEM_OK;
 }
 
+// Per-segment results of the last persistent solve (read back by run_mixed) into the statistics.
+void collect_segment_stats(gbfem_handle h)
+{
+	double worst = 0.0;
+	for (int sg = 0; sg + 1 < (int)h->segNode.size(); ++sg)
+	{
+		const SegCtl& c = h->h_seg[sg];
+		const double res = c.bb > 0 ? std::sqrt(c.rrTrue / c.bb) : 0.0;
+		h->stats.cg_iterations += c.iter;
+		h->stats.refinement_sweeps += c.updates;
+		worst = std::max(worst, res);
+		if (!c.converged) h->stats.cg_max_iterations_hit++;
+		double* ss = &h->segStats[4 * (size_t)sg];
+		ss[0] += c.iter;
+		ss[1] += c.updates;
+		ss[2] = std::min(ss[2], (double)c.converged);
+		ss[3] = std::max(ss[3], res);
+	}
+	h->stats.cg_relative_residual = worst;
+}
+
 gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 {
 	const bool keep = (flags & GBFEM_STEP_KEEP_SYSTEM) != 0;
@@ -1465,22 +1541,7 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 			gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
 			if (st != GBFEM_OK) return st;
 			tm.mark(3);
-			double worst = 0.0;
-			for (int sg = 0; sg + 1 < (int)h->segNode.size(); ++sg)
-			{
-				const SegCtl& c = h->h_seg[sg];
-				const double res = c.bb > 0 ? std::sqrt(c.rrTrue / c.bb) : 0.0;
-				h->stats.cg_iterations += c.iter;
-				h->stats.refinement_sweeps += c.updates;
-				worst = std::max(worst, res);
-				if (!c.converged) h->stats.cg_max_iterations_hit++;
-				double* ss = &h->segStats[4 * (size_t)sg];
-				ss[0] += c.iter;
-				ss[1] += c.updates;
-				ss[2] = std::min(ss[2], (double)c.converged);
-				ss[3] = std::max(ss[3], res);
-			}
-			h->stats.cg_relative_residual = worst;
+			collect_segment_stats(h);
 		}
 		else
 		{
@@ -1520,15 +1581,31 @@ gbfem_status step_once(gbfem_handle h, double dt, uint32_t flags)
 				if (est != GBFEM_OK) return est;
 			}
 			tm.mark(2);
-			gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
-			if (st != GBFEM_OK) return st;
-			tm.mark(3);
-			h->stats.cg_iterations += h->h_ctl->iter;
-			h->stats.cg_relative_residual = h->h_ctl->bb > 0 ? std::sqrt(h->h_ctl->rr / h->h_ctl->bb) : 0.0;
-			if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
-			h->segStats[0] += h->h_ctl->iter;
-			h->segStats[2] = std::min(h->segStats[2], (double)h->h_ctl->converged);
-			h->segStats[3] = std::max(h->segStats[3], h->stats.cg_relative_residual);
+			if (h->batched())
+			{
+				// FP64 batch: every mesh's Eigen CG in one persistent FP64 launch.
+				if (h->prm.autotune && !h->tuned)
+				{
+					gbfem_status tst = tune_mixed(h, xt, vt, dt, c1, c2, maxIter);
+					if (tst != GBFEM_OK) return tst;
+				}
+				gbfem_status st = run_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
+				if (st != GBFEM_OK) return st;
+				tm.mark(3);
+				collect_segment_stats(h);
+			}
+			else
+			{
+				gbfem_status st = run_cg(h, h->d_rhs.p, h->d_dv.p, maxIter, timeK);
+				if (st != GBFEM_OK) return st;
+				tm.mark(3);
+				h->stats.cg_iterations += h->h_ctl->iter;
+				h->stats.cg_relative_residual = h->h_ctl->bb > 0 ? std::sqrt(h->h_ctl->rr / h->h_ctl->bb) : 0.0;
+				if (!h->h_ctl->converged) h->stats.cg_max_iterations_hit++;
+				h->segStats[0] += h->h_ctl->iter;
+				h->segStats[2] = std::min(h->segStats[2], (double)h->h_ctl->converged);
+				h->segStats[3] = std::max(h->segStats[3], h->stats.cg_relative_residual);
+			}
 		}
 		launch_state_update(h->n, h->d_dv.p, h->d_dvPrev.p, xt, h->d_x.p, h->d_v.p, dt, newtonMax > 1, h->d_ctl.p,
 							h->d_part.p, L);
@@ -1653,8 +1730,6 @@ gbfem_status create_impl(const gbfem_mesh_desc* meshes, int32_t count, const gbf
 	}
 	const int npe = prm->element_type == GBFEM_ELEMENT_HEXAHEDRON ? 8 : 4;
 	const int slotsPerElement = prm->element_type == GBFEM_ELEMENT_HEXAHEDRON ? kHexSlots : kSlots;
-	if (count > 1 && prm->precision != GBFEM_PRECISION_MIXED)
-		return fail(nullptr, GBFEM_INVALID_ARG, "a batch of meshes is stepped in the mixed-precision form");
 	// Concatenate the meshes (node ids, boundary-condition dofs shifted by the node offsets).
 	int64_t N = 0, E = 0, B = 0;
 	for (int32_t k = 0; k < count; ++k)
@@ -1836,7 +1911,7 @@ gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t*
 gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t ctas_per_sm, int32_t refresh_weight)
 {
 	if (!h) return GBFEM_INVALID_ARG;
-	if (!h->mixed()) return fail(h, GBFEM_INVALID_ARG, "tuning applies to the mixed form");
+	if (!h->persistent()) return fail(h, GBFEM_INVALID_ARG, "tuning applies to the mixed form and to batches");
 	if ((elems_per_block != 32 && elems_per_block != 64) || ctas_per_sm < 1 || ctas_per_sm > 4 || refresh_weight < 1 ||
 		refresh_weight > kRefreshWeightMax)
 		return fail(h, GBFEM_INVALID_ARG, "tuning: elems_per_block 32|64, ctas_per_sm 1..4, refresh_weight 1..8");
@@ -1961,7 +2036,7 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 	h->launches += ek + 2;
 	tm.mark(1);
 	bool converged = true;
-	if (h->mixed())
+	if (h->persistent())
 	{
 		gbfem_status st = run_mixed(h, h->d_adjG.p, h->d_mu.p, maxIter, false);
 		if (st != GBFEM_OK) return st;

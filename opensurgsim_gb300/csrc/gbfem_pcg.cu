@@ -377,6 +377,43 @@ __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __re
 	}
 }
 
+// FP64 form: the same product on the FP64 values, p(J) = z(J) + beta p_old(J) from the 64-byte
+// records {z0 z1 | z2 - | p0 p1 | p2 -}; two slots' loads issued before either is used (four need
+// 124 registers, or spill at three CTAs per SM).
+__device__ __forceinline__ void spmv_row_zp64(const PcgArgs& a, const double2* __restrict__ zp, int c, int lane,
+											  double beta, double& a0, double& a1, double& a2)
+{
+	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
+	for (int k = k0; k < k1; k += 2)
+	{
+		const int nk = min(2, k1 - k);
+		int J[2];
+#pragma unroll
+		for (int u = 0; u < 2; ++u)
+			if (u < nk) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
+		double2 r0[2], r1[2], r2[2], r3[2];
+#pragma unroll
+		for (int u = 0; u < 2; ++u)
+			if (u < nk)
+			{
+				r0[u] = zp[4 * J[u]];
+				r1[u] = zp[4 * J[u] + 1];
+				r2[u] = zp[4 * J[u] + 2];
+				r3[u] = zp[4 * J[u] + 3];
+			}
+#pragma unroll
+		for (int u = 0; u < 2; ++u)
+			if (u < nk)
+			{
+				const double* vb = a.val64 + (size_t)(k + u) * 288 + lane;
+				const double p0 = r0[u].x + beta * r2[u].x, p1 = r0[u].y + beta * r2[u].y, p2 = r1[u].x + beta * r3[u].x;
+				a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
+				a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
+				a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
+			}
+	}
+}
+
 // Error-free transformations in FP32 (Knuth's TwoSum; the product's rounding error by FMA):
 // a + b = s + e and a * b = p + e exactly. The _rn intrinsics keep the compiler from contracting or
 // reassociating them.
@@ -453,7 +490,8 @@ __device__ __forceinline__ double residual_row(const PcgArgs& a, int c, int rs, 
 
 }  // namespace
 
-__global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
+template <bool kF64>
+__global__ void __launch_bounds__(kPcgThreads, kF64 ? 3 : 4) k_pcg_persistent(PcgArgs a)
 {
 	extern __shared__ double dsm[];
 	const int lane = threadIdx.x & 31;
@@ -481,6 +519,9 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	// zp records: float4 pair per row, .x/.y/.z used: [2*rs] = z = invdiag * r, [2*rs + 1] = p.
 	float4* zpOld = reinterpret_cast<float4*>(a.pA);
 	float4* zpNew = reinterpret_cast<float4*>(a.pB);
+	// FP64 form: {z0 z1 | z2 - | p0 p1 | p2 -} per row.
+	double2* zOld64 = reinterpret_cast<double2*>(a.zA64);
+	double2* zNew64 = reinterpret_cast<double2*>(a.zB64);
 
 	int ph = 0;  // phase id, the same in every CTA; segments finished in phase ph are stamped ph + 1
 	auto finish = [&](SegCtl& S) {
@@ -666,18 +707,35 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		const int rs = 32 * c + lane;
 		const int I = a.perm[rs];
 		double bb = 0.0;
-#pragma unroll
-		for (int k = 0; k < 3; ++k)
+		if constexpr (kF64)
 		{
-			const double bi = (I >= 0) ? a.b[3 * I + k] : 0.0;
-			a.brs[3 * rs + k] = bi;
-			a.r64[3 * rs + k] = bi;
-			a.invd[3 * rs + k] = (I >= 0) ? a.invdiag[3 * I + k] : 0.f;
-			a.xhl[3 * rs + k] = make_float2(0.f, 0.f);
-			a.xd[3 * rs + k] = 0.f;
-			bb += bi * bi;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				const double bi = (I >= 0) ? a.b[3 * I + k] : 0.0;
+				a.r64[3 * rs + k] = bi;
+				a.invd64[3 * rs + k] = (I >= 0) ? a.invdiag64[3 * I + k] : 0.0;
+				a.x64[3 * rs + k] = 0.0;
+				bb += bi * bi;
+			}
+			zOld64[4 * rs + 2] = make_double2(0.0, 0.0);
+			zOld64[4 * rs + 3] = make_double2(0.0, 0.0);
 		}
-		zpOld[2 * rs + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+		else
+		{
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				const double bi = (I >= 0) ? a.b[3 * I + k] : 0.0;
+				a.brs[3 * rs + k] = bi;
+				a.r64[3 * rs + k] = bi;
+				a.invd[3 * rs + k] = (I >= 0) ? a.invdiag[3 * I + k] : 0.f;
+				a.xhl[3 * rs + k] = make_float2(0.f, 0.f);
+				a.xd[3 * rs + k] = 0.f;
+				bb += bi * bi;
+			}
+			zpOld[2 * rs + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+		}
 		bb = warp_sum(bb);
 		if (lane == 0) sp[slot] = bb;
 	});
@@ -698,10 +756,30 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 	});
 	if (!barrier()) return;
 
-	// ---- I2: r = b / s (FP32), z = invdiag r, rz, |r|^2.
+	// ---- I2: r = b / s (FP32), z = invdiag r, rz, |r|^2. FP64 form: z = invdiag r, rz (r = b).
 	phase_start(false, true);
 	for_chunks(actC, sc, nseg, &shNext, [&](int slot, int s, int c) {
 		const int rs = 32 * c + lane;
+		if constexpr (kF64)
+		{
+			double z[3], rz = 0.0;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				const double ri = a.r64[3 * rs + k];
+				z[k] = a.invd64[3 * rs + k] * ri;
+				rz += ri * z[k];
+			}
+			zOld64[4 * rs] = make_double2(z[0], z[1]);
+			zOld64[4 * rs + 1] = make_double2(z[2], 0.0);
+			rz = warp_sum(rz);
+			if (lane == 0)
+			{
+				sp[slot] = rz;
+				sp[M + slot] = 0.0;
+			}
+			return;
+		}
 		const double inv = 1.0 / ldd(&a.seg[s].s);
 		float rz = 0.f, rr = 0.f, z[3];
 #pragma unroll
@@ -742,7 +820,21 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			double part, betaD, alphaU, sU, ratioU;
 			int mode;
 			seg_scalars(s, betaD, mode, alphaU, sU, ratioU);
-			if (mode == 0)
+			if constexpr (kF64)
+			{
+				double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+				spmv_row_zp64(a, zOld64, c, lane, betaD, a0, a1, a2);
+				const double2 z01 = zOld64[4 * rs], z2 = zOld64[4 * rs + 1], p01 = zOld64[4 * rs + 2],
+							  p2 = zOld64[4 * rs + 3];
+				const double n0 = z01.x + betaD * p01.x, n1 = z01.y + betaD * p01.y, n2 = z2.x + betaD * p2.x;
+				zNew64[4 * rs + 2] = make_double2(n0, n1);
+				zNew64[4 * rs + 3] = make_double2(n2, 0.0);
+				__stcs(&a.q64[3 * rs], a0);
+				__stcs(&a.q64[3 * rs + 1], a1);
+				__stcs(&a.q64[3 * rs + 2], a2);
+				part = warp_sum(n0 * a0 + n1 * a1 + n2 * a2);
+			}
+			else if (mode == 0)
 			{
 				const float beta = float(betaD);
 				float a0 = 0.f, a1 = 0.f, a2 = 0.f;
@@ -801,6 +893,43 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 			double betaD, alphaD, sD, ratioD;
 			int mode;
 			seg_scalars(s, betaD, mode, alphaD, sD, ratioD);
+			if constexpr (kF64)
+			{
+				// x += alpha p, r -= alpha q, z = invdiag r; |r|^2, r.z (all loads first).
+				const int d0 = 3 * rs;
+				double iv[3], xv[3], rv[3], qv[3], zz[3];
+#pragma unroll
+				for (int i = 0; i < 3; ++i)
+				{
+					iv[i] = __ldcs(&a.invd64[d0 + i]);
+					xv[i] = __ldcs(&a.x64[d0 + i]);
+					rv[i] = __ldcs(&a.r64[d0 + i]);
+					qv[i] = __ldcs(&a.q64[d0 + i]);
+				}
+				const double2 p01 = zNew64[4 * rs + 2], p2 = zNew64[4 * rs + 3];
+				const double pv[3] = {p01.x, p01.y, p2.x};
+				double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+				for (int i = 0; i < 3; ++i)
+				{
+					const double ri = rv[i] - alphaD * qv[i];
+					__stcs(&a.x64[d0 + i], xv[i] + alphaD * pv[i]);
+					__stcs(&a.r64[d0 + i], ri);
+					zz[i] = iv[i] * ri;
+					t0 += ri * ri;
+					t1 += ri * zz[i];
+				}
+				zNew64[4 * rs] = make_double2(zz[0], zz[1]);
+				zNew64[4 * rs + 1] = make_double2(zz[2], 0.0);
+				t0 = warp_sum(t0);
+				t1 = warp_sum(t1);
+				if (lane == 0)
+				{
+					sp[slot] = t0;
+					sp[M + slot] = t1;
+				}
+				return;
+			}
 			// Row-local vectors, touched once a phase: streaming hint (L2 keeps the z/p records). All
 			// of a row's loads are issued before its first store (the compiler cannot move a load
 			// of one array past a store to another), so a chunk waits on one round of latency.
@@ -876,6 +1005,36 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		});
 		reduce_segments<2>(a, actC, sc, sp, [&](int s, const double* tot) {
 			SegCtl& S = a.seg[s];
+			if constexpr (kF64)
+			{
+				// Eigen's ConjugateGradient: stop on |r|^2 < threshold (the converging iteration is not
+				// counted), else beta, and stop at the iteration cap.
+				S.rr32 = tot[0];
+				S.rrTrue = tot[0];
+				if (!isfinite(tot[0]) || !isfinite(S.alpha))
+				{
+					S.converged = 0;
+					S.nonfinite = 1;
+					finish(S);
+				}
+				else if (tot[0] < S.threshold)
+				{
+					S.converged = 1;
+					finish(S);
+				}
+				else
+				{
+					S.beta = tot[1] / S.rz;
+					S.rz = tot[1];
+					S.iter += 1;
+					if (S.iter >= seg_cap(s))
+					{
+						S.converged = 0;
+						finish(S);
+					}
+				}
+				return;
+			}
 			if (S.mode == 2)
 			{
 				S.beta = tot[1] / (S.rzPend * S.ratio * S.ratio);
@@ -912,6 +1071,9 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 		float4* t = zpOld;
 		zpOld = zpNew;
 		zpNew = t;
+		double2* t64 = zOld64;
+		zOld64 = zNew64;
+		zNew64 = t64;
 	}
 
 	// ---- Out: x (dof space) = x_hl + x_delta.
@@ -922,10 +1084,35 @@ __global__ void __launch_bounds__(kPcgThreads, 4) k_pcg_persistent(PcgArgs a)
 #pragma unroll
 		for (int k = 0; k < 3; ++k)
 		{
-			const float2 xv = a.xhl[3 * rs + k];
-			a.x[3 * I + k] = (double(xv.x) + double(xv.y)) + double(a.xd[3 * rs + k]);
+			if constexpr (kF64)
+				a.x[3 * I + k] = a.x64[3 * rs + k];
+			else
+			{
+				const float2 xv = a.xhl[3 * rs + k];
+				a.x[3 * I + k] = (double(xv.x) + double(xv.y)) + double(a.xd[3 * rs + k]);
+			}
 		}
 	});
+}
+
+template __global__ void k_pcg_persistent<false>(PcgArgs a);
+template __global__ void k_pcg_persistent<true>(PcgArgs a);
+
+cudaError_t pcg_set_max_dynamic_smem(bool f64, int bytes)
+{
+	return f64 ? cudaFuncSetAttribute(k_pcg_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+			   : cudaFuncSetAttribute(k_pcg_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t pcg_occupancy(bool f64, int* ctasPerSM, size_t smem)
+{
+	return f64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSM, k_pcg_persistent<true>, kPcgThreads, smem)
+			   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSM, k_pcg_persistent<false>, kPcgThreads, smem);
+}
+
+cudaError_t pcg_launch(bool f64, const cudaLaunchConfig_t& cfg, const PcgArgs& a)
+{
+	return f64 ? cudaLaunchKernelEx(&cfg, k_pcg_persistent<true>, a) : cudaLaunchKernelEx(&cfg, k_pcg_persistent<false>, a);
 }
 
 namespace {

@@ -1,4 +1,4 @@
-// gbfem_pcg.h -- persistent mixed-precision CG over a batch of segments (declarations).
+// gbfem_pcg.h -- persistent CG over a batch of segments, mixed-precision or FP64 (declarations).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -82,6 +82,15 @@ struct PcgArgs
 	float* q;
 	SegCtl* seg;
 	PcgGlobal* g;
+	// FP64 form (k_pcg_persistent<true>): plain FP64 CG on the FP64 SELL values, Eigen's iteration and
+	// stopping rule for every segment, no refreshes. r in r64, x in x64, b in brs.
+	const double* val64;   // FP64 SELL values (same slots as val)
+	const double* invdiag64;  // dof space
+	double* invd64;        // row space
+	double* x64;           // row space
+	double* q64;
+	double* zA64;          // 8 doubles per row: z (3), pad, p (3), pad; 64-byte aligned
+	double* zB64;
 };
 
 // Dynamic shared memory of one CTA: the chunk partials, the segment chunk prefix, the active-set
@@ -91,7 +100,16 @@ inline size_t pcg_smem_bytes(int nsegs, int maxChunksPerCta)
 	return 2 * sizeof(double) * (size_t)maxChunksPerCta + 4 * sizeof(int) * (size_t)(nsegs + 1);
 }
 
+// kF64 = false: the mixed-precision solve (FP32 CG with double-float refreshes); true: plain FP64 CG.
+template <bool kF64>
 __global__ void k_pcg_persistent(PcgArgs a);
+
+// Host access to the two instantiations (the kernel templates' host stubs are local to their
+// translation unit): the dynamic shared memory limit, the co-resident CTAs per SM, and a launch
+// with the caller's configuration (grid, block, shared memory, stream, cooperative attribute).
+cudaError_t pcg_set_max_dynamic_smem(bool f64, int bytes);
+cudaError_t pcg_occupancy(bool f64, int* ctasPerSM, size_t smem);
+cudaError_t pcg_launch(bool f64, const cudaLaunchConfig_t& cfg, const PcgArgs& a);
 
 // Self-test of the grid barrier on a PcgGlobal of its own (zeroed by the caller): `phases` barriers
 // over a cooperative grid. With `stall` set, the arrival counter starts at gridDim.x, so no block is
