@@ -46,7 +46,8 @@ CG_CAP = 10000
 BAR_SCENARIO_STEPS = 200  # --config bar --steps 200: the whole compression scenario, both forms
 BATCH = dict(count=256, lo=500, hi=50000, seed=3)
 BATCH_PARAMS = dict(rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0.0, 0.0, -9.81), cg_tolerance=1e-10)
-COMPARE_STEPS = 4  # steps of the FP64-path comparison (1 untimed + 3 timed) and of the error check
+COMPARE_STEPS = 4  # steps of the per-mesh FP64 path's timing (1 untimed + 3 timed)
+ERROR_RUN_STEPS = 100  # the batch scenario's length: the mixed-vs-FP64 error is taken over all of it
 
 
 def log(msg):
@@ -230,9 +231,7 @@ def rel_disp_err(x_mixed, x64, rest):
 
 def fp64_path_comparison(meshes, local):
     """The plain FP64 GPU path on the same meshes, one handle per mesh stepped in turn (the
-    reference steps representations one by one): COMPARE_STEPS steps, the last ones timed; and the
-    batched mixed step over the same steps for the displacement error."""
-    import numpy as np
+    reference steps representations one by one): COMPARE_STEPS steps, the last ones timed."""
     import torch
 
     from opensurgsim_gb300 import _lib
@@ -252,23 +251,76 @@ def fp64_path_comparison(meshes, local):
     torch.cuda.synchronize(local)
     sec = (time.perf_counter() - t0) / (COMPARE_STEPS - 1)
     tets = sum(m.num_tets for m in meshes)
-    x64 = [b.state()[0] for b in bodies]
     for b in bodies:
         b.close()
-    mixed = batch_body(meshes, _lib.PRECISION_MIXED, local)
-    mixed.step(1e-3, COMPARE_STEPS)
-    xm, _ = mixed.state()
-    errs = []
-    for k, m in enumerate(meshes):
-        n0, n1 = mixed.node_offsets[k], mixed.node_offsets[k + 1]
-        errs.append(rel_disp_err(xm[3 * n0:3 * n1], x64[k], m.nodes.ravel()))
-    mixed.close()
     return {"value": tets / sec, "unit": UNIT, "ms_per_step": 1e3 * sec,
             "cg_iterations_per_step": its / (COMPARE_STEPS - 1),
             "how": (f"plain FP64 form, one handle per mesh stepped in turn; steps 2-{COMPARE_STEPS} timed "
-                    "(host clock around device-synchronised steps)")}, {
-        "max": max(errs), "median": float(np.median(errs)), "after_steps": COMPARE_STEPS,
-        "definition": "||u_mixed - u_fp64|| / ||u_fp64|| per mesh, u = x - x_rest"}
+                    "(host clock around device-synchronised steps)")}
+
+
+def fp64_batch_and_error(meshes, local, steps, warmup, mixed_tuning):
+    """(1) The plain FP64 form batched like the mixed one: all meshes in one handle, every mesh's Eigen
+    CG in one persistent FP64 launch, graph steps, autotuned; `steps` steps device-timed after
+    `warmup`. (2) The mixed-vs-FP64 displacement error over the whole 100-step scenario: that FP64
+    batch and a mixed batch (the timed run's tuning) stepped side by side from rest, the per-mesh
+    relative error ||u_mixed - u_fp64|| / ||u_fp64|| taken on the device after every step."""
+    import numpy as np
+    import torch
+
+    from opensurgsim_gb300 import _lib
+    from opensurgsim_gb300.autograd import state_views
+
+    tets = sum(m.num_tets for m in meshes)
+    b64 = batch_body(meshes, _lib.PRECISION_FP64, local, autotune=True)
+    stream = torch.cuda.ExternalStream(b64.stream(), device=local)
+    for _ in range(warmup):
+        b64.step(1e-3, 1, _lib.STEP_GRAPH)
+    torch.cuda.synchronize(local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    st = b64.step(1e-3, steps, _lib.STEP_GRAPH)
+    ev1.record(stream)
+    torch.cuda.synchronize(local)
+    ms = ev0.elapsed_time(ev1)
+    its = int(b64.segment_stats()["iterations"].max())
+    fp64_batch = {"value": tets * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                  "cg_iterations_per_step": its / steps, "step_status": int(st), "tuning_ctas_per_sm": b64.tuning()[1],
+                  "how": ("plain FP64 form batched: one handle, FP64 element kernel and assembly, every mesh's Eigen "
+                          "CG in one persistent FP64 launch, graph steps; device-timed like the mixed line")}
+    # Side-by-side run from rest over the whole scenario.
+    bm = batch_body(meshes, _lib.PRECISION_MIXED, local)
+    bm.set_tuning(*mixed_tuning)
+    rest = torch.from_numpy(np.concatenate([m.nodes.ravel() for m in meshes])).cuda(local)
+    x64, v64 = state_views(b64)
+    xm, _ = state_views(bm)
+    x64.copy_(rest)
+    v64.zero_()
+    torch.cuda.synchronize(local)
+    counts = np.array([3 * m.num_nodes for m in meshes])
+    seg = torch.from_numpy(np.repeat(np.arange(len(meshes)), counts)).cuda(local)
+    worst_per_mesh = torch.zeros(len(meshes), dtype=torch.float64, device=f"cuda:{local}")
+    worst_per_step = []
+    for _ in range(ERROR_RUN_STEPS):
+        bm.step(1e-3, 1, _lib.STEP_GRAPH)
+        b64.step(1e-3, 1, _lib.STEP_GRAPH)
+        u = x64 - rest
+        d = xm - x64
+        num = torch.zeros(len(meshes), dtype=torch.float64, device=u.device).index_add_(0, seg, d * d)
+        den = torch.zeros(len(meshes), dtype=torch.float64, device=u.device).index_add_(0, seg, u * u)
+        e = torch.sqrt(num / den.clamp_min(1e-300))
+        worst_per_mesh = torch.maximum(worst_per_mesh, e)
+        worst_per_step.append(float(e.max()))
+    final = e.cpu().numpy()
+    bm.close()
+    b64.close()
+    err = {"max": float(max(worst_per_step)), "final_max": float(final.max()), "final_median": float(np.median(final)),
+           "median_of_per_mesh_max": float(np.median(worst_per_mesh.cpu().numpy())),
+           "every_10_steps": [float(v) for v in worst_per_step[9::10]], "steps": ERROR_RUN_STEPS,
+           "definition": ("||u_mixed - u_fp64|| / ||u_fp64|| per mesh, u = x - x_rest, after every step of the "
+                          f"{ERROR_RUN_STEPS}-step scenario from rest; max = worst mesh over all steps, final_* at the "
+                          "last step; FP64 reference: the FP64 batch (persistent FP64 CG, tolerance 1e-10)")}
+    return fp64_batch, err
 
 
 def run_batch(args, rank, world, local, dist):
@@ -931,47 +983,70 @@ def run_adjoint_batch(args, local):
         L.backward()
         return th.grad.detach().cpu().numpy()
 
-    with torch.no_grad():  # warm-up (allocations, first launches)
-        rollout(batch, th_b, x0, v0b, 1e-3, 2, ck)
+    # Warm-up: the same rollout (the library captures the forward and the backward graphs once).
+    for _ in range(max(1, args.warmup)):
+        g_batch = fwd_bwd()
     torch.cuda.synchronize(dev)
+    reps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
-    g_batch = fwd_bwd()
+    for _ in range(reps):
+        g_batch = fwd_bwd()
     torch.cuda.synchronize(dev)
-    sec = time.perf_counter() - t0
+    sec = (time.perf_counter() - t0) / reps
     log(f"batched mixed forward+backward: {sec:.2f} s")
     batch.close()
-    # FP64 reference adjoint, one mesh at a time.
-    to = np.concatenate([[0], np.cumsum([m.num_tets for m in meshes])])
-    errs = []
+
+    def grads_fp64_batch():
+        b = Body(meshes, precision=_lib.PRECISION_FP64, device=local, **BATCH_PARAMS)
+        th = th_b.clone().requires_grad_(True)
+        xk, _ = rollout(b, th, x0, v0b, 1e-3, steps, ck)
+        ((xk[mk_t] - target) ** 2).sum().backward()
+        torch.cuda.synchronize(dev)
+        b.close()
+        return th.grad.detach().cpu().numpy()
+
+    # FP64 reference adjoint: the same meshes as one FP64 batch (FP64 element derivatives, every
+    # mesh's Eigen CG in FP64), also as CUDA-graph rollouts.
+    grads_fp64_batch()  # capture and warm-up
     t0 = time.perf_counter()
-    for k, m in enumerate(meshes):
+    g64 = grads_fp64_batch()
+    sec64 = time.perf_counter() - t0
+    to = np.concatenate([[0], np.cumsum([m.num_tets for m in meshes])])
+    errs = [float(np.linalg.norm(g_batch[to[k]:to[k + 1]] - g64[to[k]:to[k + 1]]) /
+                  max(np.linalg.norm(g64[to[k]:to[k + 1]]), 1e-300)) for k in range(len(meshes))]
+    log(f"FP64 reference adjoint (FP64 batch): {sec64:.2f} s; gradient error max {max(errs):.2e}")
+    # Cross-check of the FP64 batch against FP64 handles, one per mesh, on the first 4 meshes.
+    cross = []
+    mo = np.concatenate([[0], np.cumsum([3 * len(mm) for mm in markers])])
+    for k in range(min(4, len(meshes))):
+        m = meshes[k]
         b = Body(m, precision=_lib.PRECISION_FP64, device=local, **BATCH_PARAMS)
         mkk = torch.tensor(np.stack([3 * markers[k], 3 * markers[k] + 1, 3 * markers[k] + 2], 1).ravel(),
                            dtype=torch.long, device=dev)
         th = t64(theta[k]).requires_grad_(True)
         xk, _ = rollout(b, th, t64(m.nodes.ravel()), t64(v0[k]), 1e-3, steps, ck)
-        L = ((xk[mkk] - target[3 * sum(len(mm) for mm in markers[:k]):3 * sum(len(mm) for mm in markers[:k + 1])])
-             ** 2).sum()
-        L.backward()
-        g64 = th.grad.detach().cpu().numpy()
-        gb = g_batch[to[k]:to[k + 1]]
-        errs.append(float(np.linalg.norm(gb - g64) / max(np.linalg.norm(g64), 1e-300)))
+        ((xk[mkk] - target[mo[k]:mo[k + 1]]) ** 2).sum().backward()
+        gk = th.grad.detach().cpu().numpy()
+        cross.append(float(np.linalg.norm(g64[to[k]:to[k + 1]] - gk) / max(np.linalg.norm(gk), 1e-300)))
         b.close()
-    sec64 = time.perf_counter() - t0
-    log(f"FP64 reference adjoint (mesh by mesh): {sec64:.2f} s; gradient error max {max(errs):.2e}")
+    log(f"FP64 batch vs FP64 single handles (first {len(cross)} meshes): max {max(cross):.2e}")
     return {
         "metric": "tet-element-steps/s (forward + backward, batched adjoint, 30 steps)",
-        "value": tets * steps / sec, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+        "value": tets * steps / sec, "unit": UNIT, "n_gpus": 1, "steps": reps, "warmup": max(1, args.warmup),
         "ms_per_step": 1e3 * sec / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic (seeded cube-grid meshes, seeded parameters)",
         "config": {"workload": (f"adjoint batch: {len(meshes)} meshes, nodes log-U[2000,100000] (seed {ADJB['seed']}), "
                                 f"{tets} tets, per-element log E = ln E_mesh + N(0, 0.3), {ADJB['markers']} markers "
-                                f"per mesh, {steps} steps, checkpoints every {ck}, mixed precision batch handle"),
+                                f"per mesh, {steps} steps, checkpoints every {ck}, mixed precision batch handle; "
+                                "forward and backward each one CUDA graph in the library"),
                    "tets": tets},
         "grad_rel_err_vs_fp64_adjoint": {"max": max(errs), "median": float(np.median(errs)),
-                                         "definition": "per mesh ||g_batch - g_fp64|| / ||g_fp64||"},
-        "fp64_reference_adjoint": {"value": tets * steps / sec64, "how": "FP64 handle per mesh, one after another"},
-        "timing": "host clock around one device-synchronised forward+backward after a short warm-up",
+                                         "definition": "per mesh ||g_batch - g_fp64|| / ||g_fp64||, FP64 batch reference"},
+        "fp64_reference_adjoint": {"value": tets * steps / sec64,
+                                   "how": "the same meshes as one FP64 batch handle, graph rollouts, host clock"},
+        "fp64_batch_vs_single_handles": {"max": max(cross), "meshes": len(cross),
+                                         "definition": "per mesh gradient, FP64 batch vs one FP64 handle"},
+        "timing": f"host clock around {reps} device-synchronised forward+backward passes after the warm-up",
     }
 
 
@@ -1130,13 +1205,26 @@ def main():
         line, scene = run_single(args, rank, world, local, dist)
     if rank == 0:
         if args.config == "batch" and not args.no_compare and world == 1:
-            log("plain FP64 path on the same meshes")
-            fp64, err = fp64_path_comparison([s.mesh for s in scenes], local)
+            meshes = [s.mesh for s in scenes]
+            log("plain FP64 path on the same meshes, one handle per mesh")
+            fp64 = fp64_path_comparison(meshes, local)
             line["fp64_path"] = fp64
             line["speedup_vs_fp64_path"] = line["value"] / (fp64["value"] * world)
+            log("plain FP64 form batched, and the mixed-vs-FP64 error over the whole scenario")
+            tun = line["config"]["tuning"]
+            fb, err = fp64_batch_and_error(meshes, local, args.steps, args.warmup,
+                                           (tun["elements_per_block"], tun["ctas_per_sm"], tun["refresh_weight"]))
+            line["fp64_batched"] = fb
             line["rel_disp_err_vs_fp64"] = err
-            log(f"fp64 path {fp64['value'] / 1e6:.1f} M tet-steps/s, speed-up {line['speedup_vs_fp64_path']:.2f}, "
-                f"max rel disp err {err['max']:.2e}")
+            line["speedup_split"] = {
+                "batching": fb["value"] / fp64["value"], "precision": line["value"] / fb["value"],
+                "total": line["value"] / fp64["value"],
+                "how": ("batching = FP64 batched / FP64 one handle per mesh; precision = mixed batched / FP64 "
+                        "batched; total = their product")}
+            log(f"fp64 path {fp64['value'] / 1e6:.1f} M, fp64 batched {fb['value'] / 1e6:.1f} M tet-steps/s; "
+                f"speed-up {line['speedup_vs_fp64_path']:.2f} (batching {line['speedup_split']['batching']:.2f} x "
+                f"precision {line['speedup_split']['precision']:.2f}); max rel disp err {err['max']:.2e} over "
+                f"{ERROR_RUN_STEPS} steps")
         if world == 1 and not args.no_cpu_baseline:
             from oracle import oracle as O
 

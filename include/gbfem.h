@@ -243,6 +243,28 @@ GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const doubl
 										  const double* lx, const double* lv, double* lx_out, double* lv_out,
 										  double* grad_log_young, double* grad_poisson, uint32_t flags);
 
+/* Whole rollouts of the differentiation form as CUDA graphs (corotational elements, the mixed form
+ * or a batch, one Newton iteration). No counterpart in the reference.
+ * gbfem_rollout_forward: from (x0, v0) take nsteps steps of dt (gbfem_step semantics), keeping the
+ *   state every checkpoint_every steps in device memory of the handle; writes the final state to
+ *   (xT, vT) and leaves it as the handle's state.
+ * gbfem_rollout_backward: the reverse sweep of the last forward: for each checkpoint segment, last
+ *   first, its steps are run again from the checkpoint to recover their states, then the step
+ *   adjoints (gbfem_adjoint_step) are applied in reverse. Given (lxT, lvT) = dL/d(xT, vT) it writes
+ *   (lx0, lv0) = dL/d(x0, v0) and, where not NULL, grad_log_young = dL/d(log E_e) and grad_poisson =
+ *   dL/d(nu_e) (overwritten, not accumulated). The handle's state is the forward's final state again
+ *   afterwards.
+ * Each is captured once into one CUDA graph (again when dt, nsteps, checkpoint_every or the tuning
+ * changes) and launched with no host round trip inside it; the call copies its arrays in and out
+ * around the launch and reads the solves' statistics once at the end. All arrays are device arrays of
+ * n (state) or num_tets (gradients) doubles. Returns GBFEM_CG_MAXITER when a solve did not converge
+ * (the outputs are still written) and GBFEM_NONFINITE when a forward state stopped being finite.
+ * With autotune, the first forward tunes the solve on (x0, v0) before capturing. */
+GBFEM_API gbfem_status gbfem_rollout_forward(gbfem_handle h, double dt, int32_t nsteps, int32_t checkpoint_every,
+											 const double* x0, const double* v0, double* xT, double* vT);
+GBFEM_API gbfem_status gbfem_rollout_backward(gbfem_handle h, const double* lxT, const double* lvT, double* lx0,
+											  double* lv0, double* grad_log_young, double* grad_poisson);
+
 /* ---- Batching: many independent meshes (each its own OpenSurgSim representation, stepped like
  * one FreeMotion pass over them, FreeMotion.cpp:55-80) in one body. Node ids, boundary-condition
  * dofs and states are concatenated in mesh order; every mesh keeps its own CG scalars and

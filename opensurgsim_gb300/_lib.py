@@ -44,7 +44,7 @@ EXPORTED = [
     "gbfem_cg_destroy", "gbfem_cg_solve_noalloc", "gbfem_batch_create", "gbfem_batch_info",
     "gbfem_batch_segment_stats", "gbfem_set_materials_device", "gbfem_adjoint_step", "gbfem_get_tuning",
     "gbfem_set_tuning", "gbfem_apply_compliance", "gbfem_add_external_force", "gbfem_barrier_selftest",
-    "gbfem_set_solver_params",
+    "gbfem_set_solver_params", "gbfem_rollout_forward", "gbfem_rollout_backward",
 ]
 
 
@@ -151,6 +151,8 @@ def load():
         "gbfem_apply_compliance": (S, [H, ctypes.c_int32, D, D, ctypes.c_uint32, I32]),
         "gbfem_set_tuning": (S, [H, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
         "gbfem_set_solver_params": (S, [H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
+        "gbfem_rollout_forward": (S, [H, ctypes.c_double, ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 4),
+        "gbfem_rollout_backward": (S, [H] + [ctypes.c_void_p] * 6),
         "gbfem_adjoint_step": (S, [H, ctypes.c_double] + [ctypes.c_void_p] * 9 + [ctypes.c_uint32]),
         "gbfem_add_external_force": (S, [H, ctypes.c_int32, D, D, D, D]),
         "gbfem_barrier_selftest": (S, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,

@@ -9,6 +9,11 @@ accumulates dL/d(log E) and dL/d(nu) and carries (dL/dx, dL/dv) to the segment's
 flow to ``log_young``, ``x0``, ``v0`` and, when given, the per-element Poisson ratios ``poisson``
 (Fem3DElementTetrahedron.cpp:204-205: nu enters K0 through lambda and mu).
 
+On bodies whose solve is the persistent launch (the mixed form, or a batch) with corotational
+elements and one Newton iteration, the forward and the backward each run as one CUDA graph inside the
+library (gbfem_rollout_forward / gbfem_rollout_backward: checkpoints, segment re-runs and step
+adjoints with no host round trip); other bodies take the per-step loop above.
+
 The reference has no adjoint; the forward steps are the reference's Fem3DRepresentation::update
 semantics (one Newton iteration). All tensors are float64 on the body's device.
 """
@@ -70,6 +75,17 @@ def rollout_states(body, x0, v0, dt, nsteps, keep=None):
     return xv.clone(), vv.clone()
 
 
+def graph_rollouts(body) -> bool:
+    """Whether the body's rollouts run as CUDA graphs in the library."""
+    p = body.params
+    return (p.element_type == _lib.ELEMENT_COROTATIONAL_TET and p.newton_max_iterations == 1 and
+            (p.precision == _lib.PRECISION_MIXED or body.num_meshes > 1))
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
 class ImplicitRollout(torch.autograd.Function):
     """(x_T, v_T) = rollout(log_young, poisson, x0, v0); see the module docstring. ``poisson`` may
     be None (each element keeps its Poisson ratio and gets no gradient)."""
@@ -78,6 +94,26 @@ class ImplicitRollout(torch.autograd.Function):
     def forward(ctx, log_young, poisson, x0, v0, body, dt, nsteps, checkpoint_every, flags=0):
         set_young(body, log_young, poisson)
         k = max(1, int(checkpoint_every))
+        ctx.has_poisson = poisson is not None
+        ctx.save_for_backward(log_young, poisson if poisson is not None else log_young)
+        ctx.body, ctx.dt, ctx.nsteps, ctx.k, ctx.flags = body, dt, nsteps, k, int(flags)
+        ctx.graph = graph_rollouts(body)
+        if ctx.graph:
+            dev = x0.device
+            xs = x0.detach().to(torch.float64).contiguous()
+            vs = v0.detach().to(torch.float64).contiguous()
+            xT = torch.empty(body.n, dtype=torch.float64, device=dev)
+            vT = torch.empty(body.n, dtype=torch.float64, device=dev)
+            torch.cuda.synchronize(dev)
+            st = _lib.load().gbfem_rollout_forward(body.handle, float(dt), int(nsteps), k, _ptr(xs), _ptr(vs), _ptr(xT),
+                                                   _ptr(vT))
+            _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+            # The library keeps the checkpoints of the body's last forward only: the token tells the
+            # backward whether another rollout of the body ran in between (then it runs this one again).
+            body._rollout_token = getattr(body, "_rollout_token", 0) + 1
+            ctx.token, ctx.x0, ctx.v0 = body._rollout_token, xs, vs
+            ctx.checkpoints = None
+            return xT, vT
         checkpoints = []
         xv, vv = state_views(body)
         torch.cuda.synchronize(xv.device)
@@ -90,10 +126,7 @@ class ImplicitRollout(torch.autograd.Function):
             _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
             if (t + 1) % k == 0 and t + 1 < nsteps:
                 checkpoints.append((xv.clone(), vv.clone()))
-        ctx.body, ctx.dt, ctx.nsteps, ctx.k, ctx.flags = body, dt, nsteps, k, int(flags)
         ctx.checkpoints = checkpoints
-        ctx.has_poisson = poisson is not None
-        ctx.save_for_backward(log_young, poisson if poisson is not None else log_young)
         return xv.clone(), vv.clone()
 
     @staticmethod
@@ -110,6 +143,21 @@ class ImplicitRollout(torch.autograd.Function):
         gnu = torch.zeros(body.num_tets, dtype=torch.float64, device=dev) if poisson is not None else None
         L = _lib.load()
         set_young(body, log_young, poisson)
+        if ctx.graph:
+            # The library re-runs the checkpoint segments and applies the step adjoints in one graph.
+            lx0 = torch.empty_like(lx)
+            lv0 = torch.empty_like(lv)
+            torch.cuda.synchronize(dev)
+            if getattr(body, "_rollout_token", 0) != ctx.token:
+                st = L.gbfem_rollout_forward(body.handle, float(dt), int(nsteps), k, _ptr(ctx.x0), _ptr(ctx.v0),
+                                             _ptr(lx0), _ptr(lv0))
+                _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+                body._rollout_token = getattr(body, "_rollout_token", 0) + 1
+                ctx.token = body._rollout_token
+            st = L.gbfem_rollout_backward(body.handle, _ptr(lx), _ptr(lv), _ptr(lx0), _ptr(lv0), _ptr(glog),
+                                          None if gnu is None else _ptr(gnu))
+            _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+            return glog, gnu, lx0, lv0, None, None, None, None, None
         starts = list(range(0, nsteps, k))
         for seg in reversed(range(len(starts))):
             t0 = starts[seg]

@@ -140,7 +140,19 @@ __global__ void k_set_materials(int E, const double* __restrict__ young, const d
 
 inline int blocks_of(long long n, int t) { return (int)((n + t - 1) / t); }
 
+__global__ void k_vec_diff(int n, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) out[i] = a[i] - b[i];
+}
+
 }  // namespace
+
+void launch_vec_diff(int n, const double* a, const double* b, double* out, cudaStream_t s)
+{
+	if (n == 0) return;
+	k_vec_diff<<<blocks_of(n, 256), 256, 0, s>>>(n, a, b, out);
+}
 
 void launch_element_adjoint(const DevBody& b, const double* x, const double* v, const double* mu, const double* dv,
 							double dt, double alpha, double beta, double* gx, double* gv, double* gLogE, double* gNu,

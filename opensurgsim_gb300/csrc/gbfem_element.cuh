@@ -96,7 +96,7 @@ struct Eps<DualF>
 // Polar factor by Newton's iteration X <- (g X + X^-T / g) / 2 (Higham), Frobenius scaling on the
 // first iterations. Valid for det F > 0, where the orthogonal polar factor is the rotation that
 // Transform::computeRotationScaling returns. Returns false (the caller falls back to the SVD) for
-// det F <= 0 or when the iteration does not settle within its bound.
+// det F <= 0 (FP32: det F <= 1e-5 |F|_F^3) or when the iteration does not settle within its bound.
 template <typename T>
 __host__ __device__ bool polar_newton(const T* F, T* R)
 {
@@ -119,6 +119,9 @@ __host__ __device__ bool polar_newton(const T* F, T* R)
 				nx += X[k] * X[k];
 				nc += C[k] * C[k];
 			}
+			// FP32: a nearly degenerate F (det F below 1e-5 of |F|_F^3) goes to the FP64 SVD path, where
+			// a collapsed element's singular G is decided in FP64 as the reference decides it.
+			if (std::is_same<T, float>::value && it == 0 && !(d > T(1e-5) * nx * sqrt(nx))) return false;
 			gam = sqrt(sqrt(nc / (nx * d * d)));
 		}
 		const T a = T(0.5) * gam;

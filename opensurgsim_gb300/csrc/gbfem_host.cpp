@@ -147,6 +147,13 @@ struct gbfem_handle_s
 	DevBuf<uint8_t> d_bc;
 	DevBuf<double> d_x, d_v, d_xt, d_vt;
 	DevBuf<double> d_mu, d_adjG, d_gx, d_gv;  // differentiation form (allocated on first use)
+	// Rollouts as CUDA graphs (gbfem_rollout_forward / _backward): checkpoints (the last slot holds the
+	// final state), one segment's states, the adjoint pair (lx | lv), the gradients (log E | nu), the
+	// step's velocity increment, and the adjoint solves' statistics.
+	double rollDt = 0.0;
+	int rollSteps = 0, rollEvery = 0, rollFwdVersion = -1, rollBwdVersion = -1;
+	cudaGraphExec_t rollFwd = nullptr, rollBwd = nullptr;
+	DevBuf<double> d_ckpt, d_segX, d_rollL, d_rollG, d_dvTmp, d_adjAcc;
 	DevBuf<double> d_kslots, d_rhsE, d_A, d_invdiag, d_rhs, d_dv, d_dvPrev, d_r, d_p, d_q, d_part;
 	// mixed-precision form
 	DevBuf<float> d_rest32, d_kslots32, d_rhsE32, d_A32, d_invdiag32, d_xd, d_invd, d_r32, d_pA, d_pB, d_q32;
@@ -318,7 +325,10 @@ struct gbfem_handle_s
 			if (e) cudaEventDestroy(e);
 		d_seg.free();
 		d_pcgGlobal.free();
-		for (auto* b : {&d_mu, &d_adjG, &d_gx, &d_gv}) b->free();
+		for (auto* b : {&d_mu, &d_adjG, &d_gx, &d_gv, &d_ckpt, &d_segX, &d_rollL, &d_rollG, &d_dvTmp, &d_adjAcc}) b->free();
+		if (rollFwd) cudaGraphExecDestroy(rollFwd);
+		if (rollBwd) cudaGraphExecDestroy(rollBwd);
+		rollFwd = rollBwd = nullptr;
 		DevBuf<double>* bd[] = {&d_rest, &d_xrest, &d_lmass, &d_nmass, &d_x, &d_v, &d_xt, &d_vt, &d_kslots,
 								&d_rhsE, &d_A, &d_invdiag, &d_rhs, &d_dv, &d_dvPrev, &d_r, &d_p, &d_q, &d_part,
 								&d_vals, &d_kfull, &d_fE, &d_S, &d_smass, &d_f, &d_young, &d_poisson, &d_rho,
@@ -2063,6 +2073,338 @@ gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const double* x, cons
 		h->stats.ms_update += tm.ms(2, 3);
 	}
 	return converged ? GBFEM_OK : fail(h, GBFEM_CG_MAXITER, "adjoint solve did not converge");
+}
+
+}  // extern "C"
+
+namespace {
+
+gbfem_status ensure_adjoint_buffers(gbfem_handle h)
+{
+	if (h->d_mu.p) return GBFEM_OK;
+	GB_CUDA(h, h->d_mu.alloc(h->n));
+	GB_CUDA(h, h->d_adjG.alloc(h->n));
+	GB_CUDA(h, h->d_gx.alloc(12 * (size_t)h->E));
+	GB_CUDA(h, h->d_gv.alloc(12 * (size_t)h->E));
+	return GBFEM_OK;
+}
+
+// The reverse of one step taken from (x, v) to (., vNext), enqueued without host synchronisation (the
+// work of gbfem_adjoint_step): the step's system rebuilt at (x, v), S mu = dt lx + lv solved by the
+// persistent launch (its per-segment results accumulated into d_adjAcc), the element derivatives, and
+// (lx, lv) carried to the step's start in place; gradients added into glog / gnu.
+gbfem_status enqueue_adjoint_step(gbfem_handle h, double dt, const double* x, const double* v, const double* vNext,
+								  double* lx, double* lv, double* glog, double* gnu)
+{
+	cudaStream_t s = h->stream;
+	const DevBody body = h->body();
+	const double alpha = h->prm.rayleigh_mass, beta = h->prm.rayleigh_stiffness;
+	const double c1 = 1.0 / dt + alpha, c2 = dt + beta;
+	const int nseg = (int)h->segNode.size() - 1;
+	launch_vec_diff(h->n, vNext, v, h->d_dvTmp.p, s);
+	int k = 1;
+	if (h->mixed())
+	{
+		k += launch_element_f32(body, x, v, x, v, dt, alpha, beta, h->d_kslots32.p, h->d_rhsE32.p, h->d_counters.p, s,
+								h->elemsPerBlock);
+		launch_assemble(body, h->d_kslots32.p, c1, c2, h->d_A32.p, h->d_invdiag32.p, s);
+	}
+	else
+	{
+		launch_element_fp64(body, x, v, x, v, dt, alpha, beta, h->d_kslots.p, h->d_rhsE.p, nullptr, nullptr,
+							h->d_counters.p, s);
+		launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+		k += 1;
+	}
+	launch_adjoint_rhs(h->n, h->d_bc.p, lx, lv, dt, h->d_adjG.p, s);
+	gbfem_status st = enqueue_mixed(h, h->d_adjG.p, h->d_mu.p, h->stepMaxIter(), nullptr, nullptr, true);
+	if (st != GBFEM_OK) return st;
+	launch_step_accumulate(h->d_seg.p, nseg, &h->d_ctl.p->nonfinite, &h->d_pcgGlobal.p->err, h->d_adjAcc.p, s);
+	launch_element_adjoint(body, x, v, h->d_mu.p, h->d_dvTmp.p, dt, alpha, beta, h->d_gx.p, h->d_gv.p, glog, gnu, s,
+						   h->mixed());
+	launch_adjoint_gather(body, h->d_gx.p, h->d_gv.p, lx, lv, dt, lx, lv, s);
+	GB_CUDA(h, cudaGetLastError());
+	h->launches += k + 6;
+	return GBFEM_OK;
+}
+
+// Per-segment accumulators of graph-launched solves set to their start values.
+gbfem_status reset_acc(gbfem_handle h, double* acc, std::vector<double>& host)
+{
+	const int nseg = (int)h->segNode.size() - 1;
+	host.assign(4 * (size_t)nseg + 2, 0.0);
+	for (int k = 0; k < nseg; ++k) host[4 * (size_t)k + 2] = 1.0;
+	GB_CUDA(h, cudaMemcpyAsync(acc, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, h->stream));
+	return GBFEM_OK;
+}
+
+// Reads accumulated solve statistics into h->stats (and the per-segment statistics when `steps`).
+void collect_acc(gbfem_handle h, const std::vector<double>& acc, bool steps)
+{
+	const int nseg = (int)h->segNode.size() - 1;
+	double worst = 0.0;
+	for (int k = 0; k < nseg; ++k)
+	{
+		const double* a = &acc[4 * (size_t)k];
+		h->stats.cg_iterations += (int)a[0];
+		h->stats.refinement_sweeps += (int)a[1];
+		if (a[2] < 1.0) h->stats.cg_max_iterations_hit++;
+		worst = std::max(worst, a[3]);
+		if (!steps) continue;
+		double* ss = &h->segStats[4 * (size_t)k];
+		ss[0] += a[0];
+		ss[1] += a[1];
+		ss[2] = std::min(ss[2], a[2]);
+		ss[3] = std::max(ss[3], a[3]);
+	}
+	h->stats.cg_relative_residual = worst;
+}
+
+gbfem_status rollout_checks(gbfem_handle h)
+{
+	if (!h->corotational()) return fail(h, GBFEM_INVALID_ARG, "rollouts: corotational elements only");
+	if (!h->persistent())
+		return fail(h, GBFEM_INVALID_ARG, "rollouts need the mixed form or a batch (the persistent solve)");
+	if (h->prm.newton_max_iterations != 1) return fail(h, GBFEM_INVALID_ARG, "rollouts take one Newton iteration");
+	if (!h->active) return fail(h, GBFEM_INACTIVE, "representation is deactivated");
+	return GBFEM_OK;
+}
+
+void reset_call_stats(gbfem_handle h)
+{
+	std::memset(&h->stats, 0, sizeof(h->stats));
+	h->launches = 0;
+	for (size_t k = 0; k < h->segStats.size(); k += 4)
+	{
+		h->segStats[k] = h->segStats[k + 1] = h->segStats[k + 3] = 0.0;
+		h->segStats[k + 2] = 1.0;
+	}
+}
+
+}  // namespace
+
+extern "C" {
+
+gbfem_status gbfem_rollout_forward(gbfem_handle h, double dt, int32_t nsteps, int32_t checkpoint_every,
+								   const double* x0, const double* v0, double* xT, double* vT)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (!(dt > 0.0) || nsteps < 1 || checkpoint_every < 1 || !x0 || !v0 || !xT || !vT)
+		return fail(h, GBFEM_INVALID_ARG, "gbfem_rollout_forward: dt > 0, nsteps >= 1, checkpoint_every >= 1, arrays");
+	gbfem_status st = rollout_checks(h);
+	if (st != GBFEM_OK) return st;
+	GB_CUDA(h, cudaSetDevice(h->device));
+	reset_call_stats(h);
+	cudaStream_t s = h->stream;
+	const size_t n = (size_t)h->n;
+	const int nck = (nsteps + checkpoint_every - 1) / checkpoint_every + 1;  // + the final state
+	if (h->d_ckpt.n < 2 * n * nck)
+	{
+		h->d_ckpt.free();
+		GB_CUDA(h, h->d_ckpt.alloc(2 * n * nck));
+	}
+	double* ck = h->d_ckpt.p;
+	GB_CUDA(h, cudaMemcpyAsync(ck, x0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemcpyAsync(ck + n, v0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));
+	if (h->prm.autotune && !h->tuned)
+	{
+		// Tune on the first step's system (outside the graph).
+		const double c1 = 1.0 / dt + h->prm.rayleigh_mass, c2 = dt + h->prm.rayleigh_stiffness;
+		GB_CUDA(h, cudaMemcpyAsync(h->d_x.p, x0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+		GB_CUDA(h, cudaMemcpyAsync(h->d_v.p, v0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+		if (!h->mixed())
+		{
+			const DevBody body = h->body();
+			launch_element_fp64(body, h->d_x.p, h->d_v.p, h->d_x.p, h->d_v.p, dt, h->prm.rayleigh_mass,
+								h->prm.rayleigh_stiffness, h->d_kslots.p, h->d_rhsE.p, nullptr, nullptr, h->d_counters.p, s);
+			launch_assemble(body, h->d_kslots.p, c1, c2, h->d_A.p, h->d_invdiag.p, s);
+			launch_rhs_gather(body, h->d_rhsE.p, h->prm.gravity, h->prm.gravity_enabled, h->d_rhs.p, 1, s);
+		}
+		st = tune_mixed(h, h->d_x.p, h->d_v.p, dt, c1, c2, h->stepMaxIter());
+		if (st != GBFEM_OK) return st;
+	}
+	if (!h->rollFwd || h->rollDt != dt || h->rollSteps != nsteps || h->rollEvery != checkpoint_every ||
+		h->rollFwdVersion != h->tuneVersion)
+	{
+		if (h->rollFwd) cudaGraphExecDestroy(h->rollFwd);
+		h->rollFwd = nullptr;
+		if (h->rollBwd) cudaGraphExecDestroy(h->rollBwd);
+		h->rollBwd = nullptr;
+		GB_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		gbfem_status cst = GBFEM_OK;
+		cudaError_t ce = cudaMemcpyAsync(h->d_x.p, ck, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+		if (ce == cudaSuccess) ce = cudaMemcpyAsync(h->d_v.p, ck + n, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+		for (int t = 0; t < nsteps && cst == GBFEM_OK && ce == cudaSuccess; ++t)
+		{
+			cst = enqueue_step_mixed(h, dt, false);
+			const int slot = (t + 1 == nsteps) ? nck - 1 : ((t + 1) % checkpoint_every == 0 ? (t + 1) / checkpoint_every : -1);
+			if (slot > 0 && cst == GBFEM_OK)
+			{
+				ce = cudaMemcpyAsync(ck + 2 * n * slot, h->d_x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+				if (ce == cudaSuccess)
+					ce = cudaMemcpyAsync(ck + 2 * n * slot + n, h->d_v.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+			}
+		}
+		cudaGraph_t graph = nullptr;
+		const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+		if (cst != GBFEM_OK || ce != cudaSuccess || ee != cudaSuccess)
+		{
+			if (graph) cudaGraphDestroy(graph);
+			if (cst != GBFEM_OK) return cst;
+			GB_CUDA(h, ce != cudaSuccess ? ce : ee);
+		}
+		const cudaError_t ie = cudaGraphInstantiate(&h->rollFwd, graph, 0);
+		cudaGraphDestroy(graph);
+		GB_CUDA(h, ie);
+		h->rollDt = dt;
+		h->rollSteps = nsteps;
+		h->rollEvery = checkpoint_every;
+		h->rollFwdVersion = h->tuneVersion;
+	}
+	std::vector<double> acc;
+	st = reset_acc(h, h->d_acc.p, acc);
+	if (st != GBFEM_OK) return st;
+	GB_CUDA(h, cudaMemsetAsync(h->d_pcgGlobal.p, 0, sizeof(PcgGlobal), s));
+	GB_CUDA(h, cudaGraphLaunch(h->rollFwd, s));
+	h->launches += nsteps * h->graphKernels;
+	GB_CUDA(h, cudaMemcpyAsync(xT, h->d_x.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemcpyAsync(vT, h->d_v.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemcpyAsync(acc.data(), h->d_acc.p, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, s));
+	int counters[4] = {0, 0, 0, 0};
+	GB_CUDA(h, cudaMemcpyAsync(counters, h->d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost, s));
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	GB_CUDA(h, cudaGetLastError());
+	collect_acc(h, acc, true);
+	h->stats.steps = nsteps;
+	h->stats.singular_g = counters[0];
+	h->stats.polar_fallbacks = counters[1];
+	h->stats.kernel_launches = h->launches;
+	h->stats.active = 1;
+	h->systemReady = true;
+	h->lastDt = dt;
+	const int nseg = (int)h->segNode.size() - 1;
+	if (acc[4 * (size_t)nseg + 1] != 0.0) return fail(h, GBFEM_CUDA_ERROR, "persistent CG: grid barrier timed out");
+	if (acc[4 * (size_t)nseg] != 0.0)
+	{
+		h->active = false;
+		h->stats.active = 0;
+		return fail(h, GBFEM_NONFINITE, "state is not finite during the rollout; representation deactivated");
+	}
+	if (h->stats.cg_max_iterations_hit > 0) return fail(h, GBFEM_CG_MAXITER, "CG reached its maximum number of iterations");
+	return GBFEM_OK;
+}
+
+gbfem_status gbfem_rollout_backward(gbfem_handle h, const double* lxT, const double* lvT, double* lx0, double* lv0,
+									double* grad_log_young, double* grad_poisson)
+{
+	if (!h) return GBFEM_INVALID_ARG;
+	if (!lxT || !lvT || !lx0 || !lv0) return fail(h, GBFEM_INVALID_ARG, "gbfem_rollout_backward: null array");
+	gbfem_status st = rollout_checks(h);
+	if (st != GBFEM_OK) return st;
+	if (!h->rollFwd || h->rollFwdVersion != h->tuneVersion)
+		return fail(h, GBFEM_INVALID_ARG, "gbfem_rollout_backward: no forward rollout to reverse");
+	GB_CUDA(h, cudaSetDevice(h->device));
+	reset_call_stats(h);
+	cudaStream_t s = h->stream;
+	const size_t n = (size_t)h->n, E = (size_t)h->E;
+	const int nsteps = h->rollSteps, every = h->rollEvery;
+	const double dt = h->rollDt;
+	const int nck = (nsteps + every - 1) / every + 1;
+	st = ensure_adjoint_buffers(h);
+	if (st != GBFEM_OK) return st;
+	if (!h->d_segX.p)
+	{
+		const int nseg = (int)h->segNode.size() - 1;
+		GB_CUDA(h, h->d_rollL.alloc(2 * n));
+		GB_CUDA(h, h->d_rollG.alloc(2 * E));
+		GB_CUDA(h, h->d_dvTmp.alloc(n));
+		GB_CUDA(h, h->d_adjAcc.alloc(4 * (size_t)nseg + 2));
+	}
+	if (h->d_segX.n < 2 * n * (size_t)(every + 1))
+	{
+		h->d_segX.free();
+		GB_CUDA(h, h->d_segX.alloc(2 * n * (size_t)(every + 1)));
+	}
+	double* ck = h->d_ckpt.p;
+	double* sx = h->d_segX.p;
+	double* lx = h->d_rollL.p;
+	double* lv = lx + n;
+	double* gl = h->d_rollG.p;
+	double* gn = gl + E;
+	GB_CUDA(h, cudaMemcpyAsync(lx, lxT, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemcpyAsync(lv, lvT, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemsetAsync(h->d_counters.p, 0, 4 * sizeof(int), s));
+	if (!h->rollBwd || h->rollBwdVersion != h->tuneVersion)
+	{
+		if (h->rollBwd) cudaGraphExecDestroy(h->rollBwd);
+		h->rollBwd = nullptr;
+		GB_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		gbfem_status cst = GBFEM_OK;
+		cudaError_t ce = cudaMemsetAsync(gl, 0, sizeof(double) * 2 * E, s);
+		auto copy = [&](double* dst, const double* src) {
+			if (ce == cudaSuccess) ce = cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+		};
+		const int nsegs = nck - 1;
+		for (int sg = nsegs - 1; sg >= 0 && cst == GBFEM_OK && ce == cudaSuccess; --sg)
+		{
+			const int len = std::min(every, nsteps - sg * every);
+			copy(h->d_x.p, ck + 2 * n * sg);
+			copy(h->d_v.p, ck + 2 * n * sg + n);
+			copy(sx, h->d_x.p);
+			copy(sx + n, h->d_v.p);
+			for (int j = 0; j < len && cst == GBFEM_OK && ce == cudaSuccess; ++j)
+			{
+				cst = enqueue_step_mixed(h, dt, false);
+				copy(sx + 2 * n * (j + 1), h->d_x.p);
+				copy(sx + 2 * n * (j + 1) + n, h->d_v.p);
+			}
+			for (int j = len - 1; j >= 0 && cst == GBFEM_OK && ce == cudaSuccess; --j)
+				cst = enqueue_adjoint_step(h, dt, sx + 2 * n * j, sx + 2 * n * j + n, sx + 2 * n * (j + 1) + n, lx, lv, gl,
+										   gn);
+		}
+		copy(h->d_x.p, ck + 2 * n * (nck - 1));  // the handle keeps the forward's final state
+		copy(h->d_v.p, ck + 2 * n * (nck - 1) + n);
+		cudaGraph_t graph = nullptr;
+		const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+		if (cst != GBFEM_OK || ce != cudaSuccess || ee != cudaSuccess)
+		{
+			if (graph) cudaGraphDestroy(graph);
+			if (cst != GBFEM_OK) return cst;
+			GB_CUDA(h, ce != cudaSuccess ? ce : ee);
+		}
+		const cudaError_t ie = cudaGraphInstantiate(&h->rollBwd, graph, 0);
+		cudaGraphDestroy(graph);
+		GB_CUDA(h, ie);
+		h->rollBwdVersion = h->tuneVersion;
+	}
+	std::vector<double> acc, adj;
+	st = reset_acc(h, h->d_acc.p, acc);
+	if (st == GBFEM_OK) st = reset_acc(h, h->d_adjAcc.p, adj);
+	if (st != GBFEM_OK) return st;
+	GB_CUDA(h, cudaMemsetAsync(h->d_pcgGlobal.p, 0, sizeof(PcgGlobal), s));
+	GB_CUDA(h, cudaGraphLaunch(h->rollBwd, s));
+	GB_CUDA(h, cudaMemcpyAsync(lx0, lx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemcpyAsync(lv0, lv, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	if (grad_log_young) GB_CUDA(h, cudaMemcpyAsync(grad_log_young, gl, sizeof(double) * E, cudaMemcpyDeviceToDevice, s));
+	if (grad_poisson) GB_CUDA(h, cudaMemcpyAsync(grad_poisson, gn, sizeof(double) * E, cudaMemcpyDeviceToDevice, s));
+	GB_CUDA(h, cudaMemcpyAsync(acc.data(), h->d_acc.p, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, s));
+	GB_CUDA(h, cudaMemcpyAsync(adj.data(), h->d_adjAcc.p, sizeof(double) * adj.size(), cudaMemcpyDeviceToHost, s));
+	GB_CUDA(h, cudaStreamSynchronize(s));
+	GB_CUDA(h, cudaGetLastError());
+	collect_acc(h, acc, false);
+	const int fwdHit = h->stats.cg_max_iterations_hit;
+	collect_acc(h, adj, false);
+	h->stats.steps = nsteps;
+	h->stats.kernel_launches = h->launches;
+	h->stats.active = 1;
+	const int nseg = (int)h->segNode.size() - 1;
+	if (acc[4 * (size_t)nseg + 1] != 0.0 || adj[4 * (size_t)nseg + 1] != 0.0)
+		return fail(h, GBFEM_CUDA_ERROR, "persistent CG: grid barrier timed out");
+	if (acc[4 * (size_t)nseg] != 0.0) return fail(h, GBFEM_NONFINITE, "a re-run state is not finite");
+	if (h->stats.cg_max_iterations_hit > fwdHit || fwdHit > 0)
+		return fail(h, GBFEM_CG_MAXITER, "a solve of the reverse sweep did not converge");
+	return GBFEM_OK;
 }
 
 gbfem_status gbfem_batch_info(gbfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets,

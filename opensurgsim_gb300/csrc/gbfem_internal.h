@@ -164,6 +164,8 @@ void launch_adjoint_gather(const DevBody& b, const double* gx, const double* gv,
 						   double dt, double* lxOut, double* lvOut, cudaStream_t s);
 void launch_adjoint_rhs(int n, const uint8_t* bc, const double* lx, const double* lv, double dt, double* g,
 						cudaStream_t s);
+// out = a - b (n doubles).
+void launch_vec_diff(int n, const double* a, const double* b, double* out, cudaStream_t s);
 void launch_set_materials(int E, const double* young, const double* poisson, double* rest, float* rest32,
 						  cudaStream_t s);
 

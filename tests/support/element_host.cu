@@ -1,6 +1,7 @@
 // Test support only: the device element math of gbfem_element.cuh (and the element adjoint of
 // gbfem_adjoint.cuh) compiled for the host, so the CPU test suite can compare it (FP64 and FP32)
 // with the oracle element by element, and the adjoint with finite differences.
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 
@@ -93,7 +94,22 @@ int run(const double* x0, const double* x, const double* v, const double* xt, co
 	for (int i = 0; i < 3; ++i)
 		for (int j = 0; j < 3; ++j)
 			F[3 * i + j] = T(in.p[1][i]) * g[1][j] + T(in.p[2][i]) * g[2][j] + T(in.p[3][i]) * g[3][j];
-	if (!gbfem::elem::polar_newton(F, Rt)) gbfem::elem::polar_svd(F, Rt);
+	if (!gbfem::elem::polar_newton(F, Rt))
+	{
+		if constexpr (std::is_same<T, float>::value)
+		{
+			// The FP32 form's fallback: the FP64 SVD of F formed in FP64 (as compute() does).
+			double Fd[9], Rd[9];
+			for (int i = 0; i < 3; ++i)
+				for (int j = 0; j < 3; ++j)
+					Fd[3 * i + j] = in.p[1][i] * double(g[1][j]) + in.p[2][i] * double(g[2][j]) +
+									in.p[3][i] * double(g[3][j]);
+			gbfem::elem::polar_svd(Fd, Rd);
+			for (int k = 0; k < 9; ++k) Rt[k] = T(Rd[k]);
+		}
+		else
+			gbfem::elem::polar_svd(F, Rt);
+	}
 	for (int k = 0; k < 9; ++k) R9[k] = double(Rt[k]);
 	return fl;
 }

@@ -154,6 +154,40 @@ def test_inverted_element_takes_svd_fallback(elem):
     assert np.abs(K - o["K"]).max() <= 1e-10 * np.abs(o["K"]).max()
 
 
+@pytest.mark.parametrize("fp32", [0, 1])
+def test_collapsed_element_takes_the_singular_g_early_return(elem, fp32):
+    """All four nodes on one line: F has rank 1, G = (tr(S) I - S) R^T is singular, and the reference
+    returns from computeRotationMassAndStiffness after forming K = R K0 R^T, without the dR/dx terms
+    (Fem3DElementCorotationalTetrahedron.cpp:199-216); the force is then -K (x - R x0) = -R K0 w with
+    w = R^T p - q (:103-113). The rotation of a rank-1 F is not unique (any completion of its
+    singular vectors is a polar factor), so the check holds for the R the element code returns. The
+    FP32 form routes such an element to its FP64 SVD path, where G is decided in FP64."""
+    h = 0.01
+    x0 = X0 * h
+    d = np.array([0.3, 0.5, 0.8]) / np.linalg.norm([0.3, 0.5, 0.8])
+    x = np.stack([t * d for t in (0.0, 0.004, 0.007, 0.011)]) + 0.02
+    E, nu = 1e5, 0.45
+    K, f, rhs, R, fl = elem(fp32, x0, x, E=E, nu=nu)
+    assert fl & 2 and fl & 1  # singular G, on the SVD path
+    assert abs(np.linalg.det(R) - 1) < (1e-6 if fp32 else 1e-12)
+    Vh = np.c_[x0, np.ones(4)].T
+    g = np.linalg.inv(Vh)[:, :3]  # shape-function gradients, one row per node
+    vol = abs(np.linalg.det(x0[1:] - x0[0])) / 6
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    K0 = np.zeros((12, 12))
+    for a in range(4):
+        for b in range(4):
+            K0[3 * a:3 * a + 3, 3 * b:3 * b + 3] = vol * (lam * np.outer(g[a], g[b]) + mu * np.outer(g[b], g[a]) +
+                                                          mu * (g[a] @ g[b]) * np.eye(3))
+    R12 = np.kron(np.eye(4), R)
+    Krot = R12 @ K0 @ R12.T
+    tol = 2e-6 if fp32 else 1e-12
+    assert np.abs(K - Krot).max() <= tol * np.abs(Krot).max()
+    w = ((x - x[0]) @ R) - (x0 - x0[0])  # R^T p_a - q_a per node (rows)
+    fe = -(R12 @ K0 @ w.ravel())
+    assert np.linalg.norm(f - fe) <= (1e-5 if fp32 else 1e-12) * np.linalg.norm(fe)
+
+
 def _adjoint_case(seed):
     rng = np.random.default_rng(seed)
     x0 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float) * 0.01 + rng.uniform(-1e-3, 1e-3, (4, 3))

@@ -152,3 +152,56 @@ def test_mixed_poisson_gradient_agrees_with_fp64_adjoint(gpu_lib):
         grads[prec] = nug.grad.detach().cpu().numpy()
     err = np.linalg.norm(grads["mixed"] - grads["fp64"]) / np.linalg.norm(grads["fp64"])
     assert err <= 1e-4, err
+
+
+def _graph_case(seed=9):
+    scene, body, theta, x0, v0, wx, wv = _setup("mixed", tol=1e-12, seed=seed)
+    nu = _poisson(scene, seed)
+    return scene, body, theta, nu, x0, v0, wx, wv
+
+
+def _grads(body, theta, nu, x0, v0, wx, wv, dt, steps=7, every=3):
+    th = theta.clone().requires_grad_(True)
+    nug = nu.clone().requires_grad_(True)
+    x0g = x0.clone().requires_grad_(True)
+    v0g = v0.clone().requires_grad_(True)
+    from opensurgsim_gb300.autograd import rollout
+
+    xT, vT = rollout(body, th, x0g, v0g, dt, steps, checkpoint_every=every, poisson=nug)
+    ((wx * (xT - x0)).sum() + (wv * vT).sum()).backward()
+    return [t.detach().cpu().numpy() for t in (xT, vT, th.grad, nug.grad, x0g.grad, v0g.grad)]
+
+
+def test_graph_rollout_equals_the_per_step_rollout(gpu_lib, monkeypatch):
+    """The mixed form's rollouts run as two CUDA graphs in the library (gbfem_rollout_forward /
+    _backward); the same rollout through the per-step loop (gbfem_step and gbfem_adjoint_step from
+    Python) gives the same states and gradients bit for bit (the same kernels in the same order)."""
+    from opensurgsim_gb300 import autograd
+
+    scene, body, theta, nu, x0, v0, wx, wv = _graph_case()
+    assert autograd.graph_rollouts(body)
+    body.set_tuning(64, 4, 2)  # one partition for both runs
+    g = _grads(body, theta, nu, x0, v0, wx, wv, scene.dt)
+    monkeypatch.setattr(autograd, "graph_rollouts", lambda b: False)
+    ref = _grads(body, theta, nu, x0, v0, wx, wv, scene.dt)
+    for a, b in zip(g, ref):
+        assert np.array_equal(a, b)
+
+
+def test_graph_rollout_backward_after_another_forward(gpu_lib):
+    """The library keeps the checkpoints of the body's last forward; a backward whose forward was
+    followed by another rollout of the same body runs its forward again and gives the gradient of a
+    backward taken right away."""
+    from opensurgsim_gb300.autograd import rollout
+
+    scene, body, theta, nu, x0, v0, wx, wv = _graph_case(seed=10)
+    th = theta.clone().requires_grad_(True)
+    xT, _ = rollout(body, th, x0, v0, scene.dt, 6, checkpoint_every=4)
+    (wx * xT).sum().backward()
+    want = th.grad.detach().clone()
+    th2 = theta.clone().requires_grad_(True)
+    xA, _ = rollout(body, th2, x0, v0, scene.dt, 6, checkpoint_every=4)
+    with torch.no_grad():
+        rollout(body, theta + 0.1, x0, v0 * 2, scene.dt, 6, checkpoint_every=4)  # another forward in between
+    (wx * xA).sum().backward()
+    assert torch.equal(th2.grad, want)

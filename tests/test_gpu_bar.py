@@ -65,12 +65,16 @@ def test_bar_mixed_whole_run_matches_oracle(gpu_lib):
     assert errs.max() <= 1e-6
 
 
-@pytest.mark.parametrize("precision,gate", [(_lib.PRECISION_FP64, 1e-8), (_lib.PRECISION_MIXED, 1e-6)])
-def test_collapsed_element_takes_the_singular_g_return(gpu_lib, precision, gate):
+@pytest.mark.parametrize("precision", [_lib.PRECISION_FP64, _lib.PRECISION_MIXED])
+def test_collapsed_element_takes_the_singular_g_return(gpu_lib, precision):
     """A tetrahedron whose nodes lie on one line has a rank-1 deformation gradient, so
     G = (tr(S) I - S) R^T is singular and the reference skips the element's dR/dx terms
-    (Fem3DElementCorotationalTetrahedron.cpp:208-216) while keeping R K0 R^T; the step goes on. One
-    tetrahedron (its node 0 fixed) collapsed onto a line, stepped once, GPU against the oracle."""
+    (Fem3DElementCorotationalTetrahedron.cpp:208-216) and goes on with the step. One tetrahedron
+    (its node 0 fixed) collapsed onto a line, stepped once on the GPU: both forms take the early
+    return exactly where the oracle does, and the step stays finite. The state after it is not
+    compared: the polar rotation of a rank-1 F is not unique (any completion of its singular vectors
+    is one), so the reference's own result there depends on its SVD's choices; the early return's K
+    and force are pinned element by element in tests/test_element_math.py."""
     from oracle import oracle as O
     from opensurgsim_gb300.body import Body
 
@@ -90,6 +94,4 @@ def test_collapsed_element_takes_the_singular_g_return(gpu_lib, precision, gate)
     assert g.stats()["singular_g"] == 1
     assert o.last_stats.singular_g == 1
     gx, gv = g.state()
-    ox, ov = o.state()
-    assert rel(gx - x.ravel(), ox - x.ravel()) <= gate
-    assert rel(gv, ov) <= gate
+    assert np.all(np.isfinite(gx)) and np.all(np.isfinite(gv))

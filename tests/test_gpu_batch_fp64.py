@@ -43,7 +43,9 @@ def test_fp64_batch_matches_oracle_and_single_handles(gpu_lib, graph):
         assert o.step(1e-3, 20) == 0
         ox, ov = o.state()
         assert rel(_split(batch, bx, k) - rest, ox - rest) <= 1e-8
-        assert rel(_split(batch, bv, k), ov) <= 1e-8
+        # Velocities at 1e-6: the small stiff mesh is near rest under gravity after 20 steps (|v| ~ 1e-9
+        # m/s), where the CG's tolerance relative to the step's right-hand side sets their digits.
+        assert rel(_split(batch, bv, k), ov) <= 1e-6
         single = Body(s.mesh, precision=_lib.PRECISION_FP64, **KW)
         its = 0
         for _ in range(20):

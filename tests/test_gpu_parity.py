@@ -224,32 +224,39 @@ def _rotation(axis, degrees):
     return np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * (K @ K)
 
 
+@pytest.mark.parametrize("precision,gate", [(_lib.PRECISION_MIXED, 1e-6), (_lib.PRECISION_FP64, 1e-8)])
 @pytest.mark.parametrize("offset", [0.0, 10.0])
-def test_mixed_form_under_large_rigid_motion(gpu_lib, offset):
+def test_large_rigid_motion(gpu_lib, offset, precision, gate):
     """The mesh rotated 75 degrees about a skew axis and moved `offset` metres away (1,000 element
-    sizes at 10 m). The FP32 element update forms the edges and the strain's Gram differences in
-    double-float, so a rigid motion reads as no strain (nothing moves), and a small strain on top of
-    it steps as the oracle's FP64 step does. Measured relative displacement errors: 3.3e-7 at the
-    origin, 1.04e-6 at 10 m, against 3.3e-7 and 1.03e-6 with FP64 edges and Gram differences (the
-    earlier form of the kernel), hence the 10 m bound."""
+    sizes at 10 m). A rigid motion reads as no strain (nothing moves). A small strain on top of it
+    steps as the oracle steps the same strained, rotated mesh at the origin: the step is invariant
+    under translation, and the GPU forms work on positions relative to an element's node 0 (the
+    mixed form's edges and strain Gram differences in double-float), so they keep it. The oracle
+    restates the reference's formula, which works on absolute positions: its own FP64 rounding moves
+    its result by ~1e-6 between the origin and 10 m (tests/test_oracle_solver.py pins this), so the
+    translation-free result is the oracle's at the origin."""
     s = mesh.scene_cube(3, 3, 4, seed=2)
-    kw = dict(precision=_lib.PRECISION_MIXED, gravity=(0.0, 0.0, 0.0), cg_tolerance=1e-10)
+    kw = dict(precision=precision, gravity=(0.0, 0.0, 0.0), cg_tolerance=1e-12)
     X = s.mesh.nodes
-    xr = (X @ _rotation((1, 2, 3), 75).T + offset).ravel()
+    R = _rotation((1, 2, 3), 75)
+    xr = (X @ R.T + offset).ravel()
     v0 = np.zeros_like(xr)
     g = Body.from_scene(s, **kw)
     g.set_state(xr, v0)
     assert g.step(1e-3, 2) == _lib.GBFEM_OK
     gx, gv = g.state()
     assert np.abs(gx - xr).max() < 1e-11 and np.abs(gv).max() < 1e-8
-    # A small strain on the rotated, moved mesh: the mixed step against the oracle.
-    rng = np.random.default_rng(8)
-    x = xr + rng.normal(0, 1e-5, xr.shape)
+    # A small strain on the rotated, moved mesh; the oracle steps the same strain at the origin.
+    noise = np.random.default_rng(8).normal(0, 1e-5, xr.shape)
+    x = xr + noise
+    x_origin = (X @ R.T).ravel() + noise
     g = Body.from_scene(s, **kw)
     o = O.OracleModel.from_scene(s, gravity=kw["gravity"], cg_tolerance=kw["cg_tolerance"])
-    for m in (g, o):
-        m.set_state(x, v0)
+    g.set_state(x, v0)
+    o.set_state(x_origin, v0)
     assert g.step(1e-3, 3) == _lib.GBFEM_OK and o.step(1e-3, 3) == 0
     gx, _ = g.state()
     ox, _ = o.state()
-    assert rel(gx - x, ox - x) < (1e-6 if offset == 0.0 else 1.5e-6), rel(gx - x, ox - x)
+    err = rel(gx - x, ox - x_origin)
+    print(f"offset {offset} m: rel disp err {err:.2e}")
+    assert err <= gate, err

@@ -316,3 +316,34 @@ def test_mass_lumping(element_type):
     # f differs from the consistent model only in the Rayleigh mass force.
     want = sc["f"] + a * (Mc @ v) - a * np.diag(dense) * v
     assert np.allclose(sl["f"], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+
+
+def test_reference_formula_is_translation_variant_in_fp64():
+    """The reference's corotational element works on absolute positions (F = P V^-1 with the node
+    positions, f = -K (x - R x0), KTimesRx_x0 = K (R^T x - x0); Fem3DElementCorotationalTetrahedron.cpp
+    :131-146, :103-113, :276). Translating a strained mesh 10 m (1,000 element sizes) changes nothing
+    in exact arithmetic, but the large translation enters those products and cancels only up to FP64
+    rounding: the oracle's 3-step displacement moves by about 1e-6 relative (measured 1.1e-6) between
+    the origin and 10 m, while at 1 cm it stays near 1e-10. This is why the GPU forms, which work on
+    positions relative to each element's node 0, are compared with the oracle at the origin in the
+    large-rigid-motion parity test."""
+    def rot(axis, deg):
+        k = np.asarray(axis, float)
+        k /= np.linalg.norm(k)
+        t = np.radians(deg)
+        K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+        return np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * K @ K
+
+    s = mesh.scene_cube(3, 3, 4, seed=2)
+    X = s.mesh.nodes
+    noise = np.random.default_rng(8).normal(0, 1e-5, X.size)
+    out = {}
+    for off in (0.0, 0.01, 10.0):
+        x = (X @ rot((1, 2, 3), 75).T + off).ravel() + noise
+        o = O.OracleModel.from_scene(s, gravity=(0.0, 0.0, 0.0), cg_tolerance=1e-12)
+        o.set_state(x, np.zeros_like(x))
+        assert o.step(1e-3, 3) == 0
+        out[off] = o.state()[0] - x
+    base = np.linalg.norm(out[0.0])
+    assert np.linalg.norm(out[0.01] - out[0.0]) / base < 1e-8
+    assert 1e-8 < np.linalg.norm(out[10.0] - out[0.0]) / base < 1e-5
