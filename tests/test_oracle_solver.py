@@ -323,8 +323,9 @@ def test_reference_formula_is_translation_variant_in_fp64():
     positions, f = -K (x - R x0), KTimesRx_x0 = K (R^T x - x0); Fem3DElementCorotationalTetrahedron.cpp
     :131-146, :103-113, :276). Translating a strained mesh 10 m (1,000 element sizes) changes nothing
     in exact arithmetic, but the large translation enters those products and cancels only up to FP64
-    rounding: the oracle's 3-step displacement moves by about 1e-6 relative (measured 1.1e-6) between
-    the origin and 10 m, while at 1 cm it stays near 1e-10. This is why the GPU forms, which work on
+    rounding: the oracle's 3-step displacement moves by about 1e-6 relative (measured 7.5e-7 at CG
+    tolerance 1e-12) between the origin and 10 m, 7.4e-9 at 1 m and 2.2e-12 at 1 cm. This is why the
+    GPU forms, which work on
     positions relative to each element's node 0, are compared with the oracle at the origin in the
     large-rigid-motion parity test."""
     def rot(axis, deg):
