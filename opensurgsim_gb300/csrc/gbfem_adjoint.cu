@@ -117,7 +117,8 @@ __global__ void k_adjoint_rhs(int n, const uint8_t* __restrict__ bc, const doubl
 	if (i < n) g[i] = bc[i] ? 0.0 : dt * lx[i] + lv[i];
 }
 
-// Per-element moduli: lambda V and mu V from E and nu (nu kept from the current moduli when null).
+// Per-element moduli: lambda V and mu V from E and nu (the host passes its stored per-element nu when
+// the caller gives none; deriving nu from the rounded lambda V, mu V would drift it call by call).
 __global__ void k_set_materials(int E, const double* __restrict__ young, const double* __restrict__ poisson,
 								double* __restrict__ rest, float* __restrict__ rest32)
 {

@@ -137,6 +137,7 @@ struct gbfem_handle_s
 	std::vector<int> adjPtr, adj;  // node adjacency incl. self (sorted) = BSR structure
 	std::vector<double> cmass;     // per element rho V / 20 (consistent mass coefficient)
 	std::vector<uint8_t> bcMask;
+	std::vector<double> poissonHost;  // tetrahedra: per-element nu at creation (gbfem_set_materials_device)
 
 	// device
 	DevBuf<int4> d_tets;
@@ -459,6 +460,7 @@ gbfem_status rebuild_hex_operators(gbfem_handle h)
 gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 {
 	const int N = m->num_nodes, E = m->num_tets;
+	if (!h->hex()) h->poissonHost.assign(m->poisson_ratio, m->poisson_ratio + E);
 	h->N = N;
 	h->E = E;
 	h->n = 3 * N;
@@ -1965,7 +1967,15 @@ gbfem_status gbfem_set_materials_device(gbfem_handle h, const double* young, con
 									   h->stream));
 		return rebuild_hex_operators(h);
 	}
-	launch_set_materials(h->E, young, poisson, h->d_rest.p, h->mixed() ? h->d_rest32.p : nullptr, h->stream);
+	if (!h->d_poisson.p)
+	{
+		// Each element's Poisson ratio as given (at creation or by the last call that set it), so that
+		// a call that changes only E does not derive nu again from the rounded lambda V, mu V.
+		GB_CUDA(h, h->d_poisson.upload(h->poissonHost.data(), h->poissonHost.size(), h->stream));
+	}
+	if (poisson)
+		GB_CUDA(h, cudaMemcpyAsync(h->d_poisson.p, poisson, sizeof(double) * h->E, cudaMemcpyDeviceToDevice, h->stream));
+	launch_set_materials(h->E, young, h->d_poisson.p, h->d_rest.p, h->mixed() ? h->d_rest32.p : nullptr, h->stream);
 	h->linearReady = false;  // the stored linear system no longer matches
 	GB_CUDA(h, cudaGetLastError());
 	GB_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -73,7 +73,7 @@ def test_fp64_batch_graph_steps_equal_plain_steps(gpu_lib):
 
 
 def test_fp64_batch_autotunes_and_adjoint_runs(gpu_lib):
-    """The autotuner picks the FP64 solve's CTAs per SM (the FP64 kernel fits at most 3); the adjoint
+    """The autotuner picks the FP64 solve's CTAs per SM among those that fit; the adjoint
     step of a batch solves its transposed system with the same persistent launch and matches the
     mixed batch's gradient within 1e-4."""
     torch = pytest.importorskip("torch")
@@ -84,7 +84,7 @@ def test_fp64_batch_autotunes_and_adjoint_runs(gpu_lib):
     b = Body([s.mesh for s in scenes], precision=_lib.PRECISION_FP64, autotune=True, **KW)
     assert b.step(1e-3, 2) == _lib.GBFEM_OK
     eb, cps, rw = b.tuning()
-    assert cps in (1, 2, 3)
+    assert cps in (1, 2, 3, 4)
     grads = {}
     dev = torch.device("cuda:0")
     for prec in ("fp64", "mixed"):
