@@ -44,6 +44,13 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 CG_CAP = 10000
 BAR_SCENARIO_STEPS = 200  # --config bar --steps 200: the whole compression scenario, both forms
+# Cube edge of the bar. The scenario leaves it open; the driven face moves 0.64 edges a step whatever h
+# is, an elastic wave crosses sqrt(E/rho) dt / h edges a step. At 4 mm the 50 ramp steps stay
+# well-posed (the timed window), but in the hold phase elements invert by the hundred thousand and the
+# FP64 CG stops converging (measured on GB300: ~3,000 iterations a step from step ~60, the FP64 state
+# non-finite by step ~120); the whole 200-step scenario runs at 2 mm.
+BAR_H_WINDOW = 0.004
+BAR_H_FULL = 0.002
 BATCH = dict(count=256, lo=500, hi=50000, seed=3)
 BATCH_PARAMS = dict(rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0.0, 0.0, -9.81), cg_tolerance=1e-10)
 COMPARE_STEPS = 4  # steps of the per-mesh FP64 path's timing (1 untimed + 3 timed)
@@ -458,7 +465,7 @@ def run_batch(args, rank, world, local, dist):
 HEX_NODES_PER_AXIS = 64  # --config hex: 63^3 = 250,047 hexahedra, 262,144 nodes
 
 
-def build_scene(config):
+def build_scene(config, h=None):
     from opensurgsim_gb300 import mesh
 
     if config == "hex":
@@ -469,7 +476,7 @@ def build_scene(config):
     # The explicit CG iteration cap only bounds the run if a solve ever stagnates; at the
     # benchmark's states CG converges in a few hundred iterations, far below it.
     if config == "bar":
-        return mesh.scene_bar_compression(cg_max_iterations=CG_CAP)
+        return mesh.scene_bar_compression(h=h or BAR_H_WINDOW, cg_max_iterations=CG_CAP)
     return mesh.scene_cube(10, 10, 10, cg_max_iterations=CG_CAP)
 
 
@@ -482,7 +489,7 @@ def run_single(args, rank, world, local, dist):
 
     build.build()
     torch.cuda.set_device(local)
-    scene = build_scene(args.config)
+    scene = build_scene(args.config, args.bar_h)
     m = scene.mesh
     log(f"scene {scene.name}: {m.num_tets} tets, {m.num_nodes} nodes")
     prec = _lib.PRECISION_MIXED if args.precision == "mixed" else _lib.PRECISION_FP64
@@ -653,9 +660,10 @@ def run_bar_full(args, rank, world, local, dist):
 
     build.build()
     torch.cuda.set_device(local)
-    scene = build_scene("bar")
+    scene = build_scene("bar", args.bar_h or BAR_H_FULL)
     m = scene.mesh
-    log(f"bar full run: {m.num_tets} tets, {m.num_nodes} nodes, {args.steps} steps, both forms")
+    log(f"bar full run: {m.num_tets} tets, {m.num_nodes} nodes, h {scene.mesh.h * 1e3:g} mm, {args.steps} steps, "
+        "both forms")
     bodies = {"fp64": Body.from_scene(scene, precision=_lib.PRECISION_FP64, device=local),
               "mixed": Body.from_scene(scene, precision=_lib.PRECISION_MIXED, device=local, autotune=True)}
     flags = {"fp64": 0, "mixed": _lib.STEP_GRAPH}
@@ -747,7 +755,8 @@ def run_bar_full(args, rank, world, local, dist):
         "warmup": args.warmup, "ms_per_step": ms["mixed"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded cube-grid mesh)",
         "config": {
-            "workload": ("bar40x40x160 (h 4 mm) whole scenario: 20% compression ramp over 50 steps, then held; "
+            "workload": (f"bar40x40x160 (h {scene.mesh.h * 1e3:g} mm) whole scenario: 20% compression ramp over 50 "
+                         "steps, then held; "
                          f"{args.steps} steps from rest; 1,280,000 tets, 270,641 nodes, E log-U[1e4,1e6], "
                          "nu U[0.40,0.49], gravity, dt 1e-3, CG tol 1e-10; plain FP64 and mixed forms side by side"),
             "elements": m.num_tets, "nodes": m.num_nodes, "dofs": bm.n, "nnz": bm.nnz, "precision": "mixed",
@@ -1130,7 +1139,7 @@ def run_reference(args, rank, world):
         split = phase_split([sum(m.last_step_times()[i] for m in models) for i in range(3)],
                             "CPU seconds of the last step summed over the meshes")
     else:
-        scene = build_scene(args.config)
+        scene = build_scene(args.config, args.bar_h)
         model = O.OracleModel.from_scene(scene)
         budget_s = float(os.environ.get("GBFEM_REFERENCE_BUDGET_S", "150"))
         step = 0
@@ -1184,6 +1193,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 path comparison (batch)")
     ap.add_argument("--meshes", type=int, default=BATCH["count"], help="batch size (smaller cases for profiling)")
+    ap.add_argument("--bar-h", type=float, default=None,
+                    help=f"bar cube edge in m (default {BAR_H_WINDOW} for a step window, {BAR_H_FULL} for the whole run)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -265,14 +265,30 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 		tk = __shfl_sync(kFull, tk, 0);
 		if (tk != (unsigned)(fl.y - fl.x)) return;
 		__syncwarp();
-		double tot[NV];
+		// The CTAs' partials, lane l adding CTAs bf + 1 + l, bf + 33 + l, ... in that order; the loads of
+		// four rounds (and of every value) are issued before they are added, since a segment can span
+		// every CTA of the grid (one large mesh: ~20 partials a lane).
+		double u[NV], tot[NV];
 #pragma unroll
-		for (int k = 0; k < NV; ++k)
+		for (int k = 0; k < NV; ++k) u[k] = (lane == 0) ? __ldcg(&a.slots[(size_t)(2 * k + 1) * G + fl.x]) : 0.0;
+		int b = fl.x + 1 + lane;
+		for (; b + 96 <= fl.y; b += 128)
 		{
-			double u = (lane == 0) ? __ldcg(&a.slots[(size_t)(2 * k + 1) * G + fl.x]) : 0.0;
-			for (int b = fl.x + 1 + lane; b <= fl.y; b += 32) u += __ldcg(&a.slots[(size_t)(2 * k) * G + b]);
-			tot[k] = warp_sum(u);
+			double t[NV][4];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+#pragma unroll
+				for (int j = 0; j < 4; ++j) t[k][j] = __ldcg(&a.slots[(size_t)(2 * k) * G + b + 32 * j]);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+#pragma unroll
+				for (int j = 0; j < 4; ++j) u[k] += t[k][j];
 		}
+		for (; b <= fl.y; b += 32)
+#pragma unroll
+			for (int k = 0; k < NV; ++k) u[k] += __ldcg(&a.slots[(size_t)(2 * k) * G + b]);
+#pragma unroll
+		for (int k = 0; k < NV; ++k) tot[k] = warp_sum(u[k]);
 		if (lane == 0)
 		{
 			a.seg[s].ticket = 0u;
