@@ -700,17 +700,20 @@ def run_bar_full(args, rank, world, local, dist):
     statuses = {k: set() for k in bodies}
     errs = []
     u64n = []
+    per_step = {k: [] for k in bodies}  # (status, CG iterations, SVD fallbacks) per step
     for s in range(args.steps):
         for k, b in bodies.items():
             drive(b, s)
             e0, e1 = evs[k][s]
             e0.record(streams[k])
             timing = _lib.STEP_TIME_KERNELS if k == "mixed" else 0  # the persistent solve's own events
-            statuses[k].add(int(b.step(scene.dt, 1, flags[k] | timing)))
+            status = int(b.step(scene.dt, 1, flags[k] | timing))
+            statuses[k].add(status)
             e1.record(streams[k])
             st = b.stats()
             for key in agg[k]:
                 agg[k][key] += st[key]
+            per_step[k].append((status, st["cg_iterations"], st["polar_fallbacks"]))
         # Relative displacement error of the mixed form against the FP64 form, on the device.
         u64 = views["fp64"][0] - rest
         d = views["mixed"][0] - views["fp64"][0]
@@ -750,6 +753,11 @@ def run_bar_full(args, rank, world, local, dist):
     achieved = per_launch / (solve_ms / 1e3) / 1e9 if solve_ms > 0 else None
     errs_a = np.array(errs)
     ramp_end = min(scene.ramp_steps, args.steps)
+    # The first step whose FP64 solve stopped at its iteration cap: from there the FP64 reference's
+    # own step no longer converges (the scene's hold phase inverts elements by the hundred thousand and
+    # the tangent stops being positive definite), and the two forms follow diverging trajectories.
+    cap64 = next((i for i, r in enumerate(per_step["fp64"]) if r[0] != 0), None)
+    well_posed = errs_a[:cap64] if cap64 is not None else errs_a
     line = {
         "metric": METRIC, "value": val["mixed"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms["mixed"] / args.steps, "higher_is_better": True,
@@ -787,7 +795,10 @@ def run_bar_full(args, rank, world, local, dist):
             "max": float(errs_a.max()), "final": float(errs_a[-1]), "max_ramp": float(errs_a[:ramp_end].max()),
             "max_hold": float(errs_a[ramp_end:].max()) if args.steps > ramp_end else None,
             "every_10_steps": [float(e) for e in errs_a[9::10]],
+            "first_step_fp64_not_converged": cap64,
+            "max_while_fp64_converges": float(well_posed.max()) if well_posed.size else None,
             "definition": "||u_mixed - u_fp64|| / ||u_fp64||, u = x - x_rest, after every step"},
+        "per_step_every_10": {k: [list(r) for r in v[9::10]] for k, v in per_step.items()},
         "inversions": {"polar_fallbacks_fp64": agg["fp64"]["polar_fallbacks"],
                        "polar_fallbacks_mixed": am["polar_fallbacks"],
                        "singular_g_fp64": agg["fp64"]["singular_g"], "singular_g_mixed": am["singular_g"],
@@ -879,12 +890,17 @@ def run_adjoint(args, local):
         sec_fwd = time.perf_counter() - t0
         # Phase split of the adjoint steps of the last (first-in-time) checkpoint segment: the stats
         # restart at every forward step, so they hold that segment's adjoint steps.
-        th = theta.clone().requires_grad_(True)
-        loss(body, th, _lib.STEP_TIME_PHASES).backward()
-        st = body.stats()
-        nadj = min(ADJ_CHECKPOINT, ADJ_STEPS)
-        split = {"system_ms": st["ms_element"] / nadj, "transposed_solve_ms": st["ms_solve"] / nadj,
-                 "element_derivatives_ms": st["ms_update"] / nadj}
+        from opensurgsim_gb300.autograd import graph_rollouts
+
+        if graph_rollouts(body):
+            split = {"how": "forward and backward each run as one CUDA graph in the library; no per-phase times"}
+        else:
+            th = theta.clone().requires_grad_(True)
+            loss(body, th, _lib.STEP_TIME_PHASES).backward()
+            st = body.stats()
+            nadj = min(ADJ_CHECKPOINT, ADJ_STEPS)
+            split = {"system_ms": st["ms_element"] / nadj, "transposed_solve_ms": st["ms_solve"] / nadj,
+                     "element_derivatives_ms": st["ms_update"] / nadj}
         results[p] = {"loss": Lval, "grad": g, "sec": sec, "sec_forward": sec_fwd, "split": split}
         log(f"adjoint {p}: forward+backward {sec:.3f} s, forward {sec_fwd:.3f} s, loss {Lval:.6e}, split {split}")
     # Central finite differences in log E on 32 random elements (FP64 form).
