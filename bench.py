@@ -780,7 +780,8 @@ def run_bar_full(args, rank, world, local, dist):
                 "how": f"{e2e_steps} hold steps after the timed run, host clock"},
         "roofline": {
             "kernel": "k_pcg_persistent (mixed)", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": load_traffic("pcg_persistent_bar"),
+            "frac": (achieved / peak) if achieved else None,
+            "traffic": load_traffic("pcg_persistent_bar") if abs(scene.mesh.h - BAR_H_WINDOW) < 1e-12 else None,
             "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": solve_ms,
             "peak_source": f"{peak_kind} (hbm_gbs)",
             "bytes_model": ("CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*n) + refreshes x "
