@@ -46,11 +46,12 @@ CG_CAP = 10000
 BAR_SCENARIO_STEPS = 200  # --config bar --steps 200: the whole compression scenario, both forms
 # Cube edge of the bar. The scenario leaves it open; the driven face moves 0.64 edges a step whatever h
 # is, an elastic wave crosses sqrt(E/rho) dt / h edges a step. At 4 mm the 50 ramp steps stay
-# well-posed (the timed window), but in the hold phase elements invert by the hundred thousand and the
-# FP64 CG stops converging (measured on GB300: ~3,000 iterations a step from step ~60, the FP64 state
-# non-finite by step ~120); the whole 200-step scenario runs at 2 mm.
+# well-posed. In the hold phase of the whole 200-step scenario, elements invert by the hundred
+# thousand (per-element E spans two decades, nu reaches 0.49) and the FP64 CG stops converging (on
+# GB300: from step ~60 at 4 mm, ~130 at 2 mm, the trajectories diverging after); the whole-scenario run
+# reports the step where the FP64 solve first fails and the error up to it.
 BAR_H_WINDOW = 0.004
-BAR_H_FULL = 0.002
+BAR_H_FULL = 0.004
 BATCH = dict(count=256, lo=500, hi=50000, seed=3)
 BATCH_PARAMS = dict(rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0.0, 0.0, -9.81), cg_tolerance=1e-10)
 COMPARE_STEPS = 4  # steps of the per-mesh FP64 path's timing (1 untimed + 3 timed)
