@@ -244,26 +244,6 @@ __device__ __forceinline__ void for_chunks(const SetView& V, const int* sc, int 
 	}
 }
 
-// The SpMV phase's work items: each chunk of the CTA's range as two half-chunks of 16 rows (a warp
-// runs a half-chunk with two lanes per row, each lane taking every other block column), drawn from
-// the shared counter like for_chunks. f(slot, s, c, half): slot = chunk position - lo.
-template <typename F>
-__device__ __forceinline__ void for_half_chunks(const SetView& V, const int* sc, int nseg, int* next, F f)
-{
-	const int lane = threadIdx.x & 31;
-	const int lo2 = 2 * V.lo, hi2 = 2 * V.hi;
-	for (;;)
-	{
-		int k = 0;
-		if (lane == 0) k = atomicAdd(next, 1);
-		const int t2 = lo2 + __shfl_sync(kFull, k, 0);
-		if (t2 >= hi2) return;
-		const int t = t2 >> 1;
-		const int s = seg_of(V.Cp, nseg, t);
-		f(t - V.lo, s, sc[s] + (t - V.Cp[s]), t2 & 1);
-	}
-}
-
 // Reduce this CTA's chunk partials per segment (sp[k * M + slot]) and complete segments across
 // CTAs; fin(s, totals) runs once per segment in lane 0 of one warp of the completing CTA. The
 // segments of the CTA's range are independent: warp w takes the range's segments w, w + 8, ...
@@ -352,38 +332,59 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 	}
 }
 
-// Half-chunk SpMV (phase 1): q(row) = sum over the row's SELL slots of A_block p(J), with
-// p(J) = z(J) + beta p_old(J) formed on the fly from the packed records. Row m of chunk c, this lane's
-// block columns k0 + h, k0 + h + 2, ... (h the lane's column parity); the caller adds the partner
-// lane's sums (lane ^ 1). Three of the lane's columns per round (four spill at 64 registers), their
-// loads issued before any is used; the round count is the same in every lane (the larger share), the
-// last round predicated. The matrix (values, columns) is read once per pass with the streaming hint
-// (evict first), so L2 keeps the gathered z/p records, which rows a mesh layer apart reuse.
-__device__ __forceinline__ void spmv_half_zp(const PcgArgs& a, const float4* __restrict__ zp, int c, int m, int h,
-											 float beta, float& a0, float& a1, float& a2)
+// q[row] (3 floats) = sum over the chunk's SELL slots of A_block * p(J), with p(J) = z(J) + beta p_old(J)
+// formed on the fly from the packed records; four slots' loads are issued before any is used. The
+// matrix (values, columns) is read once per pass with the streaming hint (evict first), so L2 keeps
+// the gathered z/p records, which rows a mesh layer apart reuse.
+__device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __restrict__ zp, int c, int lane,
+											float beta, float& a0, float& a1, float& a2)
 {
 	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
-	const int nmax = (k1 - k0 + 1) >> 1;      // columns of the h = 0 lane
-	const int nmine = (k1 - k0 + 1 - h) >> 1;  // this lane's
-	for (int j = 0; j < nmax; j += 3)
+	int k = k0;
+	for (; k + 4 <= k1; k += 4)
+	{
+		int J[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
+		float4 zj[4], pj[4];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			zj[u] = zp[2 * J[u]];
+			pj[u] = zp[2 * J[u] + 1];
+		}
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+		{
+			const float* vb = a.val + (size_t)(k + u) * 288 + lane;
+			const float p0 = zj[u].x + beta * pj[u].x, p1 = zj[u].y + beta * pj[u].y, p2 = zj[u].z + beta * pj[u].z;
+			a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
+			a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
+			a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
+		}
+	}
+	// The last 1 to 3 slots in one round as well (the count is the same in every lane), instead of
+	// one dependent column -> record -> value chain each.
+	const int rem = k1 - k;
+	if (rem > 0)
 	{
 		int J[3];
 		float4 zj[3], pj[3];
 #pragma unroll
 		for (int u = 0; u < 3; ++u)
-			if (j + u < nmine) J[u] = __ldcs(&a.col[(k0 + h + 2 * (j + u)) * 32 + m]);
+			if (u < rem) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
 #pragma unroll
 		for (int u = 0; u < 3; ++u)
-			if (j + u < nmine)
+			if (u < rem)
 			{
 				zj[u] = zp[2 * J[u]];
 				pj[u] = zp[2 * J[u] + 1];
 			}
 #pragma unroll
 		for (int u = 0; u < 3; ++u)
-			if (j + u < nmine)
+			if (u < rem)
 			{
-				const float* vb = a.val + (size_t)(k0 + h + 2 * (j + u)) * 288 + m;
+				const float* vb = a.val + (size_t)(k + u) * 288 + lane;
 				const float p0 = zj[u].x + beta * pj[u].x, p1 = zj[u].y + beta * pj[u].y, p2 = zj[u].z + beta * pj[u].z;
 				a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
 				a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
@@ -392,24 +393,24 @@ __device__ __forceinline__ void spmv_half_zp(const PcgArgs& a, const float4* __r
 	}
 }
 
-// FP64 form of the half-chunk SpMV (records {z0 z1 | z2 - | p0 p1 | p2 -}), two columns a round (80
-// registers at three CTAs per SM).
-__device__ __forceinline__ void spmv_half_zp64(const PcgArgs& a, const double2* __restrict__ zp, int c, int m, int h,
-											   double beta, double& a0, double& a1, double& a2)
+// FP64 form: the same product on the FP64 values, p(J) = z(J) + beta p_old(J) from the 64-byte
+// records {z0 z1 | z2 - | p0 p1 | p2 -}; two slots' loads issued before either is used (four need
+// 124 registers, or spill at three CTAs per SM).
+__device__ __forceinline__ void spmv_row_zp64(const PcgArgs& a, const double2* __restrict__ zp, int c, int lane,
+											  double beta, double& a0, double& a1, double& a2)
 {
 	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
-	const int nmax = (k1 - k0 + 1) >> 1;
-	const int nmine = (k1 - k0 + 1 - h) >> 1;
-	for (int j = 0; j < nmax; j += 2)
+	for (int k = k0; k < k1; k += 2)
 	{
+		const int nk = min(2, k1 - k);
 		int J[2];
+#pragma unroll
+		for (int u = 0; u < 2; ++u)
+			if (u < nk) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
 		double2 r0[2], r1[2], r2[2], r3[2];
 #pragma unroll
 		for (int u = 0; u < 2; ++u)
-			if (j + u < nmine) J[u] = __ldcs(&a.col[(k0 + h + 2 * (j + u)) * 32 + m]);
-#pragma unroll
-		for (int u = 0; u < 2; ++u)
-			if (j + u < nmine)
+			if (u < nk)
 			{
 				r0[u] = zp[4 * J[u]];
 				r1[u] = zp[4 * J[u] + 1];
@@ -418,9 +419,9 @@ __device__ __forceinline__ void spmv_half_zp64(const PcgArgs& a, const double2* 
 			}
 #pragma unroll
 		for (int u = 0; u < 2; ++u)
-			if (j + u < nmine)
+			if (u < nk)
 			{
-				const double* vb = a.val64 + (size_t)(k0 + h + 2 * (j + u)) * 288 + m;
+				const double* vb = a.val64 + (size_t)(k + u) * 288 + lane;
 				const double p0 = r0[u].x + beta * r2[u].x, p1 = r0[u].y + beta * r2[u].y, p2 = r1[u].x + beta * r3[u].x;
 				a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
 				a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
@@ -830,67 +831,44 @@ __global__ void __launch_bounds__(kPcgThreads, kF64 ? 3 : 4) k_pcg_persistent(Pc
 		phase_start(true, false);
 		if (finished >= nseg) break;
 		cache_segments(actW);
-		for_half_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c, int half) {
-			// Half-chunk item: rows half * 16 + (lane >> 1) of chunk c, two lanes per row (column parity
-			// lane & 1); the even lane of each pair finishes the row.
-			const int m = half * 16 + (lane >> 1), hp = lane & 1;
-			const int rs = 32 * c + m;
+		for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
+			const int rs = 32 * c + lane;
 			double part, betaD, alphaU, sU, ratioU;
 			int mode;
 			seg_scalars(s, betaD, mode, alphaU, sU, ratioU);
 			if constexpr (kF64)
 			{
 				double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-				spmv_half_zp64(a, zOld64, c, m, hp, betaD, a0, a1, a2);
-				a0 += __shfl_xor_sync(kFull, a0, 1);
-				a1 += __shfl_xor_sync(kFull, a1, 1);
-				a2 += __shfl_xor_sync(kFull, a2, 1);
-				double t = 0.0;
-				if (hp == 0)
-				{
-					const double2 z01 = zOld64[4 * rs], z2 = zOld64[4 * rs + 1], p01 = zOld64[4 * rs + 2],
-								  p2 = zOld64[4 * rs + 3];
-					const double n0 = z01.x + betaD * p01.x, n1 = z01.y + betaD * p01.y, n2 = z2.x + betaD * p2.x;
-					zNew64[4 * rs + 2] = make_double2(n0, n1);
-					zNew64[4 * rs + 3] = make_double2(n2, 0.0);
-					__stcs(&a.q64[3 * rs], a0);
-					__stcs(&a.q64[3 * rs + 1], a1);
-					__stcs(&a.q64[3 * rs + 2], a2);
-					t = n0 * a0 + n1 * a1 + n2 * a2;
-				}
-				part = warp_sum(t);
+				spmv_row_zp64(a, zOld64, c, lane, betaD, a0, a1, a2);
+				const double2 z01 = zOld64[4 * rs], z2 = zOld64[4 * rs + 1], p01 = zOld64[4 * rs + 2],
+							  p2 = zOld64[4 * rs + 3];
+				const double n0 = z01.x + betaD * p01.x, n1 = z01.y + betaD * p01.y, n2 = z2.x + betaD * p2.x;
+				zNew64[4 * rs + 2] = make_double2(n0, n1);
+				zNew64[4 * rs + 3] = make_double2(n2, 0.0);
+				__stcs(&a.q64[3 * rs], a0);
+				__stcs(&a.q64[3 * rs + 1], a1);
+				__stcs(&a.q64[3 * rs + 2], a2);
+				part = warp_sum(n0 * a0 + n1 * a1 + n2 * a2);
 			}
 			else if (mode == 0)
 			{
 				const float beta = float(betaD);
 				float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-				spmv_half_zp(a, zpOld, c, m, hp, beta, a0, a1, a2);
-				a0 += __shfl_xor_sync(kFull, a0, 1);
-				a1 += __shfl_xor_sync(kFull, a1, 1);
-				a2 += __shfl_xor_sync(kFull, a2, 1);
-				float t = 0.f;
-				if (hp == 0)
-				{
-					const float4 zi = zpOld[2 * rs], pi = zpOld[2 * rs + 1];
-					const float4 pn = make_float4(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z, 0.f);
-					zpNew[2 * rs + 1] = pn;
-					__stcs(&a.q[3 * rs], a0);
-					__stcs(&a.q[3 * rs + 1], a1);
-					__stcs(&a.q[3 * rs + 2], a2);
-					t = pn.x * a0 + pn.y * a1 + pn.z * a2;
-				}
-				part = warp_sum(t);
+				spmv_row_zp(a, zpOld, c, lane, beta, a0, a1, a2);
+				const float4 zi = zpOld[2 * rs], pi = zpOld[2 * rs + 1];
+				const float4 pn = make_float4(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z, 0.f);
+				zpNew[2 * rs + 1] = pn;
+				__stcs(&a.q[3 * rs], a0);
+				__stcs(&a.q[3 * rs + 1], a1);
+				__stcs(&a.q[3 * rs + 2], a2);
+				part = warp_sum(pn.x * a0 + pn.y * a1 + pn.z * a2);
 			}
 			else
-			{
-				// The true residual keeps one lane per row: the whole chunk in its first half's item.
-				part = (half == 0) ? warp_sum(residual_row(a, c, 32 * c + lane, lane)) : 0.0;
-			}
-			if (lane == 0) sp[half * M + slot] = part;
+				part = warp_sum(residual_row(a, c, rs, lane));
+			if (lane == 0) sp[slot] = part;
 		});
-		reduce_segments<2>(a, actW, sc, sp, [&](int s, const double* tot2) {
+		reduce_segments<1>(a, actW, sc, sp, [&](int s, const double* tot) {
 			SegCtl& S = a.seg[s];
-			const double tot[1] = {tot2[0] + tot2[1]};  // the chunks' first and second halves
 			if (S.mode == 0)
 			{
 				S.pq = tot[0];
