@@ -63,9 +63,18 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 	const double lamV = b.rest[13 * E + e], muV = b.rest[14 * E + e], cm = b.rest[15 * E + e];
 	const bool moduli = gLogE || gNu;
 	double pl = 0.0, pm = 0.0;
-	for (int item = 0; item < (moduli ? adj::kAdjItems : adj::kAdjItems - 1); ++item)
-		adj::adjoint_item<S>(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
-							 gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
+	S Rw[9];
+	const int rflags = adj::element_rotation<S>(nd, X, R0, g, Rw);
+	// The nine dual passes share one body (a loop, not unrolled); the velocity and modulus items follow.
+#pragma unroll 1
+	for (int item = 0; item < 9; ++item)
+		adj::adjoint_item<S>(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags,
+							 gx + (size_t)e * 12, gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
+	adj::adjoint_item<S>(9, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags, gx + (size_t)e * 12,
+						 gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
+	if (moduli)
+		adj::adjoint_item<S>(10, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags,
+							 gx + (size_t)e * 12, gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
 	if (!moduli) return;
 	// lambda V and mu V are both proportional to E: d/d log E scales each by one.
 	if (gLogE) gLogE[e] += lamV * pl + muV * pm;

@@ -13,7 +13,8 @@ namespace adj {
 
 // psi_e = mu_e . rhs_e - c2 <K_e's lower-triangle blocks, (mu, dv)>; the stored blocks are the
 // element's diagonal node blocks (read lower-triangular, like the assembled matrix) and, per node
-// pair, the block whose row node has the larger id.
+// pair, the block whose row node has the larger id. This form reads stored arrays (host checks);
+// the adjoint kernel contracts the blocks as the element code produces them (PsiOut).
 template <typename T>
 __host__ __device__ T element_psi(const int (&nd)[4], const T* ks, const T* rhs, const double (&mu)[12], const double (&dv)[12],
 						 double c2)
@@ -51,6 +52,76 @@ __host__ __device__ T element_psi(const int (&nd)[4], const T* ks, const T* rhs,
 	return s - T(c2) * sk;
 }
 
+// The two sums of psi_e = s - c2 sk, accumulated as compute_to() delivers the element's right-hand
+// side (s = mu_e . rhs_e) and stored blocks (sk, the coefficients of element_psi), so that no block
+// is held: an output policy of compute_to().
+template <typename T>
+struct PsiOut
+{
+	using G = typename elem::ScalarOf<T>::type;
+	G mu[12], dv[12];  // in the passes' arithmetic (FP32 for the mixed form's passes)
+	T s = T(0), sk = T(0);
+	static constexpr bool kAll = false;
+	__host__ __device__ __forceinline__ PsiOut(const double (&MU)[12], const double (&DV)[12])
+	{
+#pragma unroll
+		for (int j = 0; j < 12; ++j)
+		{
+			mu[j] = G(MU[j]);
+			dv[j] = G(DV[j]);
+		}
+	}
+	__host__ __device__ __forceinline__ bool blocks() const { return true; }
+	__host__ __device__ __forceinline__ void rhs_entry(int j, const T& v) { s = s + v * mu[j]; }
+	__host__ __device__ __forceinline__ void block(int a, int b, int, const T (&blk)[9])
+	{
+		if (a == b)
+		{
+#pragma unroll
+			for (int i = 0; i < 3; ++i)
+#pragma unroll
+				for (int j = 0; j <= i; ++j)
+				{
+					const G c = mu[3 * a + i] * dv[3 * a + j] + (i != j ? mu[3 * a + j] * dv[3 * a + i] : G(0));
+					sk = sk + blk[3 * i + j] * c;
+				}
+		}
+		else
+		{
+#pragma unroll
+			for (int i = 0; i < 3; ++i)
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+				{
+					const G c = mu[3 * a + i] * dv[3 * b + j] + mu[3 * b + j] * dv[3 * a + i];
+					sk = sk + blk[3 * i + j] * c;
+				}
+		}
+	}
+	__host__ __device__ __forceinline__ void full_block(int, int, const T (&)[9]) {}
+	__host__ __device__ __forceinline__ T psi(double c2) const { return s - G(c2) * sk; }
+};
+
+// (K_e^T mu_e)_c = sum_r K_e(r, c) mu_r over the full element tangent, accumulated in FP64 in r order
+// as compute_to() delivers its 16 blocks: an output policy of compute_to().
+template <typename T>
+struct KtMuOut
+{
+	const double (&mu)[12];
+	double kt[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	static constexpr bool kAll = true;
+	__host__ __device__ __forceinline__ bool blocks() const { return false; }
+	__host__ __device__ __forceinline__ void rhs_entry(int, const T&) {}
+	__host__ __device__ __forceinline__ void block(int, int, int, const T (&)[9]) {}
+	__host__ __device__ __forceinline__ void full_block(int a, int b, const T (&blk)[9])
+	{
+#pragma unroll
+		for (int q = 0; q < 3; ++q)
+#pragma unroll
+			for (int i = 0; i < 3; ++i) kt[3 * b + q] += double(blk[3 * i + q]) * mu[3 * a + i];
+	}
+};
+
 template <typename P>
 __host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
 						   const double (&V)[4][3], double dt, double alpha, double beta, int seedNode, int seedAxis,
@@ -68,11 +139,11 @@ __host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], co
 			const double dp = (k == seedAxis) ? (double(a == seedNode) - double(seedNode == 0)) : 0.0;
 			in.p[a][k] = P(X[a][k] - X[0][k]);
 			if constexpr (!std::is_same<P, double>::value) in.p[a][k].d = dp;
-			in.q[a][k] = P(R0[a][k] - R0[0][k]);
+			in.q[a][k] = R0[a][k] - R0[0][k];
 			const double va = V[a][k];
-			in.uK[a][k] = P(-beta * va + (0.0 - dt * va));  // x_n = x_t at the first Newton iteration
-			in.uM[a][k] = P(-alpha * va);                    // v_n = v_t
-			in.vv[a][k] = P(va);
+			in.uK[a][k] = -beta * va + (0.0 - dt * va);  // x_n = x_t at the first Newton iteration
+			in.uM[a][k] = -alpha * va;                    // v_n = v_t
+			in.vv[a][k] = va;
 		}
 	}
 	in.alphaDbg = alpha;
@@ -85,31 +156,51 @@ __host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], co
 // gradient, item 10 the two unit-modulus evaluations.
 constexpr int kAdjItems = 11;
 
+// The element's rotation in the passes' arithmetic S (row-major) and its polar flags, as the
+// element code forms them: computed once and shared by every item of the element.
+template <typename S = double>
+__host__ __device__ inline int element_rotation(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
+												const double (&g)[4][3], S (&R)[9])
+{
+	elem::ElemIn in;
+	const double zero[4][3] = {};
+	fill_input(in, nd, X, R0, zero, 0.0, 0.0, 0.0, -1, -1);
+	S gS[4][3], F[9];
+	for (int a = 0; a < 4; ++a)
+		for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
+	elem::deformation<S, false>(in, gS, F);
+	return elem::rotation<S, false>(in, gS, F, R);
+}
+
 // One item of one element: X, R0, V positions / rest positions / velocities of its nodes, MU and DV
-// the adjoint and the step's velocity increment at its dofs (zero on BC dofs). Writes gx[3 + item]
-// (items 0..8), gv[0..11] (item 9) or *pLam, *pMu (item 10).
+// the adjoint and the step's velocity increment at its dofs (zero on BC dofs), Rw and rflags the
+// element's rotation (element_rotation). Writes gx[3 + item] (items 0..8), gv[0..11] (item 9) or
+// *pLam, *pMu (item 10).
 // S is the arithmetic of the passes: double (FP64 form) or float (mixed form, FP32 element math
 // with the corotated strain formed as in its forward step).
 template <typename S = double>
 __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const double (&X)[4][3],
 											 const double (&R0)[4][3], const double (&V)[4][3], const double (&MU)[12],
 											 const double (&DV)[12], const double (&g)[4][3], double lamV, double muV,
-											 double cm, double dt, double alpha, double beta, double* gx, double* gv,
-											 double* pLam, double* pMu, bool lumped = false)
+											 double cm, double dt, double alpha, double beta, const S (&Rw)[9], int rflags,
+											 double* gx, double* gv, double* pLam, double* pMu, bool lumped = false)
 {
 	using D = ad::DualT<S>;
 	const double c2 = dt + beta;
+	S gS[4][3];
+	for (int a = 0; a < 4; ++a)
+		for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
 	if (item < 9)
 	{
-		D gD[4][3];
-		for (int a = 0; a < 4; ++a)
-			for (int k = 0; k < 3; ++k) gD[a][k] = D(g[a][k]);
+		// Only the positions carry the seeded derivative (the rotation's from polar_tangent); psi_e's
+		// sums are contracted as the blocks come out of the element code.
 		const int s = 3 + item;
 		elem::ElemInT<D> in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3, lumped);
-		D ks[kSlots * 9], rhs[12];
-		elem::compute<D, false, elem::ElemInT<D>>(in, gD, D(lamV), D(muV), D(cm), ks, 1, rhs, 1, nullptr, nullptr);
-		gx[s] = double(element_psi(nd, ks, rhs, MU, DV, c2).d);
+		PsiOut<D> out{MU, DV};
+		elem::compute_to<D, false, elem::ElemInT<D>, false>(in, gS, S(lamV), S(muV), S(cm), out, nullptr, nullptr, Rw,
+															 rflags);
+		gx[s] = double(out.psi(c2).d);
 	}
 	else if (item == 9)
 	{
@@ -117,34 +208,42 @@ __host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const
 		// 5 cm on the diagonal with mass lumping).
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
-		S gS[4][3], ks[kSlots * 9], rhs[12];
-		double kfull[144], fdbg[12];
-		for (int a = 0; a < 4; ++a)
-			for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
-		elem::compute<S, true>(in, gS, S(lamV), S(muV), S(cm), ks, 1, rhs, 1, kfull, fdbg);
+		KtMuOut<S> out{MU};
+		elem::compute_to<S, false, elem::ElemIn, false, KtMuOut<S>, true>(in, gS, S(lamV), S(muV), S(cm), out, nullptr,
+																		   nullptr, Rw, rflags);
 		double sm[3] = {0, 0, 0};
 		for (int a = 0; a < 4; ++a)
 			for (int k = 0; k < 3; ++k) sm[k] += MU[3 * a + k];
 		for (int c = 0; c < 12; ++c)
-		{
-			double t = 0.0;
-			for (int r = 0; r < 12; ++r) t += kfull[r * 12 + c] * MU[r];
-			gv[c] = -c2 * t - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
-		}
+			gv[c] = -c2 * out.kt[c] - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
 	}
 	else
 	{
 		// psi_e's elastic part is linear in (lambda V, mu V): evaluate it with unit moduli.
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
-		S gS[4][3], ks[kSlots * 9], rhs[12];
-		for (int a = 0; a < 4; ++a)
-			for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
-		elem::compute<S, false>(in, gS, S(1), S(0), S(0), ks, 1, rhs, 1, nullptr, nullptr);
-		*pLam = double(element_psi(nd, ks, rhs, MU, DV, c2));
-		elem::compute<S, false>(in, gS, S(0), S(1), S(0), ks, 1, rhs, 1, nullptr, nullptr);
-		*pMu = double(element_psi(nd, ks, rhs, MU, DV, c2));
+		PsiOut<S> ol{MU, DV}, om{MU, DV};
+		elem::compute_to<S, false, elem::ElemIn, false, PsiOut<S>, true>(in, gS, S(1), S(0), S(0), ol, nullptr, nullptr,
+																		  Rw, rflags);
+		*pLam = double(ol.psi(c2));
+		elem::compute_to<S, false, elem::ElemIn, false, PsiOut<S>, true>(in, gS, S(0), S(1), S(0), om, nullptr, nullptr,
+																		  Rw, rflags);
+		*pMu = double(om.psi(c2));
 	}
+}
+
+// psi_e itself in FP64 (host checks of its derivatives), through the same contraction as the
+// derivative passes.
+__host__ __device__ inline double element_psi_value(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
+													const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],
+													const double (&g)[4][3], double lamV, double muV, double cm, double dt,
+													double alpha, double beta, bool lumped = false)
+{
+	elem::ElemIn in;
+	fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
+	PsiOut<double> out{MU, DV};
+	elem::compute_to<double, false, elem::ElemIn, false>(in, g, lamV, muV, cm, out, nullptr, nullptr);
+	return out.psi(dt + beta);
 }
 
 // Chain rule from the element's moduli to its Poisson ratio: with lambda V = V E nu / ((1 + nu)
@@ -166,8 +265,10 @@ __host__ __device__ inline void adjoint_element(const int (&nd)[4], const double
 												double alpha, double beta, double* gx, double* gv, double* pLam,
 												double* pMu, bool lumped = false)
 {
+	double Rw[9];
+	const int rflags = element_rotation(nd, X, R0, g, Rw);
 	for (int item = 0; item < kAdjItems; ++item)
-		adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu, lumped);
+		adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags, gx, gv, pLam, pMu, lumped);
 	for (int k = 0; k < 3; ++k) gx[k] = -(gx[3 + k] + gx[6 + k] + gx[9 + k]);
 }
 

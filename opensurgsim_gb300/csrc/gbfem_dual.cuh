@@ -77,23 +77,36 @@ __host__ __device__ inline DualT<S> operator/(const DualT<S>& a, const DualT<S>&
 	const S q = a.v / b.v;
 	return DualT<S>::make(q, (a.d - q * b.d) / b.v);
 }
-// Mixed operands: a plain number is a constant (zero derivative).
+// Mixed operands: a plain number is a constant (zero derivative), so only the parts that carry a
+// derivative are computed (the same values as promoting it to a dual, without the products and sums
+// with a zero derivative). The plain operand converts to S (a non-deduced parameter).
 template <typename S>
-__host__ __device__ inline DualT<S> operator+(const DualT<S>& a, double b) { return a + DualT<S>(b); }
+struct Plain
+{
+	using type = S;
+};
 template <typename S>
-__host__ __device__ inline DualT<S> operator+(double a, const DualT<S>& b) { return DualT<S>(a) + b; }
+using PlainT = typename Plain<S>::type;
 template <typename S>
-__host__ __device__ inline DualT<S> operator-(const DualT<S>& a, double b) { return a - DualT<S>(b); }
+__host__ __device__ inline DualT<S> operator+(const DualT<S>& a, PlainT<S> b) { return DualT<S>::make(a.v + b, a.d); }
 template <typename S>
-__host__ __device__ inline DualT<S> operator-(double a, const DualT<S>& b) { return DualT<S>(a) - b; }
+__host__ __device__ inline DualT<S> operator+(PlainT<S> a, const DualT<S>& b) { return DualT<S>::make(a + b.v, b.d); }
 template <typename S>
-__host__ __device__ inline DualT<S> operator*(const DualT<S>& a, double b) { return a * DualT<S>(b); }
+__host__ __device__ inline DualT<S> operator-(const DualT<S>& a, PlainT<S> b) { return DualT<S>::make(a.v - b, a.d); }
 template <typename S>
-__host__ __device__ inline DualT<S> operator*(double a, const DualT<S>& b) { return DualT<S>(a) * b; }
+__host__ __device__ inline DualT<S> operator-(PlainT<S> a, const DualT<S>& b) { return DualT<S>::make(a - b.v, -b.d); }
 template <typename S>
-__host__ __device__ inline DualT<S> operator/(const DualT<S>& a, double b) { return a / DualT<S>(b); }
+__host__ __device__ inline DualT<S> operator*(const DualT<S>& a, PlainT<S> b) { return DualT<S>::make(a.v * b, a.d * b); }
 template <typename S>
-__host__ __device__ inline DualT<S> operator/(double a, const DualT<S>& b) { return DualT<S>(a) / b; }
+__host__ __device__ inline DualT<S> operator*(PlainT<S> a, const DualT<S>& b) { return DualT<S>::make(a * b.v, a * b.d); }
+template <typename S>
+__host__ __device__ inline DualT<S> operator/(const DualT<S>& a, PlainT<S> b) { return DualT<S>::make(a.v / b, a.d / b); }
+template <typename S>
+__host__ __device__ inline DualT<S> operator/(PlainT<S> a, const DualT<S>& b)
+{
+	const S q = a / b.v;
+	return DualT<S>::make(q, -(q * b.d) / b.v);
+}
 template <typename S>
 __host__ __device__ inline bool operator<(const DualT<S>& a, const DualT<S>& b) { return a.v < b.v; }
 template <typename S>

@@ -58,8 +58,8 @@ __host__ __device__ __forceinline__ T det3(const T* X)
 	return X[0] * (X[4] * X[8] - X[5] * X[7]) - X[1] * (X[3] * X[8] - X[5] * X[6]) + X[2] * (X[3] * X[7] - X[4] * X[6]);
 }
 
-template <typename T>
-__host__ __device__ __forceinline__ void cross3(const T* a, const T* b, T* c)
+template <typename A, typename B, typename T>
+__host__ __device__ __forceinline__ void cross3(const A* a, const B* b, T* c)
 {
 	c[0] = a[1] * b[2] - a[2] * b[1];
 	c[1] = a[2] * b[0] - a[0] * b[2];
@@ -91,6 +91,27 @@ struct Eps<DualF>
 {
 	static constexpr double eps = FLT_EPSILON;
 	static constexpr double newtonTol2 = 1e-11;
+};
+
+// The plain scalar under an arithmetic type: itself, or the value type of a dual number. The rest
+// shape, the moduli and the inputs other than the positions enter compute() as plain scalars.
+template <typename T>
+struct ScalarOf
+{
+	using type = T;
+};
+template <typename S>
+struct ScalarOf<ad::DualT<S>>
+{
+	using type = S;
+};
+template <typename T>
+struct IsDual : std::false_type
+{
+};
+template <typename S>
+struct IsDual<ad::DualT<S>> : std::true_type
+{
 };
 
 // Polar factor by Newton's iteration X <- (g X + X^-T / g) / 2 (Higham), Frobenius scaling on the
@@ -247,8 +268,8 @@ __host__ __device__ void polar_svd(const T* F, T* R, T* sig = nullptr)
 }
 
 // (K0 u)_a = lambdaV tr(D) g_a + muV D^T g_a + muV sum_c G_ac u_c,  D = sum_c u_c g_c^T.
-template <typename T>
-__host__ __device__ __forceinline__ void k0_apply(const T (&g)[4][3], const T (&Gab)[4][4], T lamV, T muV, const T (&u)[4][3],
+template <typename T, typename G>
+__host__ __device__ __forceinline__ void k0_apply(const G (&g)[4][3], const G (&Gab)[4][4], G lamV, G muV, const T (&u)[4][3],
 										 T (&out)[4][3])
 {
 	T D[3][3];
@@ -271,17 +292,18 @@ __host__ __device__ __forceinline__ int pair_slot(int a, int b)
 	return (a == 0) ? (3 + b) : (a == 1 ? (5 + b) : 9);
 }
 
-// Per-element inputs gathered by the kernels (node 0 is the origin of p and q), with scalar type P
-// (double, or Dual when the adjoint seeds a derivative direction in them).
+// Per-element inputs gathered by the kernels (node 0 is the origin of p and q). The positions p have
+// scalar type P (double, or a dual type when the adjoint seeds a derivative direction in them); the
+// other inputs never carry a derivative.
 template <typename P>
 struct ElemInT
 {
 	int nd[4];
-	P p[4][3];    // x_n,a - x_n,0
-	P q[4][3];    // x0_a - x0_0
-	P uK[4][3];   // -beta v_n + (x_n - x_t - dt v_n)
-	P uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
-	P vv[4][3];   // v_n (debug force only)
+	P p[4][3];         // x_n,a - x_n,0
+	double q[4][3];    // x0_a - x0_0
+	double uK[4][3];   // -beta v_n + (x_n - x_t - dt v_n)
+	double uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
+	double vv[4][3];   // v_n (debug force only)
 	double alphaDbg, betaDbg;  // Rayleigh coefficients (debug force only)
 	int lumped = 0;  // FemRepresentation::setMassLumping: the element's mass rows summed onto the diagonal
 };
@@ -513,31 +535,27 @@ __host__ __device__ __forceinline__ float rest_edge(const ElemInF& in, int a, in
 	return a == 0 ? 0.f : in.qf32[(size_t)(3 * (a - 1) + k) * in.E + in.e];
 }
 
-// Rotation, tangent blocks and right-hand-side share of one element.
-//   ks[k * ksStride], k = slot*9 + entry: the element's lower-triangle blocks (kSlots of them);
-//   rhs[j * rhsStride], j = 3a+i: f_e + K_e uK + M0 uM (the element's share of the
-//   implicit-Euler right-hand side, OdeSolverEulerImplicit.cpp:155-158, with the Rayleigh
-//   damping force of FemRepresentation.cpp:565-629 folded in).
-// Debug outputs (double only): kfull[144] the full tangent, fdbg[12] = f_e - alpha M0 v - beta K_e v.
-// ks may be null (right-hand side only). kLinear: the linear tetrahedron of
-// Fem3DElementTetrahedron::doUpdateFMDK (Fem3DElementTetrahedron.cpp:77-90): R = I, K_e = K0,
-// f_e = -K0 (x - x0), no rotation terms.
-// Returns a bitmask: 1 = polar fallback to the FP64 SVD, 2 = singular G (extra terms skipped);
-// 4 is internal (the FP32 form's FP64 singular-G decision on the SVD path).
-template <typename T, bool kDebug, typename In = ElemIn, bool kLinear = false>
-__host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV, T cm, T* ks, int ksStride, T* rhs,
-					   int rhsStride, double* kfull, double* fdbg)
+// F = sum_a p_a g_a^T (linear part of P V^-1, Fem3DElementCorotationalTetrahedron.cpp:146).
+template <typename T, bool kLinear, typename In>
+__host__ __device__ __forceinline__ void deformation(const In& in, const typename ScalarOf<T>::type (&g)[4][3], T (&F)[9])
 {
-	int flags = 0;
-	// F = sum_a p_a g_a^T (linear part of P V^-1, Fem3DElementCorotationalTetrahedron.cpp:146).
-	T F[9];
 #pragma unroll
 	for (int i = 0; i < 3; ++i)
 #pragma unroll
 		for (int j = 0; j < 3; ++j)
 			F[3 * i + j] = edge<T, kLinear>(in, 1, i) * g[1][j] + edge<T, kLinear>(in, 2, i) * g[2][j] +
 						   edge<T, kLinear>(in, 3, i) * g[3][j];
-	T R[9];
+}
+
+// The element's rotation R (row-major, F = R S) from its deformation gradient F: Newton's polar
+// iteration, the SVD path for near-inverted or degenerate elements (always at least FP64), the
+// identity for the linear tetrahedron. Returns flags 1 (SVD path) and 4 (the FP32 form's FP64
+// singular-G decision on that path) of compute_to().
+template <typename T, bool kLinear, typename In>
+__host__ __device__ __forceinline__ int rotation(const In& in, const typename ScalarOf<T>::type (&g)[4][3], const T (&F)[9],
+												 T (&R)[9])
+{
+	int flags = 0;
 	if constexpr (kLinear)
 	{
 #pragma unroll
@@ -570,6 +588,108 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			polar_svd(F, R);
 		flags |= 1;
 	}
+	return flags;
+}
+
+// Derivative of the polar factor along a dual F: with R given (its value, row-major) and F = R S, S
+// symmetric, R^T dF - dF^T R = [(tr(S) I - S) w]x for dR = R [w]x, so w solves a 3x3 system whose
+// matrix is the element's G up to the rotation (zero derivative where that matrix is singular, where
+// the tangent's rotation terms are dropped too).
+template <typename S>
+__host__ __device__ __forceinline__ void polar_tangent(const ad::DualT<S> (&F)[9], const S* Rv, ad::DualT<S> (&R)[9])
+{
+	S A[9], Sm[9];
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			A[3 * i + j] = Rv[i] * F[j].d + Rv[3 + i] * F[3 + j].d + Rv[6 + i] * F[6 + j].d;  // R^T dF
+			Sm[3 * i + j] = Rv[i] * F[j].v + Rv[3 + i] * F[3 + j].v + Rv[6 + i] * F[6 + j].v;  // R^T F
+		}
+	const S ax[3] = {A[7] - A[5], A[2] - A[6], A[3] - A[1]};  // axial(R^T dF - dF^T R)
+	const S s01 = S(0.5) * (Sm[1] + Sm[3]), s02 = S(0.5) * (Sm[2] + Sm[6]), s12 = S(0.5) * (Sm[5] + Sm[7]);
+	const S tr = Sm[0] + Sm[4] + Sm[8];
+	const S M[9] = {tr - Sm[0], -s01, -s02, -s01, tr - Sm[4], -s12, -s02, -s12, tr - Sm[8]};
+	S C[9];
+	cofactor3(M, C);  // symmetric M: M^-1 = C / det
+	const S det = M[0] * C[0] + M[1] * C[1] + M[2] * C[2];
+	const S id = (fabs(double(det)) > 1e-12) ? S(1) / det : S(0);
+	const S w[3] = {(C[0] * ax[0] + C[1] * ax[1] + C[2] * ax[2]) * id, (C[3] * ax[0] + C[4] * ax[1] + C[5] * ax[2]) * id,
+					(C[6] * ax[0] + C[7] * ax[1] + C[8] * ax[2]) * id};
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+	{
+		const S* r = Rv + 3 * i;  // row i of R times [w]x
+		const S d[3] = {r[1] * w[2] - r[2] * w[1], r[2] * w[0] - r[0] * w[2], r[0] * w[1] - r[1] * w[0]};
+#pragma unroll
+		for (int j = 0; j < 3; ++j) R[3 * i + j] = ad::DualT<S>::make(Rv[3 * i + j], d[j]);
+	}
+}
+
+// Where compute_to() delivers an element's results. An output policy has
+//   blocks()                    whether the stored lower-triangle blocks are wanted,
+//   rhs_entry(j, v)             right-hand-side entry j = 3a+i,
+//   block(a, b, slot, blk)      stored block (a, b) (a == b, or node a's id above node b's) in slot,
+//   kAll, full_block(a, b, blk) when kAll, every one of the 16 blocks of the full tangent.
+// StoreOut writes the stored blocks and the right-hand side to strided arrays (the forward kernels).
+template <typename T>
+struct StoreOut
+{
+	T* ks;
+	int ksStride;
+	T* rhs;
+	int rhsStride;
+	static constexpr bool kAll = false;
+	__host__ __device__ __forceinline__ bool blocks() const { return ks != nullptr; }
+	__host__ __device__ __forceinline__ void rhs_entry(int j, const T& v) { rhs[j * rhsStride] = v; }
+	__host__ __device__ __forceinline__ void block(int, int, int slot, const T (&blk)[9])
+	{
+#pragma unroll
+		for (int k = 0; k < 9; ++k) ks[(slot * 9 + k) * ksStride] = blk[k];
+	}
+	__host__ __device__ __forceinline__ void full_block(int, int, const T (&)[9]) {}
+};
+
+// Rotation, tangent blocks and right-hand-side share of one element, delivered to `out`:
+//   the stored blocks: the element's lower-triangle blocks (kSlots of them);
+//   the right-hand side, j = 3a+i: f_e + K_e uK + M0 uM (the element's share of the
+//   implicit-Euler right-hand side, OdeSolverEulerImplicit.cpp:155-158, with the Rayleigh
+//   damping force of FemRepresentation.cpp:565-629 folded in).
+// Debug outputs (double only): kfull[144] the full tangent, fdbg[12] = f_e - alpha M0 v - beta K_e v.
+// kLinear: the linear tetrahedron of Fem3DElementTetrahedron::doUpdateFMDK
+// (Fem3DElementTetrahedron.cpp:77-90): R = I, K_e = K0, f_e = -K0 (x - x0), no rotation terms.
+// The shape-function gradients g, the moduli and cm, and the inputs other than the positions are
+// plain scalars G (for a dual T, its value type: only the positions carry a derivative).
+// kGivenR: the rotation's value is Rgiven with the flags rflags of rotation(), as computed by a plain
+// pass over the same element; a dual T takes its derivative from polar_tangent().
+// Returns a bitmask: 1 = polar fallback to the FP64 SVD, 2 = singular G (extra terms skipped);
+// 4 is internal (the FP32 form's FP64 singular-G decision on the SVD path).
+template <typename T, bool kDebug, typename In, bool kLinear, typename Out, bool kGivenR = IsDual<T>::value>
+__host__ __device__ int compute_to(const In& in, const typename ScalarOf<T>::type (&g)[4][3],
+								   typename ScalarOf<T>::type lamV, typename ScalarOf<T>::type muV,
+								   typename ScalarOf<T>::type cm, Out& out, double* kfull, double* fdbg,
+								   const typename ScalarOf<T>::type* Rgiven = nullptr, int rflags = 0)
+{
+	static_assert(kGivenR || !IsDual<T>::value, "a dual pass takes the rotation's value from a plain pass");
+	using G = typename ScalarOf<T>::type;
+	int flags = 0;
+	T F[9];
+	deformation<T, kLinear>(in, g, F);
+	T R[9];
+	if constexpr (kGivenR)
+	{
+		flags = rflags;
+		if constexpr (IsDual<T>::value)
+			polar_tangent(F, Rgiven, R);
+		else
+		{
+#pragma unroll
+			for (int k = 0; k < 9; ++k) R[k] = Rgiven[k];
+		}
+	}
+	else
+		flags = rotation<T, kLinear>(in, g, F, R);
 	// S = sym(R^T F), G = (tr(S) I - S) R^T (:208), G^-1 with the |det| > 1e-12 check (:210).
 	T S[9];
 #pragma unroll
@@ -632,8 +752,8 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 #pragma unroll
 			for (int i = 0; i < 3; ++i)
 			{
-				w[a][i] = R[i] * T(in.p[a][0]) + R[3 + i] * T(in.p[a][1]) + R[6 + i] * T(in.p[a][2]) - T(in.q[a][i]);
-				ut[a][i] = R[i] * T(in.uK[a][0]) + R[3 + i] * T(in.uK[a][1]) + R[6 + i] * T(in.uK[a][2]) - w[a][i];
+				w[a][i] = R[i] * T(in.p[a][0]) + R[3 + i] * T(in.p[a][1]) + R[6 + i] * T(in.p[a][2]) - G(in.q[a][i]);
+				ut[a][i] = R[i] * G(in.uK[a][0]) + R[3 + i] * G(in.uK[a][1]) + R[6 + i] * G(in.uK[a][2]) - w[a][i];
 			}
 	}
 	else
@@ -677,14 +797,14 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			for (int i = 0; i < 3; ++i)
 			{
 				w[a][i] = Em[3 * i] * rest_edge(in, a, 0) + Em[3 * i + 1] * rest_edge(in, a, 1) + Em[3 * i + 2] * rest_edge(in, a, 2);
-				ut[a][i] = R[i] * T(in.uK[a][0]) + R[3 + i] * T(in.uK[a][1]) + R[6 + i] * T(in.uK[a][2]) - w[a][i];
+				ut[a][i] = R[i] * G(in.uK[a][0]) + R[3 + i] * G(in.uK[a][1]) + R[6 + i] * G(in.uK[a][2]) - w[a][i];
 			}
 	}
 #pragma unroll
 	for (int a = 0; a < 4; ++a)
 #pragma unroll
 		for (int i = 0; i < 3; ++i) wt[a][i] = R[i] * w[a][0] + R[3 + i] * w[a][1] + R[6 + i] * w[a][2];  // R^T w
-	T Gab[4][4];
+	G Gab[4][4];
 #pragma unroll
 	for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -725,21 +845,27 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 	for (int i = 0; i < 3; ++i)
 #pragma unroll
 		for (int j = 0; j < 3; ++j) W[i][j] = g[0][i] * w[0][j] + g[1][i] * w[1][j] + g[2][i] * w[2][j] + g[3][i] * w[3][j];
-	T cbq[4][3][3];
+	// g_b x r_q for every node b and row q of R: held for the whole node loop, or (dual passes, whose
+	// per-thread state is what bounds them) formed again for each block.
+	constexpr bool kLean = IsDual<T>::value;
+	T cbq[kLean ? 1 : 4][3][3];
+	if constexpr (!kLean)
+	{
 #pragma unroll
-	for (int bb = 0; bb < 4; ++bb)
+		for (int bb = 0; bb < 4; ++bb)
 #pragma unroll
-		for (int qq = 0; qq < 3; ++qq) cross3(g[bb], &R[3 * qq], cbq[bb][qq]);
+			for (int qq = 0; qq < 3; ++qq) cross3(g[bb], &R[3 * qq], cbq[bb][qq]);
+	}
 	T Ku[4][3];
 	k0_apply(g, Gab, lamV, muV, ut, Ku);
 	T KW[4][3];
 	if (kDebug) k0_apply(g, Gab, lamV, muV, w, KW);
-	T sumM[3], sumV[3];
+	G sumM[3], sumV[3];
 #pragma unroll
 	for (int k = 0; k < 3; ++k)
 	{
-		sumM[k] = T(in.uM[0][k] + in.uM[1][k] + in.uM[2][k] + in.uM[3][k]);
-		sumV[k] = T(in.vv[0][k] + in.vv[1][k] + in.vv[2][k] + in.vv[3][k]);
+		sumM[k] = G(in.uM[0][k] + in.uM[1][k] + in.uM[2][k] + in.uM[3][k]);
+		sumV[k] = G(in.vv[0][k] + in.vv[1][k] + in.vv[2][k] + in.vv[3][k]);
 	}
 
 #pragma unroll
@@ -790,33 +916,41 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 		// (FemRepresentation.cpp:499-508) each row of M0 is summed onto its diagonal, 5 cm = rho V / 4.
 #pragma unroll
 		for (int i = 0; i < 3; ++i)
-			rhs[(3 * a + i) * rhsStride] = R[3 * i] * Ku[a][0] + R[3 * i + 1] * Ku[a][1] + R[3 * i + 2] * Ku[a][2] +
-										   Tp[3 * i] * zt[0] + Tp[3 * i + 1] * zt[1] + Tp[3 * i + 2] * zt[2] +
-										   (in.lumped ? cm * T(5) * T(in.uM[a][i]) : cm * (T(in.uM[a][i]) + sumM[i]));
+			out.rhs_entry(3 * a + i, R[3 * i] * Ku[a][0] + R[3 * i + 1] * Ku[a][1] + R[3 * i + 2] * Ku[a][2] +
+										 Tp[3 * i] * zt[0] + Tp[3 * i + 1] * zt[1] + Tp[3 * i + 2] * zt[2] +
+										 (in.lumped ? cm * G(5) * G(in.uM[a][i]) : cm * (G(in.uM[a][i]) + sumM[i])));
 
 		T kv[3] = {0, 0, 0};
 #pragma unroll
 		for (int bb = 0; bb < 4; ++bb)
 		{
-			const bool store = ((a == bb) || (in.nd[a] > in.nd[bb])) && ks != nullptr;
-			if (!store && !kDebug) continue;
+			const bool store = ((a == bb) || (in.nd[a] > in.nd[bb])) && out.blocks();
+			if (!store && !kDebug && !Out::kAll) continue;
+			T cb[3][3];
+#pragma unroll
+			for (int qq = 0; qq < 3; ++qq)
+			{
+				if constexpr (kLean)
+					cross3(g[bb], &R[3 * qq], cb[qq]);
+				else
+				{
+#pragma unroll
+					for (int k = 0; k < 3; ++k) cb[qq][k] = cbq[bb][qq][k];
+				}
+			}
 			T blk[9];
 #pragma unroll
 			for (int i = 0; i < 3; ++i)
 #pragma unroll
 				for (int qq = 0; qq < 3; ++qq)
 				{
-					T v = lamV * h[a][i] * h[bb][qq] + muV * h[bb][i] * h[a][qq] + Tp[3 * i] * cbq[bb][qq][0] +
-						  Tp[3 * i + 1] * cbq[bb][qq][1] + Tp[3 * i + 2] * cbq[bb][qq][2];
-					if (i == qq) v += muV * Gab[a][bb];
+					T v = lamV * h[a][i] * h[bb][qq] + muV * h[bb][i] * h[a][qq] + Tp[3 * i] * cb[qq][0] +
+						  Tp[3 * i + 1] * cb[qq][1] + Tp[3 * i + 2] * cb[qq][2];
+					if (i == qq) v = v + muV * Gab[a][bb];
 					blk[3 * i + qq] = v;
 				}
-			if (store)
-			{
-				const int slot = (a == bb) ? a : pair_slot(a < bb ? a : bb, a < bb ? bb : a);
-#pragma unroll
-				for (int k = 0; k < 9; ++k) ks[(slot * 9 + k) * ksStride] = blk[k];
-			}
+			if (store) out.block(a, bb, (a == bb) ? a : pair_slot(a < bb ? a : bb, a < bb ? bb : a), blk);
+			if (Out::kAll) out.full_block(a, bb, blk);
 			if (kDebug)
 			{
 #pragma unroll
@@ -824,7 +958,7 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 				{
 #pragma unroll
 					for (int qq = 0; qq < 3; ++qq) kfull[(3 * a + i) * 12 + 3 * bb + qq] = double(blk[3 * i + qq]);
-					kv[i] += blk[3 * i] * T(in.vv[bb][0]) + blk[3 * i + 1] * T(in.vv[bb][1]) + blk[3 * i + 2] * T(in.vv[bb][2]);
+					kv[i] += blk[3 * i] * G(in.vv[bb][0]) + blk[3 * i + 1] * G(in.vv[bb][1]) + blk[3 * i + 2] * G(in.vv[bb][2]);
 				}
 			}
 		}
@@ -836,12 +970,22 @@ __host__ __device__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV,
 			{
 				const T fe = -(R[3 * i] * KW[a][0] + R[3 * i + 1] * KW[a][1] + R[3 * i + 2] * KW[a][2] +
 							   Tp[3 * i] * zeta[0] + Tp[3 * i + 1] * zeta[1] + Tp[3 * i + 2] * zeta[2]);
-				const T mv = in.lumped ? cm * T(5) * T(in.vv[a][i]) : cm * (T(in.vv[a][i]) + sumV[i]);
+				const G mv = in.lumped ? cm * G(5) * G(in.vv[a][i]) : cm * (G(in.vv[a][i]) + sumV[i]);
 				fdbg[3 * a + i] = double(fe) - in.alphaDbg * double(mv) - in.betaDbg * double(kv[i]);
 			}
 		}
 	}
 	return flags;
+}
+
+// compute_to() with the results written to strided arrays: ks[k * ksStride], k = slot*9 + entry,
+// the stored blocks (ks may be null: right-hand side only); rhs[j * rhsStride], j = 3a+i.
+template <typename T, bool kDebug, typename In = ElemIn, bool kLinear = false>
+__host__ __device__ __forceinline__ int compute(const In& in, const T (&g)[4][3], T lamV, T muV, T cm, T* ks,
+												int ksStride, T* rhs, int rhsStride, double* kfull, double* fdbg)
+{
+	StoreOut<T> out{ks, ksStride, rhs, rhsStride};
+	return compute_to<T, kDebug, In, kLinear>(in, g, lamV, muV, cm, out, kfull, fdbg);
 }
 
 }  // namespace elem

@@ -91,25 +91,8 @@ int run(const double* x0, const double* x, const double* v, const double* xt, co
 	}
 	// R from the Newton polar (or its fallback) on the same F
 	T F[9], Rt[9];
-	for (int i = 0; i < 3; ++i)
-		for (int j = 0; j < 3; ++j)
-			F[3 * i + j] = T(in.p[1][i]) * g[1][j] + T(in.p[2][i]) * g[2][j] + T(in.p[3][i]) * g[3][j];
-	if (!gbfem::elem::polar_newton(F, Rt))
-	{
-		if constexpr (std::is_same<T, float>::value)
-		{
-			// The FP32 form's fallback: the FP64 SVD of F formed in FP64 (as compute() does).
-			double Fd[9], Rd[9];
-			for (int i = 0; i < 3; ++i)
-				for (int j = 0; j < 3; ++j)
-					Fd[3 * i + j] = in.p[1][i] * double(g[1][j]) + in.p[2][i] * double(g[2][j]) +
-									in.p[3][i] * double(g[3][j]);
-			gbfem::elem::polar_svd(Fd, Rd);
-			for (int k = 0; k < 9; ++k) Rt[k] = T(Rd[k]);
-		}
-		else
-			gbfem::elem::polar_svd(F, Rt);
-	}
+	gbfem::elem::deformation<T, false>(in, g, F);
+	gbfem::elem::rotation<T, false>(in, g, F, Rt);
 	for (int k = 0; k < 9; ++k) R9[k] = double(Rt[k]);
 	return fl;
 }
@@ -164,7 +147,19 @@ extern "C" int gbfem_host_adjoint_element(const double* x0, const double* x, con
 	gbfem::adj::fill_input(in, ndv, X, R0, Vel, dt, alpha, beta, -1, -1);
 	double ks[90], rh[12];
 	gbfem::elem::compute<double, false>(in, g, lamV, muV, cm, ks, 1, rh, 1, nullptr, nullptr);
-	*psi = gbfem::adj::element_psi(ndv, ks, rh, MU, DV, dt + beta);
+	// psi_e two ways: contracted as the element code delivers its blocks (what the derivative passes
+	// differentiate) and from the stored blocks; they agree to rounding.
+	*psi = gbfem::adj::element_psi_value(ndv, X, R0, Vel, MU, DV, g, lamV, muV, cm, dt, alpha, beta);
+	const double psiArrays = gbfem::adj::element_psi(ndv, ks, rh, MU, DV, dt + beta);
+	double scale = 0.0, mmax = 0.0, dmax = 0.0;
+	for (int j = 0; j < 12; ++j)
+	{
+		scale += fabs(MU[j] * rh[j]);
+		mmax = fmax(mmax, fabs(MU[j]));
+		dmax = fmax(dmax, fabs(DV[j]));
+	}
+	for (int k = 0; k < 90; ++k) scale += 2.0 * (dt + beta) * fabs(ks[k]) * mmax * dmax;
+	if (!(fabs(*psi - psiArrays) <= 1e-13 * scale)) return -2;
 	gbfem::adj::adjoint_element(ndv, X, R0, Vel, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
 	return 0;
 }

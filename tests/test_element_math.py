@@ -200,11 +200,24 @@ def _adjoint_case(seed):
     return x0, x, v, mu, dv, nd
 
 
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_element_adjoint_position_gradient_matches_central_differences(elem, seed):
-    """d psi_e / d x_e from the dual-number passes vs central differences of psi_e (the element
-    share of mu.rhs - mu.S dv that the step's adjoint differentiates)."""
-    x0, x, v, mu, dv, nd = _adjoint_case(seed)
+def _inverted_case(seed):
+    """An element turned inside out (F = R diag(1.1, 0.9, -0.8) plus noise, det F < 0): its rotation
+    comes from the SVD path, and S = R^T F is indefinite."""
+    x0, _, v, mu, dv, nd = _adjoint_case(seed)
+    R = rot(0.4, [0.3, -1.0, 2.0])
+    rng = np.random.default_rng(seed + 100)
+    F = R @ np.diag([1.1, 0.9, -0.8])
+    x = x0[0] + (x0 - x0[0]) @ F.T + rng.uniform(-2e-4, 2e-4, (4, 3)) + 0.01
+    assert np.linalg.det((x[1:] - x[0]).T) < 0
+    return x0, x, v, mu, dv, nd
+
+
+@pytest.mark.parametrize("seed,inverted", [(0, False), (1, False), (2, False), (0, True), (4, True)])
+def test_element_adjoint_position_gradient_matches_central_differences(elem, seed, inverted):
+    """d psi_e / d x_e from the dual-number passes (the rotation's derivative from the polar
+    factor's tangent) vs central differences of psi_e (the element share of mu.rhs - mu.S dv that
+    the step's adjoint differentiates), on regular and inverted elements."""
+    x0, x, v, mu, dv, nd = (_inverted_case if inverted else _adjoint_case)(seed)
     _, gx, _, _, _ = elem.adjoint(x0, x, v, mu, dv, nd=nd)
     h = 1e-7
     fd = np.zeros(12)
