@@ -341,11 +341,20 @@ __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __re
 {
 	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
 	int k = k0;
+	// Column indices are loaded one round ahead of the gathers they address, so a round waits on the
+	// gathers alone, not on a column load and then the gathers.
+	int Jn[4] = {0, 0, 0, 0};
+#pragma unroll
+	for (int u = 0; u < 4; ++u)
+		if (k + u < k1) Jn[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
 	for (; k + 4 <= k1; k += 4)
 	{
 		int J[4];
 #pragma unroll
-		for (int u = 0; u < 4; ++u) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
+		for (int u = 0; u < 4; ++u) J[u] = Jn[u];
+#pragma unroll
+		for (int u = 0; u < 4; ++u)
+			if (k + 4 + u < k1) Jn[u] = __ldcs(&a.col[(k + 4 + u) * 32 + lane]);
 		float4 zj[4], pj[4];
 #pragma unroll
 		for (int u = 0; u < 4; ++u)
@@ -363,22 +372,18 @@ __device__ __forceinline__ void spmv_row_zp(const PcgArgs& a, const float4* __re
 			a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
 		}
 	}
-	// The last 1 to 3 slots in one round as well (the count is the same in every lane), instead of
-	// one dependent column -> record -> value chain each.
+	// The last 1 to 3 slots (their columns already in Jn) in one round as well (the count is the same
+	// in every lane), instead of one dependent column -> record -> value chain each.
 	const int rem = k1 - k;
 	if (rem > 0)
 	{
-		int J[3];
 		float4 zj[3], pj[3];
-#pragma unroll
-		for (int u = 0; u < 3; ++u)
-			if (u < rem) J[u] = __ldcs(&a.col[(k + u) * 32 + lane]);
 #pragma unroll
 		for (int u = 0; u < 3; ++u)
 			if (u < rem)
 			{
-				zj[u] = zp[2 * J[u]];
-				pj[u] = zp[2 * J[u] + 1];
+				zj[u] = zp[2 * Jn[u]];
+				pj[u] = zp[2 * Jn[u] + 1];
 			}
 #pragma unroll
 		for (int u = 0; u < 3; ++u)
