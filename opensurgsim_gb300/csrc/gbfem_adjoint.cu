@@ -25,9 +25,9 @@ namespace {
 
 constexpr int kAdjThreads = 64;
 
-// One thread per element, its eleven passes in turn (splitting them over threads was measured
-// slower: every pass needs the same large per-thread state, so more threads only add local-memory
-// traffic). gx[e*12 + 3..11], gv[e*12 + 0..11]; gLogE[e], gNu[e] accumulate.
+// One thread per element, its passes in turn (splitting them over threads was measured slower:
+// every pass needs the same large per-thread state). gx[e*12 + 0..11], gv[e*12 + 0..11]; gLogE[e],
+// gNu[e] accumulate.
 template <typename S>
 __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, const double* __restrict__ x,
 																 const double* __restrict__ v,
@@ -63,18 +63,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_element_adjoint(DevBody b, cons
 	const double lamV = b.rest[13 * E + e], muV = b.rest[14 * E + e], cm = b.rest[15 * E + e];
 	const bool moduli = gLogE || gNu;
 	double pl = 0.0, pm = 0.0;
-	S Rw[9];
-	const int rflags = adj::element_rotation<S>(nd, X, R0, g, Rw);
-	// The nine dual passes share one body (a loop, not unrolled); the velocity and modulus items follow.
-#pragma unroll 1
-	for (int item = 0; item < 9; ++item)
-		adj::adjoint_item<S>(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags,
-							 gx + (size_t)e * 12, gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
-	adj::adjoint_item<S>(9, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags, gx + (size_t)e * 12,
-						 gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
-	if (moduli)
-		adj::adjoint_item<S>(10, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags,
-							 gx + (size_t)e * 12, gv + (size_t)e * 12, &pl, &pm, b.lumped != 0);
+	adj::element_adjoint<S>(nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx + (size_t)e * 12,
+							gv + (size_t)e * 12, moduli ? &pl : nullptr, &pm, b.lumped != 0);
 	if (!moduli) return;
 	// lambda V and mu V are both proportional to E: d/d log E scales each by one.
 	if (gLogE) gLogE[e] += lamV * pl + muV * pm;

@@ -2,7 +2,7 @@
 //
 // psi_e(x_e, v_e, lambda V, mu V) = mu_e . rhs_e - c2 <lower-triangle blocks of K_e, (mu, dv)> is the
 // element's share of psi = mu . rhs - mu . S dv, the scalar whose gradients give the step's adjoint
-// (see gbfem_adjoint.cu). adjoint_element() returns d psi_e / d x_e (12, forward-mode dual
+// (see gbfem_adjoint.cu). element_adjoint() returns d psi_e / d x_e (12, forward-mode dual
 // numbers through the element code, nine passes), d psi_e / d v_e (12) and d psi_e / d(lambda V), d(mu V).
 #pragma once
 
@@ -59,18 +59,11 @@ template <typename T>
 struct PsiOut
 {
 	using G = typename elem::ScalarOf<T>::type;
-	G mu[12], dv[12];  // in the passes' arithmetic (FP32 for the mixed form's passes)
+	const G (&mu)[12];  // in the passes' arithmetic (FP32 for the mixed form's passes)
+	const G (&dv)[12];
 	T s = T(0), sk = T(0);
 	static constexpr bool kAll = false;
-	__host__ __device__ __forceinline__ PsiOut(const double (&MU)[12], const double (&DV)[12])
-	{
-#pragma unroll
-		for (int j = 0; j < 12; ++j)
-		{
-			mu[j] = G(MU[j]);
-			dv[j] = G(DV[j]);
-		}
-	}
+	__host__ __device__ __forceinline__ PsiOut(const G (&MU)[12], const G (&DV)[12]) : mu(MU), dv(DV) {}
 	__host__ __device__ __forceinline__ bool blocks() const { return true; }
 	__host__ __device__ __forceinline__ void rhs_entry(int j, const T& v) { s = s + v * mu[j]; }
 	__host__ __device__ __forceinline__ void block(int a, int b, int, const T (&blk)[9])
@@ -102,14 +95,15 @@ struct PsiOut
 	__host__ __device__ __forceinline__ T psi(double c2) const { return s - G(c2) * sk; }
 };
 
-// (K_e^T mu_e)_c = sum_r K_e(r, c) mu_r over the full element tangent, accumulated in FP64 in r order
-// as compute_to() delivers its 16 blocks: an output policy of compute_to().
+// (K_e^T mu_e)_c = sum_r K_e(r, c) mu_r over the full element tangent, accumulated in r order in the
+// passes' arithmetic as compute_to() delivers its 16 blocks: an output policy of compute_to().
 template <typename T>
 struct KtMuOut
 {
-	const double (&mu)[12];
-	double kt[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	const T (&mu)[12];
+	T kt[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 	static constexpr bool kAll = true;
+	__host__ __device__ __forceinline__ KtMuOut(const T (&MU)[12]) : mu(MU) {}
 	__host__ __device__ __forceinline__ bool blocks() const { return false; }
 	__host__ __device__ __forceinline__ void rhs_entry(int, const T&) {}
 	__host__ __device__ __forceinline__ void block(int, int, int, const T (&)[9]) {}
@@ -118,12 +112,12 @@ struct KtMuOut
 #pragma unroll
 		for (int q = 0; q < 3; ++q)
 #pragma unroll
-			for (int i = 0; i < 3; ++i) kt[3 * b + q] += double(blk[3 * i + q]) * mu[3 * a + i];
+			for (int i = 0; i < 3; ++i) kt[3 * b + q] += blk[3 * i + q] * mu[3 * a + i];
 	}
 };
 
-template <typename P>
-__host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
+template <typename P, typename C>
+__host__ __device__ void fill_input(elem::ElemInT<P, C>& in, const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
 						   const double (&V)[4][3], double dt, double alpha, double beta, int seedNode, int seedAxis,
 						   bool lumped = false)
 {
@@ -139,25 +133,19 @@ __host__ __device__ void fill_input(elem::ElemInT<P>& in, const int (&nd)[4], co
 			const double dp = (k == seedAxis) ? (double(a == seedNode) - double(seedNode == 0)) : 0.0;
 			in.p[a][k] = P(X[a][k] - X[0][k]);
 			if constexpr (!std::is_same<P, double>::value) in.p[a][k].d = dp;
-			in.q[a][k] = R0[a][k] - R0[0][k];
+			in.q[a][k] = C(R0[a][k] - R0[0][k]);
 			const double va = V[a][k];
-			in.uK[a][k] = -beta * va + (0.0 - dt * va);  // x_n = x_t at the first Newton iteration
-			in.uM[a][k] = -alpha * va;                    // v_n = v_t
-			in.vv[a][k] = va;
+			in.uK[a][k] = C(-beta * va + (0.0 - dt * va));  // x_n = x_t at the first Newton iteration
+			in.uM[a][k] = C(-alpha * va);                    // v_n = v_t
+			in.vv[a][k] = C(va);
 		}
 	}
 	in.alphaDbg = alpha;
 	in.betaDbg = beta;
 }
 
-// Work items of one element, each an independent pass through the element code: items 0..8 are the
-// dual passes seeded on x_(1 + item/3, item%3) (psi_e depends on the positions only through
-// p_a = x_a - x_0, so d/dx_0 = -sum_a d/dx_a needs no pass of its own), item 9 the velocity
-// gradient, item 10 the two unit-modulus evaluations.
-constexpr int kAdjItems = 11;
-
 // The element's rotation in the passes' arithmetic S (row-major) and its polar flags, as the
-// element code forms them: computed once and shared by every item of the element.
+// element code forms them: computed once and shared by every pass over the element.
 template <typename S = double>
 __host__ __device__ inline int element_rotation(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
 												const double (&g)[4][3], S (&R)[9])
@@ -172,57 +160,79 @@ __host__ __device__ inline int element_rotation(const int (&nd)[4], const double
 	return elem::rotation<S, false>(in, gS, F, R);
 }
 
-// One item of one element: X, R0, V positions / rest positions / velocities of its nodes, MU and DV
-// the adjoint and the step's velocity increment at its dofs (zero on BC dofs), Rw and rflags the
-// element's rotation (element_rotation). Writes gx[3 + item] (items 0..8), gv[0..11] (item 9) or
-// *pLam, *pMu (item 10).
+// All derivatives of psi_e for one element. X, R0, V: positions / rest positions / velocities of its
+// nodes; MU, DV: the adjoint and the step's velocity increment at its dofs (zero on BC dofs).
+//   gx[0..11] = d psi_e / d x_e: nine dual passes seeded on x_(b, k), b = 1..3 (psi_e depends on the
+//     positions only through p_a = x_a - x_0, so d/dx_0 = -sum_b d/dx_b needs no pass of its own);
+//   gv[0..11] = d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (one pass over the full tangent; M0
+//     lumped to 5 cm on the diagonal with mass lumping);
+//   *pLam, *pMu (when pLam is not null) = psi_e's elastic part at unit (lambda V, mu V), in which it is
+//     linear (two passes).
 // S is the arithmetic of the passes: double (FP64 form) or float (mixed form, FP32 element math
-// with the corotated strain formed as in its forward step).
+// with the corotated strain formed as in its forward step). The rotation, the passes' inputs and the
+// psi coefficients are formed once; a dual pass only moves its seed.
 template <typename S = double>
-__host__ __device__ inline void adjoint_item(int item, const int (&nd)[4], const double (&X)[4][3],
-											 const double (&R0)[4][3], const double (&V)[4][3], const double (&MU)[12],
-											 const double (&DV)[12], const double (&g)[4][3], double lamV, double muV,
-											 double cm, double dt, double alpha, double beta, const S (&Rw)[9], int rflags,
-											 double* gx, double* gv, double* pLam, double* pMu, bool lumped = false)
+__host__ __device__ inline void element_adjoint(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
+												const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],
+												const double (&g)[4][3], double lamV, double muV, double cm, double dt,
+												double alpha, double beta, double* gx, double* gv, double* pLam,
+												double* pMu, bool lumped = false)
 {
 	using D = ad::DualT<S>;
 	const double c2 = dt + beta;
-	S gS[4][3];
+	S Rw[9];
+	const int rflags = element_rotation<S>(nd, X, R0, g, Rw);
+	S gS[4][3], muS[12], dvS[12];
 	for (int a = 0; a < 4; ++a)
 		for (int k = 0; k < 3; ++k) gS[a][k] = S(g[a][k]);
-	if (item < 9)
+	for (int j = 0; j < 12; ++j)
 	{
-		// Only the positions carry the seeded derivative (the rotation's from polar_tangent); psi_e's
-		// sums are contracted as the blocks come out of the element code.
-		const int s = 3 + item;
-		elem::ElemInT<D> in;
-		fill_input(in, nd, X, R0, V, dt, alpha, beta, s / 3, s % 3, lumped);
-		PsiOut<D> out{MU, DV};
-		elem::compute_to<D, false, elem::ElemInT<D>, false>(in, gS, S(lamV), S(muV), S(cm), out, nullptr, nullptr, Rw,
-															 rflags);
-		gx[s] = double(out.psi(c2).d);
+		muS[j] = S(MU[j]);
+		dvS[j] = S(DV[j]);
 	}
-	else if (item == 9)
 	{
-		// d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (K_e: the full element tangent; M0 lumped to
-		// 5 cm on the diagonal with mass lumping).
+		// Positions: only they carry the seeded derivative (the rotation's from polar_tangent); psi_e's
+		// sums are contracted as the blocks come out of the element code. One body for the nine
+		// passes (a loop, not unrolled).
+		elem::ElemInT<D, S> in;
+		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
+		double sx[3] = {0.0, 0.0, 0.0};
+#pragma unroll 1
+		for (int item = 0; item < 9; ++item)
+		{
+			const int node = 1 + item / 3, axis = item % 3;
+#pragma unroll
+			for (int a = 0; a < 4; ++a)
+#pragma unroll
+				for (int k = 0; k < 3; ++k) in.p[a][k].d = (a == node && k == axis) ? S(1) : S(0);
+			PsiOut<D> out(muS, dvS);
+			elem::compute_to<D, false, elem::ElemInT<D, S>, false>(in, gS, S(lamV), S(muV), S(cm), out, nullptr,
+																   nullptr, Rw, rflags);
+			const double d = double(out.psi(c2).d);
+			gx[3 + item] = d;
+			sx[axis] += d;
+		}
+		for (int k = 0; k < 3; ++k) gx[k] = -sx[k];
+	}
+	{
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
-		KtMuOut<S> out{MU};
+		KtMuOut<S> out(muS);
 		elem::compute_to<S, false, elem::ElemIn, false, KtMuOut<S>, true>(in, gS, S(lamV), S(muV), S(cm), out, nullptr,
 																		   nullptr, Rw, rflags);
 		double sm[3] = {0, 0, 0};
 		for (int a = 0; a < 4; ++a)
 			for (int k = 0; k < 3; ++k) sm[k] += MU[3 * a + k];
 		for (int c = 0; c < 12; ++c)
-			gv[c] = -c2 * out.kt[c] - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
+			gv[c] = -c2 * double(out.kt[c]) - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
 	}
-	else
+	if (pLam)
 	{
-		// psi_e's elastic part is linear in (lambda V, mu V): evaluate it with unit moduli.
+		// psi_e's elastic part is linear in (lambda V, mu V): evaluate it with unit moduli (mass terms
+		// off, cm = 0).
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
-		PsiOut<S> ol{MU, DV}, om{MU, DV};
+		PsiOut<S> ol(muS, dvS), om(muS, dvS);
 		elem::compute_to<S, false, elem::ElemIn, false, PsiOut<S>, true>(in, gS, S(1), S(0), S(0), ol, nullptr, nullptr,
 																		  Rw, rflags);
 		*pLam = double(ol.psi(c2));
@@ -241,7 +251,7 @@ __host__ __device__ inline double element_psi_value(const int (&nd)[4], const do
 {
 	elem::ElemIn in;
 	fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
-	PsiOut<double> out{MU, DV};
+	PsiOut<double> out(MU, DV);
 	elem::compute_to<double, false, elem::ElemIn, false>(in, g, lamV, muV, cm, out, nullptr, nullptr);
 	return out.psi(dt + beta);
 }
@@ -256,20 +266,6 @@ __host__ __device__ inline void poisson_partials(double lamV, double muV, double
 	const double EV = 2.0 * muV * (1.0 + nu);
 	*dLam = EV * (1.0 + 2.0 * nu * nu) / ((1.0 + nu) * (1.0 + nu) * (1.0 - 2.0 * nu) * (1.0 - 2.0 * nu));
 	*dMu = -EV / (2.0 * (1.0 + nu) * (1.0 + nu));
-}
-
-// All items of one element in one call (gx[0..2] completed from translation invariance).
-__host__ __device__ inline void adjoint_element(const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
-												const double (&V)[4][3], const double (&MU)[12], const double (&DV)[12],
-												const double (&g)[4][3], double lamV, double muV, double cm, double dt,
-												double alpha, double beta, double* gx, double* gv, double* pLam,
-												double* pMu, bool lumped = false)
-{
-	double Rw[9];
-	const int rflags = element_rotation(nd, X, R0, g, Rw);
-	for (int item = 0; item < kAdjItems; ++item)
-		adjoint_item(item, nd, X, R0, V, MU, DV, g, lamV, muV, cm, dt, alpha, beta, Rw, rflags, gx, gv, pLam, pMu, lumped);
-	for (int k = 0; k < 3; ++k) gx[k] = -(gx[3 + k] + gx[6 + k] + gx[9 + k]);
 }
 
 }  // namespace adj

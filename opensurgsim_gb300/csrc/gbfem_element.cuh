@@ -294,16 +294,16 @@ __host__ __device__ __forceinline__ int pair_slot(int a, int b)
 
 // Per-element inputs gathered by the kernels (node 0 is the origin of p and q). The positions p have
 // scalar type P (double, or a dual type when the adjoint seeds a derivative direction in them); the
-// other inputs never carry a derivative.
-template <typename P>
+// other inputs never carry a derivative and have type C (double, or the dual passes' plain type).
+template <typename P, typename C = double>
 struct ElemInT
 {
 	int nd[4];
-	P p[4][3];         // x_n,a - x_n,0
-	double q[4][3];    // x0_a - x0_0
-	double uK[4][3];   // -beta v_n + (x_n - x_t - dt v_n)
-	double uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
-	double vv[4][3];   // v_n (debug force only)
+	P p[4][3];    // x_n,a - x_n,0
+	C q[4][3];    // x0_a - x0_0
+	C uK[4][3];   // -beta v_n + (x_n - x_t - dt v_n)
+	C uM[4][3];   // -alpha v_n - (v_n - v_t)/dt
+	C vv[4][3];   // v_n (debug force only)
 	double alphaDbg, betaDbg;  // Rayleigh coefficients (debug force only)
 	int lumped = 0;  // FemRepresentation::setMassLumping: the element's mass rows summed onto the diagonal
 };
@@ -614,7 +614,7 @@ __host__ __device__ __forceinline__ void polar_tangent(const ad::DualT<S> (&F)[9
 	S C[9];
 	cofactor3(M, C);  // symmetric M: M^-1 = C / det
 	const S det = M[0] * C[0] + M[1] * C[1] + M[2] * C[2];
-	const S id = (fabs(double(det)) > 1e-12) ? S(1) / det : S(0);
+	const S id = (fabs(det) > S(1e-12)) ? S(1) / det : S(0);
 	const S w[3] = {(C[0] * ax[0] + C[1] * ax[1] + C[2] * ax[2]) * id, (C[3] * ax[0] + C[4] * ax[1] + C[5] * ax[2]) * id,
 					(C[6] * ax[0] + C[7] * ax[1] + C[8] * ax[2]) * id};
 #pragma unroll
@@ -723,7 +723,7 @@ __host__ __device__ int compute_to(const In& in, const typename ScalarOf<T>::typ
 		const T d = Gm[0] * C[0] + Gm[1] * C[1] + Gm[2] * C[2];
 		// (An FP32 form of this test moved the FP32 element kernel from 168 to 190 registers, one
 		// block per SM fewer; the conversion costs less than that.)
-		extra = (std::is_same<T, float>::value && (flags & 1)) ? !(flags & 4) : fabs(double(d)) > 1e-12;
+		extra = (std::is_same<G, float>::value && (flags & 1)) ? !(flags & 4) : fabs(double(d)) > 1e-12;
 		const T id = T(1) / d;
 #pragma unroll
 		for (int i = 0; i < 3; ++i)

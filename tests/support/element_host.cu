@@ -160,7 +160,7 @@ extern "C" int gbfem_host_adjoint_element(const double* x0, const double* x, con
 	}
 	for (int k = 0; k < 90; ++k) scale += 2.0 * (dt + beta) * fabs(ks[k]) * mmax * dmax;
 	if (!(fabs(*psi - psiArrays) <= 1e-13 * scale)) return -2;
-	gbfem::adj::adjoint_element(ndv, X, R0, Vel, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
+	gbfem::adj::element_adjoint<double>(ndv, X, R0, Vel, MU, DV, g, lamV, muV, cm, dt, alpha, beta, gx, gv, pLam, pMu);
 	return 0;
 }
 
