@@ -954,7 +954,10 @@ def run_adjoint(args, local):
 # [2000, 100000], per-element log E, 30 steps, FP32 bulk with FP64 refreshes in one batch handle; the
 # gradient of every mesh is compared with the FP64 adjoint of that mesh alone.
 
-ADJB = dict(count=64, lo=2000, hi=100000, seed=11, steps=30, checkpoint=10, markers=16)
+# Every state of the 30 steps is kept (checkpoint after every step, ~2 GB of HBM for the 6.2M-tet batch),
+# so the reverse sweep runs no step again; the same rollout with checkpoints every 10 steps (segments
+# re-run) is timed beside it and gives the same gradient bit for bit.
+ADJB = dict(count=64, lo=2000, hi=100000, seed=11, steps=30, checkpoint=1, checkpoint_rerun=10, markers=16)
 
 
 def run_adjoint_batch(args, local):
@@ -1003,24 +1006,31 @@ def run_adjoint_batch(args, local):
         target = xT[mk_t].clone()
     th_b = t64(np.concatenate(theta))
 
-    def fwd_bwd():
+    def fwd_bwd(every):
         th = th_b.clone().requires_grad_(True)
-        xT_, _ = rollout(batch, th, x0, v0b, 1e-3, steps, ck)
+        xT_, _ = rollout(batch, th, x0, v0b, 1e-3, steps, every)
         L = ((xT_[mk_t] - target) ** 2).sum()
         L.backward()
         return th.grad.detach().cpu().numpy()
 
-    # Warm-up: the same rollout (the library captures the forward and the backward graphs once).
-    for _ in range(max(1, args.warmup)):
-        g_batch = fwd_bwd()
-    torch.cuda.synchronize(dev)
+    def timed(every):
+        # Warm-up: the same rollout (the library captures the forward and the backward graphs once).
+        for _ in range(max(1, args.warmup)):
+            g = fwd_bwd(every)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            g = fwd_bwd(every)
+        torch.cuda.synchronize(dev)
+        return g, (time.perf_counter() - t0) / reps
+
     reps = max(1, min(args.steps, 3))
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        g_batch = fwd_bwd()
-    torch.cuda.synchronize(dev)
-    sec = (time.perf_counter() - t0) / reps
-    log(f"batched mixed forward+backward: {sec:.2f} s")
+    g_batch, sec = timed(ck)
+    log(f"batched mixed forward+backward: {sec:.2f} s (checkpoint every {ck} step)")
+    g_rerun, sec_rerun = timed(ADJB["checkpoint_rerun"])
+    same = bool(np.array_equal(g_rerun, g_batch))
+    log(f"  with checkpoints every {ADJB['checkpoint_rerun']} steps (segments re-run): {sec_rerun:.2f} s, "
+        f"gradient bit-identical: {same}")
     batch.close()
 
     def grads_fp64_batch():
@@ -1064,11 +1074,15 @@ def run_adjoint_batch(args, local):
         "dtype": "f32+f64", "data": "synthetic (seeded cube-grid meshes, seeded parameters)",
         "config": {"workload": (f"adjoint batch: {len(meshes)} meshes, nodes log-U[2000,100000] (seed {ADJB['seed']}), "
                                 f"{tets} tets, per-element log E = ln E_mesh + N(0, 0.3), {ADJB['markers']} markers "
-                                f"per mesh, {steps} steps, checkpoints every {ck}, mixed precision batch handle; "
-                                "forward and backward each one CUDA graph in the library"),
+                                f"per mesh, {steps} steps, every state kept (checkpoint after every step), mixed "
+                                "precision batch handle; forward and backward each one CUDA graph in the library"),
                    "tets": tets},
         "grad_rel_err_vs_fp64_adjoint": {"max": max(errs), "median": float(np.median(errs)),
                                          "definition": "per mesh ||g_batch - g_fp64|| / ||g_fp64||, FP64 batch reference"},
+        "checkpoints_every_10": {"value": tets * steps / sec_rerun, "sec": sec_rerun,
+                                 "grad_bit_identical": same,
+                                 "how": "the same rollout with checkpoints every 10 steps, the backward re-running "
+                                        "each segment's steps"},
         "fp64_reference_adjoint": {"value": tets * steps / sec64,
                                    "how": "the same meshes as one FP64 batch handle, graph rollouts, host clock"},
         "fp64_batch_vs_single_handles": {"max": max(cross), "meshes": len(cross),

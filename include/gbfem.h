@@ -250,7 +250,8 @@ GBFEM_API gbfem_status gbfem_adjoint_step(gbfem_handle h, double dt, const doubl
  *   (xT, vT) and leaves it as the handle's state.
  * gbfem_rollout_backward: the reverse sweep of the last forward: for each checkpoint segment, last
  *   first, its steps are run again from the checkpoint to recover their states, then the step
- *   adjoints (gbfem_adjoint_step) are applied in reverse. Given (lxT, lvT) = dL/d(xT, vT) it writes
+ *   adjoints (gbfem_adjoint_step) are applied in reverse. With checkpoint_every = 1 the forward keeps
+ *   every state (2n doubles a step) and no step is run again. Given (lxT, lvT) = dL/d(xT, vT) it writes
  *   (lx0, lv0) = dL/d(x0, v0) and, where not NULL, grad_log_young = dL/d(log E_e) and grad_poisson =
  *   dL/d(nu_e) (overwritten, not accumulated). The handle's state is the forward's final state again
  *   afterwards.

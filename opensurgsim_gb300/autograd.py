@@ -3,7 +3,8 @@
 Forward: set per-element Young's moduli E = exp(log_young) (``gbfem_set_materials_device``), start
 from (x0, v0) and take ``nsteps`` steps of ``dt`` with the body's own step (FP64 or mixed form),
 keeping the state every ``checkpoint_every`` steps. Backward: for each checkpoint segment, last
-first, re-run the segment's steps to recover its states, then walk them back with
+first, re-run the segment's steps to recover its states (with ``checkpoint_every=1`` every state is
+kept, 2n doubles a step, and no step runs again), then walk them back with
 ``gbfem_adjoint_step`` (the transposed solve and the per-element derivative kernels), which
 accumulates dL/d(log E) and dL/d(nu) and carries (dL/dx, dL/dv) to the segment's start. Gradients
 flow to ``log_young``, ``x0``, ``v0`` and, when given, the per-element Poisson ratios ``poisson``
@@ -124,7 +125,7 @@ class ImplicitRollout(torch.autograd.Function):
         for t in range(nsteps):
             st = body.step(dt, 1)
             _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
-            if (t + 1) % k == 0 and t + 1 < nsteps:
+            if (t + 1) % k == 0 and (t + 1 < nsteps or k == 1):
                 checkpoints.append((xv.clone(), vv.clone()))
         ctx.checkpoints = checkpoints
         return xv.clone(), vv.clone()
@@ -158,6 +159,18 @@ class ImplicitRollout(torch.autograd.Function):
                                           None if gnu is None else _ptr(gnu))
             _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
             return glog, gnu, lx0, lv0, None, None, None, None, None
+        if k == 1:
+            # Every state was kept: no step runs again.
+            for t in reversed(range(nsteps)):
+                xt, vt = ctx.checkpoints[t]
+                dv = (ctx.checkpoints[t + 1][1] - vt).contiguous()
+                torch.cuda.synchronize(dev)
+                st = L.gbfem_adjoint_step(body.handle, float(dt), *[ctypes.c_void_p(a.data_ptr()) for a in
+                                                                     (xt, vt, dv, lx, lv, lx, lv, glog)],
+                                          None if gnu is None else ctypes.c_void_p(gnu.data_ptr()), ctx.flags)
+                _check(body, st, (_lib.GBFEM_OK, _lib.GBFEM_CG_MAXITER))
+            torch.cuda.synchronize(dev)
+            return glog, gnu, lx, lv, None, None, None, None, None
         starts = list(range(0, nsteps, k))
         for seg in reversed(range(len(starts))):
             t0 = starts[seg]

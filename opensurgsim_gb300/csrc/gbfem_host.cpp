@@ -2356,7 +2356,11 @@ gbfem_status gbfem_rollout_backward(gbfem_handle h, const double* lxT, const dou
 			if (ce == cudaSuccess) ce = cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
 		};
 		const int nsegs = nck - 1;
-		for (int sg = nsegs - 1; sg >= 0 && cst == GBFEM_OK && ce == cudaSuccess; --sg)
+		// With a checkpoint after every step (every == 1) the forward kept every state (2n doubles a
+		// step): the reverse sweep re-runs no step.
+		for (int t = nsteps - 1; every == 1 && t >= 0 && cst == GBFEM_OK && ce == cudaSuccess; --t)
+			cst = enqueue_adjoint_step(h, dt, ck + 2 * n * t, ck + 2 * n * t + n, ck + 2 * n * (t + 1) + n, lx, lv, gl, gn);
+		for (int sg = nsegs - 1; every > 1 && sg >= 0 && cst == GBFEM_OK && ce == cudaSuccess; --sg)
 		{
 			const int len = std::min(every, nsteps - sg * every);
 			copy(h->d_x.p, ck + 2 * n * sg);

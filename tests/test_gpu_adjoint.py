@@ -188,6 +188,23 @@ def test_graph_rollout_equals_the_per_step_rollout(gpu_lib, monkeypatch):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_rollout_keeping_every_state_equals_segment_reruns(gpu_lib, monkeypatch, graph):
+    """checkpoint_every=1 keeps every state, so the reverse sweep re-runs no step; its states and
+    gradients equal those of checkpoints every 3 steps (whose segments re-run their steps, with the
+    same deterministic kernels) bit for bit, in the library's graph rollouts and in the per-step loop."""
+    from opensurgsim_gb300 import autograd
+
+    scene, body, theta, nu, x0, v0, wx, wv = _graph_case(seed=12)
+    body.set_tuning(64, 4, 2)
+    if not graph:
+        monkeypatch.setattr(autograd, "graph_rollouts", lambda b: False)
+    g1 = _grads(body, theta, nu, x0, v0, wx, wv, scene.dt, steps=7, every=1)
+    g3 = _grads(body, theta, nu, x0, v0, wx, wv, scene.dt, steps=7, every=3)
+    for a, b in zip(g1, g3):
+        assert np.array_equal(a, b)
+
+
 def test_graph_rollout_backward_after_another_forward(gpu_lib):
     """The library keeps the checkpoints of the body's last forward; a backward whose forward was
     followed by another rollout of the same body runs its forward again and gives the gradient of a
