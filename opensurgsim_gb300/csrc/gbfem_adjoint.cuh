@@ -116,6 +116,20 @@ struct KtMuOut
 	}
 };
 
+// psi_e's sums and K_e^T mu_e from the same pass: an output policy of compute_to().
+template <typename T>
+struct PsiKtOut
+{
+	PsiOut<T> psi;
+	KtMuOut<T> kt;
+	static constexpr bool kAll = true;
+	__host__ __device__ __forceinline__ PsiKtOut(const T (&MU)[12], const T (&DV)[12]) : psi(MU, DV), kt(MU) {}
+	__host__ __device__ __forceinline__ bool blocks() const { return true; }
+	__host__ __device__ __forceinline__ void rhs_entry(int j, const T& v) { psi.rhs_entry(j, v); }
+	__host__ __device__ __forceinline__ void block(int a, int b, int slot, const T (&blk)[9]) { psi.block(a, b, slot, blk); }
+	__host__ __device__ __forceinline__ void full_block(int a, int b, const T (&blk)[9]) { kt.full_block(a, b, blk); }
+};
+
 template <typename P, typename C>
 __host__ __device__ void fill_input(elem::ElemInT<P, C>& in, const int (&nd)[4], const double (&X)[4][3], const double (&R0)[4][3],
 						   const double (&V)[4][3], double dt, double alpha, double beta, int seedNode, int seedAxis,
@@ -164,10 +178,10 @@ __host__ __device__ inline int element_rotation(const int (&nd)[4], const double
 // nodes; MU, DV: the adjoint and the step's velocity increment at its dofs (zero on BC dofs).
 //   gx[0..11] = d psi_e / d x_e: nine dual passes seeded on x_(b, k), b = 1..3 (psi_e depends on the
 //     positions only through p_a = x_a - x_0, so d/dx_0 = -sum_b d/dx_b needs no pass of its own);
-//   gv[0..11] = d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (one pass over the full tangent; M0
-//     lumped to 5 cm on the diagonal with mass lumping);
+//   gv[0..11] = d psi_e / d v_e = -c2 K_e^T mu_e - alpha M0 mu_e (M0 lumped to 5 cm on the diagonal
+//     with mass lumping);
 //   *pLam, *pMu (when pLam is not null) = psi_e's elastic part at unit (lambda V, mu V), in which it is
-//     linear (two passes).
+//     linear; the same two passes give K_e^T mu_e.
 // S is the arithmetic of the passes: double (FP64 form) or float (mixed form, FP32 element math
 // with the corotated strain formed as in its forward step). The rotation, the passes' inputs and the
 // psi coefficients are formed once; a dual pass only moves its seed.
@@ -215,30 +229,37 @@ __host__ __device__ inline void element_adjoint(const int (&nd)[4], const double
 		for (int k = 0; k < 3; ++k) gx[k] = -sx[k];
 	}
 	{
+		// psi_e's elastic part and K_e are linear in (lambda V, mu V) (K0, the rotated stiffness and the
+		// rotation terms all are; R and the singular-G decision do not depend on the moduli): two passes
+		// at unit moduli (mass terms off, cm = 0) give d psi_e / d(lambda V), d(mu V) and
+		// K_e^T mu_e = lambda V K_lam^T mu_e + mu V K_mu^T mu_e.
 		elem::ElemIn in;
 		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1, lumped);
-		KtMuOut<S> out(muS);
-		elem::compute_to<S, false, elem::ElemIn, false, KtMuOut<S>, true>(in, gS, S(lamV), S(muV), S(cm), out, nullptr,
-																		   nullptr, Rw, rflags);
+		double pu[2], kt[12];
+		for (int c = 0; c < 12; ++c) kt[c] = 0.0;
+		// FP32 passes: one loop body (the kernel's size costs more than the unit moduli folded in);
+		// FP64 passes, bound by the FP64 rate: unrolled, with the unit moduli folded.
+		constexpr int kUnroll = std::is_same<S, float>::value ? 1 : 2;
+#pragma unroll kUnroll
+		for (int u = 0; u < 2; ++u)
+		{
+			PsiKtOut<S> out(muS, dvS);
+			elem::compute_to<S, false, elem::ElemIn, false, PsiKtOut<S>, true>(in, gS, S(u == 0 ? 1 : 0), S(u == 0 ? 0 : 1),
+																				S(0), out, nullptr, nullptr, Rw, rflags);
+			pu[u] = double(out.psi.psi(c2));
+			const double m = (u == 0) ? lamV : muV;
+			for (int c = 0; c < 12; ++c) kt[c] += m * double(out.kt.kt[c]);
+		}
 		double sm[3] = {0, 0, 0};
 		for (int a = 0; a < 4; ++a)
 			for (int k = 0; k < 3; ++k) sm[k] += MU[3 * a + k];
 		for (int c = 0; c < 12; ++c)
-			gv[c] = -c2 * double(out.kt[c]) - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
-	}
-	if (pLam)
-	{
-		// psi_e's elastic part is linear in (lambda V, mu V): evaluate it with unit moduli (mass terms
-		// off, cm = 0).
-		elem::ElemIn in;
-		fill_input(in, nd, X, R0, V, dt, alpha, beta, -1, -1);
-		PsiOut<S> ol(muS, dvS), om(muS, dvS);
-		elem::compute_to<S, false, elem::ElemIn, false, PsiOut<S>, true>(in, gS, S(1), S(0), S(0), ol, nullptr, nullptr,
-																		  Rw, rflags);
-		*pLam = double(ol.psi(c2));
-		elem::compute_to<S, false, elem::ElemIn, false, PsiOut<S>, true>(in, gS, S(0), S(1), S(0), om, nullptr, nullptr,
-																		  Rw, rflags);
-		*pMu = double(om.psi(c2));
+			gv[c] = -c2 * kt[c] - alpha * cm * (lumped ? 5.0 * MU[c] : MU[c] + sm[c % 3]);
+		if (pLam)
+		{
+			*pLam = pu[0];
+			*pMu = pu[1];
+		}
 	}
 }
 
