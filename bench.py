@@ -204,10 +204,19 @@ def host_info():
 # Algorithmic bytes (HBM) of the solve, per CG iteration and per FP64 residual refresh, for one
 # mesh with scalar non-zeros nnz, N nodes and n = 3N dofs; s = bytes per matrix value. Block
 # sparse storage reads one 4-byte column index per 3x3 block (nnz / 9 of them) and one offset per
-# block row; ten vector passes per iteration; a refresh reads x, b and writes r in FP64.
+# block row; vector passes per iteration by CG schedule (two-phase: p, z in, p out, q out and in,
+# x_delta and r in and out, invdiag in: ten; one-phase: r, w, s in and out, p and x_delta in and out,
+# invdiag in: eleven); a refresh reads x, b and writes r in FP64.
 
-def bytes_per_iteration(nnz, N, s):
-    return nnz * s + (nnz // 9) * 4 + 4 * (N + 1) + 10 * s * 3 * N
+SCHEDULE_NAMES = {0: "two-phase", 1: "fp64", 2: "one-phase"}
+
+
+def vector_passes(schedule):
+    return 11 if schedule == 2 else 10
+
+
+def bytes_per_iteration(nnz, N, s, vectors=10):
+    return nnz * s + (nnz // 9) * 4 + 4 * (N + 1) + vectors * s * 3 * N
 
 
 def bytes_per_refresh(nnz, N, s):
@@ -361,7 +370,9 @@ def run_batch(args, rank, world, local, dist):
         body.step(1e-3, 1, flags)
     torch.cuda.synchronize(local)
     tuning = body.tuning()
-    log(f"tuning: {tuning[0]} elements per block, {tuning[1]} CTAs per SM, refresh weight {tuning[2]}")
+    log(f"tuning: {tuning[0]} elements per block, {tuning[1]} CTAs per SM, refresh weight {tuning[2]}, "
+        f"CG schedule {SCHEDULE_NAMES[tuning[3]]}")
+    vpass = vector_passes(tuning[3])
     dist.barrier()
     sampler = ClockSampler(local)
     sampler.start()
@@ -371,7 +382,7 @@ def run_batch(args, rank, world, local, dist):
     alg_bytes = 0.0
     nnz = body.nnz_per_mesh
     nn = np.diff(body.node_offsets)
-    it_bytes = np.array([bytes_per_iteration(int(z), int(N), 4) for z, N in zip(nnz, nn)], dtype=np.float64)
+    it_bytes = np.array([bytes_per_iteration(int(z), int(N), 4, vpass) for z, N in zip(nnz, nn)], dtype=np.float64)
     rf_bytes = np.array([bytes_per_refresh(int(z), int(N), 4) for z, N in zip(nnz, nn)], dtype=np.float64)
     io_bytes = float(np.sum(16 * 3 * nn))  # b in, x out (FP64)
     ev0.record(stream)
@@ -434,7 +445,7 @@ def run_batch(args, rank, world, local, dist):
                          "gravity, alpha 0.01, beta 0.001, dt 1e-3, CG tol 1e-10; batched mixed precision, one "
                          "persistent solve launch per step, steps launched as a CUDA graph"),
             "tuning": {"elements_per_block": tuning[0], "ctas_per_sm": tuning[1], "refresh_weight": tuning[2],
-                       "how": "autotuned on the first warm-up step"},
+                       "cg_schedule": SCHEDULE_NAMES[tuning[3]], "how": "autotuned on the first warm-up step"},
             "meshes": len(all_scenes), "tets": total_tets, "nodes": total_nodes, "precision": "mixed",
             "l2": "working set (~2 GB) larger than L2: no flush needed",
             "parallelism": (f"meshes sharded over {world} ranks by greedy bin-packing (opensurgsim_gb300.shard), "
@@ -453,7 +464,7 @@ def run_batch(args, rank, world, local, dist):
             "traffic": load_traffic(f"pcg_persistent_batch{len(all_scenes)}") if world == 1 else None,
             "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": launch_ms,
             "peak_source": f"{peak_kind} (hbm_gbs)",
-            "bytes_model": ("per mesh: CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*3N) + refreshes x "
+            "bytes_model": (f"per mesh: CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + {vpass}*4*3N) + refreshes x "
                             "(nnz*4 + nnz/9*4 + 4(N+1) + 3*8*3N) + 16*3N"),
         },
     }
@@ -602,10 +613,12 @@ def run_single(args, rank, world, local, dist):
         launch_ms = agg["ms_spmv"] / max(1, args.steps)
         iters = agg["cg_iterations"] / max(1, args.steps)
         sweeps = agg["refinement_sweeps"] / max(1, args.steps)
-        per_launch = (iters * bytes_per_iteration(body.nnz, body.num_nodes, 4)
+        vpass = vector_passes(body.tuning()[3])
+        per_launch = (iters * bytes_per_iteration(body.nnz, body.num_nodes, 4, vpass)
                       + sweeps * bytes_per_refresh(body.nnz, body.num_nodes, 4) + 16 * body.n)
         kernel, key = "k_pcg_persistent (mixed)", f"pcg_persistent_{args.config}"
-        model = "CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*n) + refreshes x (nnz*4 + nnz/9*4 + 4(N+1) + 3*8*n) + 16n"
+        model = (f"CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + {vpass}*4*n) + refreshes x (nnz*4 + nnz/9*4 + 4(N+1) "
+                 "+ 3*8*n) + 16n")
     achieved = per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else None
     line = {
         "metric": metric,
@@ -749,7 +762,8 @@ def run_bar_full(args, rank, world, local, dist):
     peak, peak_kind = load_peak()
     am = agg["mixed"]
     solve_ms = am["ms_spmv"] / args.steps
-    per_launch = (am["cg_iterations"] / args.steps * bytes_per_iteration(bm.nnz, bm.num_nodes, 4)
+    vpass = vector_passes(tuning[3])
+    per_launch = (am["cg_iterations"] / args.steps * bytes_per_iteration(bm.nnz, bm.num_nodes, 4, vpass)
                   + am["refinement_sweeps"] / args.steps * bytes_per_refresh(bm.nnz, bm.num_nodes, 4) + 16 * bm.n)
     achieved = per_launch / (solve_ms / 1e3) / 1e9 if solve_ms > 0 else None
     errs_a = np.array(errs)
@@ -769,7 +783,8 @@ def run_bar_full(args, rank, world, local, dist):
                          f"{args.steps} steps from rest; 1,280,000 tets, 270,641 nodes, E log-U[1e4,1e6], "
                          "nu U[0.40,0.49], gravity, dt 1e-3, CG tol 1e-10; plain FP64 and mixed forms side by side"),
             "elements": m.num_tets, "nodes": m.num_nodes, "dofs": bm.n, "nnz": bm.nnz, "precision": "mixed",
-            "tuning": {"elements_per_block": tuning[0], "ctas_per_sm": tuning[1], "refresh_weight": tuning[2]},
+            "tuning": {"elements_per_block": tuning[0], "ctas_per_sm": tuning[1], "refresh_weight": tuning[2],
+                       "cg_schedule": SCHEDULE_NAMES[tuning[3]]},
             "l2": "working set larger than L2 (no flush needed)", "parallelism": f"replicas x{world}",
         },
         "gpu_launches": int(am["kernel_launches"]),
@@ -785,7 +800,7 @@ def run_bar_full(args, rank, world, local, dist):
             "traffic": load_traffic("pcg_persistent_bar") if abs(scene.mesh.h - BAR_H_WINDOW) < 1e-12 else None,
             "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": solve_ms,
             "peak_source": f"{peak_kind} (hbm_gbs)",
-            "bytes_model": ("CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + 10*4*n) + refreshes x "
+            "bytes_model": (f"CG iterations x (nnz*4 + nnz/9*4 + 4(N+1) + {vpass}*4*n) + refreshes x "
                             "(nnz*4 + nnz/9*4 + 4(N+1) + 3*8*n) + 16n"),
         },
         "fp64_path": {"value": val["fp64"], "unit": UNIT, "ms_per_step": ms["fp64"] / args.steps,
@@ -1256,7 +1271,8 @@ def main():
             log("plain FP64 form batched, and the mixed-vs-FP64 error over the whole scenario")
             tun = line["config"]["tuning"]
             fb, err = fp64_batch_and_error(meshes, local, args.steps, args.warmup,
-                                           (tun["elements_per_block"], tun["ctas_per_sm"], tun["refresh_weight"]))
+                                           (tun["elements_per_block"], tun["ctas_per_sm"], tun["refresh_weight"],
+                                            {v: k for k, v in SCHEDULE_NAMES.items()}[tun["cg_schedule"]]))
             line["fp64_batched"] = fb
             line["rel_disp_err_vs_fp64"] = err
             line["speedup_split"] = {

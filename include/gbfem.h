@@ -211,14 +211,26 @@ GBFEM_API gbfem_status gbfem_set_solver_params(gbfem_handle h, int32_t newton_ma
 											   double cg_tolerance, int32_t cg_max_iterations);
 
 /* ---- Tuning of the mixed form (no counterpart in the reference). With params.autotune the first
- * step times the element kernel at 32 and 64 elements per block and the persistent solve at 2, 3, 4
- * CTAs per SM and refresh weights 1 to 4 on its own system, and keeps the fastest. The solve's
- * partition sets the rounding of its sums, so a run that must repeat another bit for bit reads the
- * choice with gbfem_get_tuning and pins it with gbfem_set_tuning (which also disables autotune). */
+ * step times the element kernel at 32 and 64 elements per block and the persistent solve in each CG
+ * schedule at 2, 3, 4 CTAs per SM and refresh weights 1 to 4 on its own system, and keeps the
+ * fastest. The solve's schedule and partition set the rounding of its sums, so a run that must
+ * repeat another bit for bit reads the choice with gbfem_get_tuning and pins it with
+ * gbfem_set_tuning (which also disables autotune).
+ * CG schedules of the persistent solve (the iteration the mixed form runs; results agree to the
+ * solve's tolerance, not bit for bit; both stop by the same rule on the same FP64 residual):
+ *   GBFEM_CG_TWO_PHASE: two grid-wide phases an iteration (SpMV with p.Ap; then the row update
+ *     with r.z), the textbook PCG recurrences;
+ *   GBFEM_CG_ONE_PHASE: one phase an iteration (Chronopoulos and Gear's recurrences, both dot
+ *     products from one reduction): half the phases, larger neighbour records;
+ *   GBFEM_CG_FP64: FP64 batches (their only schedule).
+ * gbfem_set_tuning's cg_schedule -1 keeps the handle's current schedule. */
+#define GBFEM_CG_TWO_PHASE 0
+#define GBFEM_CG_FP64 1
+#define GBFEM_CG_ONE_PHASE 2
 GBFEM_API gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm,
-										int32_t* refresh_weight);
+										int32_t* refresh_weight, int32_t* cg_schedule);
 GBFEM_API gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t ctas_per_sm,
-										int32_t refresh_weight);
+										int32_t refresh_weight, int32_t cg_schedule);
 
 /* ---- Differentiation form. No counterpart in the reference (it has no adjoint); these serve
  * gradient-based identification on the same step (opensurgsim_gb300.autograd).

@@ -34,6 +34,10 @@ STEP_KEEP_SYSTEM = 2
 STEP_TIME_KERNELS = 4
 STEP_GRAPH = 8
 COMPLIANCE_WARPING = 1
+# CG schedules of the persistent solve (gbfem_get_tuning / gbfem_set_tuning)
+CG_TWO_PHASE = 0
+CG_FP64 = 1
+CG_ONE_PHASE = 2
 
 # Every symbol the header declares; the CPU tests check the library exports all of them.
 EXPORTED = [
@@ -147,9 +151,9 @@ def load():
         "gbfem_batch_info": (S, [H, I32, I32, I32, ctypes.POINTER(ctypes.c_int64)]),
         "gbfem_batch_segment_stats": (S, [H, I32, I32, I32, D]),
         "gbfem_set_materials_device": (S, [H, ctypes.c_void_p, ctypes.c_void_p]),
-        "gbfem_get_tuning": (S, [H, I32, I32, I32]),
+        "gbfem_get_tuning": (S, [H, I32, I32, I32, I32]),
         "gbfem_apply_compliance": (S, [H, ctypes.c_int32, D, D, ctypes.c_uint32, I32]),
-        "gbfem_set_tuning": (S, [H, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+        "gbfem_set_tuning": (S, [H, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
         "gbfem_set_solver_params": (S, [H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
         "gbfem_rollout_forward": (S, [H, ctypes.c_double, ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 4),
         "gbfem_rollout_backward": (S, [H] + [ctypes.c_void_p] * 6),

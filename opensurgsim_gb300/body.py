@@ -118,13 +118,17 @@ class Body:
         return X, st, it.value
 
     def tuning(self):
-        """(elements per block, CTAs per SM, refresh weight) of the mixed form's kernels."""
-        e, c, r = (ctypes.c_int32() for _ in range(3))
-        self._check(_lib.load().gbfem_get_tuning(self._h, ctypes.byref(e), ctypes.byref(c), ctypes.byref(r)))
-        return e.value, c.value, r.value
+        """(elements per block, CTAs per SM, refresh weight, CG schedule) of the mixed form's kernels;
+        the schedule is one of _lib.CG_TWO_PHASE, CG_ONE_PHASE, CG_FP64."""
+        e, c, r, g = (ctypes.c_int32() for _ in range(4))
+        self._check(_lib.load().gbfem_get_tuning(self._h, ctypes.byref(e), ctypes.byref(c), ctypes.byref(r),
+                                                 ctypes.byref(g)))
+        return e.value, c.value, r.value, g.value
 
-    def set_tuning(self, elems_per_block, ctas_per_sm, refresh_weight):
-        self._check(_lib.load().gbfem_set_tuning(self._h, int(elems_per_block), int(ctas_per_sm), int(refresh_weight)))
+    def set_tuning(self, elems_per_block, ctas_per_sm, refresh_weight, cg_schedule=-1):
+        """Pins the tuning (and stops autotuning); cg_schedule -1 keeps the handle's schedule."""
+        self._check(_lib.load().gbfem_set_tuning(self._h, int(elems_per_block), int(ctas_per_sm), int(refresh_weight),
+                                                 int(cg_schedule)))
 
     @classmethod
     def from_scene(cls, scene, **over):

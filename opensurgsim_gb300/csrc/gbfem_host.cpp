@@ -7,6 +7,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -17,6 +18,9 @@
 #include "gbfem_pcg.h"
 
 using namespace gbfem;
+
+static_assert(GBFEM_CG_TWO_PHASE == kPcgMixed2 && GBFEM_CG_FP64 == kPcgF64 && GBFEM_CG_ONE_PHASE == kPcgMixed1,
+			  "the ABI's CG schedules are the persistent solve's forms");
 
 namespace {
 
@@ -170,6 +174,7 @@ struct gbfem_handle_s
 	int smCount = 0, chunkWeightMin = 1;
 	int64_t chunkWeightTotal = 0;
 	int ctasPerSM = 4, refreshWeight = kRefreshWeightDefault, elemsPerBlock = 64;
+	int cgSchedule = kPcgMixed1;  // PcgForm of the mixed solve (FP64 batches: kPcgF64)
 	bool tuned = false;
 	int tuneVersion = 0;
 	// CUDA graph of one mixed-form step (GBFEM_STEP_GRAPH), rebuilt when dt, the timing flag or the
@@ -379,34 +384,36 @@ gbfem_status fail(gbfem_handle h, gbfem_status st, const std::string& msg)
 
 // The persistent solve's dynamic shared memory limit is a process-wide attribute of the kernel:
 // only ever raised, so a launch sized for one handle never breaks another's.
-cudaError_t raise_pcg_smem_limit(size_t bytes, bool f64)
+cudaError_t raise_pcg_smem_limit(size_t bytes, int form)
 {
 	static std::mutex mu;
-	static size_t current[2] = {48 * 1024, 48 * 1024};
+	static size_t current[3] = {48 * 1024, 48 * 1024, 48 * 1024};
 	std::lock_guard<std::mutex> lock(mu);
-	if (bytes <= current[f64]) return cudaSuccess;
-	const cudaError_t e = pcg_set_max_dynamic_smem(f64, (int)bytes);
-	if (e == cudaSuccess) current[f64] = bytes;
+	if (bytes <= current[form]) return cudaSuccess;
+	const cudaError_t e = pcg_set_max_dynamic_smem(form, (int)bytes);
+	if (e == cudaSuccess) current[form] = bytes;
 	return e;
 }
 
-// Grid of the persistent solve for `cps` CTAs per SM: G = min(cps * SMs, chunks); the largest share
-// of a CTA in chunks (its shared-memory partials) is bounded from the chunk weights: a weighted share
-// holds fewer than tot / (G wmin) + 1 chunks (tot at most kRefreshWeightMax times the plain total), a
-// counted one at most ceil(n / G). Fails if that many CTAs do not fit on an SM.
+// Grid of the persistent solve for `cps` CTAs per SM and the handle's refresh weight rw:
+// G = min(cps * SMs, chunks); the largest share of a CTA in chunks (its shared-memory partials) is
+// bounded from the chunk weights: a weighted share holds fewer than tot / (G wmin) + 1 chunks (tot at
+// most rw times the plain total, a refreshing segment's chunks weighing rw times theirs), a counted one
+// at most ceil(n / G). Fails if that many CTAs do not fit on an SM. Called again whenever rw changes.
 gbfem_status configure_pcg(gbfem_handle h, int cps)
 {
 	const int nseg = (int)h->segNode.size() - 1;
 	const int G = std::max(1, std::min(cps * h->smCount, h->nchunks));
-	const int64_t mW = (int64_t)kRefreshWeightMax * h->chunkWeightTotal / ((int64_t)G * h->chunkWeightMin) + 2;
+	const int64_t rw = std::max(1, h->refreshWeight);
+	const int64_t mW = rw * h->chunkWeightTotal / ((int64_t)G * h->chunkWeightMin) + 2;
 	const int64_t mC = (int64_t)h->nchunks / G + 2;
 	const int M = (int)std::max(mW, mC);
 	const size_t smem = pcg_smem_bytes(nseg, M);
 	if (smem > 160 * 1024) return fail(h, GBFEM_INVALID_ARG, "batch too large for the persistent solve");
-	const bool f64 = !h->mixed();
-	GB_CUDA(h, raise_pcg_smem_limit(smem, f64));
+	const int form = h->mixed() ? h->cgSchedule : kPcgF64;
+	GB_CUDA(h, raise_pcg_smem_limit(smem, form));
 	int perSM = 0;
-	GB_CUDA(h, pcg_occupancy(f64, &perSM, smem));
+	GB_CUDA(h, pcg_occupancy(form, &perSM, smem));
 	if (perSM < std::min(cps, (G + h->smCount - 1) / h->smCount))
 		return fail(h, GBFEM_INVALID_ARG, "persistent solve: " + std::to_string(cps) + " CTAs per SM do not fit");
 	h->pcgGrid = G;
@@ -742,10 +749,15 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		h->chunkWeightTotal = cumW[nchunks];
 		h->chunkWeightMin = std::max(1, wmin);
 		gbfem_status cst = GBFEM_INVALID_ARG;
-		for (int cps = 4; cps >= 1 && cst != GBFEM_OK; --cps) cst = configure_pcg(h, cps);
-		if (cst != GBFEM_OK) return cst;
+		std::string why;
+		for (int cps = 4; cps >= 1 && cst != GBFEM_OK; --cps)
+		{
+			cst = configure_pcg(h, cps);
+			if (cst != GBFEM_OK) why += (why.empty() ? "" : "; ") + h->err;
+		}
+		if (cst != GBFEM_OK) return fail(h, cst, "persistent solve: no grid fits (" + why + ")");
 		GB_CUDA(h, h->d_cumW.upload(cumW.data(), cumW.size(), s));
-		GB_CUDA(h, h->d_slots.alloc(4 * 4 * (size_t)h->smCount));  // any grid of up to 4 CTAs per SM
+		GB_CUDA(h, h->d_slots.alloc(2 * kPcgNV * 4 * (size_t)h->smCount));  // any grid of up to 4 CTAs per SM
 		// Each mesh of a batch has its own default CG cap, as each representation's solver would
 		// (Eigen's 2n for its own n; the FP32 CG needs the extra 64 on systems of a few dozen dofs).
 		std::vector<int> segCap(nseg);
@@ -826,8 +838,9 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		GB_CUDA(h, h->d_invdiag32.alloc(nv));
 		const size_t nr = 3 * (size_t)nrows;  // row-space vectors of the persistent solve
 		for (DevBuf<float>* b : {&h->d_xd, &h->d_invd, &h->d_r32, &h->d_q32}) GB_CUDA(h, b->alloc(nr));
-		// z and p of each row packed in one 32-byte record (one sector per neighbour gather)
-		for (DevBuf<float>* b : {&h->d_pA, &h->d_pB}) GB_CUDA(h, b->alloc(8 * (size_t)nrows));
+		// The rows' records that neighbours gather: two-phase schedule, z and p in 32 bytes (one sector);
+		// one-phase schedules, {r, w, s} and invdiag in 48 bytes.
+		for (DevBuf<float>* b : {&h->d_pA, &h->d_pB}) GB_CUDA(h, b->alloc(12 * (size_t)nrows));
 		for (DevBuf<double>* b : {&h->d_brs, &h->d_r64, &h->d_x64}) GB_CUDA(h, b->alloc(nr));
 		gbfem_status pst = setup_persistent();
 		if (pst != GBFEM_OK) return pst;
@@ -1051,6 +1064,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	a.pA = h->d_pA.p;
 	a.pB = h->d_pB.p;
 	a.q = h->d_q32.p;
+	a.pdir = h->d_q32.p;  // the one-phase schedules keep p where the two-phase one keeps q
 	a.cumW = h->d_cumW.p;
 	a.slots = h->d_slots.p;
 	a.maxChunksPerCta = h->maxChunksPerCta;
@@ -1078,7 +1092,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	attr[0].val.cooperative = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	GB_CUDA(h, pcg_launch(!h->mixed(), cfg, a));
+	GB_CUDA(h, pcg_launch(h->mixed() ? h->cgSchedule : kPcgF64, cfg, a));
 	if (ev1) GB_CUDA(h, cudaEventRecordWithFlags(ev1, st, evFlags));
 	h->launches += 1;
 	return GBFEM_OK;
@@ -1189,36 +1203,45 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 	}
 	GB_CUDA(h, cudaGetLastError());
 	float bestS = 1e30f;
-	int cBest = h->ctasPerSM, rBest = h->refreshWeight;
-	for (int cps : {2, 3, 4})
+	int cBest = h->ctasPerSM, rBest = h->refreshWeight, fBest = h->cgSchedule;
+	for (int form : {kPcgMixed2, kPcgMixed1})
 	{
-		if (configure_pcg(h, cps) != GBFEM_OK)
+		if (f64 && form != kPcgMixed1) continue;  // FP64 batches have one schedule
+		if (!f64) h->cgSchedule = form;
+		for (int cps : {2, 3, 4})
 		{
-			(void)cudaGetLastError();  // an infeasible candidate is skipped; clear any error it left
-			continue;
-		}
-		for (int rw : {1, 2, 3, 4})
-		{
-			if (f64 && rw != kRefreshWeightDefault) continue;  // the FP64 solve has no refreshes
-			h->refreshWeight = rw;
-			gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, e0, e1);
-			if (st != GBFEM_OK) return st;
-			GB_CUDA(h, elapsed());
-			st = check_pcg_error(h);
-			if (st != GBFEM_OK) return st;
-			if (t < bestS)
+			for (int rw : {1, 2, 3, 4})
 			{
-				bestS = t;
-				cBest = cps;
-				rBest = rw;
+				if (f64 && rw != kRefreshWeightDefault) continue;  // the FP64 solve has no refreshes
+				h->refreshWeight = rw;
+				if (configure_pcg(h, cps) != GBFEM_OK)
+				{
+					(void)cudaGetLastError();  // an infeasible candidate is skipped; clear any error it left
+					continue;
+				}
+				gbfem_status st = enqueue_mixed(h, h->d_rhs.p, h->d_dv.p, maxIter, e0, e1);
+				if (st != GBFEM_OK) return st;
+				GB_CUDA(h, elapsed());
+				st = check_pcg_error(h);
+				if (st != GBFEM_OK) return st;
+				if (getenv("GBFEM_TUNE_LOG"))
+					fprintf(stderr, "[gbfem tune] schedule %d ctas/SM %d refresh weight %d: %.3f ms\n", form, cps, rw, t);
+				if (t < bestS)
+				{
+					bestS = t;
+					cBest = cps;
+					rBest = rw;
+					fBest = form;
+				}
 			}
 		}
 	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
+	if (!f64) h->cgSchedule = fBest;
+	h->refreshWeight = rBest;
 	gbfem_status st = configure_pcg(h, cBest);
 	if (st != GBFEM_OK) return st;
-	h->refreshWeight = rBest;
 	h->tuned = true;
 	h->tuneVersion++;
 	h->err.clear();
@@ -1911,27 +1934,43 @@ gbfem_status gbfem_apply_compliance(gbfem_handle h, int32_t ncols, const double*
 	return allConverged ? GBFEM_OK : fail(h, GBFEM_CG_MAXITER, "a compliance column did not converge");
 }
 
-gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm, int32_t* refresh_weight)
+gbfem_status gbfem_get_tuning(gbfem_handle h, int32_t* elems_per_block, int32_t* ctas_per_sm, int32_t* refresh_weight,
+							  int32_t* cg_schedule)
 {
 	if (!h) return GBFEM_INVALID_ARG;
 	if (elems_per_block) *elems_per_block = h->elemsPerBlock;
 	if (ctas_per_sm) *ctas_per_sm = h->ctasPerSM;
 	if (refresh_weight) *refresh_weight = h->refreshWeight;
+	if (cg_schedule) *cg_schedule = h->mixed() ? h->cgSchedule : kPcgF64;
 	return GBFEM_OK;
 }
 
-gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t ctas_per_sm, int32_t refresh_weight)
+gbfem_status gbfem_set_tuning(gbfem_handle h, int32_t elems_per_block, int32_t ctas_per_sm, int32_t refresh_weight,
+							  int32_t cg_schedule)
 {
 	if (!h) return GBFEM_INVALID_ARG;
 	if (!h->persistent()) return fail(h, GBFEM_INVALID_ARG, "tuning applies to the mixed form and to batches");
 	if ((elems_per_block != 32 && elems_per_block != 64) || ctas_per_sm < 1 || ctas_per_sm > 4 || refresh_weight < 1 ||
 		refresh_weight > kRefreshWeightMax)
 		return fail(h, GBFEM_INVALID_ARG, "tuning: elems_per_block 32|64, ctas_per_sm 1..4, refresh_weight 1..8");
+	const bool mixedSchedule = cg_schedule == GBFEM_CG_TWO_PHASE || cg_schedule == GBFEM_CG_ONE_PHASE;
+	if (cg_schedule >= 0 && (h->mixed() ? !mixedSchedule : cg_schedule != GBFEM_CG_FP64))
+		return fail(h, GBFEM_INVALID_ARG, "tuning: cg_schedule must be -1 (keep), GBFEM_CG_TWO_PHASE or GBFEM_CG_ONE_PHASE "
+										  "(mixed form), GBFEM_CG_FP64 (FP64 batches)");
 	GB_CUDA(h, cudaSetDevice(h->device));
-	gbfem_status st = configure_pcg(h, ctas_per_sm);
-	if (st != GBFEM_OK) return st;
-	h->elemsPerBlock = elems_per_block;
+	const int oldSchedule = h->cgSchedule, oldWeight = h->refreshWeight;
+	if (h->mixed() && cg_schedule >= 0) h->cgSchedule = cg_schedule;
 	h->refreshWeight = refresh_weight;
+	gbfem_status st = configure_pcg(h, ctas_per_sm);
+	if (st != GBFEM_OK)
+	{
+		const std::string msg = h->err;
+		h->cgSchedule = oldSchedule;
+		h->refreshWeight = oldWeight;
+		configure_pcg(h, h->ctasPerSM);
+		return fail(h, st, msg);
+	}
+	h->elemsPerBlock = elems_per_block;
 	h->tuned = true;
 	h->tuneVersion++;
 	return GBFEM_OK;

@@ -435,6 +435,94 @@ __device__ __forceinline__ void spmv_row_zp64(const PcgArgs& a, const double2* _
 	}
 }
 
+// kPcgMixed1: a row's next residual and preconditioned residual from its record {r, d0}, {w, d1},
+// {s, d2} (d = invdiag): s' = w + beta s (= A p), r' = r - alpha s', u' = d r'. The owning row and
+// every row that gathers it call this one function, with explicit roundings, so all of them form
+// bit-identical u' and the SpMV multiplies exactly the vector whose dot products the owner takes.
+__device__ __forceinline__ void cg1_next(const float4& R, const float4& W, const float4& S, float al, float be,
+										 float& s0, float& s1, float& s2, float& r0, float& r1, float& r2, float& u0,
+										 float& u1, float& u2)
+{
+	s0 = __fmaf_rn(be, S.x, W.x);
+	s1 = __fmaf_rn(be, S.y, W.y);
+	s2 = __fmaf_rn(be, S.z, W.z);
+	r0 = __fmaf_rn(-al, s0, R.x);
+	r1 = __fmaf_rn(-al, s1, R.y);
+	r2 = __fmaf_rn(-al, s2, R.z);
+	u0 = __fmul_rn(R.w, r0);
+	u1 = __fmul_rn(W.w, r1);
+	u2 = __fmul_rn(S.w, r2);
+}
+
+// kPcgMixed1, CG step: w[row] (3 floats) = sum over the chunk's SELL slots of A_block * u'(J), u'(J)
+// formed by cg1_next from the neighbour's 48-byte record. Rounds of U slots: the columns of the next
+// round are loaded while this round's records are gathered; the last partial round is predicated.
+template <int U>
+__device__ __forceinline__ void spmv_row_cg1(const PcgArgs& a, const float4* __restrict__ rec, int c, int lane,
+											 float al, float be, float& a0, float& a1, float& a2)
+{
+	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
+	int k = k0;
+	int Jn[U];
+#pragma unroll
+	for (int u = 0; u < U; ++u) Jn[u] = (k + u < k1) ? __ldcs(&a.col[(k + u) * 32 + lane]) : 0;
+	for (;;)
+	{
+		const int nk = min(U, k1 - k);  // the same in every lane
+		if (nk <= 0) break;
+		int J[U];
+#pragma unroll
+		for (int u = 0; u < U; ++u) J[u] = Jn[u];
+#pragma unroll
+		for (int u = 0; u < U; ++u)
+			if (k + U + u < k1) Jn[u] = __ldcs(&a.col[(k + U + u) * 32 + lane]);
+		float4 R[U], W[U], S[U];
+#pragma unroll
+		for (int u = 0; u < U; ++u)
+			if (u < nk)
+			{
+				R[u] = rec[3 * J[u]];
+				W[u] = rec[3 * J[u] + 1];
+				S[u] = rec[3 * J[u] + 2];
+			}
+#pragma unroll
+		for (int u = 0; u < U; ++u)
+			if (u < nk)
+			{
+				float s0, s1, s2, r0, r1, r2, p0, p1, p2;
+				cg1_next(R[u], W[u], S[u], al, be, s0, s1, s2, r0, r1, r2, p0, p1, p2);
+				const float* vb = a.val + (size_t)(k + u) * 288 + lane;
+				a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
+				a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
+				a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
+			}
+		k += U;
+	}
+}
+
+// kPcgMixed1, after a refresh (and to start): w[row] = sum of A_block * u(J) with u(J) = d(J) r(J),
+// r(J) = (float)(r64(J) / s) the neighbour's rescaled true residual. The owner rounds its own r and u
+// by the same expressions. One slot at a time, the next slot's column loaded ahead (a few phases a
+// solve).
+__device__ __forceinline__ void spmv_row_r64(const PcgArgs& a, int c, int lane, double inv, float& a0, float& a1,
+											 float& a2)
+{
+	const int k0 = __ldg(&a.off[c]), k1 = __ldg(&a.off[c + 1]);
+	int Jn = (k0 < k1) ? __ldcs(&a.col[k0 * 32 + lane]) : 0;
+	for (int k = k0; k < k1; ++k)
+	{
+		const int J = Jn;
+		if (k + 1 < k1) Jn = __ldcs(&a.col[(k + 1) * 32 + lane]);
+		float p[3];
+#pragma unroll
+		for (int j = 0; j < 3; ++j) p[j] = __fmul_rn(a.invd[3 * J + j], __double2float_rn(a.r64[3 * J + j] * inv));
+		const float* vb = a.val + (size_t)k * 288 + lane;
+		a0 += __ldcs(vb) * p[0] + __ldcs(vb + 32) * p[1] + __ldcs(vb + 64) * p[2];
+		a1 += __ldcs(vb + 96) * p[0] + __ldcs(vb + 128) * p[1] + __ldcs(vb + 160) * p[2];
+		a2 += __ldcs(vb + 192) * p[0] + __ldcs(vb + 224) * p[1] + __ldcs(vb + 256) * p[2];
+	}
+}
+
 // Error-free transformations in FP32 (Knuth's TwoSum; the product's rounding error by FMA):
 // a + b = s + e and a * b = p + e exactly. The _rn intrinsics keep the compiler from contracting or
 // reassociating them.
@@ -511,15 +599,18 @@ __device__ __forceinline__ double residual_row(const PcgArgs& a, int c, int rs, 
 
 }  // namespace
 
-template <bool kF64>
-__global__ void __launch_bounds__(kPcgThreads, kF64 ? 3 : 4) k_pcg_persistent(PcgArgs a)
+template <int kForm>
+__global__ void __launch_bounds__(kPcgThreads, kForm == kPcgF64 ? 3 : 4) k_pcg_persistent(PcgArgs a)
 {
+	constexpr bool kF64 = kForm == kPcgF64;
+	constexpr bool kOne = kForm == kPcgMixed1;
+	constexpr int kRound = 2;  // records gathered a round by the one-phase SpMV (64 registers)
 	extern __shared__ double dsm[];
 	const int lane = threadIdx.x & 31;
 	const int warp = threadIdx.x >> 5;
 	const int nseg = a.nsegs, M = a.maxChunksPerCta, G = gridDim.x, B = blockIdx.x;
-	double* sp = dsm;                                  // [2][M] chunk partials of this CTA
-	int* sc = reinterpret_cast<int*>(dsm + 2 * M);     // segChunk copy (chunk prefix of all segments)
+	double* sp = dsm;                                      // [kPcgNV][M] chunk partials of this CTA
+	int* sc = reinterpret_cast<int*>(dsm + kPcgNV * M);    // segChunk copy (chunk prefix of all segments)
 	int* Cp = sc + (nseg + 1);                         // active set: chunk prefix
 	int* Wp = Cp + (nseg + 1);                         // active set: weight prefix
 	int* segW = Wp + (nseg + 1);                       // per-segment SpMV weight (block columns + 2 per chunk)
@@ -753,9 +844,13 @@ __global__ void __launch_bounds__(kPcgThreads, kF64 ? 3 : 4) k_pcg_persistent(Pc
 				a.invd[3 * rs + k] = (I >= 0) ? a.invdiag[3 * I + k] : 0.f;
 				a.xhl[3 * rs + k] = make_float2(0.f, 0.f);
 				a.xd[3 * rs + k] = 0.f;
+				if constexpr (kOne) a.pdir[3 * rs + k] = 0.f;
 				bb += bi * bi;
 			}
-			zpOld[2 * rs + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if constexpr (kOne)
+				reinterpret_cast<float4*>(a.pA)[3 * rs + 2] = make_float4(0.f, 0.f, 0.f, 0.f);  // s = A p = 0
+			else
+				zpOld[2 * rs + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
 		}
 		bb = warp_sum(bb);
 		if (lane == 0) sp[slot] = bb;
@@ -768,14 +863,256 @@ __global__ void __launch_bounds__(kPcgThreads, kF64 ? 3 : 4) k_pcg_persistent(Pc
 		S.s = sqrt(tot[0]);
 		S.iter = 0;
 		S.updates = 0;
-		S.mode = 0;
+		S.mode = kOne ? 2 : 0;  // kPcgMixed1 starts with the rescale phase (r = b / s, w = A u)
 		S.refreshAt = -8;
 		S.beta = 0.0;
+		S.ratio = 0.0;
 		S.converged = (tot[0] == 0.0 || tot[0] < S.threshold) ? 1 : 0;
 		S.nonfinite = !isfinite(tot[0]);
 		if (S.converged || S.nonfinite) finish(S);
 	});
 	if (!barrier()) return;
+
+	// ---- Out: x (dof space) = x_hl + x_delta.
+	auto write_out = [&]() {
+		for_chunks(all, sc, nseg, &shNext, [&](int, int, int c) {
+			const int rs = 32 * c + lane;
+			const int I = a.perm[rs];
+			if (I < 0) return;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				if constexpr (kF64)
+					a.x[3 * I + k] = a.x64[3 * rs + k];
+				else
+				{
+					const float2 xv = a.xhl[3 * rs + k];
+					a.x[3 * I + k] = (double(xv.x) + double(xv.y)) + double(a.xd[3 * rs + k]);
+				}
+			}
+		});
+	};
+
+	if constexpr (kOne)
+	{
+		// ---- kPcgMixed1: one grid phase an iteration (Chronopoulos and Gear). Stored per row:
+		// record {r_k, d}, {w_k = A u_k, d}, {s_{k-1} = A p_{k-1}, d} (gathered by neighbours, two buffers
+		// alternating by phase), p_{k-1} and x_delta (own row only). Scalars alpha_k, beta_k per segment.
+		// mode 0: p_k = u_k + beta p_{k-1}, s_k = w_k + beta s_{k-1}, x += alpha p_k, r_{k+1} = r_k - alpha s_k,
+		//         u_{k+1} = d r_{k+1}, w_{k+1} = A u_{k+1} (u' of gathered rows formed on the fly);
+		//         partials r.u, w.u, |r|^2; then beta = g' / g, alpha = g' / (w.u - beta g' / alpha).
+		// mode 1: r64 = b - A (x_hl + x_delta) in double-float (the record's s carried to the other buffer).
+		// mode 2: fold x, r = r64 / s, u = d r, w = A u, p and s scaled by the residual's rescale; partials as
+		//         mode 0; beta from the last r.u before the refresh (rescaled), alpha as mode 0. Also the
+		//         first phase (no refresh yet: beta = 0, alpha = r.u / w.u).
+		float4* recOld = reinterpret_cast<float4*>(a.pA);
+		float4* recNew = reinterpret_cast<float4*>(a.pB);
+		const int maxLoop1 = 3 * a.maxIter + 8;  // a refresh takes two extra phases
+		for (int it = 0; it < maxLoop1; ++it)
+		{
+			phase_start(true, it == 0);
+			if (finished >= nseg) break;
+			cache_segments(actW);
+			for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
+				const int rs = 32 * c + lane;
+				const int d0 = 3 * rs;
+				double betaD, alphaD, sD, ratioD;
+				int mode;
+				seg_scalars(s, betaD, mode, alphaD, sD, ratioD);
+				float g = 0.f, dl = 0.f, rr = 0.f;
+				double rrTrue = 0.0;
+				if (mode == 0)
+				{
+					const float al = float(alphaD), be = float(betaD), as = float(alphaD * sD);
+					float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+					spmv_row_cg1<kRound>(a, recOld, c, lane, al, be, w0, w1, w2);
+					const float4 R = recOld[d0], W = recOld[d0 + 1], S = recOld[d0 + 2];
+					float po[3], xo[3];
+#pragma unroll
+					for (int i = 0; i < 3; ++i)
+					{
+						po[i] = __ldcs(&a.pdir[d0 + i]);
+						xo[i] = __ldcs(&a.xd[d0 + i]);
+					}
+					float sn[3], rn[3], un[3];
+					cg1_next(R, W, S, al, be, sn[0], sn[1], sn[2], rn[0], rn[1], rn[2], un[0], un[1], un[2]);
+					const float d[3] = {R.w, W.w, S.w}, r[3] = {R.x, R.y, R.z}, w[3] = {w0, w1, w2};
+#pragma unroll
+					for (int i = 0; i < 3; ++i)
+					{
+						const float pk = __fmaf_rn(be, po[i], __fmul_rn(d[i], r[i]));  // u_k = d r_k as formed last phase
+						__stcs(&a.pdir[d0 + i], pk);
+						__stcs(&a.xd[d0 + i], __fmaf_rn(as, pk, xo[i]));
+						g += rn[i] * un[i];
+						dl += w[i] * un[i];
+						rr += rn[i] * rn[i];
+					}
+					recNew[d0] = make_float4(rn[0], rn[1], rn[2], d[0]);
+					recNew[d0 + 1] = make_float4(w0, w1, w2, d[1]);
+					recNew[d0 + 2] = make_float4(sn[0], sn[1], sn[2], d[2]);
+				}
+				else if (mode == 1)
+				{
+					rrTrue = residual_row(a, c, rs, lane);
+					recNew[d0 + 2] = recOld[d0 + 2];  // s, read by the rescale phase from the other buffer
+				}
+				else
+				{
+					const double inv = 1.0 / sD;
+					const float ratio = float(ratioD);
+					float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+					spmv_row_r64(a, c, lane, inv, w0, w1, w2);
+					const float4 So = recOld[d0 + 2];
+					float2 xo[3];
+					float xv[3], po[3], d[3];
+					double rv[3];
+#pragma unroll
+					for (int i = 0; i < 3; ++i)
+					{
+						xo[i] = a.xhl[d0 + i];
+						xv[i] = __ldcs(&a.xd[d0 + i]);
+						po[i] = __ldcs(&a.pdir[d0 + i]);
+						rv[i] = a.r64[d0 + i];
+						d[i] = a.invd[d0 + i];
+					}
+					const float so[3] = {So.x, So.y, So.z}, w[3] = {w0, w1, w2};
+					float r[3], sn[3];
+#pragma unroll
+					for (int i = 0; i < 3; ++i)
+					{
+						// Fold x_delta into the float pair: TwoSum, then renormalise.
+						float hs, he, h2, l2;
+						two_sum(xo[i].x, xv[i], hs, he);
+						two_sum(hs, __fadd_rn(he, xo[i].y), h2, l2);
+						a.xhl[d0 + i] = make_float2(h2, l2);
+						__stcs(&a.xd[d0 + i], 0.f);
+						__stcs(&a.pdir[d0 + i], __fmul_rn(po[i], ratio));
+						sn[i] = __fmul_rn(so[i], ratio);
+						r[i] = __double2float_rn(rv[i] * inv);
+						const float u = __fmul_rn(d[i], r[i]);
+						g += r[i] * u;
+						dl += w[i] * u;
+						rr += r[i] * r[i];
+					}
+					recNew[d0] = make_float4(r[0], r[1], r[2], d[0]);
+					recNew[d0 + 1] = make_float4(w0, w1, w2, d[1]);
+					recNew[d0 + 2] = make_float4(sn[0], sn[1], sn[2], d[2]);
+				}
+				if (mode == 1)
+				{
+					rrTrue = warp_sum(rrTrue);
+					if (lane == 0)
+					{
+						sp[slot] = rrTrue;
+						sp[M + slot] = 0.0;
+						sp[2 * M + slot] = 0.0;
+					}
+				}
+				else
+				{
+					g = warp_sum(g);
+					dl = warp_sum(dl);
+					rr = warp_sum(rr);
+					if (lane == 0)
+					{
+						sp[slot] = g;
+						sp[M + slot] = dl;
+						sp[2 * M + slot] = rr;
+					}
+				}
+			});
+			reduce_segments<3>(a, actW, sc, sp, [&](int s, const double* tot) {
+				SegCtl& S = a.seg[s];
+				if (S.mode == 1)
+				{
+					S.rrTrue = tot[0];
+					S.updates += 1;
+					if (tot[0] < S.threshold)
+					{
+						S.converged = 1;  // like Eigen, the converging iteration is not counted
+						finish(S);
+					}
+					else if (!isfinite(tot[0]) || S.iter + 1 >= seg_cap(s))
+					{
+						S.converged = 0;
+						S.nonfinite = !isfinite(tot[0]);
+						S.iter += 1;
+						finish(S);
+					}
+					else
+					{
+						const double sNew = sqrt(tot[0]);
+						S.ratio = S.s / sNew;
+						S.s = sNew;
+						S.mode = 2;
+					}
+					return;
+				}
+				const double gN = tot[0], dN = tot[1], rr = tot[2];
+				S.rr32 = rr;
+				if (S.mode == 2)
+				{
+					double beta = 0.0, alpha;
+					if (S.updates == 0)
+						alpha = gN / dN;
+					else
+					{
+						beta = gN / (S.rzPend * S.ratio * S.ratio);
+						alpha = gN / (dN - beta * gN / S.alpha);
+					}
+					S.rrLast = rr;
+					if (!isfinite(rr) || !isfinite(alpha))
+					{
+						S.converged = 0;
+						S.nonfinite = 1;
+						finish(S);
+						return;
+					}
+					S.beta = beta;
+					S.alpha = alpha;
+					S.rz = gN;
+					if (S.updates > 0) S.iter += 1;
+					S.mode = 0;
+					return;
+				}
+				if (!isfinite(rr))
+				{
+					S.converged = 0;
+					S.nonfinite = 1;
+					finish(S);
+				}
+				else if (S.s * S.s * rr < S.threshold || rr < a.drop * S.rrLast || S.iter + 1 >= seg_cap(s))
+				{
+					S.mode = 1;  // true residual of x_{k+1} next
+					S.refreshAt = ph;
+					S.rzPend = S.rz;
+					atomicAdd(&a.g->refreshIn[ph & 1], 1);
+				}
+				else
+				{
+					const double beta = gN / S.rz;
+					const double alpha = gN / (dN - beta * gN / S.alpha);
+					if (!isfinite(alpha))
+					{
+						S.converged = 0;
+						S.nonfinite = 1;
+						finish(S);
+						return;
+					}
+					S.beta = beta;
+					S.alpha = alpha;
+					S.rz = gN;
+					S.iter += 1;
+				}
+			});
+			if (!barrier()) return;
+			float4* t = recOld;
+			recOld = recNew;
+			recNew = t;
+		}
+		write_out();
+		return;
+	}
 
 	// ---- I2: r = b / s (FP32), z = invdiag r, rz, |r|^2. FP64 form: z = invdiag r, rz (r = b).
 	phase_start(false, true);
@@ -1096,44 +1433,39 @@ __global__ void __launch_bounds__(kPcgThreads, kF64 ? 3 : 4) k_pcg_persistent(Pc
 		zOld64 = zNew64;
 		zNew64 = t64;
 	}
-
-	// ---- Out: x (dof space) = x_hl + x_delta.
-	for_chunks(all, sc, nseg, &shNext, [&](int, int, int c) {
-		const int rs = 32 * c + lane;
-		const int I = a.perm[rs];
-		if (I < 0) return;
-#pragma unroll
-		for (int k = 0; k < 3; ++k)
-		{
-			if constexpr (kF64)
-				a.x[3 * I + k] = a.x64[3 * rs + k];
-			else
-			{
-				const float2 xv = a.xhl[3 * rs + k];
-				a.x[3 * I + k] = (double(xv.x) + double(xv.y)) + double(a.xd[3 * rs + k]);
-			}
-		}
-	});
+	write_out();
 }
 
-template __global__ void k_pcg_persistent<false>(PcgArgs a);
-template __global__ void k_pcg_persistent<true>(PcgArgs a);
+template __global__ void k_pcg_persistent<kPcgMixed2>(PcgArgs a);
+template __global__ void k_pcg_persistent<kPcgF64>(PcgArgs a);
+template __global__ void k_pcg_persistent<kPcgMixed1>(PcgArgs a);
 
-cudaError_t pcg_set_max_dynamic_smem(bool f64, int bytes)
+namespace {
+using PcgKernel = void (*)(PcgArgs);
+PcgKernel pcg_kernel(int form)
 {
-	return f64 ? cudaFuncSetAttribute(k_pcg_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-			   : cudaFuncSetAttribute(k_pcg_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	switch (form)
+	{
+	case kPcgF64: return k_pcg_persistent<kPcgF64>;
+	case kPcgMixed1: return k_pcg_persistent<kPcgMixed1>;
+	default: return k_pcg_persistent<kPcgMixed2>;
+	}
+}
+}  // namespace
+
+cudaError_t pcg_set_max_dynamic_smem(int form, int bytes)
+{
+	return cudaFuncSetAttribute(pcg_kernel(form), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t pcg_occupancy(bool f64, int* ctasPerSM, size_t smem)
+cudaError_t pcg_occupancy(int form, int* ctasPerSM, size_t smem)
 {
-	return f64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSM, k_pcg_persistent<true>, kPcgThreads, smem)
-			   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSM, k_pcg_persistent<false>, kPcgThreads, smem);
+	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSM, pcg_kernel(form), kPcgThreads, smem);
 }
 
-cudaError_t pcg_launch(bool f64, const cudaLaunchConfig_t& cfg, const PcgArgs& a)
+cudaError_t pcg_launch(int form, const cudaLaunchConfig_t& cfg, const PcgArgs& a)
 {
-	return f64 ? cudaLaunchKernelEx(&cfg, k_pcg_persistent<true>, a) : cudaLaunchKernelEx(&cfg, k_pcg_persistent<false>, a);
+	return cudaLaunchKernelEx(&cfg, pcg_kernel(form), a);
 }
 
 namespace {

@@ -10,6 +10,27 @@ namespace gbfem {
 constexpr int kPcgThreads = 256;
 constexpr int kPcgChunkWeight = 2;  // per-chunk constant added to the block-column count (SpMV work)
 
+// Forms of the persistent solve (template argument of k_pcg_persistent).
+//  kPcgMixed2: FP32 CG in two grid phases an iteration (q = A p with p formed on the fly and p.q;
+//              then the row-local x, r, z update with r.z), double-float refreshes;
+//  kPcgF64:    plain FP64 CG (Eigen's iteration and stopping rule), the same two phases;
+//  kPcgMixed1: FP32 CG in one grid phase an iteration (Chronopoulos and Gear's recurrences: the
+//              SpMV w = A u runs on the next preconditioned residual, formed on the fly for gathered
+//              rows from their {r, w, s} records, and r.u and w.u come from the same phase), with the
+//              same refreshes and stopping rule as kPcgMixed2. Its SpMV gathers two 48-byte records a
+//              round (four would spill at 64 registers; at 80 registers and 3 CTAs per SM they measured
+//              slower on both the 256-mesh batch and the 1.28M-tet bar, and so did three with a spill).
+// Measured on GB300: the one-phase schedule halves the phases (bar: 972 -> 491 a solve, 24.8 -> 19.8
+// ms), while on the 256-mesh batch, whose phases mostly stream the whole batch, its 48-byte records
+// (two sectors a gather, against one) cost what the saved phases gain (42.1 vs 42.8 ms).
+enum PcgForm : int
+{
+	kPcgMixed2 = 0,
+	kPcgF64 = 1,
+	kPcgMixed1 = 2,
+};
+constexpr int kPcgNV = 3;  // per-chunk partial values a phase can reduce (shared memory, cross-CTA slots)
+
 // Per-segment (per-mesh) CG state, in device memory. Written by the CTA that completes a
 // segment's reduction, read by every CTA after the next grid barrier.
 struct alignas(16) SegCtl
@@ -65,7 +86,7 @@ struct PcgArgs
 	const int* segChunk;   // nsegs + 1: first chunk of each segment (segments own contiguous chunks)
 	const int* segMaxIter; // nsegs: per-segment CG iteration cap, or null: maxIter for every segment
 	const int* cumW;       // nchunks + 1: prefix of (block columns + kPcgChunkWeight) per chunk
-	double* slots;         // 4 * grid cross-CTA partials: [value k][first/last][cta]
+	double* slots;         // 2 * kPcgNV * grid cross-CTA partials: [value k][first/last][cta]
 	// in / out (dof space, FP64)
 	const double* b;
 	const float* invdiag;
@@ -77,9 +98,10 @@ struct PcgArgs
 	float* xd;
 	float* invd;
 	float* r;
-	float* pA;             // 8 floats per row: z (3), pad, p (3), pad; 32-byte aligned
-	float* pB;
+	float* pA;             // kPcgMixed2: 8 floats per row: z (3), pad, p (3), pad; 32-byte aligned
+	float* pB;             // kPcgMixed1: 12 floats per row: {r (3), d0}, {w (3), d1}, {s (3), d2}, d = invdiag
 	float* q;
+	float* pdir;           // kPcgMixed1: search direction p, 3 floats per row (read by its own row only)
 	SegCtl* seg;
 	PcgGlobal* g;
 	// FP64 form (k_pcg_persistent<true>): plain FP64 CG on the FP64 SELL values, Eigen's iteration and
@@ -97,19 +119,19 @@ struct PcgArgs
 // prefix arrays and the per-segment base weights.
 inline size_t pcg_smem_bytes(int nsegs, int maxChunksPerCta)
 {
-	return 2 * sizeof(double) * (size_t)maxChunksPerCta + 4 * sizeof(int) * (size_t)(nsegs + 1);
+	return kPcgNV * sizeof(double) * (size_t)maxChunksPerCta + 4 * sizeof(int) * (size_t)(nsegs + 1);
 }
 
-// kF64 = false: the mixed-precision solve (FP32 CG with double-float refreshes); true: plain FP64 CG.
-template <bool kF64>
+// kForm: a PcgForm.
+template <int kForm>
 __global__ void k_pcg_persistent(PcgArgs a);
 
-// Host access to the two instantiations (the kernel templates' host stubs are local to their
+// Host access to the instantiations (the kernel templates' host stubs are local to their
 // translation unit): the dynamic shared memory limit, the co-resident CTAs per SM, and a launch
 // with the caller's configuration (grid, block, shared memory, stream, cooperative attribute).
-cudaError_t pcg_set_max_dynamic_smem(bool f64, int bytes);
-cudaError_t pcg_occupancy(bool f64, int* ctasPerSM, size_t smem);
-cudaError_t pcg_launch(bool f64, const cudaLaunchConfig_t& cfg, const PcgArgs& a);
+cudaError_t pcg_set_max_dynamic_smem(int form, int bytes);
+cudaError_t pcg_occupancy(int form, int* ctasPerSM, size_t smem);
+cudaError_t pcg_launch(int form, const cudaLaunchConfig_t& cfg, const PcgArgs& a);
 
 // Self-test of the grid barrier on a PcgGlobal of its own (zeroed by the caller): `phases` barriers
 // over a cooperative grid. With `stall` set, the arrival counter starts at gridDim.x, so no block is

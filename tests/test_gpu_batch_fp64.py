@@ -83,8 +83,8 @@ def test_fp64_batch_autotunes_and_adjoint_runs(gpu_lib):
     scenes = _scenes()
     b = Body([s.mesh for s in scenes], precision=_lib.PRECISION_FP64, autotune=True, **KW)
     assert b.step(1e-3, 2) == _lib.GBFEM_OK
-    eb, cps, rw = b.tuning()
-    assert cps in (1, 2, 3, 4)
+    eb, cps, rw, sched = b.tuning()
+    assert cps in (1, 2, 3, 4) and sched == _lib.CG_FP64
     grads = {}
     dev = torch.device("cuda:0")
     for prec in ("fp64", "mixed"):

@@ -62,8 +62,9 @@ def test_autotune_picks_a_candidate_and_pinning_reproduces_it(gpu_lib):
     _, ref = _batch()
     assert t.step(1e-3, 3) == _lib.GBFEM_OK
     assert ref.step(1e-3, 3) == _lib.GBFEM_OK
-    e, c, r = t.tuning()
+    e, c, r, g = t.tuning()
     assert e in (32, 64) and c in (2, 3, 4) and r in (1, 2, 3, 4)
+    assert g in (_lib.CG_TWO_PHASE, _lib.CG_ONE_PHASE)
     xt, _ = t.state()
     xr, _ = ref.state()
     for k, s in enumerate(scenes):
@@ -73,7 +74,7 @@ def test_autotune_picks_a_candidate_and_pinning_reproduces_it(gpu_lib):
         assert np.linalg.norm(xt[3 * n0:3 * n1] - x0 - d) <= 1e-6 * np.linalg.norm(d)
     # A second body pinned to the tuned choice repeats the tuned run bit for bit.
     _, p = _batch()
-    p.set_tuning(e, c, r)
+    p.set_tuning(e, c, r, g)
     assert p.step(1e-3, 3) == _lib.GBFEM_OK
     assert np.array_equal(p.state()[0], xt)
 
@@ -87,10 +88,16 @@ def test_autotune_with_graph_steps(gpu_lib):
 
 def test_set_tuning_rejects_bad_values(gpu_lib):
     _, b = _batch()
+    before = b.tuning()
     with pytest.raises(_lib.GbfemError):
         b.set_tuning(48, 2, 6)
     with pytest.raises(_lib.GbfemError):
         b.set_tuning(64, 5, 6)
+    with pytest.raises(_lib.GbfemError):
+        b.set_tuning(64, 2, 2, _lib.CG_FP64)  # the FP64 schedule on a mixed batch
+    with pytest.raises(_lib.GbfemError):
+        b.set_tuning(64, 2, 2, 9)
+    assert b.tuning() == before  # a rejected call leaves the tuning as it was
 
 
 def test_timed_graph_steps_report_the_solve_time(gpu_lib):

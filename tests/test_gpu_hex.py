@@ -114,7 +114,7 @@ def test_hex_autotune_then_graph(gpu_lib):
     s = mesh.scene_hex_cube(6, 6, 8, seed=3, jitter=0.1)
     b = Body(s.mesh, precision=_lib.PRECISION_MIXED, element_type=HEX, autotune=True, cg_tolerance=1e-10, **KW)
     assert b.step(1e-3, 5, _lib.STEP_GRAPH) == _lib.GBFEM_OK
-    e, c, r = b.tuning()
+    e, c, r, g = b.tuning()
     assert c in (2, 3, 4) and r in (1, 2, 3, 4)
     assert np.all(np.isfinite(b.state()[0]))
 

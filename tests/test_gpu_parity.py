@@ -185,14 +185,18 @@ def test_mixed_matches_fp64_gpu_and_is_deterministic(gpu_lib):
     assert a.stats()["cg_relative_residual"] < 1e-10
 
 
-def test_batch_of_uneven_meshes_matches_individual_oracles(gpu_lib):
-    """Batched mixed form: every mesh of a batch steps like its own FP64 oracle (<= 1e-6)."""
+@pytest.mark.parametrize("schedule", [_lib.CG_TWO_PHASE, _lib.CG_ONE_PHASE])
+def test_batch_of_uneven_meshes_matches_individual_oracles(gpu_lib, schedule):
+    """Batched mixed form, each CG schedule of the persistent solve: every mesh of a batch steps like
+    its own FP64 oracle (<= 1e-6)."""
     rng = np.random.default_rng(11)
     scenes = [mesh.scene_cube(a, b, c, seed=k, young=float(E))
               for k, (a, b, c, E) in enumerate([(2, 2, 3, 1e4), (4, 3, 2, 1e5), (1, 1, 1, 3e5), (5, 5, 6, 1e6),
                                                  (3, 6, 2, 2e4), (7, 7, 7, 8e4)])]
     batch = Body([s.mesh for s in scenes], rayleigh_mass=0.01, rayleigh_stiffness=0.001, gravity=(0, 0, -9.81),
                  cg_tolerance=1e-10, precision=_lib.PRECISION_MIXED)
+    batch.set_tuning(64, 3, 2, schedule)
+    assert batch.tuning()[3] == schedule
     assert batch.num_meshes == len(scenes)
     oracles = [O.OracleModel.from_scene(s) for s in scenes]
     v0 = rng.normal(0, 0.01, batch.n)
