@@ -1185,6 +1185,8 @@ gbfem_status tune_mixed(gbfem_handle h, const double* xt, const double* vt, doub
 			GB_CUDA(h, elapsed());
 			float& best = (ept == 32) ? bestE32 : bestE64;
 			if (rep > 0) best = std::min(best, t);
+			if (rep > 0 && getenv("GBFEM_TUNE_LOG"))
+				fprintf(stderr, "[gbfem tune] element kernel %d elements per block: %.3f ms\n", ept, t);
 		}
 	if (!h->hex() && !f64) h->elemsPerBlock = (bestE32 < bestE64) ? 32 : 64;
 	if (f64)
