@@ -245,14 +245,25 @@ __device__ __forceinline__ void for_chunks(const SetView& V, const int* sc, int 
 }
 
 // Reduce this CTA's chunk partials per segment (sp[k * M + slot]) and complete segments across
-// CTAs; fin(s, totals) runs once per segment in lane 0 of one warp of the completing CTA. The
-// segments of the CTA's range are independent: warp w takes the range's segments w, w + 8, ...
+// CTAs; fin(s, totals) runs once per segment, in lane 0 of one warp (or thread 0) of the completing
+// CTA. The segments of the CTA's range are independent: warp w takes the range's segments w, w + 8, ...
+// A segment spread over CTAs bf..bl is completed by the last of them to arrive (ticket), which adds
+// the CTAs' partials in a fixed order: in the arriving warp when they are few (at most two a lane),
+// else by all threads of the CTA in one round of loads (one large mesh spans every CTA of the grid:
+// one warp would need several dependent rounds of L2 loads on the path to the grid barrier).
 template <int NV, typename Fin>
 __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* sc, const double* sp, Fin fin)
 {
 	__syncthreads();
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	const int nseg = a.nsegs, G = gridDim.x, B = blockIdx.x, M = a.maxChunksPerCta;
+	// Wide segments this CTA completes (at most two: the first and the last of its range).
+	__shared__ int shWideN;
+	__shared__ int shWideS[2];
+	__shared__ int2 shWideFl[2];
+	__shared__ double shWarpSum[kPcgNV][kWarps];
+	if (threadIdx.x == 0) shWideN = 0;
+	__syncthreads();
 	auto arrive = [&](int s, int2 fl, const double* v) {
 		const int which = (B > fl.x) ? 0 : 1;  // 0: first slot (CTAs after bf), 1: last slot (bf)
 		unsigned tk = 0;
@@ -264,31 +275,35 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 		}
 		tk = __shfl_sync(kFull, tk, 0);
 		if (tk != (unsigned)(fl.y - fl.x)) return;
-		__syncwarp();
-		// The CTAs' partials, lane l adding CTAs bf + 1 + l, bf + 33 + l, ... in that order; the loads of
-		// four rounds (and of every value) are issued before they are added, since a segment can span
-		// every CTA of the grid (one large mesh: ~20 partials a lane).
-		double u[NV], tot[NV];
-#pragma unroll
-		for (int k = 0; k < NV; ++k) u[k] = (lane == 0) ? __ldcg(&a.slots[(size_t)(2 * k + 1) * G + fl.x]) : 0.0;
-		int b = fl.x + 1 + lane;
-		for (; b + 96 <= fl.y; b += 128)
+		if (fl.y - fl.x > 64)
 		{
-			double t[NV][4];
-#pragma unroll
-			for (int k = 0; k < NV; ++k)
-#pragma unroll
-				for (int j = 0; j < 4; ++j) t[k][j] = __ldcg(&a.slots[(size_t)(2 * k) * G + b + 32 * j]);
-#pragma unroll
-			for (int k = 0; k < NV; ++k)
-#pragma unroll
-				for (int j = 0; j < 4; ++j) u[k] += t[k][j];
+			if (lane == 0)
+			{
+				const int i = atomicAdd(&shWideN, 1);
+				if (i < 2)
+				{
+					shWideS[i] = s;
+					shWideFl[i] = fl;
+				}
+				else
+					atomicExch(&a.g->err, 2);  // cannot happen (a range has one first and one last segment)
+			}
+			return;
 		}
-		for (; b <= fl.y; b += 32)
+		__syncwarp();
+		// The CTAs' partials, lane l adding CTAs bf + 1 + l, bf + 33 + l in that order, all loads issued
+		// before they are added.
+		double u[NV], t[NV], tot[NV];
+		const int b0 = fl.x + 1 + lane, b1 = b0 + 32;
 #pragma unroll
-			for (int k = 0; k < NV; ++k) u[k] += __ldcg(&a.slots[(size_t)(2 * k) * G + b]);
+		for (int k = 0; k < NV; ++k)
+		{
+			u[k] = (lane == 0) ? __ldcg(&a.slots[(size_t)(2 * k + 1) * G + fl.x]) : 0.0;
+			t[k] = (b0 <= fl.y) ? __ldcg(&a.slots[(size_t)(2 * k) * G + b0]) : 0.0;
+			tot[k] = (b1 <= fl.y) ? __ldcg(&a.slots[(size_t)(2 * k) * G + b1]) : 0.0;
+		}
 #pragma unroll
-		for (int k = 0; k < NV; ++k) tot[k] = warp_sum(u[k]);
+		for (int k = 0; k < NV; ++k) tot[k] = warp_sum((u[k] + t[k]) + tot[k]);
 		if (lane == 0)
 		{
 			a.seg[s].ticket = 0u;
@@ -329,6 +344,45 @@ __device__ void reduce_segments(const PcgArgs& a, const SetView& V, const int* s
 			for (int k = 0; k < NV; ++k) v[k] = 0.0;
 			arrive(s, seg_ctas(a, V, sc, s), v);
 		}
+	}
+	__syncthreads();
+	const int nWide = min(shWideN, 2);
+	if (nWide == 0) return;
+	// The ticket's acquire was made by one thread; every thread of the CTA reads the other CTAs' slots.
+	__threadfence();
+	for (int i = 0; i < nWide; ++i)
+	{
+		const int s = shWideS[i];
+		const int2 fl = shWideFl[i];
+		// Thread j adds CTAs bf + 1 + j, bf + 1 + j + 256, ...; thread 0 starts from bf's slot; the warps'
+		// sums are added in warp order: a fixed order whatever the timing.
+		double u[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k) u[k] = (threadIdx.x == 0) ? __ldcg(&a.slots[(size_t)(2 * k + 1) * G + fl.x]) : 0.0;
+		for (int b = fl.x + 1 + threadIdx.x; b <= fl.y; b += kPcgThreads)
+#pragma unroll
+			for (int k = 0; k < NV; ++k) u[k] += __ldcg(&a.slots[(size_t)(2 * k) * G + b]);
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+		{
+			const double w = warp_sum(u[k]);
+			if (lane == 0) shWarpSum[k][wid] = w;
+		}
+		__syncthreads();
+		if (threadIdx.x == 0)
+		{
+			double tot[NV];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+			{
+				tot[k] = 0.0;
+#pragma unroll
+				for (int w = 0; w < kWarps; ++w) tot[k] += shWarpSum[k][w];
+			}
+			a.seg[s].ticket = 0u;
+			fin(s, tot);
+		}
+		__syncthreads();
 	}
 }
 
@@ -649,7 +703,7 @@ __global__ void __launch_bounds__(kPcgThreads, kForm == kPcgF64 ? 3 : 4) k_pcg_p
 	all.tot = a.nchunks;
 	all.lo = (int)(((long long)all.n * B + G - 1) / G);
 	all.hi = (int)(((long long)all.n * (B + 1) + G - 1) / G);
-	SetView actW, actC;  // active set: block-column-weighted and chunk-count partitions
+	SetView actW{}, actC{};  // active set: block-column-weighted and chunk-count partitions (set by rebuild)
 	actW.Cp = actC.Cp = Cp;
 	actW.Wp = Wp;
 	actC.Wp = nullptr;
@@ -785,6 +839,55 @@ __global__ void __launch_bounds__(kPcgThreads, kForm == kPcgF64 ? 3 : 4) k_pcg_p
 		}
 		__syncthreads();
 	};
+	// phase_start and cache_segments for view V in one round of loads: the scalars of the segments in
+	// this CTA's range of V as the partition stands are loaded together with the previous phase's
+	// finish and refresh counts; only when those call for a new partition is the cache loaded again.
+	auto phase_begin = [&](bool phase1, bool force, const SetView& V) {
+		if (force)
+		{
+			phase_start(phase1, true);
+			cache_segments(V);
+			return;
+		}
+		if (threadIdx.x == 0)
+		{
+			int s0 = 0, cnt = 0;
+			if (V.lo < V.hi)
+			{
+				s0 = seg_of(V.Cp, nseg, V.lo);
+				cnt = min(seg_of(V.Cp, nseg, V.hi - 1) - s0 + 1, kSegCache);
+			}
+			cFirst = s0;
+			cCount = cnt;
+		}
+		__syncthreads();
+		if (threadIdx.x == kPcgThreads - 32)
+		{
+			shFinished = ldi(&a.g->finishedIn[(ph - 1) & 1]);
+			shRefresh = ldi(&a.g->refreshIn[(ph - 1) & 1]);
+		}
+		for (int i = threadIdx.x; i < cCount; i += blockDim.x)
+		{
+			const SegCtl* S = &a.seg[cFirst + i];
+			double beta;
+			int mode;
+			load_beta_mode(S, beta, mode);
+			const double2 as2 = ldv2(&S->alpha);
+			cBeta[i] = beta;
+			cMode[i] = mode;
+			cAlpha[i] = as2.x;
+			cS[i] = as2.y;
+			cRatio[i] = ldd(&S->ratio);
+		}
+		__syncthreads();
+		const int nf = shFinished;
+		finished += nf;
+		if (nf > 0 || (phase1 && (shRefresh > 0 || weighted)))
+		{
+			weighted = rebuild(phase1);
+			cache_segments(V);
+		}
+	};
 	// {beta, mode, alpha, s, ratio} of segment s: from the phase's cache, else from global memory.
 	auto seg_scalars = [&](int s, double& beta, int& mode, double& alpha, double& sv, double& ratio) {
 		const int ci = s - cFirst;
@@ -910,9 +1013,8 @@ __global__ void __launch_bounds__(kPcgThreads, kForm == kPcgF64 ? 3 : 4) k_pcg_p
 		const int maxLoop1 = 3 * a.maxIter + 8;  // a refresh takes two extra phases
 		for (int it = 0; it < maxLoop1; ++it)
 		{
-			phase_start(true, it == 0);
+			phase_begin(true, it == 0, actW);
 			if (finished >= nseg) break;
-			cache_segments(actW);
 			for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
 				const int rs = 32 * c + lane;
 				const int d0 = 3 * rs;
@@ -1170,9 +1272,8 @@ __global__ void __launch_bounds__(kPcgThreads, kForm == kPcgF64 ? 3 : 4) k_pcg_p
 	{
 		// ---- Phase 1. mode 0: p_new = z + beta p_old (own rows, and on the fly for gathered rows);
 		// q = A p_new; pq. mode 1: r64 = b - A (x_hl + x_delta), accumulated in double-float.
-		phase_start(true, false);
+		phase_begin(true, false, actW);
 		if (finished >= nseg) break;
-		cache_segments(actW);
 		for_chunks(actW, sc, nseg, &shNext, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
 			double part, betaD, alphaU, sU, ratioU;
@@ -1243,8 +1344,7 @@ __global__ void __launch_bounds__(kPcgThreads, kForm == kPcgF64 ? 3 : 4) k_pcg_p
 
 		// ---- Phase 2. mode 0: x_delta += alpha s p, r -= alpha q, z = invdiag r; |r|^2, r.z; decide
 		// on a refresh. mode 2: fold x, r = r64 / s, z = invdiag r, p *= ratio; |r|^2, r.z.
-		phase_start(false, false);
-		cache_segments(actC);
+		phase_begin(false, false, actC);
 		for_chunks(actC, sc, nseg, &shNext, [&](int slot, int s, int c) {
 			const int rs = 32 * c + lane;
 			float s0 = 0.f, s1 = 0.f, z[3];
