@@ -510,7 +510,11 @@ __device__ __forceinline__ void cg1_next(const float4& R, const float4& W, const
 
 // kPcgMixed1, CG step: w[row] (3 floats) = sum over the chunk's SELL slots of A_block * u'(J), u'(J)
 // formed by cg1_next from the neighbour's 48-byte record. Rounds of U slots: the columns of the next
-// round are loaded while this round's records are gathered; the last partial round is predicated.
+// round are loaded while this round's records are gathered, and the round's matrix values are loaded
+// together with its records, so a round waits on one memory latency (values loaded after the records
+// are gathered made each round two: one large mesh's solve 19.8 -> 17.2 ms; where the phases stream
+// nearly the whole batch this order is slower, 41.5 -> 53.1 ms, and the autotuner runs that batch
+// in the two-phase schedule). The last partial round is predicated.
 template <int U>
 __device__ __forceinline__ void spmv_row_cg1(const PcgArgs& a, const float4* __restrict__ rec, int c, int lane,
 											 float al, float be, float& a0, float& a1, float& a2)
@@ -531,6 +535,7 @@ __device__ __forceinline__ void spmv_row_cg1(const PcgArgs& a, const float4* __r
 		for (int u = 0; u < U; ++u)
 			if (k + U + u < k1) Jn[u] = __ldcs(&a.col[(k + U + u) * 32 + lane]);
 		float4 R[U], W[U], S[U];
+		float v[U][9];
 #pragma unroll
 		for (int u = 0; u < U; ++u)
 			if (u < nk)
@@ -538,6 +543,9 @@ __device__ __forceinline__ void spmv_row_cg1(const PcgArgs& a, const float4* __r
 				R[u] = rec[3 * J[u]];
 				W[u] = rec[3 * J[u] + 1];
 				S[u] = rec[3 * J[u] + 2];
+				const float* vb = a.val + (size_t)(k + u) * 288 + lane;
+#pragma unroll
+				for (int m = 0; m < 9; ++m) v[u][m] = __ldcs(vb + 32 * m);
 			}
 #pragma unroll
 		for (int u = 0; u < U; ++u)
@@ -545,10 +553,9 @@ __device__ __forceinline__ void spmv_row_cg1(const PcgArgs& a, const float4* __r
 			{
 				float s0, s1, s2, r0, r1, r2, p0, p1, p2;
 				cg1_next(R[u], W[u], S[u], al, be, s0, s1, s2, r0, r1, r2, p0, p1, p2);
-				const float* vb = a.val + (size_t)(k + u) * 288 + lane;
-				a0 += __ldcs(vb) * p0 + __ldcs(vb + 32) * p1 + __ldcs(vb + 64) * p2;
-				a1 += __ldcs(vb + 96) * p0 + __ldcs(vb + 128) * p1 + __ldcs(vb + 160) * p2;
-				a2 += __ldcs(vb + 192) * p0 + __ldcs(vb + 224) * p1 + __ldcs(vb + 256) * p2;
+				a0 += v[u][0] * p0 + v[u][1] * p1 + v[u][2] * p2;
+				a1 += v[u][3] * p0 + v[u][4] * p1 + v[u][5] * p2;
+				a2 += v[u][6] * p0 + v[u][7] * p1 + v[u][8] * p2;
 			}
 		k += U;
 	}
