@@ -211,6 +211,15 @@ def host_info():
 SCHEDULE_NAMES = {0: "two-phase", 1: "fp64", 2: "one-phase"}
 
 
+def pin_schedule(body, args):
+    """--cg-schedule: after the autotuning warm-up step, keep its block sizes and grid but run the
+    persistent solve in the named CG schedule (for comparing the schedules on one workload)."""
+    if args.cg_schedule == "auto":
+        return
+    e, c, r, _ = body.tuning()
+    body.set_tuning(e, c, r, {v: k for k, v in SCHEDULE_NAMES.items()}[args.cg_schedule])
+
+
 def vector_passes(schedule):
     return 11 if schedule == 2 else 10
 
@@ -366,8 +375,10 @@ def run_batch(args, rank, world, local, dist):
     stream = torch.cuda.ExternalStream(body.stream(), device=local)
     # Steps run as a captured CUDA graph; the first warm-up step autotunes (outside the graph).
     flags = _lib.STEP_TIME_KERNELS | _lib.STEP_GRAPH
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
         body.step(1e-3, 1, flags)
+        if w == 0:
+            pin_schedule(body, args)
     torch.cuda.synchronize(local)
     tuning = body.tuning()
     log(f"tuning: {tuning[0]} elements per block, {tuning[1]} CTAs per SM, refresh weight {tuning[2]}, "
@@ -525,9 +536,11 @@ def run_single(args, rank, world, local, dist):
     graph = _lib.STEP_GRAPH if prec == _lib.PRECISION_MIXED else 0
     flags = _lib.STEP_TIME_KERNELS | graph
     step = 0
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
         set_driven(step)
         body.step(dt, 1, flags)
+        if w == 0 and prec == _lib.PRECISION_MIXED:
+            pin_schedule(body, args)
         step += 1
     torch.cuda.synchronize(local)
     dist.barrier()
@@ -697,6 +710,8 @@ def run_bar_full(args, rank, world, local, dist):
         for s in range(args.warmup):
             drive(b, s)
             b.step(scene.dt, 1, flags[k])
+            if s == 0 and k == "mixed":
+                pin_schedule(b, args)
     torch.cuda.synchronize(local)
     for k, b in bodies.items():  # back to rest: the timed run is the scenario from its first step
         x, v = views[k]
@@ -1239,6 +1254,8 @@ def main():
                     help="bar and cube only; the batch is always mixed precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain FP64 path comparison (batch)")
+    ap.add_argument("--cg-schedule", default="auto", choices=["auto", "two-phase", "one-phase"],
+                    help="mixed form: run the persistent solve in this CG schedule instead of the autotuner's")
     ap.add_argument("--meshes", type=int, default=BATCH["count"], help="batch size (smaller cases for profiling)")
     ap.add_argument("--bar-h", type=float, default=None,
                     help=f"bar cube edge in m (default {BAR_H_WINDOW} for a step window, {BAR_H_FULL} for the whole run)")
