@@ -41,6 +41,23 @@ def test_every_declared_symbol_is_exported(lib):
     assert exported <= set(decl), "library exports undeclared symbols: %s" % (exported - set(decl))
 
 
+def test_header_constants_match_the_python_bindings():
+    """The #define'd flags and CG schedules of gbfem.h have the values the ctypes layer (and
+    bench.py's schedule names) use."""
+    from opensurgsim_gb300 import _lib
+
+    import bench
+
+    text = open(HEADER).read()
+    defines = {k: int(v) for k, v in re.findall(r"#define\s+GBFEM_(\w+)\s+(\d+)u?\b", text)}
+    for name in ("CG_TWO_PHASE", "CG_ONE_PHASE", "CG_FP64", "STEP_GRAPH", "STEP_TIME_KERNELS", "STEP_KEEP_SYSTEM",
+                 "STEP_TIME_PHASES", "ELEMENT_COROTATIONAL_TET", "ELEMENT_LINEAR_TET", "ELEMENT_HEXAHEDRON"):
+        assert defines[name] == getattr(_lib, name), name
+    assert {defines[k] for k in defines if k.startswith("CG_")} == set(bench.SCHEDULE_NAMES)
+    assert bench.SCHEDULE_NAMES[_lib.CG_ONE_PHASE] == "one-phase"
+    assert bench.vector_passes(_lib.CG_ONE_PHASE) == 11 and bench.vector_passes(_lib.CG_TWO_PHASE) == 10
+
+
 def test_params_default(lib):
     from opensurgsim_gb300 import _lib
 
