@@ -223,6 +223,8 @@ GBFEM_API gbfem_status gbfem_set_solver_params(gbfem_handle h, int32_t newton_ma
  *   GBFEM_CG_ONE_PHASE: one phase an iteration (Chronopoulos and Gear's recurrences, both dot
  *     products from one reduction): half the phases, larger neighbour records;
  *   GBFEM_CG_FP64: FP64 batches (their only schedule).
+ * Without autotuning a handle starts in GBFEM_CG_ONE_PHASE when its system has at most 64 chunks of
+ * 32 rows per SM (a few per warp: phases wait on latency), else in GBFEM_CG_TWO_PHASE.
  * gbfem_set_tuning's cg_schedule -1 keeps the handle's current schedule. */
 #define GBFEM_CG_TWO_PHASE 0
 #define GBFEM_CG_FP64 1

@@ -748,6 +748,11 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		GB_CUDA(h, cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, h->device));
 		h->chunkWeightTotal = cumW[nchunks];
 		h->chunkWeightMin = std::max(1, wmin);
+		// CG schedule until the autotuner or gbfem_set_tuning picks one: one grid phase an iteration
+		// where a phase leaves each warp a few chunks (its phases wait on latency; one 1.28M-tet mesh,
+		// 8,458 chunks: 17.2 vs 22.9 ms a solve), two phases where phases stream many chunks a warp
+		// (64 meshes, 19,549 chunks: 15.7 vs 16.3 ms; 256 meshes: 41.3 vs 53.1 ms).
+		h->cgSchedule = (nchunks <= kOnePhaseChunksPerSlot * 4 * h->smCount) ? kPcgMixed1 : kPcgMixed2;
 		gbfem_status cst = GBFEM_INVALID_ARG;
 		std::string why;
 		for (int cps = 4; cps >= 1 && cst != GBFEM_OK; --cps)

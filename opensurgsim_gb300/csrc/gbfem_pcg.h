@@ -29,6 +29,9 @@ enum PcgForm : int
 	kPcgF64 = 1,
 	kPcgMixed1 = 2,
 };
+// Default schedule without autotuning: kPcgMixed1 while the system has at most this many chunks per
+// CTA slot of a 4-CTA-per-SM grid, kPcgMixed2 above.
+constexpr int kOnePhaseChunksPerSlot = 16;
 constexpr int kPcgNV = 3;  // per-chunk partial values a phase can reduce (shared memory, cross-CTA slots)
 
 // Per-segment (per-mesh) CG state, in device memory. Written by the CTA that completes a
