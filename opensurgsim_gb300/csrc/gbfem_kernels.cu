@@ -110,11 +110,20 @@ __global__ void __launch_bounds__(kT, 384 / kT) k_element_f32(DevBody b, const d
 	const int cnt = min(kT, E - e0);
 	if (kslots)
 	{
-		float* dstK = kslots + (size_t)e0 * kV;
-		for (int idx = threadIdx.x; idx < cnt * kV; idx += kT)
+		// Split layout (k_assemble_f32): the first 8 values of element e's block k as one 32-byte
+		// sector at kslots[8 (10 e + k)], the 9th at kslots[80 E + 10 e + k].
+		float* dst8 = kslots + (size_t)e0 * (8 * kSlots);
+		for (int idx = threadIdx.x; idx < cnt * 8 * kSlots; idx += kT)
 		{
-			const int el = idx / kV;
-			dstK[idx] = sks[idx - el * kV][el];
+			const int el = idx / (8 * kSlots);
+			const int j = idx - el * (8 * kSlots);
+			dst8[idx] = sks[9 * (j >> 3) + (j & 7)][el];
+		}
+		float* dst1 = kslots + (size_t)E * (8 * kSlots) + (size_t)e0 * kSlots;
+		for (int idx = threadIdx.x; idx < cnt * kSlots; idx += kT)
+		{
+			const int el = idx / kSlots;
+			dst1[idx] = sks[9 * (idx - el * kSlots) + 8][el];
 		}
 	}
 	float* dstR = rhsE + (size_t)e0 * 12;
@@ -185,6 +194,78 @@ __global__ void k_assemble(DevBody b, const T* __restrict__ ks, double c1, doubl
 		{
 			const T d = blk[4 * i];
 			invdiag[3 * I + i] = (d != T(0)) ? T(1) / d : T(1);  // DiagonalPreconditioner
+		}
+	}
+}
+
+// FP32 assembly from the FP32 element kernel's split layout: each contribution's first 8 values are
+// one aligned 32-byte sector (two float4 loads), the 9th sits in the trailing array. The 36-byte blocks
+// of the plain layout straddle sectors, so a contribution cost two sectors of reads there. Same sums,
+// same order as k_assemble.
+__global__ void k_assemble_f32(DevBody b, const float* __restrict__ ks, double c1, double c2, float* __restrict__ A,
+							   float* __restrict__ invdiag)
+{
+	const int L = blockIdx.x * blockDim.x + threadIdx.x;
+	if (L >= b.nl) return;
+	const int4 lb = b.lblk[L];
+	float s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+	const float* ks1 = ks + (size_t)b.E * (8 * kSlots);
+	const int k1 = b.cptr[L + 1];
+	for (int k = b.cptr[L]; k < k1; ++k)
+	{
+		const int ci = b.cidx[k];
+		const float4* src = reinterpret_cast<const float4*>(ks + (size_t)ci * 8);
+		const float4 u = src[0], w = src[1];
+		const float t = ks1[ci];
+		s[0] += u.x;
+		s[1] += u.y;
+		s[2] += u.z;
+		s[3] += u.w;
+		s[4] += w.x;
+		s[5] += w.y;
+		s[6] += w.z;
+		s[7] += w.w;
+		s[8] += t;
+	}
+	const float mm = float(c1 * b.lmass[L]);
+	const float c2t = float(c2);
+	float blk[9];
+#pragma unroll
+	for (int m = 0; m < 9; ++m) blk[m] = c2t * s[m];
+	blk[0] += mm;
+	blk[4] += mm;
+	blk[8] += mm;
+	const int I = lb.x, J = lb.y;
+	if (I == J)
+	{
+		blk[1] = blk[3];
+		blk[2] = blk[6];
+		blk[5] = blk[7];
+	}
+#pragma unroll
+	for (int i = 0; i < 3; ++i)
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			const int r = 3 * I + i, c = 3 * J + j;
+			if (b.bc[r] | b.bc[c]) blk[3 * i + j] = (r == c) ? 1.f : 0.f;
+		}
+#pragma unroll
+	for (int m = 0; m < 9; ++m) A[(size_t)lb.z + 32 * m] = blk[m];
+	if (lb.w >= 0)
+	{
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j) A[(size_t)lb.w + 32 * (3 * j + i)] = blk[3 * i + j];
+	}
+	if (I == J)
+	{
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+			const float d = blk[4 * i];
+			invdiag[3 * I + i] = (d != 0.f) ? 1.f / d : 1.f;  // DiagonalPreconditioner
 		}
 	}
 }
@@ -967,7 +1048,7 @@ void launch_assemble(const DevBody& b, const float* kslots, double c1, double c2
 					 cudaStream_t s)
 {
 	if (b.nl == 0) return;
-	k_assemble<float><<<blocks(b.nl, 128), 128, 0, s>>>(b, kslots, c1, c2, A, invdiag);
+	k_assemble_f32<<<blocks(b.nl, 128), 128, 0, s>>>(b, kslots, c1, c2, A, invdiag);
 }
 
 void launch_rhs_gather(const DevBody& b, const double* rhsE, const double* gravity, int gravityOn, double* rhs,
