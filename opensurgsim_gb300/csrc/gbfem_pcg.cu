@@ -9,16 +9,19 @@
 // |r|^2 < tol^2 |b|^2 rule as the FP64 form (Eigen's ConjugateGradient).
 //
 // Work is cut into chunks of 32 matrix rows (one node row per lane); segments own contiguous
-// chunk ranges. Every iteration has two phases separated by grid barriers: phase 1 is the SpMV
-// (or, for a segment due for a refresh, the true residual), phase 2 the row-local update (or the
-// rescale after a refresh). Each phase walks only the chunks of the segments still iterating
-// (the active set), split over the CTAs by exact integer arithmetic on cumulative weights: the
-// SpMV phase balances block columns, the row-local phase chunk counts. Every CTA recomputes
-// its own range whenever the active set changes, so no CTA idles on finished meshes.
+// chunk ranges. In the two-phase CG schedule every iteration has two phases separated by grid
+// barriers: phase 1 is the SpMV (or, for a segment due for a refresh, the true residual), phase 2
+// the row-local update (or the rescale after a refresh). The one-phase schedule (Chronopoulos and
+// Gear's recurrences) does an iteration's SpMV, row update and both dot products in one phase. Each
+// phase walks only the chunks of the segments still iterating (the active set), split over the CTAs
+// by exact integer arithmetic on cumulative weights: SpMV phases balance block columns, row-local
+// phases chunk counts. Every CTA recomputes its own range whenever the active set changes, so no CTA
+// idles on finished meshes. The plain FP64 form (Eigen's CG on the FP64 values) runs the two-phase
+// structure without refreshes.
 //
 // Per-segment sums are deterministic: each CTA sums its chunk partials of a segment in chunk
 // order; a segment spread over CTAs bf..bl is completed by the last of them to arrive (ticket
-// counter), which adds the CTAs' partials in CTA order. A grid-barrier wait gives up after a
+// counter), which adds the CTAs' partials in a fixed order. A grid-barrier wait gives up after a
 // wall-time limit (1 s in the solve): the kernel records an error and returns (the host reports
 // GBFEM_CUDA_ERROR).
 
