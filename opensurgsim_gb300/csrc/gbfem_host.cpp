@@ -602,7 +602,7 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 	h->sellSlots = sellSlots;
 	h->nrows = nrows;
 	h->nchunks = nchunks;
-	// Lower blocks (I >= J) in row order, written to the SELL positions of (I,J) and (J,I).
+	// Lower blocks (I >= J), collected in row order, each written to the SELL positions of (I,J) and (J,I).
 	std::vector<int> lowerOfPos(h->nb, -1);
 	std::vector<int4> lblk;
 	lblk.reserve(h->nb / 2 + N);
@@ -614,6 +614,25 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 			lowerOfPos[k] = (int)lblk.size();
 			lblk.push_back(make_int4(I, J, sellBase[k], I == J ? -1 : sellBase[h->blockPos(J, I)]));
 		}
+	// Assembly threads run in the order of the (I,J) blocks' SELL positions, so the lanes of a warp
+	// write neighbouring lanes of one SELL block column (coalesced) instead of one row's blocks, whose
+	// positions are 288 values apart. Each block's sum is unchanged (its contributions stay in element
+	// order); only which thread forms it moves.
+	{
+		std::vector<int> order(lblk.size());
+		for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+		std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return lblk[x].z < lblk[y].z; });
+		std::vector<int> newIndex(lblk.size());
+		std::vector<int4> sorted(lblk.size());
+		for (size_t i = 0; i < order.size(); ++i)
+		{
+			newIndex[order[i]] = (int)i;
+			sorted[i] = lblk[order[i]];
+		}
+		lblk.swap(sorted);
+		for (int& L : lowerOfPos)
+			if (L >= 0) L = newIndex[L];
+	}
 	h->nl = (int)lblk.size();
 	h->lowerOfPosHost = lowerOfPos;
 	h->lblkHost = lblk;
