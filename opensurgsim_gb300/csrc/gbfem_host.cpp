@@ -174,7 +174,7 @@ struct gbfem_handle_s
 	int smCount = 0, chunkWeightMin = 1;
 	int64_t chunkWeightTotal = 0;
 	int ctasPerSM = 4, refreshWeight = kRefreshWeightDefault, elemsPerBlock = 64;
-	int cgSchedule = kPcgMixed1;  // PcgForm of the mixed solve (FP64 batches: kPcgF64)
+	int cgSchedule = kPcgMixed1;  // PcgForm of the mixed solve, set at creation from the system's size
 	bool tuned = false;
 	int tuneVersion = 0;
 	// CUDA graph of one mixed-form step (GBFEM_STEP_GRAPH), rebuilt when dt, the timing flag or the
@@ -863,7 +863,7 @@ gbfem_status build_body(gbfem_handle h, const gbfem_mesh_desc* m)
 		const size_t nr = 3 * (size_t)nrows;  // row-space vectors of the persistent solve
 		for (DevBuf<float>* b : {&h->d_xd, &h->d_invd, &h->d_r32, &h->d_q32}) GB_CUDA(h, b->alloc(nr));
 		// The rows' records that neighbours gather: two-phase schedule, z and p in 32 bytes (one sector);
-		// one-phase schedules, {r, w, s} and invdiag in 48 bytes.
+		// one-phase schedule, {r, w, s} and invdiag in 48 bytes.
 		for (DevBuf<float>* b : {&h->d_pA, &h->d_pB}) GB_CUDA(h, b->alloc(12 * (size_t)nrows));
 		for (DevBuf<double>* b : {&h->d_brs, &h->d_r64, &h->d_x64}) GB_CUDA(h, b->alloc(nr));
 		gbfem_status pst = setup_persistent();
@@ -1088,7 +1088,7 @@ gbfem_status enqueue_mixed(gbfem_handle h, const double* b, double* x, int maxIt
 	a.pA = h->d_pA.p;
 	a.pB = h->d_pB.p;
 	a.q = h->d_q32.p;
-	a.pdir = h->d_q32.p;  // the one-phase schedules keep p where the two-phase one keeps q
+	a.pdir = h->d_q32.p;  // the one-phase schedule keeps p where the two-phase one keeps q
 	a.cumW = h->d_cumW.p;
 	a.slots = h->d_slots.p;
 	a.maxChunksPerCta = h->maxChunksPerCta;
