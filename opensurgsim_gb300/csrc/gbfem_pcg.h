@@ -20,9 +20,10 @@ constexpr int kPcgChunkWeight = 2;  // per-chunk constant added to the block-col
 //              same refreshes and stopping rule as kPcgMixed2. Its SpMV gathers two 48-byte records a
 //              round (four would spill at 64 registers; at 80 registers and 3 CTAs per SM they measured
 //              slower on both the 256-mesh batch and the 1.28M-tet bar, and so did three with a spill).
-// Measured on GB300: the one-phase schedule halves the phases (bar: 972 -> 491 a solve, 24.8 -> 19.8
-// ms), while on the 256-mesh batch, whose phases mostly stream the whole batch, its 48-byte records
-// (two sectors a gather, against one) cost what the saved phases gain (42.1 vs 42.8 ms).
+// Measured on GB300: the one-phase schedule halves the phases; on one 1.28M-tet mesh, whose phases
+// wait on latency, its solve takes 17.2 ms against 22.9 ms in two phases, while on the 256-mesh batch,
+// whose phases mostly stream the whole batch, it is the slower (53.1 vs 41.3 ms). The autotuner times
+// both; without it a handle starts in the schedule its size suggests (kOnePhaseChunksPerSlot).
 enum PcgForm : int
 {
 	kPcgMixed2 = 0,
